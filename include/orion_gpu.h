@@ -1,0 +1,218 @@
+/*
+ * orion_gpu.h -- C ABI of the GB300 wavefront path tracer.
+ *
+ * This is the whole boundary between a host application and the CUDA path
+ * tracer: plain C types, caller-owned buffers, status-code returns, opaque
+ * handles, no exceptions or C++ types across it. It replaces the reference's
+ * path-tracing hot path:
+ *
+ *   Integrator::render(const Scene&)      src/core/integrator.h:26
+ *   PathTracing::render / Li              src/integrator/path.cpp:15-37, 50-99
+ *   Scene::intersect -> EmbreeKernel      src/core/scene.cpp:16-19, src/core/kernel.cpp:111-174
+ *   Parser(path).getRenderOption()        src/util/parser.cpp:45-56, 463-471
+ *
+ * Every entry point returns ORION_OK (0) or a negative ORION_ERR_* code; the
+ * message for the last failure on the calling thread is available from
+ * orion_last_error().
+ */
+#ifndef ORION_GPU_H_
+#define ORION_GPU_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------- status */
+enum {
+  ORION_OK = 0,
+  ORION_ERR_INVALID = -1,     /* bad argument or handle */
+  ORION_ERR_IO = -2,          /* file missing or unreadable */
+  ORION_ERR_PARSE = -3,       /* malformed scene XML or OBJ */
+  ORION_ERR_CUDA = -4,        /* CUDA runtime failure */
+  ORION_ERR_NOMEM = -5,       /* allocation failed or device budget exceeded */
+  ORION_ERR_UNSUPPORTED = -6, /* scene feature outside this library */
+  ORION_ERR_DEVICE = -7,      /* a kernel raised its error word (overflow / iteration cap) */
+  ORION_ERR_NOT_READY = -8,   /* serving: job still running */
+  ORION_ERR_CANCELLED = -9    /* serving: job cancelled */
+};
+
+/* Message of the last failure on this thread ("" if none). */
+const char* orion_last_error(void);
+
+/* ------------------------------------------------------------- materials */
+/* One record per <Material>; fields unused by a type are ignored.
+ * Types follow src/material/{matte,metal,mirror,glass,plastic,uber}.cpp. */
+enum {
+  ORION_MAT_MATTE = 0,   /* Kd, sigma (src/material/matte.cpp:9-21) */
+  ORION_MAT_METAL = 1,   /* eta_rgb, k, roughness (src/material/metal.cpp:8-17) */
+  ORION_MAT_MIRROR = 2,  /* Kr (src/material/mirror.cpp:6-13) */
+  ORION_MAT_GLASS = 3,   /* Kr, Kt, roughness, eta (src/material/glass.cpp:9-37) */
+  ORION_MAT_PLASTIC = 4, /* Kd, Ks, roughness (src/material/plastic.cpp:8-24) */
+  ORION_MAT_UBER = 5     /* Kd, Ks, Kr, Kt, opacity, roughness, eta (src/material/uber.cpp:9-42) */
+};
+/* Microfacet distribution. The reference has GGX only (src/bsdf/microfacet.cpp:9-40);
+ * Beckmann is an extension selected by <Param distribution="beckmann"/>. */
+enum { ORION_DIST_GGX = 0, ORION_DIST_BECKMANN = 1 };
+
+typedef struct orion_material {
+  int32_t type;
+  int32_t distribution;
+  int32_t has_sigma; /* matte: 0 = no <sigma> (Lambert) */
+  int32_t reserved;
+  float Kd[3], Ks[3], Kr[3], Kt[3], opacity[3];
+  float eta_rgb[3], k[3]; /* metal */
+  float sigma, roughness, eta;
+} orion_material;
+
+/* ---------------------------------------------------------------- lights */
+/* Order in a scene is the reference's scene.lights order: area lights (one
+ * per emissive triangle, in primitive order), then <Light> elements, then
+ * <Envmap> elements (src/util/parser.cpp:45-56). */
+enum {
+  ORION_LIGHT_AREA = 0,    /* src/light/diffuse.cpp:8-56 */
+  ORION_LIGHT_POINT = 1,   /* src/light/point.cpp:6-19 */
+  ORION_LIGHT_SPOT = 2,    /* src/light/spot.cpp:6-29 */
+  ORION_LIGHT_DISTANT = 3, /* src/light/distant.cpp:6-26 */
+  ORION_LIGHT_ENV = 4      /* constant environment, src/light/envmap.cpp:9-81 */
+};
+
+typedef struct orion_light {
+  int32_t type;
+  int32_t prim;            /* area: index of the emissive triangle */
+  float L[3];              /* area Le, point/spot I, distant/env L */
+  float p[3];              /* point/spot: world position */
+  float dir[3];            /* distant: unit direction towards which light travels from `from` */
+  float l2w[12], w2l[12];  /* spot/env: light<->world, 3x4 row-major */
+  float cos_total, cos_falloff; /* spot */
+} orion_light;
+
+/* ---------------------------------------------------------------- camera */
+typedef struct orion_camera {
+  float c2w[16];           /* camera-to-world, 4x4 row-major (src/core/transform.cpp:197-217) */
+  float fov;               /* vertical field of view, degrees */
+  float lens_radius;       /* 0 = pinhole (src/camera/pinhole.cpp:23-29) */
+  float focal_distance;
+  int32_t width, height;   /* film size */
+} orion_camera;
+
+/* ----------------------------------------------------------------- scene */
+/* Flat, de-indexed scene in primitive (primID) order: the data the
+ * reference hands to Embree plus what shading needs per primitive. */
+typedef struct orion_scene_desc {
+  int64_t num_prims;
+  const float* positions;        /* num_prims x 9: p0, p1, p2 in world space */
+  const float* normals;          /* num_prims x 9: per-corner shading normals */
+  const float* uvs;              /* num_prims x 6, or NULL */
+  const int32_t* material_of_prim;
+  const int32_t* light_of_prim;  /* index into lights of the prim's area light, or -1 */
+  int32_t num_materials;
+  int32_t num_lights;
+  const orion_material* materials;
+  const orion_light* lights;
+  orion_camera camera;
+  int32_t spp;                   /* <Integrator> nSamplesPerPixel */
+  int32_t max_depth;             /* <Integrator> maxDepth */
+} orion_scene_desc;
+
+typedef struct orion_host_scene orion_host_scene;
+
+/* Parse a .ori scene file and its OBJ meshes (src/util/parser.cpp:463-471). */
+int orion_scene_load_ori(const char* path, orion_host_scene** out);
+/* Copy a caller-built description into a new host scene. */
+int orion_scene_from_desc(const orion_scene_desc* desc, orion_host_scene** out);
+/* View of a host scene's arrays; valid until orion_scene_free. */
+int orion_scene_get_desc(const orion_host_scene* scene, orion_scene_desc* out);
+void orion_scene_free(orion_host_scene* scene);
+
+/* --------------------------------------------------------------- context */
+typedef struct orion_gpu_ctx orion_gpu_ctx;
+
+typedef struct orion_gpu_opts {
+  int32_t device;          /* CUDA device ordinal */
+  int32_t reserved;
+  int64_t memory_budget;   /* bytes the context may hold for scenes + path state; 0 = 90% of free memory */
+  const char* sobol_path;  /* Sobol matrix file; NULL = sobol_matrices.bin beside the library */
+} orion_gpu_opts;
+
+int orion_gpu_create(const orion_gpu_opts* opts, orion_gpu_ctx** out);
+int orion_gpu_destroy(orion_gpu_ctx* ctx);
+
+typedef int32_t orion_scene_id;
+
+/* Build the BVH on the host and upload the scene (replaces EmbreeKernel::build,
+ * src/core/kernel.cpp:63-110). The scene stays resident until released. */
+int orion_gpu_scene_upload(orion_gpu_ctx* ctx, const orion_host_scene* scene, orion_scene_id* out);
+int orion_gpu_scene_release(orion_gpu_ctx* ctx, orion_scene_id id);
+/* Device bytes held by a resident scene (BVH + triangles + shading data). */
+int orion_gpu_scene_bytes(orion_gpu_ctx* ctx, orion_scene_id id, int64_t* bytes);
+
+typedef struct orion_render_params {
+  int32_t spp;               /* 0 = the scene's nSamplesPerPixel */
+  int32_t max_depth;         /* -1 = the scene's maxDepth */
+  int32_t rr_depth;          /* Russian roulette when bounces > rr_depth; the reference uses 3 (path.cpp:91) */
+  int32_t flags;             /* ORION_RENDER_* */
+  int64_t first_pass;        /* k0: sample index of (i, j, k) is (k0 + k)*W*H + j*W + i */
+  int32_t wave_paths;        /* paths per wavefront wave; 0 = autotuned */
+  int32_t reserved;
+} orion_render_params;
+
+enum {
+  ORION_RENDER_FP64 = 1      /* also accumulate FP64 sums and sums of squares */
+};
+
+/* Render statistics of the last orion_gpu_render on a context. */
+typedef struct orion_render_stats {
+  int64_t paths;             /* camera paths traced */
+  int64_t rays;              /* all rays: extension + shadow + MIS */
+  int64_t ext_rays, shadow_rays, mis_rays;
+  int64_t kernel_launches;
+  double device_ms;          /* device time of the render (CUDA events) */
+} orion_render_stats;
+
+/* Integrator::render(): traces W*H*spp paths and writes the film.
+ * film_rgb_sum: W*H*3 floats, per-pixel FP32 sums in sample order (as
+ * RenderTarget::acumulate, src/texture/rendertarget.cpp:22-27).
+ * film_count: W*H sample counts, or NULL. Both are host buffers. */
+int orion_gpu_render(orion_gpu_ctx* ctx, orion_scene_id id, const orion_render_params* params,
+                     float* film_rgb_sum, uint32_t* film_count);
+/* Same, with FP64 per-pixel sums and sums of squares (W*H*3 doubles each). */
+int orion_gpu_render_fp64(orion_gpu_ctx* ctx, orion_scene_id id, const orion_render_params* params,
+                          double* sum, double* sumsq);
+int orion_gpu_last_stats(orion_gpu_ctx* ctx, orion_render_stats* out);
+
+/* Per-stage device time of the last render, filled only while profiling is
+ * on (CUDA events around every kernel; adds a little launch overhead).
+ * Stages: 0 camera, 1 extension-ray trace, 2 shade, 3 shadow-ray trace,
+ * 4 MIS-ray trace, 5 direct-light resolve, 6 film, 7 bookkeeping. */
+#define ORION_NUM_STAGES 8
+typedef struct orion_stage_times {
+  double ms[ORION_NUM_STAGES];
+  int64_t launches[ORION_NUM_STAGES];
+} orion_stage_times;
+int orion_gpu_set_profiling(orion_gpu_ctx* ctx, int32_t enable);
+int orion_gpu_stage_times(orion_gpu_ctx* ctx, orion_stage_times* out);
+
+/* ------------------------------------------------- component test hooks */
+/* sobol::sample (src/sampler/sobol.h:28-43) for n (index, dim) pairs. */
+int orion_gpu_sobol(orion_gpu_ctx* ctx, int64_t n, const uint64_t* index, const uint32_t* dim, float* out);
+/* Closest hit (any_hit = 0) or occlusion (any_hit = 1) for n rays given as
+ * n x 8 floats (o, d, tnear, tfar). prim = -1 for a miss. */
+int orion_gpu_trace(orion_gpu_ctx* ctx, orion_scene_id id, int64_t n, const float* rays, int32_t any_hit,
+                    float* t, float* u, float* v, int32_t* prim);
+/* Camera rays (src/camera/pinhole.cpp:8-33) for sample indices: n x 6 floats. */
+int orion_gpu_camera_rays(orion_gpu_ctx* ctx, orion_scene_id id, int64_t n, const int64_t* sample_index,
+                          float* rays);
+/* BSDF at a synthetic hit: frame n x 12 (ng, ns, u, v); wo, wi n x 3; rnd n x 2.
+ * Outputs f, pdf for (wi, wo), and sample_f's f, wi, pdf, sampled type, and the
+ * number of non-specular lobes (src/core/bsdf.cpp:4-106). */
+int orion_gpu_bsdf_eval(orion_gpu_ctx* ctx, const orion_material* mat, int64_t n, const float* frame,
+                        const float* wo, const float* wi, const float* rnd, int32_t type, float* f, float* pdf,
+                        float* sf, float* swi, float* spdf, int32_t* stype, int32_t* nbxdf);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ORION_GPU_H_ */

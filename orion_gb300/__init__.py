@@ -1,0 +1,391 @@
+"""GB300 wavefront path tracer behind orion's scene-file / Integrator surface.
+
+Host mirror of the reference's API for the path-tracing hot path, over the
+C ABI in include/orion_gpu.h (liborion_gb300.so, built in-tree):
+
+    reference (C++)                              here
+    Parser(path).getRenderOption()               Parser(path, ctx).getRenderOption()
+      src/util/parser.cpp:463-471
+    integrator->render(*scene)                   ro.integrator.render(ro.scene)
+      src/core/integrator.h:26
+    camera->getFilm()->getAveraged()             ro.camera.getFilm().getAveraged()
+      src/texture/rendertarget.cpp:28-37
+
+Loading the library never falls back to anything else: if the shared
+library or a CUDA device is missing, the call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "liborion_gb300.so")
+
+ORION_OK = 0
+ERRORS = {-1: "invalid", -2: "io", -3: "parse", -4: "cuda", -5: "nomem", -6: "unsupported", -7: "device",
+          -8: "not_ready", -9: "cancelled"}
+
+MAT_MATTE, MAT_METAL, MAT_MIRROR, MAT_GLASS, MAT_PLASTIC, MAT_UBER = range(6)
+DIST_GGX, DIST_BECKMANN = 0, 1
+LIGHT_AREA, LIGHT_POINT, LIGHT_SPOT, LIGHT_DISTANT, LIGHT_ENV = range(5)
+BXDF_ALL = 31
+BXDF_NONSPECULAR = 31 & ~16
+
+
+class OrionError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"{ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+class Material(C.Structure):
+    _fields_ = [("type", C.c_int32), ("distribution", C.c_int32), ("has_sigma", C.c_int32), ("reserved", C.c_int32),
+                ("Kd", C.c_float * 3), ("Ks", C.c_float * 3), ("Kr", C.c_float * 3), ("Kt", C.c_float * 3),
+                ("opacity", C.c_float * 3), ("eta_rgb", C.c_float * 3), ("k", C.c_float * 3),
+                ("sigma", C.c_float), ("roughness", C.c_float), ("eta", C.c_float)]
+
+
+class Light(C.Structure):
+    _fields_ = [("type", C.c_int32), ("prim", C.c_int32), ("L", C.c_float * 3), ("p", C.c_float * 3),
+                ("dir", C.c_float * 3), ("l2w", C.c_float * 12), ("w2l", C.c_float * 12),
+                ("cos_total", C.c_float), ("cos_falloff", C.c_float)]
+
+
+class Camera(C.Structure):
+    _fields_ = [("c2w", C.c_float * 16), ("fov", C.c_float), ("lens_radius", C.c_float),
+                ("focal_distance", C.c_float), ("width", C.c_int32), ("height", C.c_int32)]
+
+
+class SceneDesc(C.Structure):
+    _fields_ = [("num_prims", C.c_int64), ("positions", C.c_void_p), ("normals", C.c_void_p), ("uvs", C.c_void_p),
+                ("material_of_prim", C.c_void_p), ("light_of_prim", C.c_void_p), ("num_materials", C.c_int32),
+                ("num_lights", C.c_int32), ("materials", C.c_void_p), ("lights", C.c_void_p), ("camera", Camera),
+                ("spp", C.c_int32), ("max_depth", C.c_int32)]
+
+
+class GpuOpts(C.Structure):
+    _fields_ = [("device", C.c_int32), ("reserved", C.c_int32), ("memory_budget", C.c_int64),
+                ("sobol_path", C.c_char_p)]
+
+
+class RenderParams(C.Structure):
+    _fields_ = [("spp", C.c_int32), ("max_depth", C.c_int32), ("rr_depth", C.c_int32), ("flags", C.c_int32),
+                ("first_pass", C.c_int64), ("wave_paths", C.c_int32), ("reserved", C.c_int32)]
+
+
+class RenderStats(C.Structure):
+    _fields_ = [("paths", C.c_int64), ("rays", C.c_int64), ("ext_rays", C.c_int64), ("shadow_rays", C.c_int64),
+                ("mis_rays", C.c_int64), ("kernel_launches", C.c_int64), ("device_ms", C.c_double)]
+
+
+class StageTimes(C.Structure):
+    _fields_ = [("ms", C.c_double * 8), ("launches", C.c_int64 * 8)]
+
+
+STAGES = ("camera", "trace_ext", "shade", "trace_shadow", "trace_mis", "resolve", "film", "other")
+
+_lib = None
+
+
+def library() -> C.CDLL:
+    """The product library; raises if it has not been built."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise OSError(f"{LIB_PATH} is missing: run __graft_entry__.build() first")
+        lib = C.CDLL(LIB_PATH)
+        vp, i32, i64 = C.c_void_p, C.c_int32, C.c_int64
+        sigs = {
+            "orion_last_error": (C.c_char_p, []),
+            "orion_scene_load_ori": (i32, [C.c_char_p, C.POINTER(vp)]),
+            "orion_scene_from_desc": (i32, [C.POINTER(SceneDesc), C.POINTER(vp)]),
+            "orion_scene_get_desc": (i32, [vp, C.POINTER(SceneDesc)]),
+            "orion_scene_free": (None, [vp]),
+            "orion_gpu_create": (i32, [C.POINTER(GpuOpts), C.POINTER(vp)]),
+            "orion_gpu_destroy": (i32, [vp]),
+            "orion_gpu_scene_upload": (i32, [vp, vp, C.POINTER(i32)]),
+            "orion_gpu_scene_release": (i32, [vp, i32]),
+            "orion_gpu_scene_bytes": (i32, [vp, i32, C.POINTER(i64)]),
+            "orion_gpu_render": (i32, [vp, i32, C.POINTER(RenderParams), vp, vp]),
+            "orion_gpu_render_fp64": (i32, [vp, i32, C.POINTER(RenderParams), vp, vp]),
+            "orion_gpu_last_stats": (i32, [vp, C.POINTER(RenderStats)]),
+            "orion_gpu_set_profiling": (i32, [vp, i32]),
+            "orion_gpu_stage_times": (i32, [vp, C.POINTER(StageTimes)]),
+            "orion_gpu_sobol": (i32, [vp, i64, vp, vp, vp]),
+            "orion_gpu_trace": (i32, [vp, i32, i64, vp, i32, vp, vp, vp, vp]),
+            "orion_gpu_camera_rays": (i32, [vp, i32, i64, vp, vp]),
+            "orion_gpu_bsdf_eval": (i32, [vp, C.POINTER(Material), i64, vp, vp, vp, vp, i32, vp, vp, vp, vp, vp,
+                                          vp, vp]),
+        }
+        for name, (res, args) in sigs.items():
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = lib
+    return _lib
+
+
+def _check(rc: int) -> None:
+    if rc != ORION_OK:
+        raise OrionError(rc, library().orion_last_error().decode())
+
+
+def _ptr(a: np.ndarray) -> C.c_void_p:
+    return C.c_void_p(a.ctypes.data)
+
+
+# ------------------------------------------------------------------ scenes
+
+
+class HostScene:
+    """A parsed scene on the host (flat primitive arrays, materials, lights, camera)."""
+
+    def __init__(self, handle: int, keep=None):
+        self._h = C.c_void_p(handle)
+        self._keep = keep
+
+    @classmethod
+    def load(cls, path: str) -> "HostScene":
+        h = C.c_void_p()
+        _check(library().orion_scene_load_ori(os.fsencode(path), C.byref(h)))
+        return cls(h.value)
+
+    @classmethod
+    def from_arrays(cls, positions, normals, material_of_prim, materials, lights, camera: Camera, spp: int,
+                    max_depth: int, light_of_prim=None, uvs=None) -> "HostScene":
+        pos = np.ascontiguousarray(positions, dtype=np.float32).reshape(-1, 9)
+        nrm = np.ascontiguousarray(normals, dtype=np.float32).reshape(-1, 9)
+        mop = np.ascontiguousarray(material_of_prim, dtype=np.int32)
+        lop = np.ascontiguousarray(light_of_prim if light_of_prim is not None else np.full(len(pos), -1), np.int32)
+        mats = (Material * len(materials))(*materials)
+        lts = (Light * max(1, len(lights)))(*lights)
+        d = SceneDesc()
+        d.num_prims = len(pos)
+        d.positions, d.normals = pos.ctypes.data, nrm.ctypes.data
+        d.uvs = np.ascontiguousarray(uvs, np.float32).ctypes.data if uvs is not None else None
+        d.material_of_prim, d.light_of_prim = mop.ctypes.data, lop.ctypes.data
+        d.num_materials, d.num_lights = len(materials), len(lights)
+        d.materials, d.lights = C.addressof(mats), C.addressof(lts)
+        d.camera, d.spp, d.max_depth = camera, spp, max_depth
+        h = C.c_void_p()
+        _check(library().orion_scene_from_desc(C.byref(d), C.byref(h)))
+        return cls(h.value)
+
+    def desc(self) -> SceneDesc:
+        d = SceneDesc()
+        _check(library().orion_scene_get_desc(self._h, C.byref(d)))
+        return d
+
+    def arrays(self) -> dict:
+        d = self.desc()
+        T = d.num_prims
+
+        def arr(ptr, n, dt):
+            if not ptr or n == 0:
+                return np.zeros(0, dt)
+            return np.ctypeslib.as_array(C.cast(ptr, C.POINTER(np.ctypeslib.as_ctypes_type(dt))), (n,)).copy()
+
+        return {
+            "positions": arr(d.positions, 9 * T, np.float32).reshape(T, 9),
+            "normals": arr(d.normals, 9 * T, np.float32).reshape(T, 9),
+            "uvs": arr(d.uvs, 6 * T, np.float32).reshape(T, 6),
+            "material_of_prim": arr(d.material_of_prim, T, np.int32),
+            "light_of_prim": arr(d.light_of_prim, T, np.int32),
+            "materials": [Material.from_buffer_copy(C.cast(d.materials, C.POINTER(Material))[i])
+                          for i in range(d.num_materials)],
+            "lights": [Light.from_buffer_copy(C.cast(d.lights, C.POINTER(Light))[i]) for i in range(d.num_lights)],
+            "camera": d.camera, "spp": d.spp, "max_depth": d.max_depth,
+        }
+
+    def __del__(self):
+        if getattr(self, "_h", None) and self._h.value and _lib is not None:
+            _lib.orion_scene_free(self._h)
+            self._h = C.c_void_p()
+
+
+# ----------------------------------------------------------------- context
+
+
+class Context:
+    """One CUDA device: resident scenes, path-state pool, stream."""
+
+    def __init__(self, device: int = 0, memory_budget: int = 0):
+        opts = GpuOpts(device=device, memory_budget=memory_budget, sobol_path=None)
+        h = C.c_void_p()
+        _check(library().orion_gpu_create(C.byref(opts), C.byref(h)))
+        self._h = h
+
+    def close(self):
+        if self._h and self._h.value:
+            library().orion_gpu_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def upload(self, scene: HostScene) -> int:
+        sid = C.c_int32()
+        _check(library().orion_gpu_scene_upload(self._h, scene._h, C.byref(sid)))
+        return sid.value
+
+    def release(self, sid: int) -> None:
+        _check(library().orion_gpu_scene_release(self._h, sid))
+
+    def scene_bytes(self, sid: int) -> int:
+        b = C.c_int64()
+        _check(library().orion_gpu_scene_bytes(self._h, sid, C.byref(b)))
+        return b.value
+
+    def render(self, sid: int, width: int, height: int, spp: int = 0, max_depth: int = -1, rr_depth: int = 3,
+               first_pass: int = 0, wave_paths: int = 0, fp64: bool = False):
+        """Film sums: FP32 (H, W, 3) sums and (H, W) counts; or FP64 (sum, sumsq) if fp64."""
+        p = RenderParams(spp=spp, max_depth=max_depth, rr_depth=rr_depth, flags=1 if fp64 else 0,
+                         first_pass=first_pass, wave_paths=wave_paths)
+        if fp64:
+            s = np.zeros((height, width, 3), np.float64)
+            q = np.zeros((height, width, 3), np.float64)
+            _check(library().orion_gpu_render_fp64(self._h, sid, C.byref(p), _ptr(s), _ptr(q)))
+            return s, q
+        img = np.zeros((height, width, 3), np.float32)
+        cnt = np.zeros((height, width), np.uint32)
+        _check(library().orion_gpu_render(self._h, sid, C.byref(p), _ptr(img), _ptr(cnt)))
+        return img, cnt
+
+    def last_stats(self) -> dict:
+        s = RenderStats()
+        _check(library().orion_gpu_last_stats(self._h, C.byref(s)))
+        return {k: getattr(s, k) for k, _ in RenderStats._fields_}
+
+    def set_profiling(self, on: bool) -> None:
+        _check(library().orion_gpu_set_profiling(self._h, int(on)))
+
+    def stage_times(self) -> dict:
+        t = StageTimes()
+        _check(library().orion_gpu_stage_times(self._h, C.byref(t)))
+        return {name: {"ms": t.ms[i], "launches": t.launches[i]} for i, name in enumerate(STAGES)}
+
+    # component hooks -----------------------------------------------------
+    def sobol(self, index, dim) -> np.ndarray:
+        index = np.ascontiguousarray(index, np.uint64)
+        dim = np.ascontiguousarray(dim, np.uint32)
+        out = np.zeros(len(index), np.float32)
+        _check(library().orion_gpu_sobol(self._h, len(index), _ptr(index), _ptr(dim), _ptr(out)))
+        return out
+
+    def trace(self, sid: int, rays, any_hit: bool = False):
+        rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
+        n = len(rays)
+        t, u, v = (np.zeros(n, np.float32) for _ in range(3))
+        prim = np.zeros(n, np.int32)
+        _check(library().orion_gpu_trace(self._h, sid, n, _ptr(rays), int(any_hit), _ptr(t), _ptr(u), _ptr(v),
+                                         _ptr(prim)))
+        return t, u, v, prim
+
+    def camera_rays(self, sid: int, sample_index) -> np.ndarray:
+        idx = np.ascontiguousarray(sample_index, np.int64)
+        out = np.zeros((len(idx), 6), np.float32)
+        _check(library().orion_gpu_camera_rays(self._h, sid, len(idx), _ptr(idx), _ptr(out)))
+        return out
+
+    def bsdf_eval(self, mat: Material, frame, wo, wi, rnd, type_mask: int = BXDF_ALL) -> dict:
+        return _bsdf_call(lambda *a: library().orion_gpu_bsdf_eval(self._h, *a), mat, frame, wo, wi, rnd, type_mask)
+
+
+def _bsdf_call(fn, mat, frame, wo, wi, rnd, type_mask):
+    frame = np.ascontiguousarray(frame, np.float32).reshape(-1, 12)
+    n = len(frame)
+    wo = np.ascontiguousarray(wo, np.float32).reshape(n, 3)
+    wi = np.ascontiguousarray(wi, np.float32).reshape(n, 3)
+    rnd = np.ascontiguousarray(rnd, np.float32).reshape(n, 2)
+    out = {"f": np.zeros((n, 3), np.float32), "pdf": np.zeros(n, np.float32), "sf": np.zeros((n, 3), np.float32),
+           "swi": np.zeros((n, 3), np.float32), "spdf": np.zeros(n, np.float32), "stype": np.zeros(n, np.int32),
+           "nbxdf": np.zeros(n, np.int32)}
+    _check(fn(C.byref(mat), n, _ptr(frame), _ptr(wo), _ptr(wi), _ptr(rnd), type_mask, _ptr(out["f"]),
+              _ptr(out["pdf"]), _ptr(out["sf"]), _ptr(out["swi"]), _ptr(out["spdf"]), _ptr(out["stype"]),
+              _ptr(out["nbxdf"])))
+    return out
+
+
+# ------------------------------------------- reference-shaped host surface
+
+
+class RenderTarget:
+    """The film: per-pixel FP32 sums and sample counts (src/texture/rendertarget.h:15-33)."""
+
+    def __init__(self, width: int, height: int):
+        self.width, self.height = width, height
+        self.data = np.zeros((height, width, 3), np.float32)
+        self.counter = np.zeros((height, width), np.uint32)
+
+    def getWidth(self):
+        return self.width
+
+    def getHeight(self):
+        return self.height
+
+    def sample(self, x: int, y: int):
+        return self.data[y, x]
+
+    def getAveraged(self) -> np.ndarray:
+        with np.errstate(invalid="ignore", divide="ignore"):
+            return self.data / self.counter[..., None].astype(np.float32)
+
+
+class CameraHandle:
+    def __init__(self, film: RenderTarget):
+        self._film = film
+
+    def getFilm(self) -> RenderTarget:
+        return self._film
+
+
+@dataclass
+class SceneHandle:
+    ctx: Context
+    sid: int
+    host: HostScene
+
+
+class PathTracing:
+    """GPU stand-in for PathTracing (src/integrator/path.h:16-35): render() fills the camera's film."""
+
+    def __init__(self, camera: CameraHandle, max_depth: int, n_samples: int, rr_depth: int = 3):
+        self.camera, self.maxDepth, self.nSamples, self.rr_depth = camera, max_depth, n_samples, rr_depth
+        self.stats = None
+
+    def render(self, scene: SceneHandle) -> None:
+        film = self.camera.getFilm()
+        img, cnt = scene.ctx.render(scene.sid, film.width, film.height, spp=self.nSamples, max_depth=self.maxDepth,
+                                    rr_depth=self.rr_depth)
+        film.data, film.counter = img, cnt
+        self.stats = scene.ctx.last_stats()
+
+
+@dataclass
+class RenderOption:
+    scene: SceneHandle
+    camera: CameraHandle
+    integrator: PathTracing
+
+
+class Parser:
+    """Parser(path) -> getRenderOption(), with the scene already resident on `ctx`."""
+
+    def __init__(self, path: str, ctx: Context | None = None):
+        self.ctx = ctx or Context()
+        self.host = HostScene.load(path)
+        d = self.host.desc()
+        sid = self.ctx.upload(self.host)
+        film = RenderTarget(d.camera.width, d.camera.height)
+        cam = CameraHandle(film)
+        self._ro = RenderOption(SceneHandle(self.ctx, sid, self.host), cam, PathTracing(cam, d.max_depth, d.spp))
+
+    def getRenderOption(self) -> RenderOption:
+        return self._ro

@@ -1,0 +1,399 @@
+// Binned-SAH BVH build on the host, flattened for the GPU.
+//
+// Replaces the acceleration structure the reference builds inside Embree
+// (EmbreeKernel::build, src/core/kernel.cpp:63-110): one static triangle set
+// in primID order. Output layout:
+//   * 32-byte nodes (BvhNode); the children of an inner node are an
+//     adjacent pair, so one 64-byte fetch gives both child boxes;
+//   * optionally the first `top_bfs_nodes` slots hold the top levels in
+//     breadth-first order (so a kernel can stage them in shared memory),
+//     the rest of each subtree follows depth-first for locality;
+//   * Woop unit-triangle records (3 x float4 = 48 bytes) in leaf order, and
+//     the leaf-order -> primID map.
+// Subtrees below the top levels are built on worker threads.
+#include "bvh_build.h"
+
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstring>
+#include <deque>
+#include <future>
+#include <limits>
+#include <mutex>
+#include <thread>
+
+namespace orion_gb300 {
+
+void woop_record(const float* p, float out[12]) {
+  double v0[3] = {p[0], p[1], p[2]};
+  double a[3] = {(double)p[3] - p[0], (double)p[4] - p[1], (double)p[5] - p[2]};  // e1
+  double b[3] = {(double)p[6] - p[0], (double)p[7] - p[1], (double)p[8] - p[2]};  // e2
+  double c[3] = {a[1] * b[2] - a[2] * b[1], a[2] * b[0] - a[0] * b[2], a[0] * b[1] - a[1] * b[0]};  // n
+  auto cross = [](const double* x, const double* y, double* r) {
+    r[0] = x[1] * y[2] - x[2] * y[1];
+    r[1] = x[2] * y[0] - x[0] * y[2];
+    r[2] = x[0] * y[1] - x[1] * y[0];
+  };
+  double bc[3], ca[3], ab[3];
+  cross(b, c, bc);
+  cross(c, a, ca);
+  cross(a, b, ab);
+  double det = a[0] * bc[0] + a[1] * bc[1] + a[2] * bc[2];
+  if (!(std::fabs(det) > 0.0) || !std::isfinite(det)) {
+    std::memset(out, 0, 12 * sizeof(float));
+    return;
+  }
+  double r0[3], r1[3], r2[3];
+  for (int k = 0; k < 3; ++k) {
+    r0[k] = bc[k] / det;  // row giving u (along e1)
+    r1[k] = ca[k] / det;  // row giving v (along e2)
+    r2[k] = ab[k] / det;  // row giving the offset along n
+  }
+  auto dot = [](const double* x, const double* y) { return x[0] * y[0] + x[1] * y[1] + x[2] * y[2]; };
+  // w0: t = (w0.w - o.w0) / (d.w0); w1/w2: u, v = w.w + o.w + t d.w
+  out[0] = (float)r2[0];
+  out[1] = (float)r2[1];
+  out[2] = (float)r2[2];
+  out[3] = (float)dot(r2, v0);
+  out[4] = (float)r0[0];
+  out[5] = (float)r0[1];
+  out[6] = (float)r0[2];
+  out[7] = (float)-dot(r0, v0);
+  out[8] = (float)r1[0];
+  out[9] = (float)r1[1];
+  out[10] = (float)r1[2];
+  out[11] = (float)-dot(r1, v0);
+}
+
+namespace {
+
+struct TmpNode {
+  float lo[3], hi[3];
+  int32_t begin = 0, count = 0;  // leaf range in `order`
+  TmpNode* child[2] = {nullptr, nullptr};
+  int depth = 0;
+};
+
+struct Builder {
+  const BvhBuildOptions& opt;
+  const float* lo;  // per prim, 3
+  const float* hi;
+  const float* ce;
+  int32_t* order;
+  std::mutex arena_mu;
+  std::vector<std::unique_ptr<std::deque<TmpNode>>> arenas;
+  std::atomic<int> max_depth{0};
+  std::atomic<int> leaves{0};
+  int spawn_depth;
+
+  Builder(const BvhBuildOptions& o, const float* l, const float* h, const float* c, int32_t* ord, int threads)
+      : opt(o), lo(l), hi(h), ce(c), order(ord) {
+    spawn_depth = 0;
+    while ((1 << spawn_depth) < 4 * threads) ++spawn_depth;
+  }
+
+  std::deque<TmpNode>* new_arena() {
+    std::lock_guard<std::mutex> g(arena_mu);
+    arenas.emplace_back(new std::deque<TmpNode>());
+    return arenas.back().get();
+  }
+
+  static float half_area(const float* a, const float* b) {
+    float dx = b[0] - a[0], dy = b[1] - a[1], dz = b[2] - a[2];
+    return dx * dy + dy * dz + dz * dx;
+  }
+
+  void bounds(int begin, int end, float* bl, float* bh) const {
+    for (int k = 0; k < 3; ++k) {
+      bl[k] = std::numeric_limits<float>::infinity();
+      bh[k] = -std::numeric_limits<float>::infinity();
+    }
+    for (int i = begin; i < end; ++i) {
+      int p = order[i];
+      for (int k = 0; k < 3; ++k) {
+        bl[k] = std::min(bl[k], lo[3 * p + k]);
+        bh[k] = std::max(bh[k], hi[3 * p + k]);
+      }
+    }
+  }
+
+  TmpNode* build(int begin, int end, int depth, std::deque<TmpNode>* arena) {
+    arena->emplace_back();
+    TmpNode* n = &arena->back();
+    n->depth = depth;
+    bounds(begin, end, n->lo, n->hi);
+    int count = end - begin;
+    int cur = max_depth.load();
+    while (depth > cur && !max_depth.compare_exchange_weak(cur, depth)) {
+    }
+    if (count <= 1) return make_leaf(n, begin, count);
+    // Remaining depth a balanced split would need from here.
+    int need = 0;
+    while (((int64_t)opt.max_leaf << need) < count) ++need;
+    bool forced_median = depth + need + 1 >= opt.max_depth;
+    int mid = -1;
+    if (!forced_median) {
+      float cost_leaf = (float)count;
+      float split_cost;
+      mid = sah_split(begin, end, n, &split_cost);
+      if (mid < 0 || (count <= opt.max_leaf && cost_leaf <= split_cost)) {
+        if (count <= opt.max_leaf) return make_leaf(n, begin, count);
+        mid = -1;
+      }
+    }
+    if (mid < 0) mid = median_split(begin, end);
+    if (depth < spawn_depth && count > 4096) {
+      auto fut = std::async(std::launch::async, [=] {
+        std::deque<TmpNode>* a2 = new_arena();
+        return build(begin, mid, depth + 1, a2);
+      });
+      n->child[1] = build(mid, end, depth + 1, arena);
+      n->child[0] = fut.get();
+    } else {
+      n->child[0] = build(begin, mid, depth + 1, arena);
+      n->child[1] = build(mid, end, depth + 1, arena);
+    }
+    return n;
+  }
+
+  TmpNode* make_leaf(TmpNode* n, int begin, int count) {
+    n->begin = begin;
+    n->count = count;
+    leaves.fetch_add(1);
+    return n;
+  }
+
+  int median_split(int begin, int end) {
+    float cl[3], ch[3];
+    centroid_bounds(begin, end, cl, ch);
+    int axis = 0;
+    for (int k = 1; k < 3; ++k)
+      if (ch[k] - cl[k] > ch[axis] - cl[axis]) axis = k;
+    int mid = begin + (end - begin) / 2;
+    std::nth_element(order + begin, order + mid, order + end,
+                     [&](int a, int b) { return ce[3 * a + axis] < ce[3 * b + axis]; });
+    return mid;
+  }
+
+  void centroid_bounds(int begin, int end, float* cl, float* ch) const {
+    for (int k = 0; k < 3; ++k) {
+      cl[k] = std::numeric_limits<float>::infinity();
+      ch[k] = -std::numeric_limits<float>::infinity();
+    }
+    for (int i = begin; i < end; ++i) {
+      int p = order[i];
+      for (int k = 0; k < 3; ++k) {
+        cl[k] = std::min(cl[k], ce[3 * p + k]);
+        ch[k] = std::max(ch[k], ce[3 * p + k]);
+      }
+    }
+  }
+
+  // Returns the partition point of the best binned SAH split, or -1.
+  int sah_split(int begin, int end, const TmpNode* n, float* best_cost_out) {
+    const int B = std::max(2, std::min(opt.bins, 64));
+    float cl[3], ch[3];
+    centroid_bounds(begin, end, cl, ch);
+    float parent_area = half_area(n->lo, n->hi);
+    int best_axis = -1, best_bin = -1;
+    float best_cost = std::numeric_limits<float>::infinity();
+    int cnt[3][64];
+    float blo[3][64][3], bhi[3][64][3];
+    float scale[3];
+    for (int axis = 0; axis < 3; ++axis) {
+      float ext = ch[axis] - cl[axis];
+      scale[axis] = ext > 0.f ? B / ext : 0.f;
+      for (int b = 0; b < B; ++b) {
+        cnt[axis][b] = 0;
+        for (int k = 0; k < 3; ++k) {
+          blo[axis][b][k] = std::numeric_limits<float>::infinity();
+          bhi[axis][b][k] = -std::numeric_limits<float>::infinity();
+        }
+      }
+    }
+    for (int i = begin; i < end; ++i) {
+      int p = order[i];
+      for (int axis = 0; axis < 3; ++axis) {
+        if (scale[axis] == 0.f) continue;
+        int b = std::min(B - 1, (int)((ce[3 * p + axis] - cl[axis]) * scale[axis]));
+        cnt[axis][b]++;
+        for (int k = 0; k < 3; ++k) {
+          blo[axis][b][k] = std::min(blo[axis][b][k], lo[3 * p + k]);
+          bhi[axis][b][k] = std::max(bhi[axis][b][k], hi[3 * p + k]);
+        }
+      }
+    }
+    for (int axis = 0; axis < 3; ++axis) {
+      if (scale[axis] == 0.f) continue;
+      float rarea[64];
+      int rcnt[64];
+      float al[3], ah[3];
+      for (int k = 0; k < 3; ++k) {
+        al[k] = std::numeric_limits<float>::infinity();
+        ah[k] = -std::numeric_limits<float>::infinity();
+      }
+      int ac = 0;
+      for (int b = B - 1; b > 0; --b) {
+        ac += cnt[axis][b];
+        for (int k = 0; k < 3; ++k) {
+          al[k] = std::min(al[k], blo[axis][b][k]);
+          ah[k] = std::max(ah[k], bhi[axis][b][k]);
+        }
+        rcnt[b] = ac;
+        rarea[b] = ac ? half_area(al, ah) : 0.f;
+      }
+      for (int k = 0; k < 3; ++k) {
+        al[k] = std::numeric_limits<float>::infinity();
+        ah[k] = -std::numeric_limits<float>::infinity();
+      }
+      ac = 0;
+      for (int b = 0; b < B - 1; ++b) {
+        ac += cnt[axis][b];
+        for (int k = 0; k < 3; ++k) {
+          al[k] = std::min(al[k], blo[axis][b][k]);
+          ah[k] = std::max(ah[k], bhi[axis][b][k]);
+        }
+        if (ac == 0 || rcnt[b + 1] == 0) continue;
+        float cost = half_area(al, ah) * ac + rarea[b + 1] * rcnt[b + 1];
+        if (cost < best_cost) {
+          best_cost = cost;
+          best_axis = axis;
+          best_bin = b;
+        }
+      }
+    }
+    if (best_axis < 0) return -1;
+    *best_cost_out = parent_area > 0.f ? 1.f + best_cost / parent_area : 1.f;
+    float s = scale[best_axis], c0 = cl[best_axis];
+    int32_t* it = std::partition(order + begin, order + end, [&](int p) {
+      int b = std::min(B - 1, (int)((ce[3 * p + best_axis] - c0) * s));
+      return b <= best_bin;
+    });
+    int mid = (int)(it - order);
+    if (mid == begin || mid == end) return -1;
+    return mid;
+  }
+};
+
+void write_node(BvhNode* dst, const TmpNode* n) {
+  for (int k = 0; k < 3; ++k) {
+    float ext = n->hi[k] - n->lo[k];
+    float mag = std::max(std::fabs(n->lo[k]), std::fabs(n->hi[k]));
+    float pad = ext * 1e-6f + mag * 2e-7f;
+    dst->lo[k] = n->lo[k] - pad;
+    dst->hi[k] = n->hi[k] + pad;
+  }
+  dst->a = n->count > 0 ? n->begin : 0;
+  dst->b = n->count;
+}
+
+struct Flattener {
+  std::vector<BvhNode>& out;
+  explicit Flattener(std::vector<BvhNode>& o) : out(o) {}
+  int alloc_pair() {
+    int i = (int)out.size();
+    out.resize(out.size() + 2);
+    return i;
+  }
+  void dfs(const TmpNode* n, int idx) {
+    write_node(&out[idx], n);
+    if (n->count > 0) return;
+    int c = alloc_pair();
+    out[idx].a = c;
+    out[idx].b = 0;
+    dfs(n->child[0], c);
+    dfs(n->child[1], c + 1);
+  }
+  void run(const TmpNode* root, int top_bfs) {
+    out.resize(1);
+    if (top_bfs <= 1) {
+      dfs(root, 0);
+      return;
+    }
+    // Breadth-first for the first `top_bfs` slots, then depth-first below.
+    std::vector<std::pair<const TmpNode*, int>> level{{root, 0}}, frontier;
+    write_node(&out[0], root);
+    while (!level.empty()) {
+      std::vector<std::pair<const TmpNode*, int>> next;
+      for (auto& e : level) {
+        const TmpNode* n = e.first;
+        if (n->count > 0) continue;
+        if ((int)out.size() + 2 <= top_bfs) {
+          int c = alloc_pair();
+          out[e.second].a = c;
+          out[e.second].b = 0;
+          write_node(&out[c], n->child[0]);
+          write_node(&out[c + 1], n->child[1]);
+          next.push_back({n->child[0], c});
+          next.push_back({n->child[1], c + 1});
+        } else {
+          frontier.push_back(e);
+        }
+      }
+      level.swap(next);
+      if ((int)out.size() + 2 > top_bfs) {
+        for (auto& e : level)
+          if (e.first->count == 0) frontier.push_back(e);
+        break;
+      }
+    }
+    for (auto& e : frontier) dfs(e.first, e.second);
+  }
+};
+
+}  // namespace
+
+void build_bvh(const float* positions, int64_t num_tris, const BvhBuildOptions& opt, BvhBuild* out) {
+  const int T = (int)num_tris;
+  out->nodes.clear();
+  out->woop.assign(12 * (size_t)T, 0.f);
+  out->tri_prim.resize(T);
+  out->depth = 0;
+  out->leaves = 0;
+  if (T == 0) {
+    BvhNode empty;
+    std::memset(&empty, 0, sizeof(empty));
+    for (int k = 0; k < 3; ++k) {
+      empty.lo[k] = 1.f;
+      empty.hi[k] = -1.f;  // inverted box: nothing hits
+    }
+    out->nodes.push_back(empty);
+    return;
+  }
+  std::vector<float> lo(3 * (size_t)T), hi(3 * (size_t)T), ce(3 * (size_t)T);
+  for (int i = 0; i < T; ++i) {
+    const float* p = positions + 9 * (size_t)i;
+    for (int k = 0; k < 3; ++k) {
+      float a = std::min(std::min(p[k], p[3 + k]), p[6 + k]);
+      float b = std::max(std::max(p[k], p[3 + k]), p[6 + k]);
+      lo[3 * (size_t)i + k] = a;
+      hi[3 * (size_t)i + k] = b;
+      ce[3 * (size_t)i + k] = 0.5f * (a + b);
+    }
+  }
+  std::vector<int32_t> order(T);
+  for (int i = 0; i < T; ++i) order[i] = i;
+  int threads = opt.threads > 0 ? opt.threads : (int)std::max(1u, std::thread::hardware_concurrency());
+  Builder b(opt, lo.data(), hi.data(), ce.data(), order.data(), threads);
+  std::deque<TmpNode>* arena = b.new_arena();
+  TmpNode* root = b.build(0, T, 0, arena);
+  Flattener fl(out->nodes);
+  fl.run(root, opt.top_bfs_nodes);
+  out->depth = b.max_depth.load();
+  out->leaves = b.leaves.load();
+  for (int i = 0; i < T; ++i) {
+    out->tri_prim[i] = order[i];
+    woop_record(positions + 9 * (size_t)order[i], &out->woop[12 * (size_t)i]);
+  }
+  // SAH cost of the result (traversal + intersection, relative to the root).
+  double root_area = Builder::half_area(out->nodes[0].lo, out->nodes[0].hi);
+  double cost = 0.0;
+  for (const BvhNode& n : out->nodes) {
+    double a = Builder::half_area(n.lo, n.hi) / (root_area > 0 ? root_area : 1.0);
+    cost += n.b > 0 ? a * n.b : a;
+  }
+  out->sah_cost = cost;
+}
+
+}  // namespace orion_gb300

@@ -1,0 +1,598 @@
+// C ABI (include/orion_gpu.h): context, resident scenes, render driver.
+//
+// PathTracing::render (src/integrator/path.cpp:15-37) loops over spp passes
+// and pixels, one CPU thread per row. Here the sample indices
+// [k0*W*H, (k0+spp)*W*H) are cut into waves of up to `wave_paths` paths; each
+// wave is one fixed sequence of kernels on the context's stream (no host
+// synchronisation inside a render), and the film is accumulated per pixel in
+// sample order so its FP32 sums follow the reference's addition order.
+#include <cuda_runtime.h>
+#include <dlfcn.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/orion_gpu.h"
+#include "bvh_build.h"
+#include "kernels.h"
+#include "scene_host.h"
+#include "scene_prep.h"
+
+using namespace orion_gb300;
+
+struct orion_host_scene {
+  HostScene s;
+  // Host BVH and device records, built on the first upload and reused by
+  // later uploads of the same scene (resident-scene serving, re-uploads).
+  std::unique_ptr<BvhBuild> bvh;
+  std::unique_ptr<PreparedScene> prep;
+  std::mutex mu;
+};
+
+namespace {
+
+thread_local std::string g_error;
+
+int fail(int code, const std::string& msg) {
+  g_error = msg;
+  return code;
+}
+
+#define CUDA_TRY(call)                                                                             \
+  do {                                                                                             \
+    cudaError_t e_ = (call);                                                                       \
+    if (e_ != cudaSuccess) return fail(ORION_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  ~DevBuf() {
+    if (p) cudaFree(p);
+  }
+  int alloc(size_t n) {
+    if (p) cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+    if (n == 0) n = 16;
+    cudaError_t e = cudaMalloc(&p, n);
+    if (e != cudaSuccess) {
+      p = nullptr;
+      return fail(e == cudaErrorMemoryAllocation ? ORION_ERR_NOMEM : ORION_ERR_CUDA,
+                  std::string("cudaMalloc(") + std::to_string(n) + "): " + cudaGetErrorString(e));
+    }
+    bytes = n;
+    return ORION_OK;
+  }
+  template <class T>
+  T* as() const {
+    return static_cast<T*>(p);
+  }
+};
+
+struct DeviceScene {
+  DevBuf nodes, woop, tri_prim, prims, mats, lights, lfunc, lcdf;
+  SceneView view{};
+  int64_t bytes = 0;
+  int64_t num_prims = 0;
+  int width = 0, height = 0, spp = 1, max_depth = 5;
+  int bvh_depth = 0;
+};
+
+struct Wave {
+  int capacity = 0;
+  DevBuf block;  // all per-path arrays in one allocation
+  WaveView view{};
+};
+
+}  // namespace
+
+struct orion_gpu_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  int num_sms = 0;
+  DevBuf sobol;
+  std::map<int, std::unique_ptr<DeviceScene>> scenes;
+  int next_id = 1;
+  Wave wave;
+  DevBuf film_sum, film_count, film64, filmsq64;
+  int64_t film_pixels = 0;
+  int64_t budget = 0;
+  orion_render_stats last{};
+  LaunchConfig cfg{};
+  int default_wave = 1 << 22;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  bool profiling = false;
+  std::vector<cudaEvent_t> prof_events;
+  std::vector<int> prof_stage;
+  orion_stage_times stage_times{};
+  std::mutex mu;
+};
+
+extern "C" const char* orion_last_error(void) { return g_error.c_str(); }
+
+// ------------------------------------------------------------- scenes
+
+extern "C" int orion_scene_load_ori(const char* path, orion_host_scene** out) {
+  if (!path || !out) return fail(ORION_ERR_INVALID, "null argument");
+  std::unique_ptr<orion_host_scene> h(new orion_host_scene());
+  std::string err;
+  int rc = load_ori(path, &h->s, &err);
+  if (rc != ORION_OK) return fail(rc, err);
+  *out = h.release();
+  return ORION_OK;
+}
+
+extern "C" int orion_scene_from_desc(const orion_scene_desc* desc, orion_host_scene** out) {
+  if (!desc || !out) return fail(ORION_ERR_INVALID, "null argument");
+  std::unique_ptr<orion_host_scene> h(new orion_host_scene());
+  std::string err;
+  int rc = scene_from_desc(*desc, &h->s, &err);
+  if (rc != ORION_OK) return fail(rc, err);
+  *out = h.release();
+  return ORION_OK;
+}
+
+extern "C" int orion_scene_get_desc(const orion_host_scene* scene, orion_scene_desc* out) {
+  if (!scene || !out) return fail(ORION_ERR_INVALID, "null argument");
+  scene->s.desc(out);
+  return ORION_OK;
+}
+
+extern "C" void orion_scene_free(orion_host_scene* scene) { delete scene; }
+
+// ------------------------------------------------------------ context
+
+static std::string default_sobol_path() {
+  Dl_info info;
+  if (dladdr(reinterpret_cast<void*>(&default_sobol_path), &info) && info.dli_fname) {
+    std::string p(info.dli_fname);
+    size_t slash = p.find_last_of('/');
+    std::string dir = slash == std::string::npos ? std::string(".") : p.substr(0, slash);
+    return dir + "/data/sobol_matrices.bin";
+  }
+  return "data/sobol_matrices.bin";
+}
+
+static int ensure_film(orion_gpu_ctx* c, int64_t pixels, bool fp64) {
+  if (pixels > c->film_pixels) {
+    int rc;
+    if ((rc = c->film_sum.alloc(pixels * 3 * sizeof(float))) != ORION_OK) return rc;
+    if ((rc = c->film_count.alloc(pixels * sizeof(uint32_t))) != ORION_OK) return rc;
+    c->film64.alloc(0);
+    c->filmsq64.alloc(0);
+    c->film_pixels = pixels;
+  }
+  if (fp64 && c->film64.bytes < (size_t)pixels * 3 * sizeof(double)) {
+    int rc;
+    if ((rc = c->film64.alloc(pixels * 3 * sizeof(double))) != ORION_OK) return rc;
+    if ((rc = c->filmsq64.alloc(pixels * 3 * sizeof(double))) != ORION_OK) return rc;
+  }
+  return ORION_OK;
+}
+
+static int ensure_wave(orion_gpu_ctx* c, int capacity) {
+  if (c->wave.capacity >= capacity) return ORION_OK;
+  const size_t n = (size_t)capacity;
+  const size_t f4 = n * sizeof(float4), i4 = (n * sizeof(int) + 255) & ~(size_t)255;
+  const size_t bytes = 15 * f4 + 7 * i4 + 256 + 4096;
+  int rc = c->wave.block.alloc(bytes);
+  if (rc != ORION_OK) {
+    c->wave.capacity = 0;
+    return rc;
+  }
+  char* p = c->wave.block.as<char>();
+  WaveView& w = c->wave.view;
+  float4** f4s[] = {&w.ray_o, &w.ray_d, &w.beta,  &w.L,    &w.hit,   &w.nee_p, &w.nee_beta, &w.nee_ld,
+                    &w.nee_f, &w.sh_o,  &w.sh_d,  &w.mis_o, &w.mis_d, &w.mis_hit};
+  for (float4** q : f4s) {
+    *q = reinterpret_cast<float4*>(p);
+    p += f4;
+  }
+  int** i4s[] = {&w.dim, &w.occluded, &w.q_ext[0], &w.q_ext[1], &w.q_nee, &w.q_sh, &w.q_mis};
+  for (int** q : i4s) {
+    *q = reinterpret_cast<int*>(p);
+    p += i4;
+  }
+  w.counters = reinterpret_cast<int*>(p);
+  p += 128;
+  w.ray_stats = reinterpret_cast<unsigned long long*>(p);
+  p += 64;
+  w.error_word = reinterpret_cast<int*>(p);
+  w.capacity = capacity;
+  c->wave.capacity = capacity;
+  return ORION_OK;
+}
+
+extern "C" int orion_gpu_create(const orion_gpu_opts* opts, orion_gpu_ctx** out) {
+  if (!out) return fail(ORION_ERR_INVALID, "null argument");
+  std::unique_ptr<orion_gpu_ctx> c(new orion_gpu_ctx());
+  c->device = opts ? opts->device : 0;
+  int ndev = 0;
+  CUDA_TRY(cudaGetDeviceCount(&ndev));
+  if (c->device < 0 || c->device >= ndev) return fail(ORION_ERR_INVALID, "no such CUDA device");
+  CUDA_TRY(cudaSetDevice(c->device));
+  cudaDeviceProp prop;
+  CUDA_TRY(cudaGetDeviceProperties(&prop, c->device));
+  c->num_sms = prop.multiProcessorCount;
+  CUDA_TRY(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  CUDA_TRY(cudaEventCreate(&c->ev0));
+  CUDA_TRY(cudaEventCreate(&c->ev1));
+  size_t free_b = 0, total_b = 0;
+  CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
+  c->budget = (opts && opts->memory_budget > 0) ? opts->memory_budget : (int64_t)(free_b * 0.9);
+  std::string path = (opts && opts->sobol_path) ? std::string(opts->sobol_path) : default_sobol_path();
+  FILE* f = std::fopen(path.c_str(), "rb");
+  if (!f) return fail(ORION_ERR_IO, "cannot open Sobol matrices " + path);
+  std::vector<uint32_t> m((size_t)1024 * 52);
+  size_t got = std::fread(m.data(), sizeof(uint32_t), m.size(), f);
+  std::fclose(f);
+  if (got != m.size()) return fail(ORION_ERR_IO, "short Sobol matrix file " + path);
+  int rc = c->sobol.alloc(m.size() * sizeof(uint32_t));
+  if (rc != ORION_OK) return rc;
+  CUDA_TRY(cudaMemcpy(c->sobol.p, m.data(), m.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
+  c->cfg.num_sms = c->num_sms;
+  c->cfg.trace_block = 128;
+  c->cfg.shade_block = 128;
+  c->cfg.blocks_per_sm = 8;
+  c->cfg.smem_stack = 16;
+  *out = c.release();
+  return ORION_OK;
+}
+
+extern "C" int orion_gpu_destroy(orion_gpu_ctx* ctx) {
+  if (!ctx) return ORION_OK;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  ctx->scenes.clear();
+  ctx->wave.block.alloc(0);
+  for (cudaEvent_t e : ctx->prof_events) cudaEventDestroy(e);
+  if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+  if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return ORION_OK;
+}
+
+template <class T>
+static int upload(DevBuf& b, const std::vector<T>& v, cudaStream_t s, int64_t* bytes) {
+  int rc = b.alloc(v.size() * sizeof(T));
+  if (rc != ORION_OK) return rc;
+  if (!v.empty()) CUDA_TRY(cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
+  *bytes += (int64_t)b.bytes;
+  return ORION_OK;
+}
+
+extern "C" int orion_gpu_scene_upload(orion_gpu_ctx* ctx, const orion_host_scene* scene, orion_scene_id* out) {
+  if (!ctx || !scene || !out) return fail(ORION_ERR_INVALID, "null argument");
+  std::lock_guard<std::mutex> g(ctx->mu);
+  CUDA_TRY(cudaSetDevice(ctx->device));
+  const HostScene& hs = scene->s;
+  orion_host_scene* hsm = const_cast<orion_host_scene*>(scene);
+  {
+    std::lock_guard<std::mutex> sg(hsm->mu);
+    if (!hsm->prep) {
+      std::unique_ptr<PreparedScene> ps(new PreparedScene());
+      std::string err;
+      if (!prepare_scene(hs, ps.get(), &err)) return fail(ORION_ERR_INVALID, err);
+      if (ps->env_idx.size() > 8) return fail(ORION_ERR_UNSUPPORTED, "more than 8 environment lights");
+      hsm->prep = std::move(ps);
+    }
+    if (!hsm->bvh) {
+      std::unique_ptr<BvhBuild> b(new BvhBuild());
+      BvhBuildOptions bo;
+      build_bvh(hs.positions.data(), hs.num_prims(), bo, b.get());
+      hsm->bvh = std::move(b);
+    }
+  }
+  const PreparedScene& ps = *hsm->prep;
+  const BvhBuild& bvh = *hsm->bvh;
+  std::unique_ptr<DeviceScene> d(new DeviceScene());
+  int64_t bytes = 0;
+  int rc;
+  if ((rc = upload(d->nodes, bvh.nodes, ctx->stream, &bytes)) != ORION_OK) return rc;
+  if ((rc = upload(d->woop, bvh.woop, ctx->stream, &bytes)) != ORION_OK) return rc;
+  if ((rc = upload(d->tri_prim, bvh.tri_prim, ctx->stream, &bytes)) != ORION_OK) return rc;
+  if ((rc = upload(d->prims, ps.prims, ctx->stream, &bytes)) != ORION_OK) return rc;
+  if ((rc = upload(d->mats, ps.mats, ctx->stream, &bytes)) != ORION_OK) return rc;
+  if ((rc = upload(d->lights, ps.lights, ctx->stream, &bytes)) != ORION_OK) return rc;
+  if ((rc = upload(d->lfunc, ps.light_func, ctx->stream, &bytes)) != ORION_OK) return rc;
+  if ((rc = upload(d->lcdf, ps.light_cdf, ctx->stream, &bytes)) != ORION_OK) return rc;
+  CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  SceneView& v = d->view;
+  v.nodes = d->nodes.as<float4>();
+  v.woop = d->woop.as<float4>();
+  v.tri_prim = d->tri_prim.as<int>();
+  v.prims = d->prims.as<PrimShade>();
+  v.mats = d->mats.as<DevMaterial>();
+  v.lights = d->lights.as<DevLight>();
+  v.light_func = d->lfunc.as<float>();
+  v.light_cdf = d->lcdf.as<float>();
+  v.light_func_int = ps.light_func_int;
+  v.num_lights = (int)ps.lights.size();
+  v.num_env = (int)ps.env_idx.size();
+  for (int i = 0; i < v.num_env; ++i) v.env_idx[i] = ps.env_idx[i];
+  v.world_radius = ps.world_radius;
+  v.cam = ps.cam;
+  d->bytes = bytes;
+  d->num_prims = hs.num_prims();
+  d->width = hs.camera.width;
+  d->height = hs.camera.height;
+  d->spp = hs.spp;
+  d->max_depth = hs.max_depth;
+  d->bvh_depth = bvh.depth;
+  int id = ctx->next_id++;
+  ctx->scenes[id] = std::move(d);
+  *out = id;
+  return ORION_OK;
+}
+
+extern "C" int orion_gpu_scene_release(orion_gpu_ctx* ctx, orion_scene_id id) {
+  if (!ctx) return fail(ORION_ERR_INVALID, "null context");
+  std::lock_guard<std::mutex> g(ctx->mu);
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  if (!ctx->scenes.erase(id)) return fail(ORION_ERR_INVALID, "unknown scene id");
+  return ORION_OK;
+}
+
+extern "C" int orion_gpu_scene_bytes(orion_gpu_ctx* ctx, orion_scene_id id, int64_t* bytes) {
+  if (!ctx || !bytes) return fail(ORION_ERR_INVALID, "null argument");
+  auto it = ctx->scenes.find(id);
+  if (it == ctx->scenes.end()) return fail(ORION_ERR_INVALID, "unknown scene id");
+  *bytes = it->second->bytes;
+  return ORION_OK;
+}
+
+// ------------------------------------------------------------- render
+
+static int render_impl(orion_gpu_ctx* ctx, orion_scene_id id, const orion_render_params* params, float* film_rgb,
+                       uint32_t* film_count, double* sum64, double* sumsq64) {
+  if (!ctx) return fail(ORION_ERR_INVALID, "null context");
+  std::lock_guard<std::mutex> g(ctx->mu);
+  CUDA_TRY(cudaSetDevice(ctx->device));
+  auto it = ctx->scenes.find(id);
+  if (it == ctx->scenes.end()) return fail(ORION_ERR_INVALID, "unknown scene id");
+  DeviceScene& d = *it->second;
+  orion_render_params p{};
+  if (params) p = *params;
+  const int spp = p.spp > 0 ? p.spp : d.spp;
+  const int max_depth = p.max_depth >= 0 && params ? p.max_depth : d.max_depth;
+  const int rr_depth = params ? p.rr_depth : 3;
+  if (max_depth < 0 || max_depth > 120) return fail(ORION_ERR_INVALID, "max_depth out of range");
+  const int64_t wh = (int64_t)d.width * d.height;
+  const int64_t total = wh * spp;
+  const int64_t first = p.first_pass * wh;
+  // Dimensions used: 5 + 2 (lens) + per bounce up to 8; the table has 1024.
+  if (9 + 8 * (int64_t)(max_depth + 1) > 1024) return fail(ORION_ERR_INVALID, "max_depth exceeds Sobol dimensions");
+  int64_t wave = p.wave_paths > 0 ? p.wave_paths : ctx->default_wave;
+  wave = std::min<int64_t>(wave, std::max<int64_t>(total, 1));
+  int rc = ensure_wave(ctx, (int)wave);
+  if (rc != ORION_OK) return rc;
+  const bool fp64 = sum64 != nullptr;
+  if ((rc = ensure_film(ctx, wh, fp64)) != ORION_OK) return rc;
+  cudaStream_t s = ctx->stream;
+  CUDA_TRY(cudaMemsetAsync(ctx->film_sum.p, 0, wh * 3 * sizeof(float), s));
+  CUDA_TRY(cudaMemsetAsync(ctx->film_count.p, 0, wh * sizeof(uint32_t), s));
+  if (fp64) {
+    CUDA_TRY(cudaMemsetAsync(ctx->film64.p, 0, wh * 3 * sizeof(double), s));
+    CUDA_TRY(cudaMemsetAsync(ctx->filmsq64.p, 0, wh * 3 * sizeof(double), s));
+  }
+  CUDA_TRY(cudaMemsetAsync(ctx->wave.view.ray_stats, 0, 3 * sizeof(unsigned long long), s));
+  CUDA_TRY(cudaMemsetAsync(ctx->wave.view.error_word, 0, sizeof(int), s));
+  FilmView film{ctx->film_sum.as<float>(), ctx->film_count.as<uint32_t>(), fp64 ? ctx->film64.as<double>() : nullptr,
+                fp64 ? ctx->filmsq64.as<double>() : nullptr};
+  int launches = 0;
+  StageTimer timer{nullptr, nullptr, 0, 0};
+  if (ctx->profiling) {
+    const int64_t waves = (total + wave - 1) / wave;
+    const int need = (int)std::min<int64_t>(waves * (6 * (max_depth + 1) + 4), 200000);
+    while ((int)ctx->prof_events.size() < 2 * need) {
+      cudaEvent_t e;
+      CUDA_TRY(cudaEventCreate(&e));
+      ctx->prof_events.push_back(e);
+    }
+    ctx->prof_stage.resize(need);
+    timer = StageTimer{ctx->prof_events.data(), ctx->prof_stage.data(), need, 0};
+  }
+  CUDA_TRY(cudaEventRecord(ctx->ev0, s));
+  for (int64_t off = 0; off < total; off += wave) {
+    WaveArgs a;
+    a.sobol = ctx->sobol.as<uint32_t>();
+    a.base_index = first + off;
+    a.n_paths = (int)std::min<int64_t>(wave, total - off);
+    a.width = d.width;
+    a.height = d.height;
+    a.max_depth = max_depth;
+    a.rr_depth = rr_depth;
+    launch_wave(d.view, ctx->wave.view, a, film, ctx->cfg, s, &launches, ctx->profiling ? &timer : nullptr);
+  }
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaEventRecord(ctx->ev1, s));
+  if (film_rgb)
+    CUDA_TRY(cudaMemcpyAsync(film_rgb, ctx->film_sum.p, wh * 3 * sizeof(float), cudaMemcpyDeviceToHost, s));
+  if (film_count)
+    CUDA_TRY(cudaMemcpyAsync(film_count, ctx->film_count.p, wh * sizeof(uint32_t), cudaMemcpyDeviceToHost, s));
+  if (fp64) {
+    CUDA_TRY(cudaMemcpyAsync(sum64, ctx->film64.p, wh * 3 * sizeof(double), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaMemcpyAsync(sumsq64, ctx->filmsq64.p, wh * 3 * sizeof(double), cudaMemcpyDeviceToHost, s));
+  }
+  unsigned long long stats[3] = {0, 0, 0};
+  int err_word = 0;
+  CUDA_TRY(cudaMemcpyAsync(stats, ctx->wave.view.ray_stats, sizeof(stats), cudaMemcpyDeviceToHost, s));
+  CUDA_TRY(cudaMemcpyAsync(&err_word, ctx->wave.view.error_word, sizeof(int), cudaMemcpyDeviceToHost, s));
+  CUDA_TRY(cudaStreamSynchronize(s));
+  float ms = 0.f;
+  CUDA_TRY(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+  ctx->last.paths = total;
+  ctx->last.ext_rays = (int64_t)stats[0];
+  ctx->last.shadow_rays = (int64_t)stats[1];
+  ctx->last.mis_rays = (int64_t)stats[2];
+  ctx->last.rays = (int64_t)(stats[0] + stats[1] + stats[2]);
+  ctx->last.kernel_launches = launches;
+  ctx->last.device_ms = ms;
+  std::memset(&ctx->stage_times, 0, sizeof(ctx->stage_times));
+  for (int i = 0; i < std::min(timer.used, timer.capacity); ++i) {
+    float e = 0.f;
+    CUDA_TRY(cudaEventElapsedTime(&e, timer.events[2 * i], timer.events[2 * i + 1]));
+    ctx->stage_times.ms[timer.stage[i]] += e;
+    ctx->stage_times.launches[timer.stage[i]] += 1;
+  }
+  if (err_word) return fail(ORION_ERR_DEVICE, "kernel error word " + std::to_string(err_word));
+  return ORION_OK;
+}
+
+extern "C" int orion_gpu_render(orion_gpu_ctx* ctx, orion_scene_id id, const orion_render_params* params,
+                                float* film_rgb_sum, uint32_t* film_count) {
+  return render_impl(ctx, id, params, film_rgb_sum, film_count, nullptr, nullptr);
+}
+
+extern "C" int orion_gpu_render_fp64(orion_gpu_ctx* ctx, orion_scene_id id, const orion_render_params* params,
+                                     double* sum, double* sumsq) {
+  if (!sum || !sumsq) return fail(ORION_ERR_INVALID, "null output");
+  return render_impl(ctx, id, params, nullptr, nullptr, sum, sumsq);
+}
+
+extern "C" int orion_gpu_last_stats(orion_gpu_ctx* ctx, orion_render_stats* out) {
+  if (!ctx || !out) return fail(ORION_ERR_INVALID, "null argument");
+  *out = ctx->last;
+  return ORION_OK;
+}
+
+extern "C" int orion_gpu_set_profiling(orion_gpu_ctx* ctx, int32_t enable) {
+  if (!ctx) return fail(ORION_ERR_INVALID, "null context");
+  std::lock_guard<std::mutex> g(ctx->mu);
+  ctx->profiling = enable != 0;
+  return ORION_OK;
+}
+
+extern "C" int orion_gpu_stage_times(orion_gpu_ctx* ctx, orion_stage_times* out) {
+  if (!ctx || !out) return fail(ORION_ERR_INVALID, "null argument");
+  *out = ctx->stage_times;
+  return ORION_OK;
+}
+
+// --------------------------------------------------------- test hooks
+
+namespace {
+template <class T>
+int to_device(DevBuf& b, const T* host, size_t n, cudaStream_t s) {
+  int rc = b.alloc(n * sizeof(T));
+  if (rc != ORION_OK) return rc;
+  if (n) CUDA_TRY(cudaMemcpyAsync(b.p, host, n * sizeof(T), cudaMemcpyHostToDevice, s));
+  return ORION_OK;
+}
+template <class T>
+int to_host(T* host, const DevBuf& b, size_t n, cudaStream_t s) {
+  if (n) CUDA_TRY(cudaMemcpyAsync(host, b.p, n * sizeof(T), cudaMemcpyDeviceToHost, s));
+  return ORION_OK;
+}
+}  // namespace
+
+#define RC(x)                      \
+  do {                             \
+    int rc_ = (x);                 \
+    if (rc_ != ORION_OK) return rc_; \
+  } while (0)
+
+extern "C" int orion_gpu_sobol(orion_gpu_ctx* ctx, int64_t n, const uint64_t* index, const uint32_t* dim, float* out) {
+  if (!ctx || n < 0 || (n > 0 && (!index || !dim || !out))) return fail(ORION_ERR_INVALID, "bad argument");
+  for (int64_t i = 0; i < n; ++i)
+    if (dim[i] >= 1024) return fail(ORION_ERR_INVALID, "Sobol dimension >= 1024");
+  std::lock_guard<std::mutex> g(ctx->mu);
+  CUDA_TRY(cudaSetDevice(ctx->device));
+  DevBuf di, dd, dout;
+  RC(to_device(di, index, n, ctx->stream));
+  RC(to_device(dd, dim, n, ctx->stream));
+  RC(dout.alloc(n * sizeof(float)));
+  launch_sobol(ctx->sobol.as<uint32_t>(), n, di.as<uint64_t>(), dd.as<uint32_t>(), dout.as<float>(), ctx->stream);
+  CUDA_TRY(cudaGetLastError());
+  RC(to_host(out, dout, n, ctx->stream));
+  CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return ORION_OK;
+}
+
+extern "C" int orion_gpu_trace(orion_gpu_ctx* ctx, orion_scene_id id, int64_t n, const float* rays, int32_t any_hit,
+                               float* t, float* u, float* v, int32_t* prim) {
+  if (!ctx || n < 0 || (n > 0 && (!rays || !t || !u || !v || !prim))) return fail(ORION_ERR_INVALID, "bad argument");
+  std::lock_guard<std::mutex> g(ctx->mu);
+  CUDA_TRY(cudaSetDevice(ctx->device));
+  auto it = ctx->scenes.find(id);
+  if (it == ctx->scenes.end()) return fail(ORION_ERR_INVALID, "unknown scene id");
+  DevBuf dr, dt, du, dv, dp;
+  RC(to_device(dr, rays, 8 * (size_t)n, ctx->stream));
+  RC(dt.alloc(n * 4));
+  RC(du.alloc(n * 4));
+  RC(dv.alloc(n * 4));
+  RC(dp.alloc(n * 4));
+  launch_trace(it->second->view, n, dr.as<float>(), any_hit, dt.as<float>(), du.as<float>(), dv.as<float>(),
+               dp.as<int>(), ctx->cfg, ctx->stream);
+  CUDA_TRY(cudaGetLastError());
+  RC(to_host(t, dt, n, ctx->stream));
+  RC(to_host(u, du, n, ctx->stream));
+  RC(to_host(v, dv, n, ctx->stream));
+  RC(to_host(prim, dp, n, ctx->stream));
+  CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return ORION_OK;
+}
+
+extern "C" int orion_gpu_camera_rays(orion_gpu_ctx* ctx, orion_scene_id id, int64_t n, const int64_t* sample_index,
+                                     float* rays) {
+  if (!ctx || n < 0 || (n > 0 && (!sample_index || !rays))) return fail(ORION_ERR_INVALID, "bad argument");
+  std::lock_guard<std::mutex> g(ctx->mu);
+  CUDA_TRY(cudaSetDevice(ctx->device));
+  auto it = ctx->scenes.find(id);
+  if (it == ctx->scenes.end()) return fail(ORION_ERR_INVALID, "unknown scene id");
+  for (int64_t i = 0; i < n; ++i)
+    if (sample_index[i] < 0) return fail(ORION_ERR_INVALID, "negative sample index");
+  DevBuf di, dr;
+  RC(to_device(di, sample_index, n, ctx->stream));
+  RC(dr.alloc(6 * n * sizeof(float)));
+  launch_camera_rays(it->second->view, ctx->sobol.as<uint32_t>(), n, di.as<int64_t>(), dr.as<float>(), ctx->stream);
+  CUDA_TRY(cudaGetLastError());
+  RC(to_host(rays, dr, 6 * (size_t)n, ctx->stream));
+  CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return ORION_OK;
+}
+
+extern "C" int orion_gpu_bsdf_eval(orion_gpu_ctx* ctx, const orion_material* mat, int64_t n, const float* frame,
+                                   const float* wo, const float* wi, const float* rnd, int32_t type, float* f,
+                                   float* pdf, float* sf, float* swi, float* spdf, int32_t* stype, int32_t* nbxdf) {
+  if (!ctx || !mat || n < 0) return fail(ORION_ERR_INVALID, "bad argument");
+  if (mat->type < ORION_MAT_MATTE || mat->type > ORION_MAT_UBER) return fail(ORION_ERR_INVALID, "bad material type");
+  std::lock_guard<std::mutex> g(ctx->mu);
+  CUDA_TRY(cudaSetDevice(ctx->device));
+  DevMaterial dm = prepare_material(*mat);
+  DevBuf dmat, dfr, dwo, dwi, drn, df, dpdf, dsf, dswi, dspdf, dst, dnb;
+  RC(to_device(dmat, &dm, 1, ctx->stream));
+  RC(to_device(dfr, frame, 12 * (size_t)n, ctx->stream));
+  RC(to_device(dwo, wo, 3 * (size_t)n, ctx->stream));
+  RC(to_device(dwi, wi, 3 * (size_t)n, ctx->stream));
+  RC(to_device(drn, rnd, 2 * (size_t)n, ctx->stream));
+  RC(df.alloc(12 * n));
+  RC(dpdf.alloc(4 * n));
+  RC(dsf.alloc(12 * n));
+  RC(dswi.alloc(12 * n));
+  RC(dspdf.alloc(4 * n));
+  RC(dst.alloc(4 * n));
+  RC(dnb.alloc(4 * n));
+  launch_bsdf_eval(dmat.as<DevMaterial>(), n, dfr.as<float>(), dwo.as<float>(), dwi.as<float>(), drn.as<float>(), type,
+                   df.as<float>(), dpdf.as<float>(), dsf.as<float>(), dswi.as<float>(), dspdf.as<float>(),
+                   dst.as<int>(), dnb.as<int>(), ctx->stream);
+  CUDA_TRY(cudaGetLastError());
+  RC(to_host(f, df, 3 * (size_t)n, ctx->stream));
+  RC(to_host(pdf, dpdf, (size_t)n, ctx->stream));
+  RC(to_host(sf, dsf, 3 * (size_t)n, ctx->stream));
+  RC(to_host(swi, dswi, 3 * (size_t)n, ctx->stream));
+  RC(to_host(spdf, dspdf, (size_t)n, ctx->stream));
+  RC(to_host(stype, dst, (size_t)n, ctx->stream));
+  RC(to_host(nbxdf, dnb, (size_t)n, ctx->stream));
+  CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return ORION_OK;
+}

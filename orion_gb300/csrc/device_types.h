@@ -1,0 +1,119 @@
+// Records shared by the host scene builder and the CUDA kernels.
+//
+// Everything a kernel reads about a scene is flattened into these plain
+// structs at upload time: materials become fixed lobe lists (the BxDF list
+// that Material::getBSDF builds per hit in the reference,
+// src/material/*.cpp), lights become typed records with their derived
+// constants, and the camera becomes its matrix and projection constants.
+#pragma once
+#include <stdint.h>
+
+#ifdef __CUDACC__
+#define ORION_HD __host__ __device__
+#else
+#define ORION_HD
+#endif
+
+namespace orion_gb300 {
+
+// BxDFType bits (src/core/bsdf.h:16-24).
+enum : int32_t {
+  BXDF_REFLECTION = 1,
+  BXDF_TRANSMISSION = 2,
+  BXDF_DIFFUSE = 4,
+  BXDF_GLOSSY = 8,
+  BXDF_SPECULAR = 16,
+  BXDF_ALL = 31,
+};
+
+enum LobeKind : int32_t {
+  LOBE_LAMBERT_R = 0,      // src/bsdf/lambert.cpp:5-8
+  LOBE_OREN_NAYAR = 1,     // src/bsdf/orennayar.cpp:5-37
+  LOBE_MICROFACET_R = 2,   // src/bsdf/microfacet.cpp:42-74
+  LOBE_MICROFACET_T = 3,   // src/bsdf/microfacet.cpp:76-120
+  LOBE_SPECULAR_R = 4,     // src/bsdf/specular.cpp:20-25
+  LOBE_SPECULAR_T = 5,     // src/bsdf/specular.cpp:4-18
+  LOBE_FRESNEL_SPECULAR = 6,  // src/bsdf/specular.cpp:28-54
+};
+
+enum FresnelKind : int32_t {
+  FRESNEL_NOOP = 0,        // src/core/bsdf.h:96-99
+  FRESNEL_CONDUCTOR = 1,   // src/core/bsdf.cpp:124-147
+  FRESNEL_DIELECTRIC = 2,  // src/core/bsdf.cpp:149-170
+};
+
+enum DistKind : int32_t { DIST_GGX = 0, DIST_BECKMANN = 1 };
+
+struct DevLobe {       // 64 bytes
+  int32_t kind;        // LobeKind
+  int32_t type;        // BxDFType bits of this lobe
+  int32_t fresnel;     // FresnelKind (reflection lobes)
+  int32_t dist;        // DistKind (microfacet lobes)
+  float c[3];          // R or T
+  float alpha;         // microfacet alpha (roughnessToAlpha applied)
+  float c2[3];         // FresnelSpecular: T
+  float etaA;          // etaA / fresnel etaI
+  float etaB;          // etaB / fresnel etaT (scalar dielectric)
+  float on_a, on_b;    // Oren-Nayar A, B
+  float fr_eta[3];     // conductor etaT
+  float fr_k[3];       // conductor k
+  float pad;
+};
+
+constexpr int kMaxLobes = 5;
+
+struct DevMaterial {   // 16 + 5 * 64 = 336 bytes
+  int32_t num_lobes;
+  int32_t num_nonspecular;  // numBxDF(BxDF_ALL & ~BxDF_SPECULAR)
+  int32_t pad[2];
+  DevLobe lobes[kMaxLobes];
+};
+
+enum DevLightKind : int32_t { DL_AREA = 0, DL_POINT = 1, DL_SPOT = 2, DL_DISTANT = 3, DL_ENV = 4 };
+
+struct DevLight {      // 128 bytes
+  int32_t kind;
+  int32_t prim;        // area: emissive primitive
+  float area;          // area: triangle area (src/core/triangle.cpp:77-83);
+                       // env: intensity of the constant map (0 disables sampling)
+  float pad0;
+  float L[3];          // Le / I / L
+  float pad1;
+  float p[3];          // point/spot position; distant: direction
+  float pad2;
+  float m[9];          // spot: world->light 3x3; env: light->world 3x3
+  float minv[9];       // env: world->light 3x3
+  float cos_total, cos_falloff;
+  float pad3[2];
+};
+
+struct DevCamera {
+  float c2w[16];       // camera-to-world 4x4 row-major
+  float tan_half_fov;
+  float aspect;
+  float lens_radius;
+  float focal_distance;
+  int32_t width, height;
+  int32_t pad[2];
+};
+
+// Per-primitive shading record, primID order: 96 bytes = 6 x float4.
+struct PrimShade {
+  float p[9];          // p0, p1, p2
+  float n[9];          // n0, n1, n2
+  int32_t material;
+  int32_t light;       // area light index or -1
+  int32_t pad[4];
+};
+
+// One BVH node: 32 bytes = 2 x float4. Children of an inner node are the
+// adjacent pair (a, a + 1); a leaf holds triangles [a, a + b) of the
+// leaf-ordered triangle array.
+struct BvhNode {
+  float lo[3];
+  int32_t a;
+  float hi[3];
+  int32_t b;           // 0 = inner node, > 0 = leaf triangle count
+};
+
+}  // namespace orion_gb300

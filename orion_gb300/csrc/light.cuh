@@ -1,0 +1,155 @@
+// Device light sampling (src/core/light.h, src/light/*.cpp) and the
+// light-selection distribution (Distribution1D::sampleDiscrete,
+// src/sampler/sampling.h:71-125 with findInterval, src/core/geometry.h:877-889).
+#pragma once
+#include "device_types.h"
+#include "dmath.cuh"
+
+namespace orion_gb300 {
+
+struct LightDistrib {
+  const float* func;  // n light powers (intensity)
+  const float* cdf;   // n + 1
+  float func_int;
+  int n;
+};
+
+__device__ __forceinline__ int find_interval(const float* cdf, int size, float u) {
+  int first = 0, len = size;
+  while (len > 0) {
+    int half = len >> 1, middle = first + half;
+    if (__ldg(cdf + middle) <= u) {
+      first = middle + 1;
+      len -= half + 1;
+    } else {
+      len = half;
+    }
+  }
+  int r = first - 1;
+  return r < 0 ? 0 : (r > size - 2 ? size - 2 : r);
+}
+
+__device__ __forceinline__ int sample_discrete(const LightDistrib& d, float u, float* pdf) {
+  int off = find_interval(d.cdf, d.n + 1, u);
+  *pdf = d.func_int > 0.f ? __ldg(d.func + off) / (d.func_int * d.n) : 0.f;
+  return off;
+}
+
+// What a light sample needs from the shading point.
+struct LightSample {
+  V3 Li;       // incident radiance (before visibility)
+  V3 wi;       // unit direction to the light
+  float pdf;   // solid-angle pdf (1 for delta lights)
+  V3 p_light;  // the point the shadow ray ends at
+  bool valid;
+};
+
+__device__ __forceinline__ V3 mat3_mul(const float* m, V3 v) {
+  return V3{m[0] * v.x + m[1] * v.y + m[2] * v.z, m[3] * v.x + m[4] * v.y + m[5] * v.z,
+            m[6] * v.x + m[7] * v.y + m[8] * v.z};
+}
+
+// Light::sample_Li for every light type. `prims` gives the emissive
+// triangle of an area light; `world_radius` bounds the scene for distant and
+// environment lights (Bounds3::boundingSphere, src/core/geometry.h:551-554).
+__device__ __forceinline__ LightSample sample_li(const DevLight& L, const PrimShade* __restrict__ prims, V3 ref_p,
+                                                 float u0, float u1, float world_radius) {
+  LightSample s;
+  s.valid = false;
+  s.pdf = 0.f;
+  s.Li = V3{0, 0, 0};
+  s.wi = V3{0, 0, 1};
+  s.p_light = ref_p;
+  switch (L.kind) {
+    case DL_AREA: {
+      // Triangle::sample (src/core/triangle.cpp:85-121) + DiffuseAreaLight::sample_Li (diffuse.cpp:12-26)
+      const PrimShade& sh = prims[L.prim];
+      V3 p0 = ld3(sh.p), p1 = ld3(sh.p + 3), p2 = ld3(sh.p + 6);
+      V3 n0 = ld3(sh.n), n1 = ld3(sh.n + 3), n2 = ld3(sh.n + 6);
+      float b0, b1;
+      uniform_sample_triangle(u0, u1, &b0, &b1);
+      float b2 = 1.f - b0 - b1;
+      V3 p = b0 * p0 + b1 * p1 + b2 * p2;
+      V3 ng = normalize(cross(p1 - p0, p2 - p0));
+      V3 ns = n0 * b0 + n1 * b1 + n2 * b2;
+      ng = faceforward(ng, ns);
+      float pdf = 1.f / L.area;
+      V3 w = p - ref_p;
+      if (length_sq(w) == 0.f) {
+        pdf = 0.f;
+      } else {
+        w = normalize(w);
+        pdf *= length_sq(ref_p - p) / absdot(ng, -w);
+        if (isinf(pdf)) pdf = 0.f;
+      }
+      s.p_light = p;
+      if (pdf == 0.f || length_sq(p - ref_p) == 0.f) return s;
+      s.wi = normalize(p - ref_p);
+      s.pdf = pdf;
+      s.Li = dot(ng, -s.wi) > 0.f ? ld3(L.L) : V3{0, 0, 0};
+      s.valid = true;
+      return s;
+    }
+    case DL_POINT: {  // src/light/point.cpp:10-19
+      V3 lp = ld3(L.p);
+      s.wi = normalize(lp - ref_p);
+      s.pdf = 1.f;
+      s.p_light = lp;
+      s.Li = sdiv(ld3(L.L), length_sq(lp - ref_p));
+      s.valid = true;
+      return s;
+    }
+    case DL_SPOT: {  // src/light/spot.cpp:10-29
+      V3 lp = ld3(L.p);
+      s.wi = normalize(lp - ref_p);
+      s.pdf = 1.f;
+      s.p_light = lp;
+      V3 wl = normalize(mat3_mul(L.m, -s.wi));
+      float c = wl.z, fall;
+      if (c < L.cos_total)
+        fall = 0.f;
+      else if (c > L.cos_falloff)
+        fall = 1.f;
+      else {
+        float delta = (c - L.cos_total) / (L.cos_falloff - L.cos_total);
+        fall = (delta * delta) * (delta * delta);
+      }
+      s.Li = sdiv(ld3(L.L) * fall, length_sq(lp - ref_p));
+      s.valid = true;
+      return s;
+    }
+    case DL_DISTANT: {  // src/light/distant.cpp:15-25
+      s.wi = ld3(L.p);
+      s.pdf = 1.f;
+      s.p_light = ref_p + s.wi * (2.f * world_radius);
+      s.Li = ld3(L.L);
+      s.valid = true;
+      return s;
+    }
+    case DL_ENV: {  // constant map: src/light/envmap.cpp:45-60 with a 1x1 Distribution2D
+      if (L.area == 0.f) return s;  // zero-intensity map: the distribution's pdf is 0
+      float theta = u1 * kPi, phi = u0 * 2.f * kPi;
+      float ct = cosf(theta), st = sinf(theta), sp = sinf(phi), cp = cosf(phi);
+      s.wi = mat3_mul(L.m, V3{st * cp, st * sp, ct});
+      s.pdf = 1.f / (2.f * kPi * kPi * st);
+      if (st == 0.f) s.pdf = 0.f;
+      s.p_light = ref_p + s.wi * (2.f * world_radius);
+      s.Li = ld3(L.L);
+      s.valid = true;  // the reference returns the radiance even when the pdf is 0
+      return s;
+    }
+  }
+  return s;
+}
+
+// Envmap::pdf_Li for the constant map (src/light/envmap.cpp:70-80).
+__device__ __forceinline__ float env_pdf_li(const DevLight& L, V3 wi) {
+  V3 w = mat3_mul(L.minv, wi);
+  float theta = spherical_theta(w);
+  float st = sinf(theta);
+  return 1.f / (2.f * kPi * kPi * st);
+}
+
+__device__ __forceinline__ bool is_delta_light(int kind) { return kind == DL_POINT || kind == DL_SPOT || kind == DL_DISTANT; }
+
+}  // namespace orion_gb300

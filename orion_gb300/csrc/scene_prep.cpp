@@ -1,0 +1,333 @@
+// Device scene records from a HostScene.
+//
+// All host-side float arithmetic here restates the reference's operation
+// order (compiled without FP contraction), so lobe constants, light powers
+// and the light-selection CDF are bit-identical to the values the reference
+// computes per hit or at preprocess time.
+#include "scene_prep.h"
+
+#include <cmath>
+#include <cstring>
+#include <limits>
+
+namespace orion_gb300 {
+
+namespace {
+constexpr float kPiF = 3.14159265358979323846f;
+
+bool black3(const float* c) { return c[0] == 0.f && c[1] == 0.f && c[2] == 0.f; }
+void clamp0(const float* in, float* out) {
+  for (int k = 0; k < 3; ++k) out[k] = in[k] < 0.f ? 0.f : in[k];
+}
+void set3(float* d, const float* s) {
+  d[0] = s[0];
+  d[1] = s[1];
+  d[2] = s[2];
+}
+
+DevLobe lobe(int kind, int type) {
+  DevLobe l;
+  std::memset(&l, 0, sizeof(l));
+  l.kind = kind;
+  l.type = type;
+  l.fresnel = FRESNEL_NOOP;
+  l.dist = DIST_GGX;
+  return l;
+}
+
+void add(DevMaterial* m, const DevLobe& l) {
+  if (m->num_lobes < kMaxLobes) m->lobes[m->num_lobes++] = l;
+}
+
+DevLobe microfacet_r(const float* R, int dist, float alpha) {
+  DevLobe l = lobe(LOBE_MICROFACET_R, BXDF_REFLECTION | BXDF_GLOSSY);
+  set3(l.c, R);
+  l.dist = dist;
+  l.alpha = alpha;
+  return l;
+}
+
+DevLobe dielectric_fresnel(DevLobe l, float eta_i, float eta_t) {
+  l.fresnel = FRESNEL_DIELECTRIC;
+  l.etaA = eta_i;
+  l.etaB = eta_t;
+  return l;
+}
+}  // namespace
+
+float roughness_to_alpha(float roughness) {
+  roughness = std::max(roughness, 1e-3f);
+  float x = std::log(roughness);
+  return 1.62142f + 0.819955f * x + 0.1734f * x * x + 0.0171201f * x * x * x + 0.000640711f * x * x * x * x;
+}
+
+float spectrum_intensity(const float c[3]) { return 0.212671f * c[0] + 0.715160f * c[1] + 0.072169f * c[2]; }
+
+DevMaterial prepare_material(const orion_material& mt) {
+  DevMaterial m;
+  std::memset(&m, 0, sizeof(m));
+  const int dist = mt.distribution == ORION_DIST_BECKMANN ? DIST_BECKMANN : DIST_GGX;
+  switch (mt.type) {
+    case ORION_MAT_MATTE: {  // src/material/matte.cpp:9-21
+      float r[3];
+      clamp0(mt.Kd, r);
+      float sig = mt.has_sigma ? (mt.sigma < 0.f ? 0.f : mt.sigma) : 0.f;
+      if (!black3(r)) {
+        if (sig == 0.f) {
+          DevLobe l = lobe(LOBE_LAMBERT_R, BXDF_REFLECTION | BXDF_DIFFUSE);
+          set3(l.c, r);
+          add(&m, l);
+        } else {  // src/bsdf/orennayar.cpp:5-12
+          DevLobe l = lobe(LOBE_OREN_NAYAR, BXDF_REFLECTION | BXDF_DIFFUSE);
+          set3(l.c, r);
+          float s = sig * static_cast<float>(0.01745329251994329576923690768489);
+          float s2 = s * s;
+          l.on_a = 1.f - (s2 / (2.f * (s2 + 0.33f)));
+          l.on_b = 0.45f * s2 / (s2 + 0.09f);
+          add(&m, l);
+        }
+      }
+      break;
+    }
+    case ORION_MAT_METAL: {  // src/material/metal.cpp:8-17
+      const float one[3] = {1.f, 1.f, 1.f};
+      DevLobe l = microfacet_r(one, dist, roughness_to_alpha(mt.roughness));
+      l.fresnel = FRESNEL_CONDUCTOR;
+      set3(l.fr_eta, mt.eta_rgb);
+      set3(l.fr_k, mt.k);
+      add(&m, l);
+      break;
+    }
+    case ORION_MAT_MIRROR: {  // src/material/mirror.cpp:6-13
+      float r[3];
+      clamp0(mt.Kr, r);
+      if (!black3(r)) {
+        DevLobe l = lobe(LOBE_SPECULAR_R, BXDF_REFLECTION | BXDF_SPECULAR);
+        set3(l.c, r);
+        add(&m, l);
+      }
+      break;
+    }
+    case ORION_MAT_GLASS: {  // src/material/glass.cpp:9-37
+      float e = mt.eta, rough = mt.roughness;
+      if (black3(mt.Kr) && black3(mt.Kt)) break;
+      float alpha = roughness_to_alpha(rough);
+      if (rough == 0.f) {
+        DevLobe l = lobe(LOBE_FRESNEL_SPECULAR, BXDF_REFLECTION | BXDF_TRANSMISSION | BXDF_SPECULAR);
+        set3(l.c, mt.Kr);
+        set3(l.c2, mt.Kt);
+        l.etaA = 1.f;
+        l.etaB = e;
+        add(&m, l);
+      } else {
+        if (!black3(mt.Kr)) add(&m, dielectric_fresnel(microfacet_r(mt.Kr, dist, alpha), 1.f, e));
+        if (!black3(mt.Kt)) {
+          DevLobe l = lobe(LOBE_MICROFACET_T, BXDF_TRANSMISSION | BXDF_GLOSSY);
+          set3(l.c, mt.Kt);
+          l.dist = dist;
+          l.alpha = alpha;
+          l.etaA = 1.f;
+          l.etaB = e;
+          add(&m, l);
+        }
+      }
+      break;
+    }
+    case ORION_MAT_PLASTIC: {  // src/material/plastic.cpp:8-24
+      float kd[3], ks[3];
+      clamp0(mt.Kd, kd);
+      if (!black3(kd)) {
+        DevLobe l = lobe(LOBE_LAMBERT_R, BXDF_REFLECTION | BXDF_DIFFUSE);
+        set3(l.c, kd);
+        add(&m, l);
+      }
+      clamp0(mt.Ks, ks);
+      if (!black3(ks))  // the reference's fixed Fresnel has the etas reversed (plastic.cpp:17)
+        add(&m, dielectric_fresnel(microfacet_r(ks, dist, roughness_to_alpha(mt.roughness)), 1.5f, 1.0f));
+      break;
+    }
+    case ORION_MAT_UBER: {  // src/material/uber.cpp:9-42
+      const float* op = mt.opacity;
+      float e = mt.eta;
+      float one_minus[3] = {1.f - op[0], 1.f - op[1], 1.f - op[2]}, t[3];
+      clamp0(one_minus, t);
+      if (!black3(t)) {
+        DevLobe l = lobe(LOBE_SPECULAR_T, BXDF_TRANSMISSION | BXDF_SPECULAR);
+        set3(l.c, t);
+        l.etaA = 1.f;
+        l.etaB = 1.f;
+        add(&m, l);
+      }
+      float tmp[3], c[3];
+      clamp0(mt.Kd, tmp);
+      for (int k = 0; k < 3; ++k) c[k] = tmp[k] * op[k];
+      if (!black3(c)) {
+        DevLobe l = lobe(LOBE_LAMBERT_R, BXDF_REFLECTION | BXDF_DIFFUSE);
+        set3(l.c, c);
+        add(&m, l);
+      }
+      clamp0(mt.Ks, tmp);
+      for (int k = 0; k < 3; ++k) c[k] = tmp[k] * op[k];
+      if (!black3(c)) add(&m, dielectric_fresnel(microfacet_r(c, dist, roughness_to_alpha(mt.roughness)), 1.f, e));
+      clamp0(mt.Kr, tmp);
+      for (int k = 0; k < 3; ++k) c[k] = tmp[k] * op[k];
+      if (!black3(c)) {
+        DevLobe l = lobe(LOBE_SPECULAR_R, BXDF_REFLECTION | BXDF_SPECULAR);
+        set3(l.c, c);
+        add(&m, dielectric_fresnel(l, 1.f, e));
+      }
+      clamp0(mt.Kt, tmp);
+      for (int k = 0; k < 3; ++k) c[k] = tmp[k] * op[k];
+      if (!black3(c)) {
+        DevLobe l = lobe(LOBE_SPECULAR_T, BXDF_TRANSMISSION | BXDF_SPECULAR);
+        set3(l.c, c);
+        l.etaA = 1.f;
+        l.etaB = e;
+        add(&m, l);
+      }
+      break;
+    }
+  }
+  for (int i = 0; i < m.num_lobes; ++i) {
+    int t = m.lobes[i].type;
+    const int ns = BXDF_ALL & ~BXDF_SPECULAR;
+    if ((t & ns) == t) ++m.num_nonspecular;
+  }
+  return m;
+}
+
+bool prepare_scene(const HostScene& s, PreparedScene* out, std::string* err) {
+  const int64_t T = s.num_prims();
+  out->prims.resize(T);
+  float lo[3] = {std::numeric_limits<float>::max(), std::numeric_limits<float>::max(),
+                 std::numeric_limits<float>::max()};
+  float hi[3] = {std::numeric_limits<float>::lowest(), std::numeric_limits<float>::lowest(),
+                 std::numeric_limits<float>::lowest()};
+  for (int64_t i = 0; i < T; ++i) {
+    PrimShade& p = out->prims[i];
+    std::memset(&p, 0, sizeof(p));
+    std::memcpy(p.p, &s.positions[9 * i], 9 * sizeof(float));
+    std::memcpy(p.n, &s.normals[9 * i], 9 * sizeof(float));
+    p.material = s.material_of_prim[i];
+    p.light = s.light_of_prim[i];
+    for (int c = 0; c < 3; ++c)
+      for (int k = 0; k < 3; ++k) {
+        lo[k] = std::min(lo[k], p.p[3 * c + k]);
+        hi[k] = std::max(hi[k], p.p[3 * c + k]);
+      }
+  }
+  // Bounds3::boundingSphere (src/core/geometry.h:551-554).
+  for (int k = 0; k < 3; ++k) out->world_center[k] = (lo[k] + hi[k]) * 0.5f;
+  bool inside = T > 0;
+  for (int k = 0; k < 3; ++k) inside = inside && out->world_center[k] >= lo[k] && out->world_center[k] <= hi[k];
+  if (inside) {
+    float d[3] = {out->world_center[0] - hi[0], out->world_center[1] - hi[1], out->world_center[2] - hi[2]};
+    out->world_radius = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+  } else {
+    out->world_radius = 0.f;
+  }
+
+  out->mats.clear();
+  for (const orion_material& m : s.materials) out->mats.push_back(prepare_material(m));
+
+  const float pi = kPiF, r = out->world_radius;
+  out->lights.clear();
+  out->env_idx.clear();
+  std::vector<float> power;
+  for (size_t i = 0; i < s.lights.size(); ++i) {
+    const orion_light& l = s.lights[i];
+    DevLight d;
+    std::memset(&d, 0, sizeof(d));
+    set3(d.L, l.L);
+    float pw[3];
+    switch (l.type) {
+      case ORION_LIGHT_AREA: {  // src/light/diffuse.cpp:8-11, src/core/triangle.cpp:77-83
+        if (l.prim < 0 || l.prim >= T) {
+          *err = "area light references a missing primitive";
+          return false;
+        }
+        d.kind = DL_AREA;
+        d.prim = l.prim;
+        const float* p = &s.positions[9 * (size_t)l.prim];
+        float e1[3] = {p[3] - p[0], p[4] - p[1], p[5] - p[2]};
+        float e2[3] = {p[6] - p[0], p[7] - p[1], p[8] - p[2]};
+        float c[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2], e1[0] * e2[1] - e1[1] * e2[0]};
+        d.area = 0.5f * std::sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]);
+        for (int k = 0; k < 3; ++k) pw[k] = l.L[k] * d.area * pi;
+        break;
+      }
+      case ORION_LIGHT_POINT: {  // src/light/point.cpp:6-9
+        d.kind = DL_POINT;
+        set3(d.p, l.p);
+        float s4 = 4 * pi;
+        for (int k = 0; k < 3; ++k) pw[k] = l.L[k] * s4;
+        break;
+      }
+      case ORION_LIGHT_SPOT: {  // src/light/spot.cpp:6-9
+        d.kind = DL_SPOT;
+        set3(d.p, l.p);
+        for (int rr = 0; rr < 3; ++rr)
+          for (int c = 0; c < 3; ++c) d.m[3 * rr + c] = l.w2l[4 * rr + c];
+        d.cos_total = l.cos_total;
+        d.cos_falloff = l.cos_falloff;
+        float f = 1 - .5f * (l.cos_falloff + l.cos_total);
+        for (int k = 0; k < 3; ++k) pw[k] = l.L[k] * 2 * pi * f;
+        break;
+      }
+      case ORION_LIGHT_DISTANT: {  // src/light/distant.cpp:11-14
+        d.kind = DL_DISTANT;
+        set3(d.p, l.dir);
+        for (int k = 0; k < 3; ++k) pw[k] = l.L[k] * pi * r * r;
+        break;
+      }
+      case ORION_LIGHT_ENV: {  // src/light/envmap.cpp:9-44, 62-65 (constant map)
+        d.kind = DL_ENV;
+        for (int rr = 0; rr < 3; ++rr)
+          for (int c = 0; c < 3; ++c) {
+            d.m[3 * rr + c] = l.l2w[4 * rr + c];
+            d.minv[3 * rr + c] = l.w2l[4 * rr + c];
+          }
+        d.area = spectrum_intensity(l.L) * std::sin(pi * 0.5f);
+        float f = pi * r * r;
+        for (int k = 0; k < 3; ++k) pw[k] = l.L[k] * f;
+        out->env_idx.push_back((int)i);
+        break;
+      }
+      default:
+        *err = "unknown light type";
+        return false;
+    }
+    out->lights.push_back(d);
+    power.push_back(spectrum_intensity(pw));
+  }
+  // Distribution1D (src/sampler/sampling.h:71-90).
+  const int n = (int)power.size();
+  out->light_func = power;
+  out->light_cdf.assign(n + 1, 0.f);
+  for (int i = 1; i < n + 1; ++i) out->light_cdf[i] = out->light_cdf[i - 1] + power[i - 1] / n;
+  out->light_func_int = n > 0 ? out->light_cdf[n] : 0.f;
+  if (n > 0) {
+    if (out->light_func_int == 0.f) {
+      for (int i = 1; i < n + 1; ++i) out->light_cdf[i] = float(i) / float(n);
+    } else {
+      for (int i = 1; i < n + 1; ++i) out->light_cdf[i] /= out->light_func_int;
+    }
+  }
+  if (out->light_func.empty()) {  // keep device pointers valid
+    out->light_func.push_back(0.f);
+  }
+
+  // Pinhole (src/camera/pinhole.h:22-26, src/core/camera.h:24-25).
+  DevCamera& c = out->cam;
+  std::memset(&c, 0, sizeof(c));
+  std::memcpy(c.c2w, s.camera.c2w, sizeof(c.c2w));
+  c.tan_half_fov = std::tan(s.camera.fov * 0.5f * static_cast<float>(0.01745329251994329576923690768489));
+  c.aspect = (float)s.camera.width / s.camera.height;
+  c.lens_radius = s.camera.lens_radius;
+  c.focal_distance = s.camera.focal_distance;
+  c.width = s.camera.width;
+  c.height = s.camera.height;
+  return true;
+}
+
+}  // namespace orion_gb300

@@ -1,0 +1,30 @@
+// Host preparation of the device scene records from a HostScene.
+#pragma once
+#include <vector>
+
+#include "device_types.h"
+#include "scene_host.h"
+
+namespace orion_gb300 {
+
+struct PreparedScene {
+  std::vector<PrimShade> prims;
+  std::vector<DevMaterial> mats;
+  std::vector<DevLight> lights;
+  std::vector<float> light_func, light_cdf;  // Distribution1D over light power
+  float light_func_int = 0.f;
+  std::vector<int> env_idx;
+  float world_center[3] = {0, 0, 0};
+  float world_radius = 0.f;
+  DevCamera cam{};
+};
+
+// Materials -> lobe lists (Material::getBSDF, src/material/*.cpp).
+DevMaterial prepare_material(const orion_material& m);
+// Everything else; returns false with `err` set on inconsistent input.
+bool prepare_scene(const HostScene& s, PreparedScene* out, std::string* err);
+
+float roughness_to_alpha(float roughness);  // src/bsdf/microfacet.h:44-50
+float spectrum_intensity(const float rgb[3]);  // src/core/spectrum.h:88-91
+
+}  // namespace orion_gb300

@@ -1,0 +1,143 @@
+"""CPU tests of the C ABI library: exports, scene loader, error handling.
+
+No GPU is touched here: the library loads without a device, the loader is
+host code, and context creation without a device must fail with a status
+code, not crash.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import hashlib
+import os
+import re
+import shutil
+import tempfile
+
+import numpy as np
+import pytest
+
+import helpers
+
+ROOT = helpers.ROOT
+
+
+def declared_symbols():
+    text = open(os.path.join(ROOT, "include", "orion_gpu.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(orion_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_library_exports_every_declared_symbol(built):
+    import orion_gb300 as og
+    lib = og.library()
+    syms = declared_symbols()
+    assert len(syms) >= 15
+    missing = [s for s in syms if not hasattr(lib, s)]
+    assert not missing, f"declared but not exported: {missing}"
+
+
+def test_loader_matches_reference_geometry(built, tmp_path):
+    import orion_gb300 as og
+    g = helpers.golden("geometry.npz")
+    path = helpers.write_scene("cornell", str(tmp_path / "cornell256"))
+    assert helpers.scene_hash(path) == bytes(helpers.golden("trace.npz")["hash"]).decode()
+    a = og.HostScene.load(path).arrays()
+    assert hashlib.sha256(a["positions"].tobytes()).hexdigest() == bytes(g["cornell/positions_sha"]).decode()
+    assert hashlib.sha256(a["normals"].tobytes()).hexdigest() == bytes(g["cornell/normals_sha"]).decode()
+    assert np.array_equal(a["light_of_prim"], g["cornell/light_of_prim"])
+    assert len(a["lights"]) == len(g["cornell/light_power"])
+    assert a["spp"] == 16 and a["max_depth"] == 5
+    assert (a["camera"].width, a["camera"].height) == (256, 256)
+
+
+def test_loader_zoo_lights_and_order(built, tmp_path):
+    import orion_gb300 as og
+    g = helpers.golden("geometry.npz")
+    path = helpers.write_scene("zoo", str(tmp_path / "zoo"), res=48, spp=16)
+    a = og.HostScene.load(path).arrays()
+    assert hashlib.sha256(a["positions"].tobytes()).hexdigest() == bytes(g["zoo/positions_sha"]).decode()
+    kinds = [l.type for l in a["lights"]]
+    # area lights first (one per emissive triangle), then point, spot, distant, then the environment
+    assert kinds == [og.LIGHT_AREA, og.LIGHT_AREA, og.LIGHT_POINT, og.LIGHT_SPOT, og.LIGHT_DISTANT, og.LIGHT_ENV]
+    assert len(a["lights"]) == len(g["zoo/light_power"])
+
+
+def test_context_without_device_reports_error(built):
+    import orion_gb300 as og
+    if shutil.which("nvidia-smi") and os.system("nvidia-smi -L > /dev/null 2>&1") == 0:
+        pytest.skip("a GPU is present")
+    with pytest.raises(og.OrionError) as e:
+        og.Context(0)
+    assert e.value.code in (-4, -1)
+
+
+def _write(d, name, text):
+    p = os.path.join(d, name)
+    with open(p, "w") as f:
+        f.write(text)
+    return p
+
+
+GOOD = """<Scene>
+  <Resource filename="./"/>
+  <Camera type="pinhole"><Transform><Param lookat="0,0,3, 0,0,0, 0,1,0"/></Transform>
+    <Param fov="40"/><Param filmsize="8,8"/></Camera>
+  <Model type="meshHandy">
+    <Param p="-1,-1,0, 1,-1,0, 1,1,0"/><Param n="0,0,1"/>
+    <Material type="matte"><Kd><Param type="constant"/><Param color="0.5,0.5,0.5"/></Kd></Material>
+    <AreaLight><Param Le="1,1,1"/><Param nLightSamples="1"/></AreaLight>
+  </Model>
+  <Integrator type="path"><Param maxDepth="3"/><Param nSamplesPerPixel="2"/></Integrator>
+  <Sampler type="sobol"/>
+</Scene>
+"""
+
+
+@pytest.mark.parametrize("mutate,code", [
+    (lambda s: s.replace("</Scene>", ""), -3),                                  # truncated XML
+    (lambda s: s.replace('type="meshHandy"', 'type="mesh" filename="missing.obj"'), -2),
+    (lambda s: s.replace('<Param n="0,0,1"/>', ""), -3),                        # normals are required
+    (lambda s: s.replace('type="sobol"', 'type="pseudo"'), -6),
+    (lambda s: s.replace('type="path"', 'type="sppm"'), -6),
+    (lambda s: s.replace('<Kd><Param type="constant"/><Param color="0.5,0.5,0.5"/></Kd>', ""), -3),
+    (lambda s: s.replace('<Param fov="40"/>', ""), -3),
+])
+def test_loader_rejects_bad_scenes(built, mutate, code):
+    import orion_gb300 as og
+    with tempfile.TemporaryDirectory() as d:
+        og.HostScene.load(_write(d, "ok.ori", GOOD))
+        with pytest.raises(og.OrionError) as e:
+            og.HostScene.load(_write(d, "bad.ori", mutate(GOOD)))
+        assert e.value.code == code, str(e.value)
+
+
+def test_obj_without_normals_rejected(built, tmp_path):
+    import orion_gb300 as og
+    (tmp_path / "m.obj").write_text("v 0 0 0\nv 1 0 0\nv 0 1 0\nf 1 2 3\n")
+    text = GOOD.replace('type="meshHandy"', 'type="mesh" filename="m.obj"')
+    p = tmp_path / "s.ori"
+    p.write_text(text)
+    with pytest.raises(og.OrionError) as e:
+        og.HostScene.load(str(p))
+    assert e.value.code == -3 and "normal" in str(e.value)
+
+
+def test_obj_quads_are_fan_triangulated(built, tmp_path):
+    import orion_gb300 as og
+    (tmp_path / "q.obj").write_text("v 0 0 0\nv 1 0 0\nv 1 1 0\nv 0 1 0\nvn 0 0 1\nf 1//1 2//1 3//1 4//1\n")
+    p = tmp_path / "s.ori"
+    p.write_text(GOOD.replace('type="meshHandy"', 'type="mesh" filename="q.obj"'))
+    a = og.HostScene.load(str(p)).arrays()
+    assert a["positions"].shape == (2, 9)
+    assert np.allclose(a["positions"][1], [0, 0, 0, 1, 1, 0, 0, 1, 0])
+
+
+def test_scene_from_desc_validates(built):
+    import orion_gb300 as og
+    m = helpers.make_material(dict(type=0, Kd=(0.5, 0.5, 0.5)))
+    cam = og.Camera(width=4, height=4, fov=40.0)
+    pos = np.zeros((1, 9), np.float32)
+    with pytest.raises(og.OrionError):
+        og.HostScene.from_arrays(pos, pos, [3], [m], [], cam, 1, 2)        # material index out of range
+    s = og.HostScene.from_arrays(pos, pos, [0], [m], [], cam, 1, 2)
+    assert s.desc().num_prims == 1
