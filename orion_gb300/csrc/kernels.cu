@@ -77,9 +77,13 @@ __device__ __forceinline__ V3 point_on(const PrimShade& sh, float u, float v) {
 __device__ __forceinline__ TraceScene trace_scene(const SceneView& s) { return TraceScene{s.nodes, s.woop, s.tri_prim}; }
 
 // Pinhole::generateRay (src/camera/pinhole.cpp:8-33).
+// Sampler::next2() builds Point2f(next(), next()) (src/core/sampler.h:29); the
+// two calls are unsequenced and the compiled reference evaluates the second
+// first, so .x holds the later dimension. All 2-D samples follow that order.
 __device__ __forceinline__ void camera_ray(const DevCamera& c, PathSampler& smp, int i, int j, V3* o, V3* d) {
-  float rx = (float)i + smp.next();
-  float ry = (float)j + smp.next();
+  float s0 = smp.next(), s1 = smp.next();
+  float rx = (float)i + s1;
+  float ry = (float)j + s0;
   float xx = (2.f * rx / (float)c.width - 1.f) * c.aspect * c.tan_half_fov;
   float yy = (1.f - 2.f * ry / (float)c.height) * c.tan_half_fov;
   V3 dir = normalize(V3{xx, yy, -1.f});
@@ -88,7 +92,7 @@ __device__ __forceinline__ void camera_ray(const DevCamera& c, PathSampler& smp,
     V3 target = org + dir * c.focal_distance;
     float lx, ly;
     float l0 = smp.next(), l1 = smp.next();
-    concentric_sample_disk(l0, l1, &lx, &ly);
+    concentric_sample_disk(l1, l0, &lx, &ly);
     org = V3{lx * c.lens_radius, ly * c.lens_radius, 0.f};
     dir = normalize(target - org);
   }
@@ -211,8 +215,8 @@ __global__ void k_shade(SceneView s, WaveView w, WaveArgs a, int bounce, int cur
         float sel_pdf;
         int li = sample_discrete(distrib, smp.next(), &sel_pdf);
         if (sel_pdf != 0.f) {
-          float ul0 = smp.next(), ul1 = smp.next();
-          float ub0 = smp.next(), ub1 = smp.next();
+          float ul1 = smp.next(), ul0 = smp.next();  // next2(): .x is the later dimension
+          float ub1 = smp.next(), ub0 = smp.next();
           const DevLight& lt = s.lights[li];
           V3 wo = normalize(-rd);
           // estimateDirect, light-sampling half (integrator.cpp:39-60).
@@ -273,7 +277,7 @@ __global__ void k_shade(SceneView s, WaveView w, WaveArgs a, int bounce, int cur
       }
 
       // Continuation: BSDF sample, throughput, spawn, Russian roulette (path.cpp:81-96).
-      float u0 = smp.next(), u1 = smp.next();
+      float u1 = smp.next(), u0 = smp.next();  // next2(): .x is the later dimension
       V3 wi;
       float pdf;
       int stype;

@@ -1,0 +1,108 @@
+"""The CPU oracle (oracle/port) pinned against the reference's golden vectors.
+
+On the machine the fixtures were generated on (x86-64, same glibc) the
+restatement is bit-identical to the reference; elsewhere the C library's
+float transcendentals may differ in the last bit, so comparisons allow a
+relative 1e-6 there and report the exact fraction.
+"""
+from __future__ import annotations
+
+import os
+import platform
+
+import numpy as np
+import pytest
+
+import helpers
+
+EXACT = platform.machine() in ("x86_64", "AMD64")
+
+
+@pytest.fixture(scope="module")
+def port(built):
+    from oracle import port as p
+    p.lib()
+    return p
+
+
+def _same(a, b, rtol=1e-6):
+    a, b = np.asarray(a), np.asarray(b)
+    if EXACT and a.dtype == np.float32:
+        return np.array_equal(a.view(np.uint32), b.view(np.uint32))
+    if a.dtype.kind == "f":
+        return bool(np.all((np.abs(a - b) <= rtol * np.abs(b) + 1e-7) | (a == b) | (np.isnan(a) & np.isnan(b))))
+    return np.array_equal(a, b)
+
+
+def test_port_sobol_bit_exact(port):
+    g = helpers.golden("sobol.npz")
+    v = port.sobol(g["index"], g["dim"])
+    assert np.array_equal(v.view(np.uint32), g["value"].view(np.uint32))  # integer work: exact everywhere
+
+
+@pytest.mark.parametrize("case", [c[0] for c in helpers.BSDF_CASES])
+def test_port_bsdf_matches_reference(port, case):
+    g = helpers.golden("bsdf.npz")
+    mat = helpers.make_material(dict(helpers.BSDF_CASES)[case])
+    for tm in (31, 15):
+        out = port.bsdf_eval(mat, *(g[f"{case}/{k}"] for k in ("frame", "wo", "wi", "rnd")), tm)
+        for k, v in out.items():
+            ref = g[f"{case}/{tm}/{k}"]
+            if k in ("stype", "nbxdf") and not EXACT:
+                assert (v == ref).mean() > 0.995, k
+            else:
+                assert _same(v, ref), f"{case} type {tm}: {k} differs"
+
+
+def test_port_camera_matches_reference(port, tmp_path):
+    g = helpers.golden("camera.npz")
+    for name, kw in [("cornell", dict(res=64, spp=4)),
+                     ("mixed", dict(width=96, height=54, spp=4, subdivs=(1, 1, 1, 1, 1, 1, 1, 1)))]:
+        path = helpers.write_scene(name, str(tmp_path / name), **kw)
+        assert helpers.scene_hash(path) == bytes(g[f"{name}/hash"]).decode()
+        rays = port.Scene.load(path).camera_rays(g[f"{name}/index"])
+        assert _same(rays, g[f"{name}/rays"]), name
+
+
+def test_port_trace_matches_reference_and_brute_force(port, tmp_path):
+    g = helpers.golden("trace.npz")
+    path = helpers.write_scene("cornell", str(tmp_path / "c"))
+    sc = port.Scene.load(path)
+    t, u, v, prim = sc.trace(g["rays"])
+    assert np.array_equal(prim, g["prim"])
+    assert _same(t, g["t"])
+    tb, ub, vb, pb = sc.trace(g["rays"], brute_force=True)
+    assert np.array_equal(prim, pb) and np.array_equal(t, tb), "BVH must equal the brute-force loop"
+
+
+@pytest.mark.parametrize("name,kw", [("cornell", dict(res=64, spp=16)), ("zoo", dict(res=48, spp=16))])
+def test_port_image_matches_reference_render(port, tmp_path, name, kw):
+    g = helpers.golden(f"image_{name}.npz")
+    path = helpers.write_scene(name, str(tmp_path / name), **kw)
+    assert helpers.scene_hash(path) == bytes(g["hash"]).decode()
+    film, rays = port.Scene.load(path).render()
+    if EXACT:
+        assert np.array_equal(film.view(np.uint32), g["film"].view(np.uint32)), "oracle image differs from the reference"
+    else:
+        close = (np.abs(film - g["film"]) <= 1e-4 * np.abs(g["film"]) + 1e-5).all(2).mean()
+        assert close > 0.98
+    assert rays > 0
+
+
+def test_port_statistics_agree_with_high_spp_reference(port, tmp_path):
+    """The oracle at 1k spp vs the reference's high-spp FP64 pixel means, within 3 sigma."""
+    g = helpers.golden("stats_cornell.npz")
+    path = helpers.write_scene("cornell", str(tmp_path / "c"))
+    assert helpers.scene_hash(path) == bytes(g["hash"]).decode()
+    sc = port.Scene.load(path)
+    n = 256
+    pix = g["pix"][:32]
+    s, q = sc.render_pixels(pix, n, first_pass=int(g["spp"]))   # passes disjoint from the reference's
+    mean = s / n
+    var = np.maximum(q / n - mean ** 2, 0)
+    rs, rq, rn = g["sum"][:32], g["sumsq"][:32], float(g["spp"])
+    rmean = rs / rn
+    rvar = np.maximum(rq / rn - rmean ** 2, 0)
+    sigma = np.sqrt(var / n + rvar / rn) + 1e-6
+    z = np.abs(mean - rmean) / sigma
+    assert (z <= 3).mean() >= 0.9, f"3-sigma agreement {(z <= 3).mean():.3f}"

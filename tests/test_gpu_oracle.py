@@ -1,0 +1,111 @@
+"""GPU path vs the CPU oracle at sizes the oracle finishes in seconds.
+
+* 1M seeded rays: closest-hit primitive equal except ties, t within 1e-5
+  relative, occlusion equal to "closest hit exists" (the oracle's BVH is
+  checked equal to a brute-force loop in the CPU suite).
+* images: the GPU and the oracle trace the same Sobol sample per path, so
+  per-pixel sums match except where FP32 rounding sends a path down another
+  branch; at least 97% of pixels must match to 1e-4 relative.
+* statistics: a 1024-spp FP64 GPU render against the reference's 65,536-spp
+  FP64 per-pixel means, |difference| <= 3 sigma for >= 95% of the tested
+  pixels; relative RMSE is printed.
+"""
+from __future__ import annotations
+
+import os
+
+import numpy as np
+import pytest
+
+import helpers
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def port(built):
+    from oracle import port as p
+    p.lib()
+    return p
+
+
+def _bounds(host):
+    p = host.arrays()["positions"].reshape(-1, 3)
+    return p.min(0), p.max(0)
+
+
+@pytest.mark.parametrize("name,kw", [("cornell", {}), ("displaced", dict(res=64, spp=4, subdiv=6))])
+def test_million_rays_match_oracle(ctx, port, tmp_path, name, kw):
+    import orion_gb300 as og
+    path = helpers.write_scene(name, str(tmp_path / name), **kw)
+    host = og.HostScene.load(path)
+    lo, hi = _bounds(host)
+    n = 1 << 20
+    rays = helpers.random_rays(n, lo, hi, seed=17)
+    rays[: n // 8, 7] = (helpers.splitmix_uniform(n // 8, 18) * float(np.max(hi - lo))).astype(np.float32)
+    sid = ctx.upload(host)
+    t, u, v, prim = ctx.trace(sid, rays)
+    _, _, _, occ = ctx.trace(sid, rays, any_hit=True)
+    ctx.release(sid)
+    rt, ru, rv, rprim = port.Scene(host).trace(rays)
+    hit = rprim >= 0
+    miss_mismatch = np.count_nonzero((prim >= 0) != hit)
+    assert miss_mismatch <= n * 1e-5, f"hit/miss differs on {miss_mismatch} rays"
+    assert np.count_nonzero((occ >= 0) != hit) <= n * 1e-5
+    both = hit & (prim >= 0)
+    t_ok = np.abs(t - rt) <= 1e-5 * np.abs(rt) + 1e-7
+    same = prim == rprim
+    assert (same | t_ok)[both].all(), "a different primitive at a different distance"
+    assert t_ok[both].mean() > 0.99999, f"t differs on {np.count_nonzero(both & ~t_ok)} rays"
+    print(f"{name}: {n} rays, {hit.mean():.3f} hit, primitive identical on {same[both].mean():.6f} of hits "
+          f"(rest are ties), max rel t error {np.max(np.abs(t - rt)[both] / np.maximum(np.abs(rt[both]), 1e-30)):.2e}")
+
+
+@pytest.mark.parametrize("name,kw", [
+    ("cornell", dict(res=96, spp=8)),
+    ("zoo", dict(res=64, spp=8, beckmann=True)),
+    ("mixed", dict(width=96, height=54, spp=8, subdivs=(2, 2, 2, 2, 2, 2, 2, 2))),
+    ("displaced", dict(res=64, spp=8, subdiv=5)),
+])
+def test_image_matches_oracle_path_for_path(ctx, port, tmp_path, name, kw):
+    import orion_gb300 as og
+    path = helpers.write_scene(name, str(tmp_path / name), **kw)
+    host = og.HostScene.load(path)
+    sc = port.Scene(host)
+    ref, _ = sc.render()
+    sid = ctx.upload(host)
+    gpu, cnt = ctx.render(sid, sc.width, sc.height)
+    ctx.release(sid)
+    assert (cnt == sc.spp).all()
+    close = (np.abs(gpu.astype(np.float64) - ref) <= 1e-4 * np.abs(ref) + 1e-5).all(2).mean()
+    rmse = float(np.sqrt(np.mean((gpu.astype(np.float64) - ref) ** 2)) / max(np.sqrt(np.mean(ref.astype(np.float64) ** 2)), 1e-12))
+    print(f"{name}: {close:.4f} of pixels identical path-for-path, relative RMSE {rmse:.2e}")
+    assert close >= 0.97
+    assert rmse < 0.05
+
+
+def test_render_statistics_within_3_sigma_of_reference(ctx, tmp_path):
+    """Cornell box at the benchmark resolution: GPU FP64 film vs the reference's 64k-spp FP64 pixel means."""
+    import orion_gb300 as og
+    g = helpers.golden("stats_cornell.npz")
+    path = helpers.write_scene("cornell", str(tmp_path / "c"))
+    assert helpers.scene_hash(path) == bytes(g["hash"]).decode()
+    host = og.HostScene.load(path)
+    sid = ctx.upload(host)
+    n = 1024
+    ref_spp = int(g["spp"])
+    s, q = ctx.render(sid, 256, 256, spp=n, first_pass=ref_spp, fp64=True)  # sample passes disjoint from the reference's
+    ctx.release(sid)
+    pix = g["pix"]
+    s, q = s[pix[:, 1], pix[:, 0]], q[pix[:, 1], pix[:, 0]]
+    mean = s / n
+    var = np.maximum(q / n - mean ** 2, 0)
+    rmean = g["sum"] / ref_spp
+    rvar = np.maximum(g["sumsq"] / ref_spp - rmean ** 2, 0)
+    sigma = np.sqrt(var / n + rvar / ref_spp) + 1e-7
+    z = np.abs(mean - rmean) / sigma
+    frac = (z <= 3).all(1).mean()
+    rmse = float(np.sqrt(np.mean((mean - rmean) ** 2)) / np.sqrt(np.mean(rmean ** 2)))
+    print(f"{len(pix)} pixels: {frac:.3f} within 3 sigma, relative RMSE {rmse:.4f} vs {ref_spp}-spp FP64 reference")
+    assert frac >= 0.95
+    assert rmse < 0.05
