@@ -50,20 +50,22 @@ void woop_record(const float* p, float out[12]) {
     r1[k] = ca[k] / det;  // row giving v (along e2)
     r2[k] = ab[k] / det;  // row giving the offset along n
   }
-  auto dot = [](const double* x, const double* y) { return x[0] * y[0] + x[1] * y[1] + x[2] * y[2]; };
-  // w0: t = (w0.w - o.w0) / (d.w0); w1/w2: u, v = w.w + o.w + t d.w
+  // Origin-relative form: the fourth components hold v0, and the kernel
+  // works with C = o - v0, so t = -(r2.C) / (r2.d), u = r0.C + t r0.d,
+  // v = r1.C + t r1.d. Subtracting v0 first keeps t accurate for ray
+  // origins close to the triangle's plane (every secondary ray).
   out[0] = (float)r2[0];
   out[1] = (float)r2[1];
   out[2] = (float)r2[2];
-  out[3] = (float)dot(r2, v0);
+  out[3] = (float)v0[0];
   out[4] = (float)r0[0];
   out[5] = (float)r0[1];
   out[6] = (float)r0[2];
-  out[7] = (float)-dot(r0, v0);
+  out[7] = (float)v0[1];
   out[8] = (float)r1[0];
   out[9] = (float)r1[1];
   out[10] = (float)r1[2];
-  out[11] = (float)-dot(r1, v0);
+  out[11] = (float)v0[2];
 }
 
 namespace {

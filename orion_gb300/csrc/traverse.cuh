@@ -61,19 +61,22 @@ __device__ __forceinline__ float box_entry(float4 lo, float4 hi, V3 idir, V3 oid
   return tn <= tf ? tn : __int_as_float(0x7f800000);
 }
 
-// Woop unit-triangle test. Returns true with t, u, v for a hit in (tnear, tfar].
+// Woop unit-triangle test on an origin-relative record: rows (r2, r0, r1)
+// of the inverse of [e1 e2 n] with v0 in the .w components. Returns true
+// with t, u, v for a hit in (tnear, tfar].
 __device__ __forceinline__ bool woop_hit(const float4* __restrict__ woop, int k, V3 o, V3 d, float tnear, float tfar,
                                          float* t, float* u, float* v) {
   float4 w0 = __ldg(woop + 3 * k);
-  float oz = w0.w - o.x * w0.x - o.y * w0.y - o.z * w0.z;
+  float4 w1 = __ldg(woop + 3 * k + 1);
+  float4 w2 = __ldg(woop + 3 * k + 2);
+  float cx = o.x - w0.w, cy = o.y - w1.w, cz = o.z - w2.w;
+  float oz = -(cx * w0.x + cy * w0.y + cz * w0.z);
   float dz = d.x * w0.x + d.y * w0.y + d.z * w0.z;
   float tt = oz * __frcp_rn(dz);
   if (!(tt > tnear && tt <= tfar)) return false;
-  float4 w1 = __ldg(woop + 3 * k + 1);
-  float uu = (w1.w + o.x * w1.x + o.y * w1.y + o.z * w1.z) + tt * (d.x * w1.x + d.y * w1.y + d.z * w1.z);
+  float uu = (cx * w1.x + cy * w1.y + cz * w1.z) + tt * (d.x * w1.x + d.y * w1.y + d.z * w1.z);
   if (!(uu >= 0.f && uu <= 1.f)) return false;
-  float4 w2 = __ldg(woop + 3 * k + 2);
-  float vv = (w2.w + o.x * w2.x + o.y * w2.y + o.z * w2.z) + tt * (d.x * w2.x + d.y * w2.y + d.z * w2.z);
+  float vv = (cx * w2.x + cy * w2.y + cz * w2.z) + tt * (d.x * w2.x + d.y * w2.y + d.z * w2.z);
   if (!(vv >= 0.f && uu + vv <= 1.f)) return false;
   *t = tt;
   *u = uu;
