@@ -50,10 +50,12 @@ WORKLOADS = {
 }
 
 
-def scene_path(workload: str) -> str:
+def scene_path(workload: str, **override) -> str:
     from orion_gb300 import scenegen
     fn, kw, _ = WORKLOADS[workload]
-    d = os.path.join(CACHE, workload)
+    kw = {**kw, **{k: v for k, v in override.items() if v is not None}}
+    tag = "_".join(f"{k}{v}" for k, v in sorted(kw.items()))
+    d = os.path.join(CACHE, workload + ("_" + tag if tag else ""))
     marker = os.path.join(d, "done")
     if not os.path.exists(marker):
         s = getattr(scenegen, fn)(**kw)
@@ -145,6 +147,10 @@ def cpu_baseline(workload: str, threads: int, seconds: float = 15.0) -> dict | N
     return port.time_sample(scene_path(workload), threads=threads, seconds=seconds)
 
 
+def scale_kw(args) -> dict:
+    return {"res": getattr(args, "res", None), "spp": getattr(args, "spp", None)}
+
+
 def run_ours(args) -> dict:
     import orion_gb300 as og
     rank = int(os.environ.get("RANK", "0"))
@@ -157,7 +163,7 @@ def run_ours(args) -> dict:
         torch.cuda.set_device(local)
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
 
-    path = scene_path(args.workload)
+    path = scene_path(args.workload, **scale_kw(args))
     host = og.HostScene.load(path)
     d = host.desc()
     W, H, spp, depth = d.camera.width, d.camera.height, d.spp, d.max_depth
@@ -204,14 +210,18 @@ def run_ours(args) -> dict:
     # End to end through the C ABI: upload scene arrays, render, read the film back.
     e2e_ms = []
     film_bytes = W * H * (3 * 4 + 4)
-    for i in range(max(1, min(args.steps, 5))):
+    for i in range(0 if args.quick else max(1, min(args.steps, 5))):
         t = time.time()
         sid2 = ctx.upload(host)
         img, cnt = ctx.render(sid2, W, H, spp=spp, first_pass=first)
         ctx.release(sid2)
         e2e_ms.append((time.time() - t) * 1e3)
-    e2e_step = float(np.median(e2e_ms))
+    e2e_step = float(np.median(e2e_ms)) if e2e_ms else float("nan")
 
+    if args.quick:
+        ctx.close()
+        return {"metric": METRIC, "value": round(value, 3), "unit": "Mpaths/s", "ms_per_step": ms_per_step,
+                "config": {"workload": args.workload, "scale": scale_kw(args)}} if rank == 0 else None
     # Roofline: one profiled render, per-stage device times.
     ctx.set_profiling(True)
     ctx.render(sid, W, H, spp=spp, first_pass=first)
@@ -296,6 +306,9 @@ def main():
     ap.add_argument("--workload", default="displaced", choices=sorted(WORKLOADS))
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--res", type=int, help="scale the workload down: square image side (profiling runs)")
+    ap.add_argument("--spp", type=int, help="scale the workload down: samples per pixel (profiling runs)")
+    ap.add_argument("--quick", action="store_true", help="timed steps only: no e2e, roofline or CPU legs")
     args = ap.parse_args()
     from orion_gb300 import build
     build.build_product()
