@@ -195,6 +195,51 @@ typedef struct orion_stage_times {
 int orion_gpu_set_profiling(orion_gpu_ctx* ctx, int32_t enable);
 int orion_gpu_stage_times(orion_gpu_ctx* ctx, orion_stage_times* out);
 
+/* ------------------------------------------------------------- batches */
+/* Many render() calls in one launch. There is no single reference call for
+ * this: it runs PathTracing::render (src/integrator/path.cpp:15-37) for every
+ * job, sharing one pool of path slots across jobs (finished slots are
+ * refilled with the next job's paths), inside one CUDA graph launch whose
+ * device-side loop runs until every job's paths are done. Per-path results
+ * are the plain render's; films are accumulated in FP64. */
+typedef struct orion_job {
+  orion_scene_id scene;
+  int32_t reserved;
+  orion_render_params params;  /* spp 0 = scene's; max_depth -1 = scene's; rr_depth; first_pass */
+  double* sum;                 /* host W*H*3 FP64 radiance sums, or NULL */
+  double* sumsq;               /* host W*H*3 FP64 sums of squares, or NULL */
+  uint32_t* count;             /* host W*H samples per pixel, or NULL */
+} orion_job;
+
+typedef struct orion_batch_stats {
+  int64_t paths;               /* camera paths traced */
+  int64_t rays;                /* extension + shadow + MIS rays */
+  int64_t iterations;          /* device loop iterations */
+  int64_t capacity;            /* path slots in the pool */
+  double device_ms;            /* device time of the graph launch */
+} orion_batch_stats;
+
+int orion_gpu_render_batch(orion_gpu_ctx* ctx, int32_t njobs, const orion_job* jobs, orion_batch_stats* stats);
+
+/* Launch configuration: the autotuned knobs. */
+typedef struct orion_launch_config {
+  int32_t trace_block;    /* threads per block of the traversal kernels (64..512) */
+  int32_t shade_block;    /* threads per block of the shading kernels (64..512) */
+  int32_t smem_stack;     /* traversal stack entries kept in shared memory: 0, 8, 16, 24 or 32 */
+  int32_t blocks_per_sm;  /* grid size factor of the grid-stride kernels */
+  int32_t wave_paths;     /* paths per plain-render wave */
+  int32_t batch_slots;    /* path slots of the batched pool */
+} orion_launch_config;
+
+int orion_gpu_get_config(orion_gpu_ctx* ctx, orion_launch_config* out);
+int orion_gpu_set_config(orion_gpu_ctx* ctx, const orion_launch_config* cfg);
+
+/* Autotuner: times renders of `id` (at `spp` samples per pixel) over a grid
+ * of launch configurations within about `budget_ms` of device time, keeps
+ * the fastest on the context and returns it. */
+int orion_gpu_autotune(orion_gpu_ctx* ctx, orion_scene_id id, int32_t spp, double budget_ms,
+                       orion_launch_config* best, double* best_mpaths);
+
 /* ------------------------------------------------- component test hooks */
 /* sobol::sample (src/sampler/sobol.h:28-43) for n (index, dim) pairs. */
 int orion_gpu_sobol(orion_gpu_ctx* ctx, int64_t n, const uint64_t* index, const uint32_t* dim, float* out);

@@ -88,6 +88,21 @@ class StageTimes(C.Structure):
 
 STAGES = ("camera", "trace_ext", "shade", "trace_shadow", "trace_mis", "resolve", "film", "other")
 
+
+class Job(C.Structure):
+    _fields_ = [("scene", C.c_int32), ("reserved", C.c_int32), ("params", RenderParams), ("sum", C.c_void_p),
+                ("sumsq", C.c_void_p), ("count", C.c_void_p)]
+
+
+class BatchStats(C.Structure):
+    _fields_ = [("paths", C.c_int64), ("rays", C.c_int64), ("iterations", C.c_int64), ("capacity", C.c_int64),
+                ("device_ms", C.c_double)]
+
+
+class LaunchConfig(C.Structure):
+    _fields_ = [("trace_block", C.c_int32), ("shade_block", C.c_int32), ("smem_stack", C.c_int32),
+                ("blocks_per_sm", C.c_int32), ("wave_paths", C.c_int32), ("batch_slots", C.c_int32)]
+
 _lib = None
 
 
@@ -115,6 +130,10 @@ def library() -> C.CDLL:
             "orion_gpu_last_stats": (i32, [vp, C.POINTER(RenderStats)]),
             "orion_gpu_set_profiling": (i32, [vp, i32]),
             "orion_gpu_stage_times": (i32, [vp, C.POINTER(StageTimes)]),
+            "orion_gpu_render_batch": (i32, [vp, i32, vp, C.POINTER(BatchStats)]),
+            "orion_gpu_get_config": (i32, [vp, C.POINTER(LaunchConfig)]),
+            "orion_gpu_set_config": (i32, [vp, C.POINTER(LaunchConfig)]),
+            "orion_gpu_autotune": (i32, [vp, i32, i32, C.c_double, C.POINTER(LaunchConfig), C.POINTER(C.c_double)]),
             "orion_gpu_sobol": (i32, [vp, i64, vp, vp, vp]),
             "orion_gpu_trace": (i32, [vp, i32, i64, vp, i32, vp, vp, vp, vp]),
             "orion_gpu_camera_rays": (i32, [vp, i32, i64, vp, vp]),
@@ -270,6 +289,43 @@ class Context:
         t = StageTimes()
         _check(library().orion_gpu_stage_times(self._h, C.byref(t)))
         return {name: {"ms": t.ms[i], "launches": t.launches[i]} for i, name in enumerate(STAGES)}
+
+    def render_batch(self, jobs: list) -> tuple:
+        """jobs: dicts with sid, width, height and optional spp, max_depth, rr_depth, first_pass.
+
+        Returns ([(sum, sumsq, count) per job], stats): FP64 (H, W, 3) sums and
+        sums of squares, (H, W) sample counts.
+        """
+        arr = (Job * max(1, len(jobs)))()
+        outs = []
+        for i, j in enumerate(jobs):
+            h, w = j["height"], j["width"]
+            s, q = np.zeros((h, w, 3), np.float64), np.zeros((h, w, 3), np.float64)
+            c = np.zeros((h, w), np.uint32)
+            outs.append((s, q, c))
+            arr[i].scene = j["sid"]
+            arr[i].params = RenderParams(spp=j.get("spp", 0), max_depth=j.get("max_depth", -1),
+                                         rr_depth=j.get("rr_depth", 3), first_pass=j.get("first_pass", 0))
+            arr[i].sum, arr[i].sumsq, arr[i].count = s.ctypes.data, q.ctypes.data, c.ctypes.data
+        st = BatchStats()
+        _check(library().orion_gpu_render_batch(self._h, len(jobs), C.cast(arr, C.c_void_p), C.byref(st)))
+        return outs, {k: getattr(st, k) for k, _ in BatchStats._fields_}
+
+    def get_config(self) -> dict:
+        c = LaunchConfig()
+        _check(library().orion_gpu_get_config(self._h, C.byref(c)))
+        return {k: getattr(c, k) for k, _ in LaunchConfig._fields_}
+
+    def set_config(self, **kw) -> None:
+        cur = self.get_config()
+        cur.update(kw)
+        _check(library().orion_gpu_set_config(self._h, C.byref(LaunchConfig(**cur))))
+
+    def autotune(self, sid: int, spp: int = 1, budget_ms: float = 2000.0) -> tuple:
+        c = LaunchConfig()
+        mp = C.c_double()
+        _check(library().orion_gpu_autotune(self._h, sid, spp, budget_ms, C.byref(c), C.byref(mp)))
+        return {k: getattr(c, k) for k, _ in LaunchConfig._fields_}, mp.value
 
     # component hooks -----------------------------------------------------
     def sobol(self, index, dim) -> np.ndarray:

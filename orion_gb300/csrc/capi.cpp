@@ -97,7 +97,7 @@ struct orion_gpu_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
   int num_sms = 0;
-  DevBuf sobol;
+  DevBuf sobol, sobol_bitmajor;
   std::map<int, std::unique_ptr<DeviceScene>> scenes;
   int next_id = 1;
   Wave wave;
@@ -112,6 +112,16 @@ struct orion_gpu_ctx {
   std::vector<cudaEvent_t> prof_events;
   std::vector<int> prof_stage;
   orion_stage_times stage_times{};
+  // batched mode
+  DevBuf b_job_of, b_bounce_of, b_index_of, b_retire, b_free, b_ctl, b_jobs, b_films;
+  int batch_slots_alloc = 0;
+  int jobs_alloc = 0;
+  int default_batch_slots = 1 << 22;
+  cudaGraph_t bgraph = nullptr;
+  cudaGraphExec_t bexec = nullptr;
+  const void* bgraph_key[4] = {nullptr, nullptr, nullptr, nullptr};
+  LaunchConfig bgraph_cfg{};
+  int bgraph_slots = 0;
   std::mutex mu;
 };
 
@@ -237,6 +247,11 @@ extern "C" int orion_gpu_create(const orion_gpu_opts* opts, orion_gpu_ctx** out)
   int rc = c->sobol.alloc(m.size() * sizeof(uint32_t));
   if (rc != ORION_OK) return rc;
   CUDA_TRY(cudaMemcpy(c->sobol.p, m.data(), m.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
+  std::vector<uint32_t> bm(m.size());
+  for (int d = 0; d < 1024; ++d)
+    for (int b = 0; b < 52; ++b) bm[(size_t)b * 1024 + d] = m[(size_t)d * 52 + b];
+  if ((rc = c->sobol_bitmajor.alloc(bm.size() * sizeof(uint32_t))) != ORION_OK) return rc;
+  CUDA_TRY(cudaMemcpy(c->sobol_bitmajor.p, bm.data(), bm.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
   c->cfg.num_sms = c->num_sms;
   c->cfg.trace_block = 128;
   c->cfg.shade_block = 128;
@@ -252,6 +267,8 @@ extern "C" int orion_gpu_destroy(orion_gpu_ctx* ctx) {
   cudaStreamSynchronize(ctx->stream);
   ctx->scenes.clear();
   ctx->wave.block.alloc(0);
+  if (ctx->bexec) cudaGraphExecDestroy(ctx->bexec);
+  if (ctx->bgraph) cudaGraphDestroy(ctx->bgraph);
   for (cudaEvent_t e : ctx->prof_events) cudaEventDestroy(e);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
@@ -353,9 +370,10 @@ extern "C" int orion_gpu_scene_bytes(orion_gpu_ctx* ctx, orion_scene_id id, int6
 // ------------------------------------------------------------- render
 
 static int render_impl(orion_gpu_ctx* ctx, orion_scene_id id, const orion_render_params* params, float* film_rgb,
-                       uint32_t* film_count, double* sum64, double* sumsq64) {
+                       uint32_t* film_count, double* sum64, double* sumsq64, bool take_lock = true) {
   if (!ctx) return fail(ORION_ERR_INVALID, "null context");
-  std::lock_guard<std::mutex> g(ctx->mu);
+  std::unique_lock<std::mutex> g(ctx->mu, std::defer_lock);
+  if (take_lock) g.lock();
   CUDA_TRY(cudaSetDevice(ctx->device));
   auto it = ctx->scenes.find(id);
   if (it == ctx->scenes.end()) return fail(ORION_ERR_INVALID, "unknown scene id");
@@ -405,6 +423,7 @@ static int render_impl(orion_gpu_ctx* ctx, orion_scene_id id, const orion_render
   for (int64_t off = 0; off < total; off += wave) {
     WaveArgs a;
     a.sobol = ctx->sobol.as<uint32_t>();
+    a.sobol_bitmajor = ctx->sobol_bitmajor.as<uint32_t>();
     a.base_index = first + off;
     a.n_paths = (int)std::min<int64_t>(wave, total - off);
     a.width = d.width;
@@ -475,6 +494,275 @@ extern "C" int orion_gpu_set_profiling(orion_gpu_ctx* ctx, int32_t enable) {
 extern "C" int orion_gpu_stage_times(orion_gpu_ctx* ctx, orion_stage_times* out) {
   if (!ctx || !out) return fail(ORION_ERR_INVALID, "null argument");
   *out = ctx->stage_times;
+  return ORION_OK;
+}
+
+// ------------------------------------------------------------ batches
+
+static int build_batch_graph(orion_gpu_ctx* ctx, const BatchView& bv, int slots) {
+  const void* key[4] = {ctx->wave.block.p, ctx->b_jobs.p, ctx->b_job_of.p, ctx->b_ctl.p};
+  bool same = ctx->bexec && ctx->bgraph_slots == slots && std::memcmp(key, ctx->bgraph_key, sizeof(key)) == 0 &&
+              std::memcmp(&ctx->bgraph_cfg, &ctx->cfg, sizeof(LaunchConfig)) == 0;
+  if (same) return ORION_OK;
+  if (ctx->bexec) cudaGraphExecDestroy(ctx->bexec);
+  if (ctx->bgraph) cudaGraphDestroy(ctx->bgraph);
+  ctx->bexec = nullptr;
+  ctx->bgraph = nullptr;
+  CUDA_TRY(cudaGraphCreate(&ctx->bgraph, 0));
+  cudaGraphConditionalHandle cond;
+  CUDA_TRY(cudaGraphConditionalHandleCreate(&cond, ctx->bgraph, 1, cudaGraphCondAssignDefault));
+  // cudaGraphNodeParams has no usable default constructor in host C++;
+  // zeroed storage is its documented initial state.
+  alignas(cudaGraphNodeParams) unsigned char np_storage[sizeof(cudaGraphNodeParams)] = {};
+  cudaGraphNodeParams& np = *reinterpret_cast<cudaGraphNodeParams*>(np_storage);
+  np.type = cudaGraphNodeTypeConditional;
+  np.conditional.handle = cond;
+  np.conditional.type = cudaGraphCondTypeWhile;
+  np.conditional.size = 1;
+  cudaGraphNode_t node;
+  CUDA_TRY(cudaGraphAddNode(&node, ctx->bgraph, nullptr, nullptr, 0, &np));
+  cudaGraph_t body = np.conditional.phGraph_out[0];
+  CUDA_TRY(capture_batch_iteration(ctx->wave.view, bv, ctx->sobol.as<uint32_t>(), ctx->sobol_bitmajor.as<uint32_t>(),
+                                   ctx->cfg, cond, ctx->stream, body));
+  CUDA_TRY(cudaGraphInstantiate(&ctx->bexec, ctx->bgraph, 0));
+  std::memcpy(ctx->bgraph_key, key, sizeof(key));
+  ctx->bgraph_cfg = ctx->cfg;
+  ctx->bgraph_slots = slots;
+  return ORION_OK;
+}
+
+extern "C" int orion_gpu_render_batch(orion_gpu_ctx* ctx, int32_t njobs, const orion_job* jobs,
+                                      orion_batch_stats* stats) {
+  if (!ctx || njobs < 0 || (njobs > 0 && !jobs)) return fail(ORION_ERR_INVALID, "bad argument");
+  std::lock_guard<std::mutex> g(ctx->mu);
+  CUDA_TRY(cudaSetDevice(ctx->device));
+  if (njobs == 0) {
+    if (stats) std::memset(stats, 0, sizeof(*stats));
+    return ORION_OK;
+  }
+  // Job table and film layout.
+  std::vector<DevJob> dj(njobs);
+  std::vector<size_t> film_off(njobs);
+  size_t film_bytes = 0;
+  unsigned long long total = 0;
+  int max_depth_all = 0;
+  for (int i = 0; i < njobs; ++i) {
+    auto it = ctx->scenes.find(jobs[i].scene);
+    if (it == ctx->scenes.end()) return fail(ORION_ERR_INVALID, "job " + std::to_string(i) + ": unknown scene id");
+    const DeviceScene& d = *it->second;
+    const orion_render_params& p = jobs[i].params;
+    DevJob& J = dj[i];
+    std::memset(&J, 0, sizeof(J));
+    J.scene = d.view;
+    J.width = d.width;
+    J.height = d.height;
+    const int spp = p.spp > 0 ? p.spp : d.spp;
+    J.max_depth = p.max_depth >= 0 ? p.max_depth : d.max_depth;
+    J.rr_depth = p.rr_depth;
+    if (J.max_depth > 120 || 17 + 8 * (int64_t)J.max_depth > 1024)
+      return fail(ORION_ERR_INVALID, "job " + std::to_string(i) + ": max_depth out of range");
+    const long long wh = (long long)d.width * d.height;
+    J.first_index = p.first_pass * wh;
+    J.num_paths = wh * spp;
+    J.work_begin = (long long)total;
+    total += (unsigned long long)J.num_paths;
+    max_depth_all = std::max(max_depth_all, J.max_depth);
+    film_off[i] = film_bytes;
+    film_bytes += (size_t)((wh * (3 * 8 * 2 + 4) + 255) & ~255LL);
+  }
+  const int slots = (int)std::min<unsigned long long>((unsigned long long)ctx->default_batch_slots,
+                                                       std::max<unsigned long long>(total, 1024ULL));
+  int rc;
+  if ((rc = ensure_wave(ctx, slots)) != ORION_OK) return rc;
+  const int cap = ctx->wave.capacity;
+  if (ctx->batch_slots_alloc < cap) {
+    if ((rc = ctx->b_job_of.alloc((size_t)cap * 4)) != ORION_OK) return rc;
+    if ((rc = ctx->b_bounce_of.alloc((size_t)cap * 4)) != ORION_OK) return rc;
+    if ((rc = ctx->b_index_of.alloc((size_t)cap * 8)) != ORION_OK) return rc;
+    if ((rc = ctx->b_retire.alloc((size_t)cap * 4)) != ORION_OK) return rc;
+    if ((rc = ctx->b_free.alloc((size_t)cap * 4)) != ORION_OK) return rc;
+    ctx->batch_slots_alloc = cap;
+  }
+  if (!ctx->b_ctl.p && (rc = ctx->b_ctl.alloc(sizeof(BatchCtl))) != ORION_OK) return rc;
+  if (ctx->jobs_alloc < njobs) {
+    int n = std::max(njobs, 64);
+    if ((rc = ctx->b_jobs.alloc((size_t)n * sizeof(DevJob))) != ORION_OK) return rc;
+    ctx->jobs_alloc = n;
+  }
+  if (ctx->b_films.bytes < film_bytes && (rc = ctx->b_films.alloc(film_bytes)) != ORION_OK) return rc;
+  char* fb = ctx->b_films.as<char>();
+  for (int i = 0; i < njobs; ++i) {
+    const long long wh = (long long)dj[i].width * dj[i].height;
+    dj[i].sum = reinterpret_cast<double*>(fb + film_off[i]);
+    dj[i].sumsq = dj[i].sum + 3 * wh;
+    dj[i].count = reinterpret_cast<unsigned int*>(dj[i].sumsq + 3 * wh);
+  }
+  BatchView bv;
+  bv.jobs = ctx->b_jobs.as<DevJob>();
+  bv.ctl = ctx->b_ctl.as<BatchCtl>();
+  bv.job_of = ctx->b_job_of.as<int>();
+  bv.bounce_of = ctx->b_bounce_of.as<int>();
+  bv.index_of = ctx->b_index_of.as<long long>();
+  bv.q_retire = ctx->b_retire.as<int>();
+  bv.q_free = ctx->b_free.as<int>();
+  if ((rc = build_batch_graph(ctx, bv, cap)) != ORION_OK) return rc;
+
+  BatchCtl c;
+  std::memset(&c, 0, sizeof(c));
+  c.total = total;
+  c.njobs = njobs;
+  c.counters[CNT_FREE] = cap;
+  // Every live path advances one bounce per iteration: a bound on the loop.
+  const unsigned long long refills = (total + cap - 1) / cap + 1;
+  c.max_iterations = (int)std::min<unsigned long long>(2ULL * refills * (max_depth_all + 2) + 64, 1u << 30);
+  cudaStream_t s = ctx->stream;
+  CUDA_TRY(cudaMemcpyAsync(bv.jobs, dj.data(), njobs * sizeof(DevJob), cudaMemcpyHostToDevice, s));
+  CUDA_TRY(cudaMemcpyAsync(bv.ctl, &c, sizeof(c), cudaMemcpyHostToDevice, s));
+  CUDA_TRY(cudaMemsetAsync(ctx->b_films.p, 0, film_bytes, s));
+  launch_batch_init(ctx->wave.view, bv, cap, s);
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaEventRecord(ctx->ev0, s));
+  CUDA_TRY(cudaGraphLaunch(ctx->bexec, s));
+  CUDA_TRY(cudaEventRecord(ctx->ev1, s));
+  BatchCtl out;
+  CUDA_TRY(cudaMemcpyAsync(&out, bv.ctl, sizeof(out), cudaMemcpyDeviceToHost, s));
+  for (int i = 0; i < njobs; ++i) {
+    const size_t wh = (size_t)dj[i].width * dj[i].height;
+    if (jobs[i].sum) CUDA_TRY(cudaMemcpyAsync(jobs[i].sum, dj[i].sum, wh * 24, cudaMemcpyDeviceToHost, s));
+    if (jobs[i].sumsq) CUDA_TRY(cudaMemcpyAsync(jobs[i].sumsq, dj[i].sumsq, wh * 24, cudaMemcpyDeviceToHost, s));
+    if (jobs[i].count) CUDA_TRY(cudaMemcpyAsync(jobs[i].count, dj[i].count, wh * 4, cudaMemcpyDeviceToHost, s));
+  }
+  CUDA_TRY(cudaStreamSynchronize(s));
+  float ms = 0.f;
+  CUDA_TRY(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+  if (stats) {
+    stats->paths = (int64_t)out.paths_done;
+    stats->rays = (int64_t)(out.rays[0] + out.rays[1] + out.rays[2]);
+    stats->iterations = out.iterations;
+    stats->capacity = cap;
+    stats->device_ms = ms;
+  }
+  ctx->last.paths = (int64_t)out.paths_done;
+  ctx->last.ext_rays = (int64_t)out.rays[0];
+  ctx->last.shadow_rays = (int64_t)out.rays[1];
+  ctx->last.mis_rays = (int64_t)out.rays[2];
+  ctx->last.rays = (int64_t)(out.rays[0] + out.rays[1] + out.rays[2]);
+  ctx->last.kernel_launches = 9LL * out.iterations + 1;
+  ctx->last.device_ms = ms;
+  if (out.error) return fail(ORION_ERR_DEVICE, "batch loop reached its iteration cap");
+  if (out.paths_done != total)
+    return fail(ORION_ERR_DEVICE, "batch finished " + std::to_string(out.paths_done) + " of " + std::to_string(total) +
+                                      " paths");
+  return ORION_OK;
+}
+
+// ---------------------------------------------------- launch config, tuning
+
+extern "C" int orion_gpu_get_config(orion_gpu_ctx* ctx, orion_launch_config* out) {
+  if (!ctx || !out) return fail(ORION_ERR_INVALID, "null argument");
+  out->trace_block = ctx->cfg.trace_block;
+  out->shade_block = ctx->cfg.shade_block;
+  out->smem_stack = ctx->cfg.smem_stack;
+  out->blocks_per_sm = ctx->cfg.blocks_per_sm;
+  out->wave_paths = ctx->default_wave;
+  out->batch_slots = ctx->default_batch_slots;
+  return ORION_OK;
+}
+
+static bool valid_block(int b) { return b >= 32 && b <= 1024 && b % 32 == 0; }
+
+extern "C" int orion_gpu_set_config(orion_gpu_ctx* ctx, const orion_launch_config* cfg) {
+  if (!ctx || !cfg) return fail(ORION_ERR_INVALID, "null argument");
+  const int st = cfg->smem_stack;
+  if (!valid_block(cfg->trace_block) || !valid_block(cfg->shade_block) ||
+      !(st == 0 || st == 8 || st == 16 || st == 24 || st == 32) || cfg->blocks_per_sm < 1 || cfg->blocks_per_sm > 64 ||
+      cfg->wave_paths < 1024 || cfg->batch_slots < 1024)
+    return fail(ORION_ERR_INVALID, "launch configuration out of range");
+  if ((size_t)st * cfg->trace_block * 8 > 96 * 1024) return fail(ORION_ERR_INVALID, "traversal stack too large");
+  std::lock_guard<std::mutex> g(ctx->mu);
+  ctx->cfg.trace_block = cfg->trace_block;
+  ctx->cfg.shade_block = cfg->shade_block;
+  ctx->cfg.smem_stack = st;
+  ctx->cfg.blocks_per_sm = cfg->blocks_per_sm;
+  ctx->default_wave = cfg->wave_paths;
+  ctx->default_batch_slots = cfg->batch_slots;
+  return ORION_OK;
+}
+
+// Coordinate descent over the launch knobs: each knob in turn is swept with
+// the others held at the best values so far; each trial is one timed render
+// (device time), repeated until the budget is used.
+extern "C" int orion_gpu_autotune(orion_gpu_ctx* ctx, orion_scene_id id, int32_t spp, double budget_ms,
+                                  orion_launch_config* best_out, double* best_mpaths) {
+  if (!ctx) return fail(ORION_ERR_INVALID, "null context");
+  std::lock_guard<std::mutex> g(ctx->mu);
+  auto it = ctx->scenes.find(id);
+  if (it == ctx->scenes.end()) return fail(ORION_ERR_INVALID, "unknown scene id");
+  const DeviceScene& d = *it->second;
+  const int64_t paths = (int64_t)d.width * d.height * std::max(1, spp);
+  orion_render_params p{};
+  p.spp = std::max(1, spp);
+  p.max_depth = -1;
+  p.rr_depth = 3;
+  LaunchConfig best = ctx->cfg;
+  int best_wave = ctx->default_wave;
+  double best_ms = 1e30, used = 0;
+  auto trial = [&](const LaunchConfig& c, int wave, double* ms) -> int {
+    LaunchConfig saved = ctx->cfg;
+    int saved_wave = ctx->default_wave;
+    ctx->cfg = c;
+    ctx->default_wave = wave;
+    int rc = render_impl(ctx, id, &p, nullptr, nullptr, nullptr, nullptr, false);
+    *ms = ctx->last.device_ms;
+    ctx->cfg = saved;
+    ctx->default_wave = saved_wave;
+    used += *ms;
+    return rc;
+  };
+  double ms;
+  int rc = trial(best, best_wave, &ms);  // warm-up and baseline
+  if (rc != ORION_OK) return rc;
+  rc = trial(best, best_wave, &best_ms);
+  if (rc != ORION_OK) return rc;
+  const int trace_blocks[] = {64, 128, 256};
+  const int stacks[] = {8, 16, 32};
+  const int shade_blocks[] = {64, 128, 256};
+  const int bpsm[] = {4, 8, 16};
+  const int waves[] = {1 << 20, 1 << 21, 1 << 22, 1 << 23};
+  for (int knob = 0; knob < 5 && used < budget_ms; ++knob) {
+    int n = knob == 4 ? 4 : 3;
+    for (int v = 0; v < n && used < budget_ms; ++v) {
+      LaunchConfig c = best;
+      int wave = best_wave;
+      if (knob == 0) c.trace_block = trace_blocks[v];
+      if (knob == 1) c.smem_stack = stacks[v];
+      if (knob == 2) c.shade_block = shade_blocks[v];
+      if (knob == 3) c.blocks_per_sm = bpsm[v];
+      if (knob == 4) wave = waves[v];
+      if (wave > 2 * paths && wave != best_wave) continue;
+      if (std::memcmp(&c, &best, sizeof(c)) == 0 && wave == best_wave) continue;
+      rc = trial(c, wave, &ms);
+      if (rc == ORION_ERR_NOMEM) continue;
+      if (rc != ORION_OK) return rc;
+      if (ms < best_ms) {
+        best_ms = ms;
+        best = c;
+        best_wave = wave;
+      }
+    }
+  }
+  ctx->cfg = best;
+  ctx->default_wave = best_wave;
+  ctx->default_batch_slots = best_wave;
+  if (best_out) {
+    best_out->trace_block = best.trace_block;
+    best_out->shade_block = best.shade_block;
+    best_out->smem_stack = best.smem_stack;
+    best_out->blocks_per_sm = best.blocks_per_sm;
+    best_out->wave_paths = best_wave;
+    best_out->batch_slots = best_wave;
+  }
+  if (best_mpaths) *best_mpaths = paths / (best_ms * 1e-3) / 1e6;
   return ORION_OK;
 }
 

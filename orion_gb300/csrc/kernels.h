@@ -53,10 +53,56 @@ struct WaveView {
   int capacity;
 };
 
-enum CounterSlot { CNT_EXT0 = 0, CNT_EXT1 = 1, CNT_NEE = 2, CNT_SH = 3, CNT_MIS = 4, kCounterSlots = 8 };
+enum CounterSlot { CNT_EXT0 = 0, CNT_EXT1 = 1, CNT_NEE = 2, CNT_SH = 3, CNT_MIS = 4, CNT_RETIRE = 5, CNT_FREE = 6,
+                   kCounterSlots = 8 };
+
+// ------------------------------------------------------------ batched mode
+//
+// Many render jobs (scenes, views, resolutions, spp, depths) share one pool
+// of path slots. Each loop iteration refills free slots from the global work
+// list (job by job, sample index by sample index), runs one bounce for every
+// live path, and retires finished paths into their job's FP64 film.
+
+struct DevJob {
+  SceneView scene;
+  int width, height;
+  int max_depth, rr_depth;
+  long long first_index;  // sample index of the job's first path: k0 * W * H
+  long long num_paths;    // W * H * spp
+  long long work_begin;   // offset of the job in the global work list
+  double* sum;            // W*H*3
+  double* sumsq;          // W*H*3
+  unsigned int* count;    // W*H
+};
+
+struct BatchCtl {
+  unsigned long long cursor;     // next work item
+  unsigned long long total;      // total work items
+  unsigned long long take_base;  // first work item taken this iteration
+  int take;                      // slots refilled this iteration
+  int cur;                       // parity of the current extension queue
+  int counters[kCounterSlots];
+  int njobs;
+  int iterations;
+  int max_iterations;
+  int error;                     // 1: iteration cap reached
+  unsigned long long rays[3];    // ext, shadow, mis
+  unsigned long long paths_done;
+};
+
+struct BatchView {
+  DevJob* jobs;
+  BatchCtl* ctl;
+  int* job_of;          // per slot
+  int* bounce_of;       // per slot
+  long long* index_of;  // per slot
+  int* q_retire;
+  int* q_free;
+};
 
 struct WaveArgs {
-  const uint32_t* sobol;
+  const uint32_t* sobol;          // dimension-major Sobol matrices (1024 x 52)
+  const uint32_t* sobol_bitmajor; // the same words bit-major (52 x 1024)
   int64_t base_index;  // sample index of path slot 0
   int n_paths;
   int width, height;
@@ -104,6 +150,15 @@ struct StageTimer {
 // resolve) per bounce, then film accumulation. All on `stream`, no host sync.
 void launch_wave(const SceneView& s, const WaveView& w, const WaveArgs& a, const FilmView& film,
                  const LaunchConfig& cfg, cudaStream_t stream, int* launches, StageTimer* timer = nullptr);
+
+// Batched mode: builds the body of the device-side loop (one iteration)
+// into `body` by stream capture on `stream`. The loop keeps running while
+// work or live paths remain; `cond` is the graph's while-condition handle.
+cudaError_t capture_batch_iteration(const WaveView& w, const BatchView& b, const uint32_t* sobol,
+                                    const uint32_t* sobol_bitmajor, const LaunchConfig& cfg,
+                                    cudaGraphConditionalHandle cond, cudaStream_t stream, cudaGraph_t body);
+// Resets the batch control block and the free-slot list for `capacity` slots.
+void launch_batch_init(const WaveView& w, const BatchView& b, int capacity, cudaStream_t stream);
 
 // Component hooks for the parity tests.
 void launch_sobol(const uint32_t* sobol, int64_t n, const uint64_t* index, const uint32_t* dim, float* out,
