@@ -101,7 +101,8 @@ class BatchStats(C.Structure):
 
 class LaunchConfig(C.Structure):
     _fields_ = [("trace_block", C.c_int32), ("shade_block", C.c_int32), ("smem_stack", C.c_int32),
-                ("blocks_per_sm", C.c_int32), ("wave_paths", C.c_int32), ("batch_slots", C.c_int32)]
+                ("blocks_per_sm", C.c_int32), ("wave_paths", C.c_int32), ("batch_slots", C.c_int32),
+                ("refill_below", C.c_int32), ("reserved", C.c_int32)]
 
 _lib = None
 

@@ -1,0 +1,230 @@
+// Batched wavefront path tracing: many render jobs in one graph launch.
+//
+// The jobs' sample ranges are concatenated into one work list. A pool of
+// path slots is shared by all jobs; one iteration of the device-side loop
+//
+//   k_b_plan     take = min(free slots, work left); reset this iteration's queues
+//   k_b_regen    start `take` new camera paths in free slots (Pinhole::generateRay)
+//   k_b_trace    closest hit for every live path (each against its job's scene)
+//   k_b_shade    one bounce of PathTracing::Li per path (shared shade_one)
+//   k_b_trace    shadow rays (any hit) and MIS rays (closest hit)
+//   k_b_resolve  direct-light estimate into the path radiance
+//   k_b_retire   finished paths: radiance into the job's FP64 film, slot freed
+//   k_b_control  flip queues; keep looping while work or live paths remain
+//
+// runs inside a CUDA graph while-node, so the whole batch is a single
+// cudaGraphLaunch. Paths of different jobs, depths and bounces share every
+// launch; finished slots are refilled each iteration, so the trace kernels
+// see a full pool until the work list runs dry. Each path's arithmetic is
+// exactly the plain path's; only the film's order of accumulation differs
+// (FP64 atomics, so the per-pixel sums agree to FP64 rounding).
+#include <cuda_runtime.h>
+
+#include "kernels.h"
+#include "shade.cuh"
+
+namespace orion_gb300 {
+
+namespace {
+
+__global__ void k_b_init(BatchView b, int capacity) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < capacity; i += gridDim.x * blockDim.x) b.q_free[i] = i;
+}
+
+__global__ void k_b_plan(BatchView b) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  BatchCtl& c = *b.ctl;
+  unsigned long long rem = c.total - c.cursor;
+  int nfree = c.counters[CNT_FREE];
+  int take = (unsigned long long)nfree < rem ? nfree : (int)rem;
+  c.take = take;
+  c.take_base = c.cursor;
+  c.cursor += (unsigned long long)take;
+  c.counters[CNT_FREE] = nfree - take;
+  c.counters[CNT_NEE] = 0;
+  c.counters[CNT_SH] = 0;
+  c.counters[CNT_MIS] = 0;
+  c.counters[CNT_RETIRE] = 0;
+  c.counters[CNT_EXT0 + (c.cur ^ 1)] = 0;
+  c.counters[CNT_FETCH_EXT] = 0;
+  c.counters[CNT_FETCH_SH] = 0;
+  c.counters[CNT_FETCH_MIS] = 0;
+}
+
+__device__ __forceinline__ int job_of_work(const DevJob* jobs, int njobs, unsigned long long work) {
+  int lo = 0, hi = njobs - 1;
+  while (lo < hi) {  // last job with work_begin <= work
+    int mid = (lo + hi + 1) >> 1;
+    if ((unsigned long long)jobs[mid].work_begin <= work)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  return lo;
+}
+
+__global__ void k_b_regen(WaveView w, BatchView b, const uint32_t* sobol) {
+  BatchCtl& c = *b.ctl;
+  const int take = c.take;
+  const int free_after = c.counters[CNT_FREE];
+  const int cur = c.cur;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < take; i += gridDim.x * blockDim.x) {
+    const int slot = b.q_free[free_after + i];
+    const unsigned long long work = c.take_base + (unsigned long long)i;
+    const int job = job_of_work(b.jobs, c.njobs, work);
+    const DevJob& J = b.jobs[job];
+    const long long index = J.first_index + (long long)(work - (unsigned long long)J.work_begin);
+    const long long wh = (long long)J.width * J.height;
+    const long long pix = index % wh;
+    PathSampler smp{sobol, (uint64_t)index, 5u};
+    V3 o, d;
+    camera_ray(J.scene.cam, smp, (int)(pix % J.width), (int)(pix / J.width), &o, &d);
+    w.ray_o[slot] = f4(o, 0.f);
+    w.ray_d[slot] = f4(d, 0.f);
+    w.beta[slot] = make_float4(1.f, 1.f, 1.f, 0.f);
+    w.L[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
+    w.dim[slot] = (int)smp.dim;
+    b.job_of[slot] = job;
+    b.bounce_of[slot] = 0;
+    b.index_of[slot] = index;
+    queue_append(&c.counters[CNT_EXT0 + cur], w.q_ext[cur], slot, true);
+  }
+}
+
+// kind 0: extension rays (current queue), 1: shadow rays, 2: MIS rays.
+template <int SMEM>
+__global__ void k_b_trace(WaveView w, BatchView b, int kind, int refill_below) {
+  extern __shared__ int2 stack_smem[];
+  BatchCtl& c = *b.ctl;
+  JobScene js{b.jobs, b.job_of};
+  int n;
+  if (kind == 0) {
+    n = c.counters[CNT_EXT0 + c.cur];
+    trace_persistent<false, SMEM>(js, w.q_ext[c.cur], n, &c.counters[CNT_FETCH_EXT], w.ray_o, w.ray_d, w.hit,
+                                  nullptr, stack_smem, refill_below);
+  } else if (kind == 1) {
+    n = c.counters[CNT_SH];
+    trace_persistent<true, SMEM>(js, w.q_sh, n, &c.counters[CNT_FETCH_SH], w.sh_o, w.sh_d, nullptr, w.occluded,
+                                 stack_smem, refill_below);
+  } else {
+    n = c.counters[CNT_MIS];
+    trace_persistent<false, SMEM>(js, w.q_mis, n, &c.counters[CNT_FETCH_MIS], w.mis_o, w.mis_d, w.mis_hit, nullptr,
+                                  stack_smem, refill_below);
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&c.rays[kind], (unsigned long long)n);
+}
+
+__global__ void k_b_shade(WaveView w, BatchView b, const uint32_t* sobol_bitmajor) {
+  BatchCtl& c = *b.ctl;
+  const int cur = c.cur;
+  const int n = c.counters[CNT_EXT0 + cur];
+  const int* in_q = w.q_ext[cur];
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+    const int pid = in_q[q];
+    const DevJob& J = b.jobs[b.job_of[pid]];
+    const int bounce = b.bounce_of[pid];
+    ShadeResult r = shade_one(J.scene, w, sobol_bitmajor, pid, (uint64_t)b.index_of[pid], bounce, J.max_depth,
+                              J.rr_depth);
+    if (r.alive) b.bounce_of[pid] = bounce + 1;
+    queue_append(&c.counters[CNT_NEE], w.q_nee, pid, r.did_nee);
+    queue_append(&c.counters[CNT_SH], w.q_sh, pid, r.want_sh);
+    queue_append(&c.counters[CNT_MIS], w.q_mis, pid, r.want_mis);
+    queue_append(&c.counters[CNT_EXT0 + (cur ^ 1)], w.q_ext[cur ^ 1], pid, r.alive);
+    queue_append(&c.counters[CNT_RETIRE], b.q_retire, pid, !r.alive);
+  }
+}
+
+__global__ void k_b_resolve(WaveView w, BatchView b) {
+  const int n = b.ctl->counters[CNT_NEE];
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+    const int pid = w.q_nee[q];
+    resolve_one(b.jobs[b.job_of[pid]].scene, w, pid);
+  }
+}
+
+__global__ void k_b_retire(WaveView w, BatchView b) {
+  BatchCtl& c = *b.ctl;
+  const int n = c.counters[CNT_RETIRE];
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+    const int pid = b.q_retire[q];
+    const DevJob& J = b.jobs[b.job_of[pid]];
+    const long long pix = b.index_of[pid] % ((long long)J.width * J.height);
+    const float4 l = w.L[pid];
+    atomicAdd(&J.sum[3 * pix], (double)l.x);
+    atomicAdd(&J.sum[3 * pix + 1], (double)l.y);
+    atomicAdd(&J.sum[3 * pix + 2], (double)l.z);
+    atomicAdd(&J.sumsq[3 * pix], (double)l.x * l.x);
+    atomicAdd(&J.sumsq[3 * pix + 1], (double)l.y * l.y);
+    atomicAdd(&J.sumsq[3 * pix + 2], (double)l.z * l.z);
+    atomicAdd(&J.count[pix], 1u);
+    queue_append(&c.counters[CNT_FREE], b.q_free, pid, true);
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&c.paths_done, (unsigned long long)n);
+}
+
+__global__ void k_b_control(BatchView b, cudaGraphConditionalHandle cond) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  BatchCtl& c = *b.ctl;
+  c.cur ^= 1;
+  c.iterations += 1;
+  bool more = c.cursor < c.total || c.counters[CNT_EXT0 + c.cur] > 0;
+  if (more && c.iterations >= c.max_iterations) {
+    c.error = 1;  // bounded loop: report instead of spinning on
+    more = false;
+  }
+  cudaGraphSetConditional(cond, more ? 1u : 0u);
+}
+
+template <int SMEM>
+void launch_b_trace(const WaveView& w, const BatchView& b, int kind, int grid, int block, int refill, cudaStream_t s) {
+  k_b_trace<SMEM><<<grid, block, (size_t)SMEM * block * sizeof(int2), s>>>(w, b, kind, refill);
+}
+
+void b_trace(const LaunchConfig& cfg, const WaveView& w, const BatchView& b, int kind, int grid, cudaStream_t s) {
+  const int block = cfg.trace_block;
+  const int refill = cfg.refill_below < 1 ? 1 : (cfg.refill_below > 32 ? 32 : cfg.refill_below);
+  switch (cfg.smem_stack) {
+    case 0: launch_b_trace<0>(w, b, kind, grid, block, refill, s); break;
+    case 8: launch_b_trace<8>(w, b, kind, grid, block, refill, s); break;
+    case 24: launch_b_trace<24>(w, b, kind, grid, block, refill, s); break;
+    case 32: launch_b_trace<32>(w, b, kind, grid, block, refill, s); break;
+    default: launch_b_trace<16>(w, b, kind, grid, block, refill, s); break;
+  }
+}
+
+int grid_cap(int64_t n, int block, int cap) {
+  int64_t g = (n + block - 1) / block;
+  return (int)(g < 1 ? 1 : (g > cap ? cap : g));
+}
+
+}  // namespace
+
+void launch_batch_init(const WaveView& w, const BatchView& b, int capacity, cudaStream_t stream) {
+  k_b_init<<<grid_cap(capacity, 256, 4096), 256, 0, stream>>>(b, capacity);
+}
+
+cudaError_t capture_batch_iteration(const WaveView& w, const BatchView& b, const uint32_t* sobol,
+                                    const uint32_t* sobol_bitmajor, const LaunchConfig& cfg,
+                                    cudaGraphConditionalHandle cond, cudaStream_t stream, cudaGraph_t body) {
+  cudaError_t e = cudaStreamBeginCaptureToGraph(stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return e;
+  const int cap = w.capacity;
+  const int persistent = cfg.num_sms * cfg.blocks_per_sm;
+  const int tgrid = grid_cap(cap, cfg.trace_block, persistent * 2);
+  const int sgrid = grid_cap(cap, cfg.shade_block, persistent * 2);
+  k_b_plan<<<1, 32, 0, stream>>>(b);
+  k_b_regen<<<grid_cap(cap, 256, persistent * 4), 256, 0, stream>>>(w, b, sobol);
+  b_trace(cfg, w, b, 0, tgrid, stream);
+  k_b_shade<<<sgrid, cfg.shade_block, 0, stream>>>(w, b, sobol_bitmajor);
+  b_trace(cfg, w, b, 1, tgrid, stream);
+  b_trace(cfg, w, b, 2, tgrid, stream);
+  k_b_resolve<<<sgrid, cfg.shade_block, 0, stream>>>(w, b);
+  k_b_retire<<<sgrid, cfg.shade_block, 0, stream>>>(w, b);
+  k_b_control<<<1, 32, 0, stream>>>(b, cond);
+  cudaGraph_t out = body;
+  cudaError_t e2 = cudaStreamEndCapture(stream, &out);
+  cudaError_t e3 = cudaGetLastError();
+  return e2 != cudaSuccess ? e2 : e3;
+}
+
+}  // namespace orion_gb300

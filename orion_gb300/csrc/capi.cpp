@@ -257,6 +257,7 @@ extern "C" int orion_gpu_create(const orion_gpu_opts* opts, orion_gpu_ctx** out)
   c->cfg.shade_block = 128;
   c->cfg.blocks_per_sm = 8;
   c->cfg.smem_stack = 16;
+  c->cfg.refill_below = 20;
   *out = c.release();
   return ORION_OK;
 }
@@ -666,6 +667,8 @@ extern "C" int orion_gpu_get_config(orion_gpu_ctx* ctx, orion_launch_config* out
   out->blocks_per_sm = ctx->cfg.blocks_per_sm;
   out->wave_paths = ctx->default_wave;
   out->batch_slots = ctx->default_batch_slots;
+  out->refill_below = ctx->cfg.refill_below;
+  out->reserved = 0;
   return ORION_OK;
 }
 
@@ -676,7 +679,7 @@ extern "C" int orion_gpu_set_config(orion_gpu_ctx* ctx, const orion_launch_confi
   const int st = cfg->smem_stack;
   if (!valid_block(cfg->trace_block) || !valid_block(cfg->shade_block) ||
       !(st == 0 || st == 8 || st == 16 || st == 24 || st == 32) || cfg->blocks_per_sm < 1 || cfg->blocks_per_sm > 64 ||
-      cfg->wave_paths < 1024 || cfg->batch_slots < 1024)
+      cfg->wave_paths < 1024 || cfg->batch_slots < 1024 || cfg->refill_below < 1 || cfg->refill_below > 32)
     return fail(ORION_ERR_INVALID, "launch configuration out of range");
   if ((size_t)st * cfg->trace_block * 8 > 96 * 1024) return fail(ORION_ERR_INVALID, "traversal stack too large");
   std::lock_guard<std::mutex> g(ctx->mu);
@@ -686,6 +689,7 @@ extern "C" int orion_gpu_set_config(orion_gpu_ctx* ctx, const orion_launch_confi
   ctx->cfg.blocks_per_sm = cfg->blocks_per_sm;
   ctx->default_wave = cfg->wave_paths;
   ctx->default_batch_slots = cfg->batch_slots;
+  ctx->cfg.refill_below = cfg->refill_below;
   return ORION_OK;
 }
 
@@ -729,8 +733,9 @@ extern "C" int orion_gpu_autotune(orion_gpu_ctx* ctx, orion_scene_id id, int32_t
   const int shade_blocks[] = {64, 128, 256};
   const int bpsm[] = {4, 8, 16};
   const int waves[] = {1 << 20, 1 << 21, 1 << 22, 1 << 23};
-  for (int knob = 0; knob < 5 && used < budget_ms; ++knob) {
-    int n = knob == 4 ? 4 : 3;
+  const int refills[] = {8, 16, 24, 32};
+  for (int knob = 0; knob < 6 && used < budget_ms; ++knob) {
+    int n = knob >= 4 ? 4 : 3;
     for (int v = 0; v < n && used < budget_ms; ++v) {
       LaunchConfig c = best;
       int wave = best_wave;
@@ -739,6 +744,7 @@ extern "C" int orion_gpu_autotune(orion_gpu_ctx* ctx, orion_scene_id id, int32_t
       if (knob == 2) c.shade_block = shade_blocks[v];
       if (knob == 3) c.blocks_per_sm = bpsm[v];
       if (knob == 4) wave = waves[v];
+      if (knob == 5) c.refill_below = refills[v];
       if (wave > 2 * paths && wave != best_wave) continue;
       if (std::memcmp(&c, &best, sizeof(c)) == 0 && wave == best_wave) continue;
       rc = trial(c, wave, &ms);
@@ -761,6 +767,8 @@ extern "C" int orion_gpu_autotune(orion_gpu_ctx* ctx, orion_scene_id id, int32_t
     best_out->blocks_per_sm = best.blocks_per_sm;
     best_out->wave_paths = best_wave;
     best_out->batch_slots = best_wave;
+    best_out->refill_below = best.refill_below;
+    best_out->reserved = 0;
   }
   if (best_mpaths) *best_mpaths = paths / (best_ms * 1e-3) / 1e6;
   return ORION_OK;

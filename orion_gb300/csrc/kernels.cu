@@ -46,20 +46,22 @@ __global__ void k_camera(SceneView s, WaveView w, WaveArgs a) {
 }
 
 template <int SMEM>
-__global__ void k_trace(SceneView s, const int* queue, const int* count, const float4* ray_o, const float4* ray_d,
-                        float4* hit, unsigned long long* stat) {
+__global__ void k_trace(SceneView s, const int* queue, const int* count, int* fetch, const float4* ray_o,
+                        const float4* ray_d, float4* hit, unsigned long long* stat, int refill_below) {
   extern __shared__ int2 stack_smem[];
   const int n = *count;
-  trace_list<false, SMEM>(SingleScene{&s}, queue, n, ray_o, ray_d, hit, nullptr, stack_smem);
+  trace_persistent<false, SMEM>(SingleScene{&s}, queue, n, fetch, ray_o, ray_d, hit, nullptr, stack_smem,
+                                refill_below);
   if (stat && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(stat, (unsigned long long)n);
 }
 
 template <int SMEM>
-__global__ void k_trace_sh(SceneView s, const int* queue, const int* count, const float4* ray_o,
-                           const float4* ray_d, int* occluded, unsigned long long* stat) {
+__global__ void k_trace_sh(SceneView s, const int* queue, const int* count, int* fetch, const float4* ray_o,
+                           const float4* ray_d, int* occluded, unsigned long long* stat, int refill_below) {
   extern __shared__ int2 stack_smem[];
   const int n = *count;
-  trace_list<true, SMEM>(SingleScene{&s}, queue, n, ray_o, ray_d, nullptr, occluded, stack_smem);
+  trace_persistent<true, SMEM>(SingleScene{&s}, queue, n, fetch, ray_o, ray_d, nullptr, occluded, stack_smem,
+                               refill_below);
   if (stat && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(stat, (unsigned long long)n);
 }
 
@@ -130,12 +132,16 @@ __global__ void k_reset_counters(int* counters, int slots, int keep_slot, int ke
   if (i < slots) counters[i] = (i == keep_slot) ? keep_value : 0;
 }
 
-__global__ void k_reset_nee_counters(int* counters, int next_ext) {
+// Start of a bounce: empty the queues this bounce fills, zero the fetch counters.
+__global__ void k_reset_bounce_counters(int* counters, int next_ext) {
   int i = threadIdx.x;
   if (i == 0) counters[next_ext] = 0;
   if (i == 1) counters[CNT_NEE] = 0;
   if (i == 2) counters[CNT_SH] = 0;
   if (i == 3) counters[CNT_MIS] = 0;
+  if (i == 4) counters[CNT_FETCH_EXT] = 0;
+  if (i == 5) counters[CNT_FETCH_SH] = 0;
+  if (i == 6) counters[CNT_FETCH_MIS] = 0;
 }
 
 // ------------------------------------------------------------ test hooks
@@ -216,26 +222,37 @@ int grid_for(int64_t n, int block, int max_blocks) {
   return (int)(g < 1 ? 1 : g);
 }
 
+struct TraceLaunch {
+  const int* queue;
+  const int* count;
+  int* fetch;
+  const float4* o;
+  const float4* d;
+  float4* hit;
+  int* occl;
+  unsigned long long* stat;
+};
+
 template <int SMEM>
-void launch_trace_kernels(bool shadow, const SceneView& s, const int* queue, const int* count, const float4* o,
-                          const float4* d, float4* hit, int* occl, unsigned long long* stat, int grid, int block,
+void launch_trace_kernels(bool shadow, const SceneView& s, const TraceLaunch& t, const LaunchConfig& cfg, int grid,
                           cudaStream_t stream) {
+  const int block = cfg.trace_block;
+  const int refill = cfg.refill_below < 1 ? 1 : (cfg.refill_below > 32 ? 32 : cfg.refill_below);
   size_t smem = (size_t)SMEM * block * sizeof(int2);
   if (shadow)
-    k_trace_sh<SMEM><<<grid, block, smem, stream>>>(s, queue, count, o, d, occl, stat);
+    k_trace_sh<SMEM><<<grid, block, smem, stream>>>(s, t.queue, t.count, t.fetch, t.o, t.d, t.occl, t.stat, refill);
   else
-    k_trace<SMEM><<<grid, block, smem, stream>>>(s, queue, count, o, d, hit, stat);
+    k_trace<SMEM><<<grid, block, smem, stream>>>(s, t.queue, t.count, t.fetch, t.o, t.d, t.hit, t.stat, refill);
 }
 
-void trace_dispatch(int smem_stack, bool shadow, const SceneView& s, const int* queue, const int* count,
-                    const float4* o, const float4* d, float4* hit, int* occl, unsigned long long* stat, int grid,
-                    int block, cudaStream_t stream) {
-  switch (smem_stack) {
-    case 0: launch_trace_kernels<0>(shadow, s, queue, count, o, d, hit, occl, stat, grid, block, stream); break;
-    case 8: launch_trace_kernels<8>(shadow, s, queue, count, o, d, hit, occl, stat, grid, block, stream); break;
-    case 24: launch_trace_kernels<24>(shadow, s, queue, count, o, d, hit, occl, stat, grid, block, stream); break;
-    case 32: launch_trace_kernels<32>(shadow, s, queue, count, o, d, hit, occl, stat, grid, block, stream); break;
-    default: launch_trace_kernels<16>(shadow, s, queue, count, o, d, hit, occl, stat, grid, block, stream); break;
+void trace_dispatch(bool shadow, const SceneView& s, const TraceLaunch& t, const LaunchConfig& cfg, int grid,
+                    cudaStream_t stream) {
+  switch (cfg.smem_stack) {
+    case 0: launch_trace_kernels<0>(shadow, s, t, cfg, grid, stream); break;
+    case 8: launch_trace_kernels<8>(shadow, s, t, cfg, grid, stream); break;
+    case 24: launch_trace_kernels<24>(shadow, s, t, cfg, grid, stream); break;
+    case 32: launch_trace_kernels<32>(shadow, s, t, cfg, grid, stream); break;
+    default: launch_trace_kernels<16>(shadow, s, t, cfg, grid, stream); break;
   }
 }
 
@@ -262,24 +279,30 @@ void launch_wave(const SceneView& s, const WaveView& w, const WaveArgs& a, const
   const int sgrid = grid_for(a.n_paths, cfg.shade_block, persistent * 2);
   int cur = 0;
   for (int bounce = 0; bounce <= a.max_depth; ++bounce) {
-    begin(ST_TRACE_EXT);
-    trace_dispatch(cfg.smem_stack, false, s, w.q_ext[cur], w.counters + cur, w.ray_o, w.ray_d, w.hit, nullptr,
-                   w.ray_stats, tgrid, cfg.trace_block, stream);
-    end();
     begin(ST_OTHER);
-    k_reset_nee_counters<<<1, 32, 0, stream>>>(w.counters, cur ^ 1);
+    k_reset_bounce_counters<<<1, 32, 0, stream>>>(w.counters, cur ^ 1);
+    end();
+    begin(ST_TRACE_EXT);
+    trace_dispatch(false, s,
+                   TraceLaunch{w.q_ext[cur], w.counters + cur, w.counters + CNT_FETCH_EXT, w.ray_o, w.ray_d, w.hit,
+                               nullptr, w.ray_stats},
+                   cfg, tgrid, stream);
     end();
     begin(ST_SHADE);
     k_shade<<<sgrid, cfg.shade_block, 0, stream>>>(s, w, a, bounce, cur);
     end();
     if (bounce < a.max_depth) {
       begin(ST_TRACE_SHADOW);
-      trace_dispatch(cfg.smem_stack, true, s, w.q_sh, w.counters + CNT_SH, w.sh_o, w.sh_d, nullptr, w.occluded,
-                     w.ray_stats + 1, tgrid, cfg.trace_block, stream);
+      trace_dispatch(true, s,
+                     TraceLaunch{w.q_sh, w.counters + CNT_SH, w.counters + CNT_FETCH_SH, w.sh_o, w.sh_d, nullptr,
+                                 w.occluded, w.ray_stats + 1},
+                     cfg, tgrid, stream);
       end();
       begin(ST_TRACE_MIS);
-      trace_dispatch(cfg.smem_stack, false, s, w.q_mis, w.counters + CNT_MIS, w.mis_o, w.mis_d, w.mis_hit, nullptr,
-                     w.ray_stats + 2, tgrid, cfg.trace_block, stream);
+      trace_dispatch(false, s,
+                     TraceLaunch{w.q_mis, w.counters + CNT_MIS, w.counters + CNT_FETCH_MIS, w.mis_o, w.mis_d,
+                                 w.mis_hit, nullptr, w.ray_stats + 2},
+                     cfg, tgrid, stream);
       end();
       begin(ST_RESOLVE);
       k_resolve<<<sgrid, cfg.shade_block, 0, stream>>>(s, w);

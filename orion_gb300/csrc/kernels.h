@@ -54,7 +54,7 @@ struct WaveView {
 };
 
 enum CounterSlot { CNT_EXT0 = 0, CNT_EXT1 = 1, CNT_NEE = 2, CNT_SH = 3, CNT_MIS = 4, CNT_RETIRE = 5, CNT_FREE = 6,
-                   kCounterSlots = 8 };
+                   CNT_FETCH_EXT = 8, CNT_FETCH_SH = 9, CNT_FETCH_MIS = 10, kCounterSlots = 16 };
 
 // ------------------------------------------------------------ batched mode
 //
@@ -123,6 +123,7 @@ struct LaunchConfig {
   int shade_block;
   int blocks_per_sm; // persistent grid size factor
   int smem_stack;    // shared-memory stack entries per thread (0, 8, 16, 24, 32)
+  int refill_below;  // a traversal warp refills idle lanes when fewer lanes than this hold a ray (1..32)
 };
 
 enum Stage { ST_CAMERA = 0, ST_TRACE_EXT, ST_SHADE, ST_TRACE_SHADOW, ST_TRACE_MIS, ST_RESOLVE, ST_FILM, ST_OTHER,

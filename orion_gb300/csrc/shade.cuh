@@ -1,0 +1,378 @@
+// Per-path stages of the wavefront path tracer shared by the plain
+// (one image per launch) and batched (many jobs per launch) drivers.
+#pragma once
+#include "bsdf.cuh"
+#include "dmath.cuh"
+#include "kernels.h"
+#include "light.cuh"
+#include "traverse.cuh"
+
+namespace orion_gb300 {
+
+constexpr int kNonSpecular = BXDF_ALL & ~BXDF_SPECULAR;
+constexpr int kFlagShadow = 1, kFlagMis = 2, kFlagEnv = 4;
+
+__device__ __forceinline__ void queue_append(int* counter, int* queue, int value, bool pred) {
+  unsigned active = __activemask();
+  unsigned m = __ballot_sync(active, pred);
+  if (!pred) return;
+  int lane = threadIdx.x & 31;
+  int leader = __ffs(m) - 1;
+  int base = 0;
+  if (lane == leader) base = atomicAdd(counter, __popc(m));
+  base = __shfl_sync(m, base, leader);
+  queue[base + __popc(m & ((1u << lane) - 1u))] = value;
+}
+
+struct Hit {
+  V3 p, ng, ns, su, sv;
+};
+
+// Post-hit reconstruction (src/core/kernel.cpp:127-169).
+__device__ __forceinline__ Hit reconstruct(const PrimShade& sh, float u, float v) {
+  Hit h;
+  V3 p0 = ld3(sh.p), p1 = ld3(sh.p + 3), p2 = ld3(sh.p + 6);
+  float w = 1.f - u - v;
+  h.p = w * p0 + u * p1 + v * p2;
+  h.ns = ld3(sh.n) * w + ld3(sh.n + 3) * u + ld3(sh.n + 6) * v;
+  h.ng = normalize(cross(p1 - p0, p2 - p0));
+  V3 su = normalize(p1 - p0);
+  h.sv = normalize(cross(h.ns, su));
+  h.su = normalize(cross(h.sv, h.ns));
+  return h;
+}
+
+__device__ __forceinline__ V3 geometric_normal(const PrimShade& sh) {
+  V3 p0 = ld3(sh.p), p1 = ld3(sh.p + 3), p2 = ld3(sh.p + 6);
+  return normalize(cross(p1 - p0, p2 - p0));
+}
+
+__device__ __forceinline__ V3 point_on(const PrimShade& sh, float u, float v) {
+  V3 p0 = ld3(sh.p), p1 = ld3(sh.p + 3), p2 = ld3(sh.p + 6);
+  float w = 1.f - u - v;
+  return w * p0 + u * p1 + v * p2;
+}
+
+__device__ __forceinline__ TraceScene trace_scene(const SceneView& s) { return TraceScene{s.nodes, s.woop, s.tri_prim}; }
+
+// Pinhole::generateRay (src/camera/pinhole.cpp:8-33).
+// Sampler::next2() builds Point2f(next(), next()) (src/core/sampler.h:29); the
+// two calls are unsequenced and the compiled reference evaluates the second
+// first, so .x holds the later dimension. All 2-D samples follow that order.
+__device__ __forceinline__ void camera_ray(const DevCamera& c, PathSampler& smp, int i, int j, V3* o, V3* d) {
+  float s0 = smp.next(), s1 = smp.next();
+  float rx = (float)i + s1;
+  float ry = (float)j + s0;
+  float xx = (2.f * rx / (float)c.width - 1.f) * c.aspect * c.tan_half_fov;
+  float yy = (1.f - 2.f * ry / (float)c.height) * c.tan_half_fov;
+  V3 dir = normalize(V3{xx, yy, -1.f});
+  V3 org = V3{0.f, 0.f, 0.f};
+  if (c.lens_radius > 0.f) {
+    V3 target = org + dir * c.focal_distance;
+    float lx, ly;
+    float l0 = smp.next(), l1 = smp.next();
+    concentric_sample_disk(l1, l0, &lx, &ly);
+    org = V3{lx * c.lens_radius, ly * c.lens_radius, 0.f};
+    dir = normalize(target - org);
+  }
+  const float* m = c.c2w;
+  float xp = m[0] * org.x + m[1] * org.y + m[2] * org.z + m[3];
+  float yp = m[4] * org.x + m[5] * org.y + m[6] * org.z + m[7];
+  float zp = m[8] * org.x + m[9] * org.y + m[10] * org.z + m[11];
+  float wp = m[12] * org.x + m[13] * org.y + m[14] * org.z + m[15];
+  if (wp == 1.f)
+    *o = V3{xp, yp, zp};
+  else
+    *o = vdiv(V3{xp, yp, zp}, wp);
+  *d = V3{m[0] * dir.x + m[1] * dir.y + m[2] * dir.z, m[4] * dir.x + m[5] * dir.y + m[6] * dir.z,
+          m[8] * dir.x + m[9] * dir.y + m[10] * dir.z};
+}
+
+// One bounce of PathTracing::Li (src/integrator/path.cpp:56-97) for path slot
+// `pid`: emission, BSDF, light sample (uniformSampleOneLight /
+// estimateDirect, src/core/integrator.cpp:8-90), continuation, roulette.
+// Writes the path state and NEE records; the caller appends the slot to the
+// queues the result asks for.
+struct ShadeResult {
+  bool alive, did_nee, want_sh, want_mis;
+};
+
+__device__ __forceinline__ ShadeResult shade_one(const SceneView& s, const WaveView& w, const uint32_t* sobol_bitmajor,
+                                                 int pid, uint64_t index, int bounce, int max_depth, int rr_depth) {
+  LightDistrib distrib{s.light_func, s.light_cdf, s.light_func_int, s.num_lights};
+    const float4 hv = w.hit[pid];
+    const int tri = __float_as_int(hv.w);
+    const V3 ro = xyz(w.ray_o[pid]);
+    const V3 rd = xyz(w.ray_d[pid]);
+    float4 b4 = w.beta[pid];
+    V3 beta = xyz(b4);
+    const bool spec_prev = b4.w != 0.f;
+    V3 L = xyz(w.L[pid]);
+    const int prim = tri >= 0 ? __ldg(s.tri_prim + tri) : -1;
+
+    // Emission on the first hit or after a specular bounce (path.cpp:61-69).
+    if (bounce == 0 || spec_prev) {
+      if (prim >= 0) {
+        int li = __ldg(&s.prims[prim].light);
+        if (li >= 0) {
+          V3 ng = geometric_normal(s.prims[prim]);
+          if (dot(ng, -rd) > 0.f) L = L + mul(beta, ld3(s.lights[li].L));
+        }
+      } else {
+        for (int e = 0; e < s.num_env; ++e) L = L + mul(beta, ld3(s.lights[s.env_idx[e]].L));
+      }
+    }
+    bool alive = prim >= 0 && bounce < max_depth;
+    bool did_nee = false, want_sh = false, want_mis = false;
+    if (alive) {
+      const PrimShade& sh = s.prims[prim];
+      Hit h = reconstruct(sh, hv.y, hv.z);
+      const DevMaterial& m = s.mats[sh.material];
+      Frame fr{h.ng, h.ns, h.su, h.sv};
+      // This bounce consumes at most 8 sample dimensions (light choice 1,
+      // light point 2, BSDF for MIS 2, continuation 2, roulette 1), all from
+      // one pass over the sample index.
+      const uint32_t d0 = (uint32_t)w.dim[pid];
+      float u[8];
+      sobol_block8(sobol_bitmajor, index, d0, u);
+      int used = 0;
+
+      // uniformSampleOneLight (integrator.cpp:8-27) when a non-specular lobe exists.
+      if (m.num_nonspecular > 0 && s.num_lights > 0) {
+        float sel_pdf;
+        int li = sample_discrete(distrib, u[0], &sel_pdf);
+        used = 1;
+        if (sel_pdf != 0.f) {
+          used = 5;
+          float ul1 = u[1], ul0 = u[2];  // next2(): .x is the later dimension
+          float ub1 = u[3], ub0 = u[4];
+          const DevLight& lt = s.lights[li];
+          V3 wo = normalize(-rd);
+          // estimateDirect, light-sampling half (integrator.cpp:39-60).
+          LightSample ls = sample_li(lt, s.prims, h.p, ul0, ul1, s.world_radius);
+          V3 ld = V3{0, 0, 0};
+          if (ls.pdf > 0.f && !is_black(ls.Li)) {
+            V3 f = bsdf_f(m, fr, ls.wi, wo, kNonSpecular) * absdot(ls.wi, h.ns);
+            float bpdf = bsdf_pdf(m, fr, ls.wi, wo, kNonSpecular);
+            if (!is_black(f)) {
+              if (is_delta_light(lt.kind)) {
+                ld = sdiv(mul(f, ls.Li), ls.pdf);
+              } else {
+                float wgt = power_heuristic(ls.pdf, bpdf);
+                ld = sdiv(mul(f, ls.Li) * wgt, ls.pdf);
+              }
+              // ShadowTester::unoccluded (light.h:26-29): Intersection::spawnRay to a point.
+              V3 so = offset_ray_origin(h.p, h.ng, ls.p_light - h.p);
+              w.sh_o[pid] = f4(so, 1.f - kShadowEpsilon);
+              w.sh_d[pid] = f4(ls.p_light - so, 0.f);
+              want_sh = true;
+            }
+          }
+          // estimateDirect, BSDF-sampling half (integrator.cpp:62-89).
+          int flags = want_sh ? kFlagShadow : 0;
+          float mis_pdf = 0.f, env_w = 0.f;
+          V3 fb = V3{0, 0, 0};
+          if (!is_delta_light(lt.kind)) {
+            V3 wib;
+            int st;
+            fb = bsdf_sample_f(m, fr, wo, ub0, ub1, kNonSpecular, &wib, &mis_pdf, &st);
+            fb = fb * absdot(wib, h.ns);
+            if (!is_black(fb) && mis_pdf > 0.f) {
+              bool ok = true;
+              if (lt.kind == DL_ENV) {
+                float lpdf = env_pdf_li(lt, wib);
+                if (lpdf == 0.f)
+                  ok = false;
+                else {
+                  env_w = power_heuristic(mis_pdf, lpdf);
+                  flags |= kFlagEnv;
+                }
+              }
+              if (ok) {
+                V3 mo = offset_ray_origin(h.p, h.ng, wib);
+                w.mis_o[pid] = f4(mo, 0.f);
+                w.mis_d[pid] = f4(wib, 0.f);
+                want_mis = true;
+                flags |= kFlagMis;
+              }
+            }
+          }
+          w.nee_p[pid] = f4(h.p, sel_pdf);
+          w.nee_beta[pid] = f4(beta, __int_as_float(flags | (li << 8)));
+          w.nee_ld[pid] = f4(ld, mis_pdf);
+          w.nee_f[pid] = f4(fb, env_w);
+          did_nee = true;
+        }
+      }
+
+      // Continuation: BSDF sample, throughput, spawn, Russian roulette (path.cpp:81-96).
+      float u1 = used == 0 ? u[0] : (used == 1 ? u[1] : u[5]);  // next2(): .x is the later dimension
+      float u0 = used == 0 ? u[1] : (used == 1 ? u[2] : u[6]);
+      used += 2;
+      V3 wi;
+      float pdf;
+      int stype;
+      V3 f = bsdf_sample_f(m, fr, -rd, u0, u1, BXDF_ALL, &wi, &pdf, &stype);
+      if (is_black(f) || pdf == 0.f) {
+        alive = false;
+      } else {
+        beta = mul(beta, sdiv(f * absdot(wi, h.ns), pdf));
+        bool spec = (stype & BXDF_SPECULAR) != 0;
+        V3 no = offset_ray_origin(h.p, h.ng, wi);
+        if (bounce > rr_depth) {
+          float qq = fmaxf(0.05f, 1.f - max_comp(beta));
+          float rr = used == 2 ? u[2] : (used == 3 ? u[3] : u[7]);
+          used += 1;
+          if (rr < qq)
+            alive = false;
+          else
+            beta = sdiv(beta, 1.f - qq);
+        }
+        if (alive) {
+          w.ray_o[pid] = f4(no, 0.f);
+          w.ray_d[pid] = f4(wi, 0.f);
+          w.beta[pid] = f4(beta, spec ? 1.f : 0.f);
+        }
+      }
+      w.dim[pid] = (int)(d0 + used);
+    }
+    w.L[pid] = f4(L, 0.f);
+  return ShadeResult{alive, did_nee, want_sh, want_mis};
+}
+
+// The scene a path slot traces against: one scene for a plain wave, the
+// slot's job's scene in batched mode.
+struct SingleScene {
+  const SceneView* s;
+  __device__ __forceinline__ const SceneView& operator()(int) const { return *s; }
+};
+struct JobScene {
+  const DevJob* jobs;
+  const int* job_of;
+  __device__ __forceinline__ const SceneView& operator()(int pid) const { return jobs[job_of[pid]].scene; }
+};
+
+// Traces the rays of `n` queued path slots. ANY: occlusion within the ray's
+// tmax (origin.w), result in occluded[]; otherwise closest hit over
+// (0, FLT_MAX], result in hit[].
+template <bool ANY, int SMEM, class SceneOf>
+__device__ __forceinline__ void trace_list(const SceneOf& scene_of, const int* queue, int n, const float4* ray_o,
+                                           const float4* ray_d, float4* hit, int* occluded, int2* stack_smem) {
+  TraversalStack<SMEM> st;
+  st.smem = stack_smem + threadIdx.x;
+  st.stride = blockDim.x;
+  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
+    const int pid = queue[q];
+    const SceneView& s = scene_of(pid);
+    TraceScene ts{s.nodes, s.woop, s.tri_prim};
+    float4 o4 = ray_o[pid], d4 = ray_d[pid];
+    if (ANY) {
+      RayHit h = traverse<true, SMEM>(ts, xyz(o4), xyz(d4), 0.f, o4.w, st);
+      occluded[pid] = h.tri >= 0;
+    } else {
+      RayHit h = traverse<false, SMEM>(ts, xyz(o4), xyz(d4), 0.f, kFloatMax, st);
+      hit[pid] = make_float4(h.t, h.u, h.v, __int_as_float(h.tri));
+    }
+  }
+}
+
+// Persistent-warp tracing of `n` queued rays (see traverse.cuh): warps stay
+// in the kernel and refill idle lanes from the queue through `fetch`, a
+// counter that must be zero at launch. Block size must be a multiple of 32.
+template <bool ANY, int SMEM, class SceneOf>
+__device__ __forceinline__ void trace_persistent(const SceneOf& scene_of, const int* queue, int n, int* fetch,
+                                                 const float4* ray_o, const float4* ray_d, float4* hit,
+                                                 int* occluded, int2* stack_smem, int refill_below) {
+  constexpr unsigned kFull = 0xffffffffu;
+  const int lane = threadIdx.x & 31;
+  TraversalStack<SMEM> st;
+  st.smem = stack_smem + threadIdx.x;
+  st.stride = blockDim.x;
+  LaneRay r;
+  TraceScene ts{nullptr, nullptr, nullptr};
+  int pid = -1;
+  bool active = false, exhausted = false;
+  while (true) {
+    unsigned act = __ballot_sync(kFull, active);
+    if (!exhausted && __popc(act) < refill_below) {
+      const unsigned idle = ~act;
+      const int cnt = __popc(idle);
+      int base = 0;
+      if (lane == 0) base = atomicAdd(fetch, cnt);
+      base = __shfl_sync(kFull, base, 0);
+      if (base + cnt >= n) exhausted = true;
+      if (!active) {
+        const int my = base + __popc(idle & ((1u << lane) - 1u));
+        if (my < n) {
+          pid = queue[my];
+          const SceneView& s = scene_of(pid);
+          ts = TraceScene{s.nodes, s.woop, s.tri_prim};
+          const float4 o4 = ray_o[pid], d4 = ray_d[pid];
+          st.sp = 0;
+          lane_start(r, ts, o4, d4, ANY ? o4.w : kFloatMax);
+          active = true;
+        }
+      }
+      act = __ballot_sync(kFull, active);
+    }
+    if (act == 0) {
+      if (exhausted) break;
+      continue;
+    }
+    if (active) {
+      lane_inner<SMEM>(r, ts, st);
+      bool found = lane_leaves<ANY, SMEM>(r, ts, st);
+      if (found || (r.na < 0 && r.lb == 0)) {
+        if (ANY)
+          occluded[pid] = r.tri >= 0;
+        else
+          hit[pid] = make_float4(r.tri >= 0 ? r.tmax : kFloatMax, r.u, r.v, __int_as_float(r.tri));
+        active = false;
+      }
+    }
+  }
+}
+
+// Adds beta * Ld / selPdf for a path that sampled a light this bounce
+// (path.cpp:77-80 with the shadow and MIS rays traced).
+__device__ __forceinline__ void resolve_one(const SceneView& s, const WaveView& w, int pid) {
+    float4 pb = w.nee_beta[pid];
+    int fl = __float_as_int(pb.w);
+    int li = fl >> 8;
+    float4 np = w.nee_p[pid];
+    float4 ldv = w.nee_ld[pid];
+    V3 Ld = V3{0, 0, 0};
+    if ((fl & kFlagShadow) && !w.occluded[pid]) Ld = Ld + xyz(ldv);
+    if (fl & kFlagMis) {
+      const DevLight& lt = s.lights[li];
+      float4 fv = w.nee_f[pid];
+      V3 fb = xyz(fv);
+      float bpdf = ldv.w;
+      float4 mh = w.mis_hit[pid];
+      int tri = __float_as_int(mh.w);
+      V3 wi = xyz(w.mis_d[pid]);
+      if (fl & kFlagEnv) {
+        if (tri < 0) Ld = Ld + sdiv(mul(fb, ld3(lt.L)) * fv.w, bpdf);
+      } else if (tri >= 0) {
+        int prim = __ldg(s.tri_prim + tri);
+        if (prim == lt.prim) {
+          // Triangle::pdf (src/core/triangle.cpp:123-135) on the traced hit.
+          const PrimShade& sh = s.prims[prim];
+          V3 ip = point_on(sh, mh.y, mh.z);
+          V3 ing = geometric_normal(sh);
+          float lpdf = length_sq(xyz(np) - ip) / (absdot(ing, -wi) * lt.area);
+          if (isinf(lpdf)) lpdf = 0.f;
+          if (lpdf != 0.f) {
+            float wgt = power_heuristic(bpdf, lpdf);
+            V3 Li = dot(ing, -wi) > 0.f ? ld3(lt.L) : V3{0, 0, 0};
+            if (!is_black(Li)) Ld = Ld + sdiv(mul(fb, Li) * wgt, bpdf);
+          }
+        }
+      }
+    }
+    V3 L = xyz(w.L[pid]);
+    L = L + mul(xyz(pb), sdiv(Ld, np.w));
+    w.L[pid] = f4(L, 0.f);
+}
+
+}  // namespace orion_gb300

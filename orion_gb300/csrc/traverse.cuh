@@ -159,4 +159,133 @@ __device__ __forceinline__ RayHit traverse(const TraceScene& s, V3 o, V3 d, floa
   return h;
 }
 
+// ------------------------------------------------ persistent warp traversal
+//
+// The kernels below trace a queue of rays with warps that stay resident:
+//  * while-while: each lane walks inner nodes until every active lane of the
+//    warp has found a leaf (the first leaf a lane finds is postponed and the
+//    lane keeps traversing), then all lanes test triangles together, so the
+//    two phases do not interleave within a warp;
+//  * dynamic fetch: when fewer than `refill_below` lanes still hold a ray,
+//    the warp takes new rays for its idle lanes from the queue with one
+//    atomicAdd, instead of idling until its slowest ray ends.
+// Warp votes only steer scheduling; each ray's result does not depend on them.
+
+struct LaneRay {
+  V3 o, d, idir, oid;
+  float tnear, tmax;  // tmax shrinks to the closest hit found so far
+  float u, v;
+  int tri, best_prim;
+  int na, nb;  // node to visit: (a, b) fields; na < 0 when the stack is empty
+  int la, lb;  // postponed leaf, lb == 0 when none
+};
+
+__device__ __forceinline__ void lane_start(LaneRay& r, const TraceScene& s, float4 o4, float4 d4, float tmax) {
+  r.o = xyz(o4);
+  r.d = xyz(d4);
+  r.idir = V3{safe_inv(r.d.x), safe_inv(r.d.y), safe_inv(r.d.z)};
+  r.oid = V3{r.o.x * r.idir.x, r.o.y * r.idir.y, r.o.z * r.idir.z};
+  r.tnear = 0.f;
+  r.tmax = tmax;
+  r.u = r.v = 0.f;
+  r.tri = -1;
+  r.best_prim = 0x7fffffff;
+  r.lb = 0;
+  r.la = 0;
+  float4 lo = __ldg(s.nodes), hi = __ldg(s.nodes + 1);
+  if (box_entry(lo, hi, r.idir, r.oid, r.tnear, r.tmax) < __int_as_float(0x7f800000)) {
+    r.na = __float_as_int(lo.w);
+    r.nb = __float_as_int(hi.w);
+  } else {
+    r.na = -1;
+    r.nb = 0;
+  }
+}
+
+template <int SMEM>
+__device__ __forceinline__ void lane_pop(LaneRay& r, TraversalStack<SMEM>& st) {
+  if (st.sp == 0) {
+    r.na = -1;
+    r.nb = 0;
+  } else {
+    int2 e = st.pop();
+    r.na = e.x;
+    r.nb = e.y;
+  }
+}
+
+// Inner nodes until this lane holds a postponed leaf and every active lane
+// in the warp does too (or has no inner node left).
+template <int SMEM>
+__device__ __forceinline__ void lane_inner(LaneRay& r, const TraceScene& s, TraversalStack<SMEM>& st) {
+  while (r.na >= 0 && r.nb == 0) {
+    const int a = r.na;
+    float4 l0 = __ldg(s.nodes + 2 * a), h0 = __ldg(s.nodes + 2 * a + 1);
+    float4 l1 = __ldg(s.nodes + 2 * a + 2), h1 = __ldg(s.nodes + 2 * a + 3);
+    float t0 = box_entry(l0, h0, r.idir, r.oid, r.tnear, r.tmax);
+    float t1 = box_entry(l1, h1, r.idir, r.oid, r.tnear, r.tmax);
+    bool hit0 = t0 < __int_as_float(0x7f800000), hit1 = t1 < __int_as_float(0x7f800000);
+    if (hit0 && hit1) {
+      int2 n0 = make_int2(__float_as_int(l0.w), __float_as_int(h0.w));
+      int2 n1 = make_int2(__float_as_int(l1.w), __float_as_int(h1.w));
+      if (t1 < t0) {
+        int2 tmp = n0;
+        n0 = n1;
+        n1 = tmp;
+      }
+      st.push(n1);
+      r.na = n0.x;
+      r.nb = n0.y;
+    } else if (hit0) {
+      r.na = __float_as_int(l0.w);
+      r.nb = __float_as_int(h0.w);
+    } else if (hit1) {
+      r.na = __float_as_int(l1.w);
+      r.nb = __float_as_int(h1.w);
+    } else {
+      lane_pop(r, st);
+    }
+    if (r.nb > 0 && r.lb == 0) {  // first leaf: postpone it, keep traversing
+      r.la = r.na;
+      r.lb = r.nb;
+      lane_pop(r, st);
+    }
+    if (!__any_sync(__activemask(), r.lb == 0)) break;
+  }
+}
+
+// Triangles of the postponed leaf, then of any leaves the lane is standing on.
+// Returns true when an occlusion query found its hit (ANY).
+template <bool ANY, int SMEM>
+__device__ __forceinline__ bool lane_leaves(LaneRay& r, const TraceScene& s, TraversalStack<SMEM>& st) {
+  while (r.lb > 0) {
+    for (int k = r.la; k < r.la + r.lb; ++k) {
+      float t, u, v;
+      if (woop_hit(s.woop, k, r.o, r.d, r.tnear, r.tmax, &t, &u, &v)) {
+        if (ANY) {
+          r.tmax = t;
+          r.tri = k;
+          return true;
+        }
+        int prim = __ldg(s.tri_prim + k);
+        if (t < r.tmax || r.tri < 0 || prim < r.best_prim) {
+          r.tmax = t;
+          r.u = u;
+          r.v = v;
+          r.tri = k;
+          r.best_prim = prim;
+        }
+      }
+    }
+    if (r.na >= 0 && r.nb > 0) {
+      r.la = r.na;
+      r.lb = r.nb;
+      lane_pop(r, st);
+    } else {
+      r.lb = 0;
+    }
+  }
+  return false;
+}
+
 }  // namespace orion_gb300
