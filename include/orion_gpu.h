@@ -206,6 +206,7 @@ typedef struct orion_job {
   orion_scene_id scene;
   int32_t reserved;
   orion_render_params params;  /* spp 0 = scene's; max_depth -1 = scene's; rr_depth; first_pass */
+  const orion_camera* camera;  /* another view of the resident scene (its own film size), or NULL */
   double* sum;                 /* host W*H*3 FP64 radiance sums, or NULL */
   double* sumsq;               /* host W*H*3 FP64 sums of squares, or NULL */
   uint32_t* count;             /* host W*H samples per pixel, or NULL */

@@ -141,7 +141,7 @@ __device__ __forceinline__ float md_pdf(int dist, float alpha, V3 wh) { return m
 
 // The lobe evaluators are out of line: the shading kernel calls them from
 // several places and inlining every copy overflows the instruction cache.
-__device__ __noinline__ V3 lobe_f(const DevLobe& l, V3 wi, V3 wo) {
+static __device__ __noinline__ V3 lobe_f(const DevLobe& l, V3 wi, V3 wo) {
   switch (l.kind) {
     case LOBE_LAMBERT_R:
       return ld3(l.c) * kInvPi;
@@ -192,7 +192,7 @@ __device__ __noinline__ V3 lobe_f(const DevLobe& l, V3 wi, V3 wo) {
   }
 }
 
-__device__ __noinline__ float lobe_pdf(const DevLobe& l, V3 wi, V3 wo) {
+static __device__ __noinline__ float lobe_pdf(const DevLobe& l, V3 wi, V3 wo) {
   switch (l.kind) {
     case LOBE_LAMBERT_R:
     case LOBE_OREN_NAYAR:
@@ -216,7 +216,7 @@ __device__ __noinline__ float lobe_pdf(const DevLobe& l, V3 wi, V3 wo) {
 }
 
 // Samples one lobe; *pdf is left untouched (0) on the reference's early exits.
-__device__ __noinline__ V3 lobe_sample_f(const DevLobe& l, V3 wo, float u0, float u1, V3* wi, float* pdf,
+static __device__ __noinline__ V3 lobe_sample_f(const DevLobe& l, V3 wo, float u0, float u1, V3* wi, float* pdf,
                                             int* stype) {
   switch (l.kind) {
     case LOBE_LAMBERT_R:
@@ -312,7 +312,7 @@ __device__ __forceinline__ float bsdf_pdf(const DevMaterial& m, const Frame& fr,
 }
 
 // Returns f; *pdf = 0 and *stype = 0 on failure. *wi is written only on success.
-__device__ __noinline__ V3 bsdf_sample_f(const DevMaterial& m, const Frame& fr, V3 wo_w, float u0, float u1,
+static __device__ __noinline__ V3 bsdf_sample_f(const DevMaterial& m, const Frame& fr, V3 wo_w, float u0, float u1,
                                             int type, V3* wi_w, float* pdf, int* stype) {
   int n = bsdf_num_matching(m, type);
   *pdf = 0.f;

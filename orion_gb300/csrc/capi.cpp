@@ -532,6 +532,77 @@ static int build_batch_graph(orion_gpu_ctx* ctx, const BatchView& bv, int slots)
   return ORION_OK;
 }
 
+// One batch launch over `dj` (film pointers set; films zeroed or holding
+// earlier passes to add to, in stream order before this call). Caller holds
+// ctx->mu. On return `out` is the final control block, `ms` the device time.
+static int run_batch_locked(orion_gpu_ctx* ctx, std::vector<DevJob>& dj, unsigned long long total, int max_depth_all,
+                            BatchCtl* out_ctl, float* ms_out) {
+  const int njobs = (int)dj.size();
+  int rc;
+  const int slots = (int)std::min<unsigned long long>((unsigned long long)ctx->default_batch_slots,
+                                                       std::max<unsigned long long>(total, 1024ULL));
+  if ((rc = ensure_wave(ctx, slots)) != ORION_OK) return rc;
+  const int cap = ctx->wave.capacity;
+  if (ctx->batch_slots_alloc < cap) {
+    if ((rc = ctx->b_job_of.alloc((size_t)cap * 4)) != ORION_OK) return rc;
+    if ((rc = ctx->b_bounce_of.alloc((size_t)cap * 4)) != ORION_OK) return rc;
+    if ((rc = ctx->b_index_of.alloc((size_t)cap * 8)) != ORION_OK) return rc;
+    if ((rc = ctx->b_retire.alloc((size_t)cap * 4)) != ORION_OK) return rc;
+    if ((rc = ctx->b_free.alloc((size_t)cap * 4)) != ORION_OK) return rc;
+    ctx->batch_slots_alloc = cap;
+  }
+  if (!ctx->b_ctl.p && (rc = ctx->b_ctl.alloc(sizeof(BatchCtl))) != ORION_OK) return rc;
+  if (ctx->jobs_alloc < njobs) {
+    int n = std::max(njobs, 64);
+    if ((rc = ctx->b_jobs.alloc((size_t)n * sizeof(DevJob))) != ORION_OK) return rc;
+    ctx->jobs_alloc = n;
+  }
+  BatchView bv;
+  bv.jobs = ctx->b_jobs.as<DevJob>();
+  bv.ctl = ctx->b_ctl.as<BatchCtl>();
+  bv.job_of = ctx->b_job_of.as<int>();
+  bv.bounce_of = ctx->b_bounce_of.as<int>();
+  bv.index_of = ctx->b_index_of.as<long long>();
+  bv.q_retire = ctx->b_retire.as<int>();
+  bv.q_free = ctx->b_free.as<int>();
+  if ((rc = build_batch_graph(ctx, bv, cap)) != ORION_OK) return rc;
+
+  BatchCtl c;
+  std::memset(&c, 0, sizeof(c));
+  c.total = total;
+  c.njobs = njobs;
+  c.counters[CNT_FREE] = cap;
+  // Every live path advances one bounce per iteration: a bound on the loop.
+  const unsigned long long refills = (total + cap - 1) / cap + 1;
+  c.max_iterations = (int)std::min<unsigned long long>(2ULL * refills * (max_depth_all + 2) + 64, 1u << 30);
+  cudaStream_t s = ctx->stream;
+  CUDA_TRY(cudaMemcpyAsync(bv.jobs, dj.data(), njobs * sizeof(DevJob), cudaMemcpyHostToDevice, s));
+  CUDA_TRY(cudaMemcpyAsync(bv.ctl, &c, sizeof(c), cudaMemcpyHostToDevice, s));
+  launch_batch_init(ctx->wave.view, bv, cap, s);
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaEventRecord(ctx->ev0, s));
+  CUDA_TRY(cudaGraphLaunch(ctx->bexec, s));
+  CUDA_TRY(cudaEventRecord(ctx->ev1, s));
+  CUDA_TRY(cudaMemcpyAsync(out_ctl, bv.ctl, sizeof(BatchCtl), cudaMemcpyDeviceToHost, s));
+  CUDA_TRY(cudaStreamSynchronize(s));
+  float ms = 0.f;
+  CUDA_TRY(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+  *ms_out = ms;
+  const BatchCtl& out = *out_ctl;
+  ctx->last.paths = (int64_t)out.paths_done;
+  ctx->last.ext_rays = (int64_t)out.rays[0];
+  ctx->last.shadow_rays = (int64_t)out.rays[1];
+  ctx->last.mis_rays = (int64_t)out.rays[2];
+  ctx->last.rays = (int64_t)(out.rays[0] + out.rays[1] + out.rays[2]);
+  ctx->last.kernel_launches = 9LL * out.iterations + 1;
+  ctx->last.device_ms = ms;
+  if (out.error) return fail(ORION_ERR_DEVICE, "batch loop reached its iteration cap");
+  if (out.paths_done != total)
+    return fail(ORION_ERR_DEVICE, "batch finished " + std::to_string(out.paths_done) + " of " + std::to_string(total) +
+                                      " paths");
+  return ORION_OK;
+}
+
 extern "C" int orion_gpu_render_batch(orion_gpu_ctx* ctx, int32_t njobs, const orion_job* jobs,
                                       orion_batch_stats* stats) {
   if (!ctx || njobs < 0 || (njobs > 0 && !jobs)) return fail(ORION_ERR_INVALID, "bad argument");
@@ -555,8 +626,13 @@ extern "C" int orion_gpu_render_batch(orion_gpu_ctx* ctx, int32_t njobs, const o
     DevJob& J = dj[i];
     std::memset(&J, 0, sizeof(J));
     J.scene = d.view;
-    J.width = d.width;
-    J.height = d.height;
+    if (jobs[i].camera) {
+      if (jobs[i].camera->width <= 0 || jobs[i].camera->height <= 0)
+        return fail(ORION_ERR_INVALID, "job " + std::to_string(i) + ": film size must be positive");
+      J.scene.cam = prepare_camera(*jobs[i].camera);
+    }
+    J.width = J.scene.cam.width;
+    J.height = J.scene.cam.height;
     const int spp = p.spp > 0 ? p.spp : d.spp;
     J.max_depth = p.max_depth >= 0 ? p.max_depth : d.max_depth;
     J.rr_depth = p.rr_depth;
@@ -571,25 +647,7 @@ extern "C" int orion_gpu_render_batch(orion_gpu_ctx* ctx, int32_t njobs, const o
     film_off[i] = film_bytes;
     film_bytes += (size_t)((wh * (3 * 8 * 2 + 4) + 255) & ~255LL);
   }
-  const int slots = (int)std::min<unsigned long long>((unsigned long long)ctx->default_batch_slots,
-                                                       std::max<unsigned long long>(total, 1024ULL));
   int rc;
-  if ((rc = ensure_wave(ctx, slots)) != ORION_OK) return rc;
-  const int cap = ctx->wave.capacity;
-  if (ctx->batch_slots_alloc < cap) {
-    if ((rc = ctx->b_job_of.alloc((size_t)cap * 4)) != ORION_OK) return rc;
-    if ((rc = ctx->b_bounce_of.alloc((size_t)cap * 4)) != ORION_OK) return rc;
-    if ((rc = ctx->b_index_of.alloc((size_t)cap * 8)) != ORION_OK) return rc;
-    if ((rc = ctx->b_retire.alloc((size_t)cap * 4)) != ORION_OK) return rc;
-    if ((rc = ctx->b_free.alloc((size_t)cap * 4)) != ORION_OK) return rc;
-    ctx->batch_slots_alloc = cap;
-  }
-  if (!ctx->b_ctl.p && (rc = ctx->b_ctl.alloc(sizeof(BatchCtl))) != ORION_OK) return rc;
-  if (ctx->jobs_alloc < njobs) {
-    int n = std::max(njobs, 64);
-    if ((rc = ctx->b_jobs.alloc((size_t)n * sizeof(DevJob))) != ORION_OK) return rc;
-    ctx->jobs_alloc = n;
-  }
   if (ctx->b_films.bytes < film_bytes && (rc = ctx->b_films.alloc(film_bytes)) != ORION_OK) return rc;
   char* fb = ctx->b_films.as<char>();
   for (int i = 0; i < njobs; ++i) {
@@ -598,35 +656,12 @@ extern "C" int orion_gpu_render_batch(orion_gpu_ctx* ctx, int32_t njobs, const o
     dj[i].sumsq = dj[i].sum + 3 * wh;
     dj[i].count = reinterpret_cast<unsigned int*>(dj[i].sumsq + 3 * wh);
   }
-  BatchView bv;
-  bv.jobs = ctx->b_jobs.as<DevJob>();
-  bv.ctl = ctx->b_ctl.as<BatchCtl>();
-  bv.job_of = ctx->b_job_of.as<int>();
-  bv.bounce_of = ctx->b_bounce_of.as<int>();
-  bv.index_of = ctx->b_index_of.as<long long>();
-  bv.q_retire = ctx->b_retire.as<int>();
-  bv.q_free = ctx->b_free.as<int>();
-  if ((rc = build_batch_graph(ctx, bv, cap)) != ORION_OK) return rc;
-
-  BatchCtl c;
-  std::memset(&c, 0, sizeof(c));
-  c.total = total;
-  c.njobs = njobs;
-  c.counters[CNT_FREE] = cap;
-  // Every live path advances one bounce per iteration: a bound on the loop.
-  const unsigned long long refills = (total + cap - 1) / cap + 1;
-  c.max_iterations = (int)std::min<unsigned long long>(2ULL * refills * (max_depth_all + 2) + 64, 1u << 30);
   cudaStream_t s = ctx->stream;
-  CUDA_TRY(cudaMemcpyAsync(bv.jobs, dj.data(), njobs * sizeof(DevJob), cudaMemcpyHostToDevice, s));
-  CUDA_TRY(cudaMemcpyAsync(bv.ctl, &c, sizeof(c), cudaMemcpyHostToDevice, s));
   CUDA_TRY(cudaMemsetAsync(ctx->b_films.p, 0, film_bytes, s));
-  launch_batch_init(ctx->wave.view, bv, cap, s);
-  CUDA_TRY(cudaGetLastError());
-  CUDA_TRY(cudaEventRecord(ctx->ev0, s));
-  CUDA_TRY(cudaGraphLaunch(ctx->bexec, s));
-  CUDA_TRY(cudaEventRecord(ctx->ev1, s));
   BatchCtl out;
-  CUDA_TRY(cudaMemcpyAsync(&out, bv.ctl, sizeof(out), cudaMemcpyDeviceToHost, s));
+  float ms = 0.f;
+  rc = run_batch_locked(ctx, dj, total, max_depth_all, &out, &ms);
+  if (rc != ORION_OK) return rc;
   for (int i = 0; i < njobs; ++i) {
     const size_t wh = (size_t)dj[i].width * dj[i].height;
     if (jobs[i].sum) CUDA_TRY(cudaMemcpyAsync(jobs[i].sum, dj[i].sum, wh * 24, cudaMemcpyDeviceToHost, s));
@@ -634,26 +669,13 @@ extern "C" int orion_gpu_render_batch(orion_gpu_ctx* ctx, int32_t njobs, const o
     if (jobs[i].count) CUDA_TRY(cudaMemcpyAsync(jobs[i].count, dj[i].count, wh * 4, cudaMemcpyDeviceToHost, s));
   }
   CUDA_TRY(cudaStreamSynchronize(s));
-  float ms = 0.f;
-  CUDA_TRY(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
   if (stats) {
     stats->paths = (int64_t)out.paths_done;
     stats->rays = (int64_t)(out.rays[0] + out.rays[1] + out.rays[2]);
     stats->iterations = out.iterations;
-    stats->capacity = cap;
+    stats->capacity = ctx->wave.capacity;
     stats->device_ms = ms;
   }
-  ctx->last.paths = (int64_t)out.paths_done;
-  ctx->last.ext_rays = (int64_t)out.rays[0];
-  ctx->last.shadow_rays = (int64_t)out.rays[1];
-  ctx->last.mis_rays = (int64_t)out.rays[2];
-  ctx->last.rays = (int64_t)(out.rays[0] + out.rays[1] + out.rays[2]);
-  ctx->last.kernel_launches = 9LL * out.iterations + 1;
-  ctx->last.device_ms = ms;
-  if (out.error) return fail(ORION_ERR_DEVICE, "batch loop reached its iteration cap");
-  if (out.paths_done != total)
-    return fail(ORION_ERR_DEVICE, "batch finished " + std::to_string(out.paths_done) + " of " + std::to_string(total) +
-                                      " paths");
   return ORION_OK;
 }
 

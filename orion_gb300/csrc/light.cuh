@@ -52,7 +52,7 @@ __device__ __forceinline__ V3 mat3_mul(const float* m, V3 v) {
 // Light::sample_Li for every light type. `prims` gives the emissive
 // triangle of an area light; `world_radius` bounds the scene for distant and
 // environment lights (Bounds3::boundingSphere, src/core/geometry.h:551-554).
-__device__ __noinline__ LightSample sample_li(const DevLight& L, const PrimShade* __restrict__ prims, V3 ref_p,
+static __device__ __noinline__ LightSample sample_li(const DevLight& L, const PrimShade* __restrict__ prims, V3 ref_p,
                                                  float u0, float u1, float world_radius) {
   LightSample s;
   s.valid = false;

@@ -317,17 +317,22 @@ bool prepare_scene(const HostScene& s, PreparedScene* out, std::string* err) {
     out->light_func.push_back(0.f);
   }
 
-  // Pinhole (src/camera/pinhole.h:22-26, src/core/camera.h:24-25).
-  DevCamera& c = out->cam;
-  std::memset(&c, 0, sizeof(c));
-  std::memcpy(c.c2w, s.camera.c2w, sizeof(c.c2w));
-  c.tan_half_fov = std::tan(s.camera.fov * 0.5f * static_cast<float>(0.01745329251994329576923690768489));
-  c.aspect = (float)s.camera.width / s.camera.height;
-  c.lens_radius = s.camera.lens_radius;
-  c.focal_distance = s.camera.focal_distance;
-  c.width = s.camera.width;
-  c.height = s.camera.height;
+  out->cam = prepare_camera(s.camera);
   return true;
+}
+
+// Pinhole (src/camera/pinhole.h:22-26, src/core/camera.h:24-25).
+DevCamera prepare_camera(const orion_camera& cam) {
+  DevCamera c;
+  std::memset(&c, 0, sizeof(c));
+  std::memcpy(c.c2w, cam.c2w, sizeof(c.c2w));
+  c.tan_half_fov = std::tan(cam.fov * 0.5f * static_cast<float>(0.01745329251994329576923690768489));
+  c.aspect = (float)cam.width / cam.height;
+  c.lens_radius = cam.lens_radius;
+  c.focal_distance = cam.focal_distance;
+  c.width = cam.width;
+  c.height = cam.height;
+  return c;
 }
 
 }  // namespace orion_gb300

@@ -23,6 +23,7 @@ struct PreparedScene {
 DevMaterial prepare_material(const orion_material& m);
 // Everything else; returns false with `err` set on inconsistent input.
 bool prepare_scene(const HostScene& s, PreparedScene* out, std::string* err);
+DevCamera prepare_camera(const orion_camera& cam);
 
 float roughness_to_alpha(float roughness);  // src/bsdf/microfacet.h:44-50
 float spectrum_intensity(const float rgb[3]);  // src/core/spectrum.h:88-91
