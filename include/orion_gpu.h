@@ -243,6 +243,53 @@ int orion_gpu_set_config(orion_gpu_ctx* ctx, const orion_launch_config* cfg);
 int orion_gpu_autotune(orion_gpu_ctx* ctx, orion_scene_id id, int32_t spp, double budget_ms,
                        orion_launch_config* best, double* best_mpaths);
 
+/* ------------------------------------------------------------- serving */
+/* A request loop on a context: render requests (a resident scene, a view,
+ * render parameters) are admitted as device memory allows, progress in
+ * chunks of samples per pixel, and every launch traces all admitted requests
+ * together (orion_gpu_render_batch), so requests that arrive while others are
+ * running join the next launch. Scenes are uploaded on first use and stay
+ * resident (least recently used ones are evicted when memory is needed).
+ * A request's result is its film's FP64 sums over all its samples; it does
+ * not depend on which other requests shared its launches. */
+typedef struct orion_server orion_server;
+
+typedef struct orion_server_opts {
+  int64_t memory_budget;   /* bytes for resident scenes + request films + path slots; 0 = context budget */
+  int32_t spp_chunk;       /* samples per pixel a request advances per launch; 0 = 4 */
+  int32_t max_jobs;        /* requests in one launch; 0 = 512 */
+} orion_server_opts;
+
+enum { ORION_REQ_QUEUED = 0, ORION_REQ_RUNNING = 1, ORION_REQ_DONE = 2, ORION_REQ_CANCELLED = 3, ORION_REQ_FAILED = 4 };
+
+typedef struct orion_request_status {
+  int32_t state;
+  int32_t spp_done, spp_total;
+  int32_t width, height;
+  int32_t reserved;
+  double t_submit, t_admit, t_done;  /* seconds since the server started; 0 until reached */
+} orion_request_status;
+
+typedef struct orion_server_stats {
+  int64_t submitted, completed, launches, paths, resident_scenes, bytes_in_use;
+  double device_ms;
+} orion_server_stats;
+
+int orion_server_create(orion_gpu_ctx* ctx, const orion_server_opts* opts, orion_server** out);
+/* `scene` must stay alive until the request is released. camera: NULL = the scene's view. */
+int orion_server_submit(orion_server* srv, const orion_host_scene* scene, const orion_render_params* params,
+                        const orion_camera* camera, int64_t* ticket);
+int orion_server_status(orion_server* srv, int64_t ticket, orion_request_status* out);
+/* ORION_OK once the request is done, ORION_ERR_NOT_READY after `timeout_s` seconds. */
+int orion_server_wait(orion_server* srv, int64_t ticket, double timeout_s);
+/* Copies the request's film so far (progressive results): W*H*3 sums and sums of squares, W*H counts. */
+int orion_server_result(orion_server* srv, int64_t ticket, double* sum, double* sumsq, uint32_t* count);
+int orion_server_cancel(orion_server* srv, int64_t ticket);
+/* Frees a finished, failed or cancelled request's film. */
+int orion_server_release(orion_server* srv, int64_t ticket);
+int orion_server_stats_get(orion_server* srv, orion_server_stats* out);
+int orion_server_destroy(orion_server* srv);
+
 /* ------------------------------------------------- component test hooks */
 /* sobol::sample (src/sampler/sobol.h:28-43) for n (index, dim) pairs. */
 int orion_gpu_sobol(orion_gpu_ctx* ctx, int64_t n, const uint64_t* index, const uint32_t* dim, float* out);

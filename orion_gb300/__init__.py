@@ -90,8 +90,8 @@ STAGES = ("camera", "trace_ext", "shade", "trace_shadow", "trace_mis", "resolve"
 
 
 class Job(C.Structure):
-    _fields_ = [("scene", C.c_int32), ("reserved", C.c_int32), ("params", RenderParams), ("sum", C.c_void_p),
-                ("sumsq", C.c_void_p), ("count", C.c_void_p)]
+    _fields_ = [("scene", C.c_int32), ("reserved", C.c_int32), ("params", RenderParams), ("camera", C.c_void_p),
+                ("sum", C.c_void_p), ("sumsq", C.c_void_p), ("count", C.c_void_p)]
 
 
 class BatchStats(C.Structure):
@@ -103,6 +103,23 @@ class LaunchConfig(C.Structure):
     _fields_ = [("trace_block", C.c_int32), ("shade_block", C.c_int32), ("smem_stack", C.c_int32),
                 ("blocks_per_sm", C.c_int32), ("wave_paths", C.c_int32), ("batch_slots", C.c_int32),
                 ("refill_below", C.c_int32), ("reserved", C.c_int32)]
+
+class ServerOpts(C.Structure):
+    _fields_ = [("memory_budget", C.c_int64), ("spp_chunk", C.c_int32), ("max_jobs", C.c_int32)]
+
+
+class RequestStatus(C.Structure):
+    _fields_ = [("state", C.c_int32), ("spp_done", C.c_int32), ("spp_total", C.c_int32), ("width", C.c_int32),
+                ("height", C.c_int32), ("reserved", C.c_int32), ("t_submit", C.c_double), ("t_admit", C.c_double),
+                ("t_done", C.c_double)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_int64), ("completed", C.c_int64), ("launches", C.c_int64), ("paths", C.c_int64),
+                ("resident_scenes", C.c_int64), ("bytes_in_use", C.c_int64), ("device_ms", C.c_double)]
+
+
+REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_CANCELLED, REQ_FAILED = range(5)
 
 _lib = None
 
@@ -135,6 +152,15 @@ def library() -> C.CDLL:
             "orion_gpu_get_config": (i32, [vp, C.POINTER(LaunchConfig)]),
             "orion_gpu_set_config": (i32, [vp, C.POINTER(LaunchConfig)]),
             "orion_gpu_autotune": (i32, [vp, i32, i32, C.c_double, C.POINTER(LaunchConfig), C.POINTER(C.c_double)]),
+            "orion_server_create": (i32, [vp, C.POINTER(ServerOpts), C.POINTER(vp)]),
+            "orion_server_submit": (i32, [vp, vp, C.POINTER(RenderParams), vp, C.POINTER(i64)]),
+            "orion_server_status": (i32, [vp, i64, C.POINTER(RequestStatus)]),
+            "orion_server_wait": (i32, [vp, i64, C.c_double]),
+            "orion_server_result": (i32, [vp, i64, vp, vp, vp]),
+            "orion_server_cancel": (i32, [vp, i64]),
+            "orion_server_release": (i32, [vp, i64]),
+            "orion_server_stats_get": (i32, [vp, C.POINTER(ServerStats)]),
+            "orion_server_destroy": (i32, [vp]),
             "orion_gpu_sobol": (i32, [vp, i64, vp, vp, vp]),
             "orion_gpu_trace": (i32, [vp, i32, i64, vp, i32, vp, vp, vp, vp]),
             "orion_gpu_camera_rays": (i32, [vp, i32, i64, vp, vp]),
@@ -308,6 +334,8 @@ class Context:
             arr[i].params = RenderParams(spp=j.get("spp", 0), max_depth=j.get("max_depth", -1),
                                          rr_depth=j.get("rr_depth", 3), first_pass=j.get("first_pass", 0))
             arr[i].sum, arr[i].sumsq, arr[i].count = s.ctypes.data, q.ctypes.data, c.ctypes.data
+            if j.get("camera") is not None:
+                arr[i].camera = C.addressof(j["camera"])
         st = BatchStats()
         _check(library().orion_gpu_render_batch(self._h, len(jobs), C.cast(arr, C.c_void_p), C.byref(st)))
         return outs, {k: getattr(st, k) for k, _ in BatchStats._fields_}
@@ -446,3 +474,86 @@ class Parser:
 
     def getRenderOption(self) -> RenderOption:
         return self._ro
+
+
+# ------------------------------------------------------------------ serving
+
+
+def look_at_camera(eye, look, up, fov: float, width: int, height: int, lens_radius: float = 0.0,
+                   focal_distance: float = 0.0) -> Camera:
+    """A pinhole / thin-lens view for serving requests (camera-to-world as the reference's lookAt)."""
+    f = np.asarray(look, np.float64) - np.asarray(eye, np.float64)
+    f /= np.linalg.norm(f)
+    s = np.cross(f, np.asarray(up, np.float64))
+    s /= np.linalg.norm(s)
+    u = np.cross(s, f)
+    m = np.eye(4)
+    m[:3, 0], m[:3, 1], m[:3, 2], m[:3, 3] = s, u, -f, eye
+    cam = Camera()
+    cam.c2w[:] = [float(x) for x in m.astype(np.float32).ravel()]
+    cam.fov, cam.lens_radius, cam.focal_distance = fov, lens_radius, focal_distance
+    cam.width, cam.height = width, height
+    return cam
+
+
+class Server:
+    """Request loop on a context: submit(scene, view, params) -> ticket; wait; result; release."""
+
+    def __init__(self, ctx: Context, memory_budget: int = 0, spp_chunk: int = 4, max_jobs: int = 512):
+        h = C.c_void_p()
+        _check(library().orion_server_create(ctx._h, C.byref(ServerOpts(memory_budget, spp_chunk, max_jobs)),
+                                             C.byref(h)))
+        self._h, self.ctx = h, ctx
+        self._keep = {}
+
+    def submit(self, scene: HostScene, spp: int = 0, max_depth: int = -1, rr_depth: int = 3, first_pass: int = 0,
+               camera: Camera | None = None) -> int:
+        t = C.c_int64()
+        p = RenderParams(spp=spp, max_depth=max_depth, rr_depth=rr_depth, first_pass=first_pass)
+        cam = C.byref(camera) if camera is not None else None
+        _check(library().orion_server_submit(self._h, scene._h, C.byref(p), cam, C.byref(t)))
+        self._keep[t.value] = scene
+        return t.value
+
+    def status(self, ticket: int) -> dict:
+        st = RequestStatus()
+        _check(library().orion_server_status(self._h, ticket, C.byref(st)))
+        return {k: getattr(st, k) for k, _ in RequestStatus._fields_}
+
+    def wait(self, ticket: int, timeout: float = 60.0) -> bool:
+        rc = library().orion_server_wait(self._h, ticket, timeout)
+        if rc == -8:
+            return False
+        _check(rc)
+        return True
+
+    def result(self, ticket: int):
+        st = self.status(ticket)
+        h, w = st["height"], st["width"]
+        s, q = np.zeros((h, w, 3), np.float64), np.zeros((h, w, 3), np.float64)
+        c = np.zeros((h, w), np.uint32)
+        _check(library().orion_server_result(self._h, ticket, _ptr(s), _ptr(q), _ptr(c)))
+        return s, q, c
+
+    def cancel(self, ticket: int) -> None:
+        _check(library().orion_server_cancel(self._h, ticket))
+
+    def release(self, ticket: int) -> None:
+        _check(library().orion_server_release(self._h, ticket))
+        self._keep.pop(ticket, None)
+
+    def stats(self) -> dict:
+        st = ServerStats()
+        _check(library().orion_server_stats_get(self._h, C.byref(st)))
+        return {k: getattr(st, k) for k, _ in ServerStats._fields_}
+
+    def close(self) -> None:
+        if self._h and self._h.value:
+            library().orion_server_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

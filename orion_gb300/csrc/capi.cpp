@@ -20,6 +20,7 @@
 
 #include "../../include/orion_gpu.h"
 #include "bvh_build.h"
+#include "internal.h"
 #include "kernels.h"
 #include "scene_host.h"
 #include "scene_prep.h"
@@ -678,6 +679,76 @@ extern "C" int orion_gpu_render_batch(orion_gpu_ctx* ctx, int32_t njobs, const o
   }
   return ORION_OK;
 }
+
+// ------------------------------------------------------ internal hooks
+
+namespace orion_gb300 {
+
+int ctx_fail(int code, const char* msg) { return fail(code, msg); }
+int ctx_device(orion_gpu_ctx* ctx) { return ctx->device; }
+cudaStream_t ctx_stream(orion_gpu_ctx* ctx) { return ctx->stream; }
+int64_t ctx_pool_bytes(orion_gpu_ctx* ctx) { return (int64_t)ctx->wave.block.bytes; }
+
+int ctx_copy_to_host(orion_gpu_ctx* ctx, void* dst, const void* src, size_t bytes) {
+  std::lock_guard<std::mutex> g(ctx->mu);
+  CUDA_TRY(cudaSetDevice(ctx->device));
+  CUDA_TRY(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return ORION_OK;
+}
+
+int ctx_scene_info(orion_gpu_ctx* ctx, orion_scene_id id, int* width, int* height, int* spp, int* max_depth) {
+  std::lock_guard<std::mutex> g(ctx->mu);
+  auto it = ctx->scenes.find(id);
+  if (it == ctx->scenes.end()) return fail(ORION_ERR_INVALID, "unknown scene id");
+  *width = it->second->width;
+  *height = it->second->height;
+  *spp = it->second->spp;
+  *max_depth = it->second->max_depth;
+  return ORION_OK;
+}
+
+int ctx_run_device_jobs(orion_gpu_ctx* ctx, const DeviceFilmJob* jobs, int njobs, double* device_ms,
+                        int64_t* paths) {
+  std::lock_guard<std::mutex> g(ctx->mu);
+  CUDA_TRY(cudaSetDevice(ctx->device));
+  std::vector<DevJob> dj(njobs);
+  unsigned long long total = 0;
+  int max_depth_all = 0;
+  for (int i = 0; i < njobs; ++i) {
+    auto it = ctx->scenes.find(jobs[i].scene);
+    if (it == ctx->scenes.end()) return fail(ORION_ERR_INVALID, "unknown scene id");
+    const DeviceScene& d = *it->second;
+    const orion_render_params& p = jobs[i].params;
+    DevJob& J = dj[i];
+    std::memset(&J, 0, sizeof(J));
+    J.scene = d.view;
+    if (jobs[i].camera) J.scene.cam = prepare_camera(*jobs[i].camera);
+    J.width = J.scene.cam.width;
+    J.height = J.scene.cam.height;
+    const int spp = p.spp > 0 ? p.spp : d.spp;
+    J.max_depth = p.max_depth >= 0 ? p.max_depth : d.max_depth;
+    J.rr_depth = p.rr_depth;
+    if (J.max_depth > 120) return fail(ORION_ERR_INVALID, "max_depth out of range");
+    const long long wh = (long long)J.width * J.height;
+    J.first_index = p.first_pass * wh;
+    J.num_paths = wh * spp;
+    J.work_begin = (long long)total;
+    total += (unsigned long long)J.num_paths;
+    max_depth_all = std::max(max_depth_all, J.max_depth);
+    J.sum = jobs[i].sum;
+    J.sumsq = jobs[i].sumsq;
+    J.count = jobs[i].count;
+  }
+  BatchCtl out;
+  float ms = 0.f;
+  int rc = run_batch_locked(ctx, dj, total, max_depth_all, &out, &ms);
+  if (device_ms) *device_ms = ms;
+  if (paths) *paths = (int64_t)out.paths_done;
+  return rc;
+}
+
+}  // namespace orion_gb300
 
 // ---------------------------------------------------- launch config, tuning
 
