@@ -531,3 +531,115 @@ def zoo(res: int = 64, spp: int = 16, max_depth: int = 6, subdiv: int = 2, beckm
     s.lights.append({"type": "distant", "L": (0.4, 0.35, 0.3), "from": (1.0, 3.0, 1.0), "to": (0.0, 0.0, 0.0)})
     s.envmaps.append({"L": (0.05, 0.06, 0.08), "worldUp": (0, 1, 0)})
     return s
+
+
+# --------------------------------------------------------------------------
+# in-memory host scenes (no OBJ text): for the batched and served workloads
+
+
+def _material_record(m: dict):
+    from orion_gb300 import Material
+    r = Material()
+    kinds = {"matte": 0, "metal": 1, "mirror": 2, "glass": 3, "plastic": 4, "uber": 5}
+    r.type = kinds[m["type"]]
+    r.distribution = 1 if m.get("distribution") == "beckmann" else 0
+    for src, dst in [("Kd", "Kd"), ("Ks", "Ks"), ("Kr", "Kr"), ("Kt", "Kt"), ("opacity", "opacity"),
+                     ("eta", "eta_rgb" if m["type"] == "metal" else None), ("k", "k")]:
+        if src in m and dst is not None:
+            getattr(r, dst)[:] = [float(np.float32(x)) for x in m[src]]
+    if m["type"] == "matte" and "sigma" in m:
+        r.has_sigma, r.sigma = 1, m["sigma"]
+    if "roughness" in m:
+        r.roughness = m["roughness"]
+    if m["type"] in ("glass", "uber"):
+        r.eta = m["eta"]
+    return r
+
+
+def _basis_rows(d):
+    """Rows (x, y, d) of the frame the reference builds for a spot light (coordinateSystem)."""
+    d = np.asarray(d, np.float64) / np.linalg.norm(d)
+    if abs(d[0]) > abs(d[1]):
+        y = np.array([-d[2], 0.0, d[0]]) / np.hypot(d[0], d[2])
+    else:
+        y = np.array([0.0, d[2], -d[1]]) / np.hypot(d[1], d[2])
+    return np.cross(y, d), y, d
+
+
+def to_host_scene(scene: Scene):
+    """The scene as an orion_gb300.HostScene built from arrays.
+
+    Geometry, materials and light order are identical to writing the scene out and loading it;
+    light frames agree with the loader's to float rounding (computed here in float64)."""
+    import orion_gb300 as og
+    P, N, mesh_of = scene.flat()
+    mats = [_material_record(m.material) for m in scene.meshes]
+    lights, light_of = [], np.full(len(P), -1, np.int32)
+    for i, m in enumerate(scene.meshes):
+        if m.area_le is None:
+            continue
+        for prim in np.flatnonzero(mesh_of == i):
+            L = og.Light()
+            L.type, L.prim = og.LIGHT_AREA, int(prim)
+            L.L[:] = list(m.area_le)
+            light_of[prim] = len(lights)
+            lights.append(L)
+    for l in scene.lights:
+        L = og.Light()
+        if l["type"] == "point":
+            L.type = og.LIGHT_POINT
+            L.L[:], L.p[:] = list(l["I"]), list(l["from"])
+        elif l["type"] == "spot":
+            L.type = og.LIGHT_SPOT
+            L.L[:], L.p[:] = list(l["intensity"]), list(l["from"])
+            x, y, d = _basis_rows(np.asarray(l["to"], np.float64) - np.asarray(l["from"], np.float64))
+            w2l = np.zeros((3, 4))
+            w2l[:, :3] = np.stack([x, y, d])
+            w2l[:, 3] = -w2l[:, :3] @ np.asarray(l["from"], np.float64)
+            l2w = np.zeros((3, 4))
+            l2w[:, :3] = w2l[:, :3].T
+            l2w[:, 3] = np.asarray(l["from"], np.float64)
+            L.w2l[:] = [float(v) for v in w2l.astype(np.float32).ravel()]
+            L.l2w[:] = [float(v) for v in l2w.astype(np.float32).ravel()]
+            L.cos_total = float(np.float32(math.cos(math.radians(l["angle"]))))
+            L.cos_falloff = float(np.float32(math.cos(math.radians(l["angle"] - l["delta"]))))
+        elif l["type"] == "distant":
+            L.type = og.LIGHT_DISTANT
+            L.L[:] = list(l["L"])
+            d = np.asarray(l["to"], np.float64) - np.asarray(l["from"], np.float64)
+            L.dir[:] = list(d / np.linalg.norm(d))
+        lights.append(L)
+    for e in scene.envmaps:
+        L = og.Light()
+        L.type = og.LIGHT_ENV
+        L.L[:] = list(e["L"])
+        up = np.asarray(e["worldUp"], np.float64)
+        up /= np.linalg.norm(up)
+        z = np.array([0.0, 0.0, 1.0])
+        R = np.eye(3)
+        c = float(up @ z)
+        if -0.99 < c < 0.99:
+            R = rotation(np.cross(z, up), math.degrees(math.acos(c)))
+        l2w = np.zeros((3, 4))
+        l2w[:, :3] = R
+        w2l = np.zeros((3, 4))
+        w2l[:, :3] = R.T
+        L.l2w[:] = [float(v) for v in l2w.astype(np.float32).ravel()]
+        L.w2l[:] = [float(v) for v in w2l.astype(np.float32).ravel()]
+        lights.append(L)
+    cam = og.look_at_camera(scene.eye, scene.look, scene.up, scene.fov, scene.width, scene.height,
+                            scene.lens_radius, scene.focal_distance)
+    return og.HostScene.from_arrays(P, N, mesh_of, mats, lights, cam, scene.spp, scene.max_depth,
+                                    light_of_prim=light_of)
+
+
+def job_views(seed: int, views: int = 16):
+    """`views` cameras orbiting a job's scene (serving: one resident scene, many views)."""
+    import orion_gb300 as og
+    s = job(seed)
+    out = []
+    for v in range(views):
+        ang = 2 * math.pi * v / views
+        eye = (7.0 * math.sin(ang), 1.5 + 0.5 * math.sin(3 * ang), 7.0 * math.cos(ang))
+        out.append(og.look_at_camera(eye, (0.0, 0.0, 0.0), (0, 1, 0), 45.0, s.width, s.height))
+    return out
