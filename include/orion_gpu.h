@@ -297,6 +297,21 @@ int orion_gpu_sobol(orion_gpu_ctx* ctx, int64_t n, const uint64_t* index, const 
  * n x 8 floats (o, d, tnear, tfar). prim = -1 for a miss. */
 int orion_gpu_trace(orion_gpu_ctx* ctx, orion_scene_id id, int64_t n, const float* rays, int32_t any_hit,
                     float* t, float* u, float* v, int32_t* prim);
+/* orion_gpu_trace without any device allocation. No counterpart in the
+ * reference: it exists for callers that must not allocate, such as a ray query
+ * (picking) from a second context while a long render runs on the same device
+ * (cudaFree in orion_gpu_trace synchronises the whole device, and a serving
+ * memory budget has already committed every device byte). Rays and hits go
+ * through one fixed static device array of ORION_NOALLOC_MAX_RAYS rays
+ * (3 MiB); larger n is rejected with ORION_ERR_INVALID. Nothing in that array
+ * must start at zero. Calls on one context are serialised by the context; calls
+ * that overlap on one device from different contexts race on the array. The
+ * first call on a device looks up the array's address and should come before
+ * any stream capture on that device. Same arguments and results as
+ * orion_gpu_trace. */
+#define ORION_NOALLOC_MAX_RAYS 65536
+int orion_gpu_trace_noalloc(orion_gpu_ctx* ctx, orion_scene_id id, int64_t n, const float* rays, int32_t any_hit,
+                            float* t, float* u, float* v, int32_t* prim);
 /* Camera rays (src/camera/pinhole.cpp:8-33) for sample indices: n x 6 floats. */
 int orion_gpu_camera_rays(orion_gpu_ctx* ctx, orion_scene_id id, int64_t n, const int64_t* sample_index,
                           float* rays);

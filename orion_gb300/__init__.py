@@ -32,6 +32,7 @@ ERRORS = {-1: "invalid", -2: "io", -3: "parse", -4: "cuda", -5: "nomem", -6: "un
 MAT_MATTE, MAT_METAL, MAT_MIRROR, MAT_GLASS, MAT_PLASTIC, MAT_UBER = range(6)
 DIST_GGX, DIST_BECKMANN = 0, 1
 LIGHT_AREA, LIGHT_POINT, LIGHT_SPOT, LIGHT_DISTANT, LIGHT_ENV = range(5)
+NOALLOC_MAX_RAYS = 65536  # ORION_NOALLOC_MAX_RAYS
 BXDF_ALL = 31
 BXDF_NONSPECULAR = 31 & ~16
 
@@ -163,6 +164,7 @@ def library() -> C.CDLL:
             "orion_server_destroy": (i32, [vp]),
             "orion_gpu_sobol": (i32, [vp, i64, vp, vp, vp]),
             "orion_gpu_trace": (i32, [vp, i32, i64, vp, i32, vp, vp, vp, vp]),
+            "orion_gpu_trace_noalloc": (i32, [vp, i32, i64, vp, i32, vp, vp, vp, vp]),
             "orion_gpu_camera_rays": (i32, [vp, i32, i64, vp, vp]),
             "orion_gpu_bsdf_eval": (i32, [vp, C.POINTER(Material), i64, vp, vp, vp, vp, i32, vp, vp, vp, vp, vp,
                                           vp, vp]),
@@ -371,6 +373,16 @@ class Context:
         prim = np.zeros(n, np.int32)
         _check(library().orion_gpu_trace(self._h, sid, n, _ptr(rays), int(any_hit), _ptr(t), _ptr(u), _ptr(v),
                                          _ptr(prim)))
+        return t, u, v, prim
+
+    def trace_noalloc(self, sid: int, rays, any_hit: bool = False):
+        """trace() through a fixed device scratch of NOALLOC_MAX_RAYS rays: no device allocation."""
+        rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
+        n = len(rays)
+        t, u, v = (np.zeros(n, np.float32) for _ in range(3))
+        prim = np.zeros(n, np.int32)
+        _check(library().orion_gpu_trace_noalloc(self._h, sid, n, _ptr(rays), int(any_hit), _ptr(t), _ptr(u),
+                                                 _ptr(v), _ptr(prim)))
         return t, u, v, prim
 
     def camera_rays(self, sid: int, sample_index) -> np.ndarray:

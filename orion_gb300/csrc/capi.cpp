@@ -931,6 +931,36 @@ extern "C" int orion_gpu_trace(orion_gpu_ctx* ctx, orion_scene_id id, int64_t n,
   return ORION_OK;
 }
 
+extern "C" int orion_gpu_trace_noalloc(orion_gpu_ctx* ctx, orion_scene_id id, int64_t n, const float* rays,
+                                       int32_t any_hit, float* t, float* u, float* v, int32_t* prim) {
+  if (!ctx || n < 0 || (n > 0 && (!rays || !t || !u || !v || !prim))) return fail(ORION_ERR_INVALID, "bad argument");
+  if (n > ORION_NOALLOC_MAX_RAYS)
+    return fail(ORION_ERR_INVALID, "orion_gpu_trace_noalloc: " + std::to_string(n) +
+                                       " rays exceed its fixed scratch of ORION_NOALLOC_MAX_RAYS = " +
+                                       std::to_string(ORION_NOALLOC_MAX_RAYS) +
+                                       " rays; split the query or call orion_gpu_trace");
+  std::lock_guard<std::mutex> g(ctx->mu);
+  CUDA_TRY(cudaSetDevice(ctx->device));
+  auto it = ctx->scenes.find(id);
+  if (it == ctx->scenes.end()) return fail(ORION_ERR_INVALID, "unknown scene id");
+  unsigned char* base = nullptr;
+  std::string err;
+  if (noalloc_trace_scratch(ctx->device, &base, &err) != cudaSuccess) return fail(ORION_ERR_CUDA, err);
+  if (n == 0) return ORION_OK;
+  float *dr, *dt, *du, *dv;
+  int* dp;
+  noalloc_trace_layout(base, &dr, &dt, &du, &dv, &dp);
+  CUDA_TRY(cudaMemcpyAsync(dr, rays, (size_t)n * 8 * sizeof(float), cudaMemcpyHostToDevice, ctx->stream));
+  launch_trace(it->second->view, n, dr, any_hit, dt, du, dv, dp, ctx->cfg, ctx->stream);
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaMemcpyAsync(t, dt, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+  CUDA_TRY(cudaMemcpyAsync(u, du, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+  CUDA_TRY(cudaMemcpyAsync(v, dv, (size_t)n * sizeof(float), cudaMemcpyDeviceToHost, ctx->stream));
+  CUDA_TRY(cudaMemcpyAsync(prim, dp, (size_t)n * sizeof(int32_t), cudaMemcpyDeviceToHost, ctx->stream));
+  CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return ORION_OK;
+}
+
 extern "C" int orion_gpu_camera_rays(orion_gpu_ctx* ctx, orion_scene_id id, int64_t n, const int64_t* sample_index,
                                      float* rays) {
   if (!ctx || n < 0 || (n > 0 && (!sample_index || !rays))) return fail(ORION_ERR_INVALID, "bad argument");

@@ -4,6 +4,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <string>
+
 #include "../../include/orion_gpu.h"
 
 namespace orion_gb300 {
@@ -30,5 +32,11 @@ int64_t ctx_pool_bytes(orion_gpu_ctx* ctx);
 int ctx_copy_to_host(orion_gpu_ctx* ctx, void* dst, const void* src, size_t bytes);
 // Records an error message for orion_last_error() and returns `code`.
 int ctx_fail(int code, const char* msg);
+
+// Fixed trace scratch of orion_gpu_trace_noalloc (noalloc.cu): the device's
+// array address (looked up once per device; returns a cudaError_t) and its
+// sections.
+int noalloc_trace_scratch(int device, unsigned char** out, std::string* err);
+void noalloc_trace_layout(unsigned char* base, float** rays, float** t, float** u, float** v, int** prim);
 
 }  // namespace orion_gb300
