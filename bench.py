@@ -18,6 +18,14 @@ Russian roulette after bounce 3.
   one path per OpenMP thread, project CPU BVH in Embree's place) timed on a
   bounded sample of the same workload on this machine's host cores.
 
+* batched -- 64 seeded jobs (1-6 displaced icospheres, 1k-500k triangles,
+  128^2..1024^2, 4/16/64 spp, depth 4-12): one render call per image against
+  one batched graph launch tuned by the batch autotuner; requests/s of each.
+* served -- an open-loop Poisson request stream (16 resident scenes x 16
+  views) through the serving loop at several arrival rates: requests/s,
+  Mpaths/s and p50/p95/p99 latency, beside the plain per-image path with the
+  scene resident and with the scene built and uploaded per image.
+
 N > 1: one process per GPU (torchrun), independent replicas rendering
 disjoint sample passes of the same image; value = all paths / max time.
 """
@@ -262,12 +270,184 @@ def run_ours(args) -> dict:
         "host_build_s": round(build_s, 3),
         "wall_s": round(wall, 3),
     }
+    ctx.release(sid)
+    if rank == 0 and args.batch_jobs > 0:
+        out["batched"] = run_batched(ctx, args.batch_jobs, steps=max(1, min(args.steps, 3)), tune_ms=args.tune_ms)
+    if rank == 0 and args.serve_scenes > 0:
+        out["served"] = run_served(ctx, args.serve_scenes, args.serve_views, args.serve_rates, args.serve_requests,
+                                   budget_gb=150.0, spp_chunk=args.spp_chunk, plain_n=args.plain_requests)
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(args.workload, threads=os.cpu_count() or 1, seconds=args.cpu_seconds)
     ctx.close()
     if dist is not None:
         dist.destroy_process_group()
     return out if rank == 0 else None
+
+
+def make_jobs(first_seed: int, n: int) -> list:
+    """(scene, host scene) for `n` seeded jobs of the batched/served distribution."""
+    from orion_gb300 import scenegen
+    out = []
+    for i in range(n):
+        s = scenegen.job(first_seed + i)
+        out.append((s, scenegen.to_host_scene(s)))
+    return out
+
+
+def _rel_rmse(a: np.ndarray, b: np.ndarray) -> float:
+    return float(np.sqrt(np.mean((a - b) ** 2)) / max(float(np.sqrt(np.mean(b ** 2))), 1e-30))
+
+
+def run_batched(ctx, n_jobs: int, steps: int, tune_ms: float) -> dict:
+    """64 independent jobs: one render call per image (plain) against one batched graph launch.
+
+    Both arms render the same sample indices of the same jobs, so their images
+    agree to float rounding (matched RMSE by construction; rmse_batched_vs_plain
+    checks it on the first jobs). Scenes are resident in both arms.
+    """
+    t0 = time.time()
+    jobs = make_jobs(0, n_jobs)
+    gen_s = time.time() - t0
+    t0 = time.time()
+    sids = [ctx.upload(h) for _, h in jobs]
+    upload_s = time.time() - t0
+    specs = [dict(sid=sid, width=s.width, height=s.height, spp=s.spp) for sid, (s, _) in zip(sids, jobs)]
+    paths = sum(s.width * s.height * s.spp for s, _ in jobs)
+    tris = [int(h.desc().num_prims) for _, h in jobs]
+
+    def plain_pass():
+        t, dev, imgs = time.perf_counter(), 0.0, []
+        for j in specs:
+            img, cnt = ctx.render(j["sid"], j["width"], j["height"], spp=j["spp"])
+            dev += ctx.last_stats()["device_ms"]
+            if len(imgs) < 4:
+                imgs.append(img / np.maximum(cnt, 1)[..., None])
+        return (time.perf_counter() - t) * 1e3, dev, imgs
+
+    def batch_pass():
+        t = time.perf_counter()
+        outs, st = ctx.render_batch(specs)
+        return (time.perf_counter() - t) * 1e3, st["device_ms"], [s / np.maximum(c, 1)[..., None]
+                                                                  for s, _, c in outs[:4]], st
+
+    plain_pass()  # warm-up
+    plain = [plain_pass() for _ in range(steps)]
+    tuned, tuned_mp = ctx.autotune_batch(specs, spp_cap=4, budget_ms=tune_ms)
+    batch_pass()  # warm-up (graph instantiation at the tuned configuration)
+    batched = [batch_pass() for _ in range(steps)]
+    p_wall = float(np.median([p[0] for p in plain]))
+    b_wall = float(np.median([b[0] for b in batched]))
+    p_dev = float(np.median([p[1] for p in plain]))
+    b_dev = float(np.median([b[1] for b in batched]))
+    rmse = max(_rel_rmse(b, p.astype(np.float64)) for b, p in zip(batched[-1][2], plain[-1][2]))
+    for sid in sids:
+        ctx.release(sid)
+    return {
+        "jobs": n_jobs, "seeds": [0, n_jobs - 1], "paths_per_step": int(paths), "triangles_total": int(sum(tris)),
+        "plain": {"req_s": round(n_jobs / (p_wall * 1e-3), 2), "mpaths_s": round(paths / (p_wall * 1e-3) / 1e6, 2),
+                  "wall_ms": round(p_wall, 2), "device_ms": round(p_dev, 2), "launch_calls": n_jobs},
+        "batched": {"req_s": round(n_jobs / (b_wall * 1e-3), 2), "mpaths_s": round(paths / (b_wall * 1e-3) / 1e6, 2),
+                    "wall_ms": round(b_wall, 2), "device_ms": round(b_dev, 2), "launch_calls": 1,
+                    "loop_iterations": int(batched[-1][3]["iterations"]), "slots": int(batched[-1][3]["capacity"])},
+        "req_s_ratio": round(p_wall / b_wall, 3),
+        "rmse_batched_vs_plain": rmse,
+        "autotuned": {**tuned, "tuning_mpaths_s": round(tuned_mp, 2), "budget_ms": tune_ms, "spp_cap": 4},
+        "scene_gen_s": round(gen_s, 2), "upload_build_s": round(upload_s, 2),
+    }
+
+
+def run_served(ctx, n_scenes: int, views: int, rates: list, per_rate: int, budget_gb: float, spp_chunk: int,
+               plain_n: int) -> dict:
+    """Open-loop Poisson request stream through the serving loop, against the plain per-image path.
+
+    Requests are (scene, view) pairs of `n_scenes` seeded jobs x `views` orbit
+    cameras, shuffled with a fixed seed. A warm-up request per scene makes
+    every scene resident first. Latency = completion - submission on the
+    server's clock. The plain arms render the first `plain_n` requests one
+    orion_gpu_render call each: `plain_resident` with every view's scene
+    already uploaded, `plain_cold` uploading (BVH build + copy) per image.
+    """
+    import orion_gb300 as og
+    from orion_gb300 import scenegen
+    rng = np.random.default_rng(2024)
+    jobs = make_jobs(1000, n_scenes)
+    cams = [scenegen.job_views(s, views) for s, _ in jobs]
+    reqs = [(i, v) for i in range(n_scenes) for v in range(views)]
+    rng.shuffle(reqs)
+    srv = og.Server(ctx, memory_budget=int(budget_gb * 1e9), spp_chunk=spp_chunk)
+    warm = [srv.submit(h, spp=s.spp, camera=cams[i][0]) for i, (s, h) in enumerate(jobs)]
+    for t in warm:
+        srv.wait(t, timeout=600)
+        srv.release(t)
+    sweeps = []
+    for rate in rates:
+        sel = [reqs[k % len(reqs)] for k in range(per_rate)]
+        gaps = rng.exponential(1.0 / rate, size=len(sel))
+        t0 = time.perf_counter()
+        arrive = t0 + np.cumsum(gaps)
+        tickets = []
+        for (i, v), ta in zip(sel, arrive):
+            dt = ta - time.perf_counter()
+            if dt > 0:
+                time.sleep(dt)
+            s, h = jobs[i]
+            tickets.append(srv.submit(h, spp=s.spp, camera=cams[i][v]))
+        for t in tickets:
+            srv.wait(t, timeout=900)
+        st = [srv.status(t) for t in tickets]
+        for t in tickets:
+            srv.release(t)
+        lat = np.array([x["t_done"] - x["t_submit"] for x in st]) * 1e3
+        span = max(x["t_done"] for x in st) - min(x["t_submit"] for x in st)
+        paths = sum(jobs[i][0].width * jobs[i][0].height * jobs[i][0].spp for i, _ in sel)
+        sweeps.append({"rate_req_s": rate, "requests": len(sel), "req_s": round(len(sel) / span, 2),
+                       "mpaths_s": round(paths / span / 1e6, 2), "p50_ms": round(float(np.percentile(lat, 50)), 1),
+                       "p95_ms": round(float(np.percentile(lat, 95)), 1),
+                       "p99_ms": round(float(np.percentile(lat, 99)), 1)})
+    stats = srv.stats()
+    srv.close()
+
+    # Plain per-image path on the first plain_n requests.
+    sel = reqs[:plain_n]
+    arrays = {i: jobs[i][1].arrays() for i in {i for i, _ in sel}}
+
+    def view_host(i, v):  # the job's scene seen from view v, as a scene of its own
+        a = arrays[i]
+        return og.HostScene.from_arrays(a["positions"], a["normals"], a["material_of_prim"], a["materials"],
+                                        a["lights"], cams[i][v], a["spp"], a["max_depth"],
+                                        light_of_prim=a["light_of_prim"])
+
+    def render(sid, i, v):
+        ctx.render(sid, cams[i][v].width, cams[i][v].height)
+
+    paths = sum(jobs[i][0].width * jobs[i][0].height * jobs[i][0].spp for i, _ in sel)
+    sids = {k: ctx.upload(view_host(*k)) for k in sel}
+    for k in sel[:2]:
+        render(sids[k], *k)  # warm-up
+    t = time.perf_counter()
+    for k in sel:
+        render(sids[k], *k)
+    resident_s = time.perf_counter() - t
+    for s in sids.values():
+        ctx.release(s)
+    cold = {k: view_host(*k) for k in sel}  # no BVH built yet
+    t = time.perf_counter()
+    for k in sel:
+        sid = ctx.upload(cold[k])
+        render(sid, *k)
+        ctx.release(sid)
+    cold_s = time.perf_counter() - t
+    return {
+        "scenes": n_scenes, "views_per_scene": views, "scene_seeds": [1000, 1000 + n_scenes - 1],
+        "budget_gb": budget_gb, "spp_chunk": spp_chunk, "arrivals": "Poisson, seed 2024",
+        "sweep": sweeps,
+        "plain_resident": {"requests": len(sel), "req_s": round(len(sel) / resident_s, 2),
+                           "mpaths_s": round(paths / resident_s / 1e6, 2)},
+        "plain_cold": {"requests": len(sel), "req_s": round(len(sel) / cold_s, 2),
+                       "mpaths_s": round(paths / cold_s / 1e6, 2), "includes": "BVH build + upload per image"},
+        "server": {"launches": int(stats["launches"]), "paths": int(stats["paths"]),
+                   "device_ms": round(stats["device_ms"], 1), "resident_scenes": int(stats["resident_scenes"])},
+    }
 
 
 def run_reference(args) -> dict | None:
@@ -309,10 +489,27 @@ def main():
     ap.add_argument("--res", type=int, help="scale the workload down: square image side (profiling runs)")
     ap.add_argument("--spp", type=int, help="scale the workload down: samples per pixel (profiling runs)")
     ap.add_argument("--quick", action="store_true", help="timed steps only: no e2e, roofline or CPU legs")
+    ap.add_argument("--batch-jobs", type=int, default=64, help="batched leg: jobs per launch (0 = skip)")
+    ap.add_argument("--tune-ms", type=float, default=6000.0, help="batched leg: autotuner budget (device ms)")
+    ap.add_argument("--serve-scenes", type=int, default=16, help="served leg: resident scenes (0 = skip)")
+    ap.add_argument("--serve-views", type=int, default=16)
+    ap.add_argument("--serve-rates", type=float, nargs="+", default=[10.0, 40.0, 160.0])
+    ap.add_argument("--serve-requests", type=int, default=128, help="served leg: requests per arrival rate")
+    ap.add_argument("--spp-chunk", type=int, default=4, help="served leg: progressive spp per pass")
+    ap.add_argument("--plain-requests", type=int, default=32, help="served leg: requests timed on the plain path")
+    ap.add_argument("--batch-only", action="store_true", help="run the batched leg alone (profiling)")
     args = ap.parse_args()
+    if args.quick:
+        args.batch_jobs = args.serve_scenes = 0
     from orion_gb300 import build
     build.build_product()
     build.build_port()
+    if args.batch_only:  # profiling runs of the batched engine alone
+        import orion_gb300 as og
+        ctx = og.Context(0)
+        print(json.dumps(run_batched(ctx, args.batch_jobs or 64, steps=max(1, args.steps), tune_ms=args.tune_ms)))
+        ctx.close()
+        return
     out = run_reference(args) if args.impl == "reference" else run_ours(args)
     if out is not None:
         print(json.dumps(out), flush=True)

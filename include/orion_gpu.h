@@ -242,6 +242,12 @@ int orion_gpu_set_config(orion_gpu_ctx* ctx, const orion_launch_config* cfg);
  * the fastest on the context and returns it. */
 int orion_gpu_autotune(orion_gpu_ctx* ctx, orion_scene_id id, int32_t spp, double budget_ms,
                        orion_launch_config* best, double* best_mpaths);
+/* Autotuner for the batched engine: times orion_gpu_render_batch-style
+ * launches of `jobs` (spp capped at `spp_cap` when > 0; films are scratch and
+ * discarded) over the same knobs plus the path-slot count, keeps the fastest
+ * on the context and returns it. best_mpaths: paths/s of the best trial. */
+int orion_gpu_autotune_batch(orion_gpu_ctx* ctx, int32_t njobs, const orion_job* jobs, int32_t spp_cap,
+                             double budget_ms, orion_launch_config* best, double* best_mpaths);
 
 /* ------------------------------------------------------------- serving */
 /* A request loop on a context: render requests (a resident scene, a view,

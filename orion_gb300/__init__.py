@@ -153,6 +153,8 @@ def library() -> C.CDLL:
             "orion_gpu_get_config": (i32, [vp, C.POINTER(LaunchConfig)]),
             "orion_gpu_set_config": (i32, [vp, C.POINTER(LaunchConfig)]),
             "orion_gpu_autotune": (i32, [vp, i32, i32, C.c_double, C.POINTER(LaunchConfig), C.POINTER(C.c_double)]),
+            "orion_gpu_autotune_batch": (i32, [vp, i32, vp, i32, C.c_double, C.POINTER(LaunchConfig),
+                                               C.POINTER(C.c_double)]),
             "orion_server_create": (i32, [vp, C.POINTER(ServerOpts), C.POINTER(vp)]),
             "orion_server_submit": (i32, [vp, vp, C.POINTER(RenderParams), vp, C.POINTER(i64)]),
             "orion_server_status": (i32, [vp, i64, C.POINTER(RequestStatus)]),
@@ -325,22 +327,37 @@ class Context:
         Returns ([(sum, sumsq, count) per job], stats): FP64 (H, W, 3) sums and
         sums of squares, (H, W) sample counts.
         """
-        arr = (Job * max(1, len(jobs)))()
-        outs = []
-        for i, j in enumerate(jobs):
-            h, w = j["height"], j["width"]
-            s, q = np.zeros((h, w, 3), np.float64), np.zeros((h, w, 3), np.float64)
-            c = np.zeros((h, w), np.uint32)
-            outs.append((s, q, c))
-            arr[i].scene = j["sid"]
-            arr[i].params = RenderParams(spp=j.get("spp", 0), max_depth=j.get("max_depth", -1),
-                                         rr_depth=j.get("rr_depth", 3), first_pass=j.get("first_pass", 0))
-            arr[i].sum, arr[i].sumsq, arr[i].count = s.ctypes.data, q.ctypes.data, c.ctypes.data
-            if j.get("camera") is not None:
-                arr[i].camera = C.addressof(j["camera"])
+        arr, outs = self._job_array(jobs, films=True)
         st = BatchStats()
         _check(library().orion_gpu_render_batch(self._h, len(jobs), C.cast(arr, C.c_void_p), C.byref(st)))
         return outs, {k: getattr(st, k) for k, _ in BatchStats._fields_}
+
+    @staticmethod
+    def _job_array(jobs: list, films: bool):
+        arr = (Job * max(1, len(jobs)))()
+        outs = []
+        for i, j in enumerate(jobs):
+            arr[i].scene = j["sid"]
+            arr[i].params = RenderParams(spp=j.get("spp", 0), max_depth=j.get("max_depth", -1),
+                                         rr_depth=j.get("rr_depth", 3), first_pass=j.get("first_pass", 0))
+            if j.get("camera") is not None:
+                arr[i].camera = C.addressof(j["camera"])
+            if films:
+                h, w = j["height"], j["width"]
+                s, q = np.zeros((h, w, 3), np.float64), np.zeros((h, w, 3), np.float64)
+                c = np.zeros((h, w), np.uint32)
+                outs.append((s, q, c))
+                arr[i].sum, arr[i].sumsq, arr[i].count = s.ctypes.data, q.ctypes.data, c.ctypes.data
+        return arr, outs
+
+    def autotune_batch(self, jobs: list, spp_cap: int = 0, budget_ms: float = 4000.0) -> tuple:
+        """Tune the batched engine's launch knobs and path-slot count on `jobs` (render_batch job dicts)."""
+        arr, _ = self._job_array(jobs, films=False)
+        c = LaunchConfig()
+        mp = C.c_double()
+        _check(library().orion_gpu_autotune_batch(self._h, len(jobs), C.cast(arr, C.c_void_p), spp_cap, budget_ms,
+                                                  C.byref(c), C.byref(mp)))
+        return {k: getattr(c, k) for k, _ in LaunchConfig._fields_}, mp.value
 
     def get_config(self) -> dict:
         c = LaunchConfig()

@@ -192,12 +192,39 @@ void b_trace(const LaunchConfig& cfg, const WaveView& w, const BatchView& b, int
   }
 }
 
+cudaError_t batch_limit_of(const void* f, int smem_bytes, int* max_block) {
+  if (smem_bytes > 0) {
+    cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
+    if (e != cudaSuccess) return e;
+  }
+  cudaFuncAttributes a;
+  cudaError_t e = cudaFuncGetAttributes(&a, f);
+  if (e != cudaSuccess) return e;
+  *max_block = *max_block < a.maxThreadsPerBlock ? *max_block : a.maxThreadsPerBlock;
+  return cudaSuccess;
+}
+
 int grid_cap(int64_t n, int block, int cap) {
   int64_t g = (n + block - 1) / block;
   return (int)(g < 1 ? 1 : (g > cap ? cap : g));
 }
 
 }  // namespace
+
+cudaError_t configure_batch_kernels(int smem_bytes, KernelLimits* lim) {
+  const void* trace[] = {(const void*)k_b_trace<0>, (const void*)k_b_trace<8>, (const void*)k_b_trace<16>,
+                         (const void*)k_b_trace<24>, (const void*)k_b_trace<32>};
+  const void* shade[] = {(const void*)k_b_shade, (const void*)k_b_resolve, (const void*)k_b_retire};
+  for (const void* f : trace) {
+    cudaError_t e = batch_limit_of(f, smem_bytes, &lim->max_trace_block);
+    if (e != cudaSuccess) return e;
+  }
+  for (const void* f : shade) {
+    cudaError_t e = batch_limit_of(f, 0, &lim->max_shade_block);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
 
 void launch_batch_init(const WaveView& w, const BatchView& b, int capacity, cudaStream_t stream) {
   k_b_init<<<grid_cap(capacity, 256, 4096), 256, 0, stream>>>(b, capacity);

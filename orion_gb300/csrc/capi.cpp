@@ -51,6 +51,12 @@ int fail(int code, const std::string& msg) {
     if (e_ != cudaSuccess) return fail(ORION_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
   } while (0)
 
+#define RC(x)                      \
+  do {                             \
+    int rc_ = (x);                 \
+    if (rc_ != ORION_OK) return rc_; \
+  } while (0)
+
 struct DevBuf {
   void* p = nullptr;
   size_t bytes = 0;
@@ -123,8 +129,26 @@ struct orion_gpu_ctx {
   const void* bgraph_key[4] = {nullptr, nullptr, nullptr, nullptr};
   LaunchConfig bgraph_cfg{};
   int bgraph_slots = 0;
+  int smem_limit = 48 * 1024;  // opt-in dynamic shared memory per block
+  KernelLimits limits{1024, 1024};
   std::mutex mu;
 };
+
+// Why a launch configuration cannot run on this context ("" if it can).
+static std::string config_problem(const orion_gpu_ctx* ctx, const LaunchConfig& c) {
+  const int st = c.smem_stack;
+  if (c.trace_block < 32 || c.trace_block % 32 || c.trace_block > ctx->limits.max_trace_block)
+    return "trace_block must be a multiple of 32 up to " + std::to_string(ctx->limits.max_trace_block);
+  if (c.shade_block < 32 || c.shade_block % 32 || c.shade_block > ctx->limits.max_shade_block)
+    return "shade_block must be a multiple of 32 up to " + std::to_string(ctx->limits.max_shade_block);
+  if (!(st == 0 || st == 8 || st == 16 || st == 24 || st == 32)) return "smem_stack must be 0, 8, 16, 24 or 32";
+  if ((int64_t)st * c.trace_block * 8 > ctx->smem_limit)
+    return "traversal stack (smem_stack x trace_block x 8 bytes) exceeds " + std::to_string(ctx->smem_limit) +
+           " bytes of shared memory";
+  if (c.blocks_per_sm < 1 || c.blocks_per_sm > 64) return "blocks_per_sm out of range (1..64)";
+  if (c.refill_below < 1 || c.refill_below > 32) return "refill_below out of range (1..32)";
+  return std::string();
+}
 
 extern "C" const char* orion_last_error(void) { return g_error.c_str(); }
 
@@ -259,6 +283,10 @@ extern "C" int orion_gpu_create(const orion_gpu_opts* opts, orion_gpu_ctx** out)
   c->cfg.blocks_per_sm = 8;
   c->cfg.smem_stack = 16;
   c->cfg.refill_below = 20;
+  c->smem_limit = (int)prop.sharedMemPerBlockOptin;
+  c->limits = KernelLimits{1024, 1024};
+  CUDA_TRY(configure_kernels(c->smem_limit, &c->limits));
+  CUDA_TRY(configure_batch_kernels(c->smem_limit, &c->limits));
   *out = c.release();
   return ORION_OK;
 }
@@ -524,8 +552,15 @@ static int build_batch_graph(orion_gpu_ctx* ctx, const BatchView& bv, int slots)
   cudaGraphNode_t node;
   CUDA_TRY(cudaGraphAddNode(&node, ctx->bgraph, nullptr, nullptr, 0, &np));
   cudaGraph_t body = np.conditional.phGraph_out[0];
-  CUDA_TRY(capture_batch_iteration(ctx->wave.view, bv, ctx->sobol.as<uint32_t>(), ctx->sobol_bitmajor.as<uint32_t>(),
-                                   ctx->cfg, cond, ctx->stream, body));
+  cudaError_t ce = capture_batch_iteration(ctx->wave.view, bv, ctx->sobol.as<uint32_t>(),
+                                           ctx->sobol_bitmajor.as<uint32_t>(), ctx->cfg, cond, ctx->stream, body);
+  if (ce != cudaSuccess) {
+    // A graph whose loop-body capture was invalidated is dropped, not
+    // destroyed: nothing is assumed about its state after the failure.
+    ctx->bgraph = nullptr;
+    cudaGetLastError();
+    return fail(ORION_ERR_CUDA, std::string("batch loop capture: ") + cudaGetErrorString(ce));
+  }
   CUDA_TRY(cudaGraphInstantiate(&ctx->bexec, ctx->bgraph, 0));
   std::memcpy(ctx->bgraph_key, key, sizeof(key));
   ctx->bgraph_cfg = ctx->cfg;
@@ -604,18 +639,12 @@ static int run_batch_locked(orion_gpu_ctx* ctx, std::vector<DevJob>& dj, unsigne
   return ORION_OK;
 }
 
-extern "C" int orion_gpu_render_batch(orion_gpu_ctx* ctx, int32_t njobs, const orion_job* jobs,
-                                      orion_batch_stats* stats) {
-  if (!ctx || njobs < 0 || (njobs > 0 && !jobs)) return fail(ORION_ERR_INVALID, "bad argument");
-  std::lock_guard<std::mutex> g(ctx->mu);
-  CUDA_TRY(cudaSetDevice(ctx->device));
-  if (njobs == 0) {
-    if (stats) std::memset(stats, 0, sizeof(*stats));
-    return ORION_OK;
-  }
-  // Job table and film layout.
-  std::vector<DevJob> dj(njobs);
-  std::vector<size_t> film_off(njobs);
+// Job table and film layout of a batch (films packed into one device block).
+static int plan_batch(orion_gpu_ctx* ctx, int32_t njobs, const orion_job* jobs, int spp_cap, std::vector<DevJob>& dj,
+                      std::vector<size_t>& film_off, size_t* film_bytes_out, unsigned long long* total_out,
+                      int* max_depth_out) {
+  dj.assign(njobs, DevJob{});
+  film_off.assign(njobs, 0);
   size_t film_bytes = 0;
   unsigned long long total = 0;
   int max_depth_all = 0;
@@ -634,12 +663,13 @@ extern "C" int orion_gpu_render_batch(orion_gpu_ctx* ctx, int32_t njobs, const o
     }
     J.width = J.scene.cam.width;
     J.height = J.scene.cam.height;
-    const int spp = p.spp > 0 ? p.spp : d.spp;
+    int spp = p.spp > 0 ? p.spp : d.spp;
+    if (spp_cap > 0) spp = std::min(spp, spp_cap);
     J.max_depth = p.max_depth >= 0 ? p.max_depth : d.max_depth;
     J.rr_depth = p.rr_depth;
     if (J.max_depth > 120 || 17 + 8 * (int64_t)J.max_depth > 1024)
       return fail(ORION_ERR_INVALID, "job " + std::to_string(i) + ": max_depth out of range");
-    const long long wh = (long long)d.width * d.height;
+    const long long wh = (long long)J.width * J.height;
     J.first_index = p.first_pass * wh;
     J.num_paths = wh * spp;
     J.work_begin = (long long)total;
@@ -648,6 +678,27 @@ extern "C" int orion_gpu_render_batch(orion_gpu_ctx* ctx, int32_t njobs, const o
     film_off[i] = film_bytes;
     film_bytes += (size_t)((wh * (3 * 8 * 2 + 4) + 255) & ~255LL);
   }
+  *film_bytes_out = film_bytes;
+  *total_out = total;
+  *max_depth_out = max_depth_all;
+  return ORION_OK;
+}
+
+extern "C" int orion_gpu_render_batch(orion_gpu_ctx* ctx, int32_t njobs, const orion_job* jobs,
+                                      orion_batch_stats* stats) {
+  if (!ctx || njobs < 0 || (njobs > 0 && !jobs)) return fail(ORION_ERR_INVALID, "bad argument");
+  std::lock_guard<std::mutex> g(ctx->mu);
+  CUDA_TRY(cudaSetDevice(ctx->device));
+  if (njobs == 0) {
+    if (stats) std::memset(stats, 0, sizeof(*stats));
+    return ORION_OK;
+  }
+  std::vector<DevJob> dj;
+  std::vector<size_t> film_off;
+  size_t film_bytes = 0;
+  unsigned long long total = 0;
+  int max_depth_all = 0;
+  RC(plan_batch(ctx, njobs, jobs, 0, dj, film_off, &film_bytes, &total, &max_depth_all));
   int rc;
   if (ctx->b_films.bytes < film_bytes && (rc = ctx->b_films.alloc(film_bytes)) != ORION_OK) return rc;
   char* fb = ctx->b_films.as<char>();
@@ -765,24 +816,22 @@ extern "C" int orion_gpu_get_config(orion_gpu_ctx* ctx, orion_launch_config* out
   return ORION_OK;
 }
 
-static bool valid_block(int b) { return b >= 32 && b <= 1024 && b % 32 == 0; }
-
 extern "C" int orion_gpu_set_config(orion_gpu_ctx* ctx, const orion_launch_config* cfg) {
   if (!ctx || !cfg) return fail(ORION_ERR_INVALID, "null argument");
-  const int st = cfg->smem_stack;
-  if (!valid_block(cfg->trace_block) || !valid_block(cfg->shade_block) ||
-      !(st == 0 || st == 8 || st == 16 || st == 24 || st == 32) || cfg->blocks_per_sm < 1 || cfg->blocks_per_sm > 64 ||
-      cfg->wave_paths < 1024 || cfg->batch_slots < 1024 || cfg->refill_below < 1 || cfg->refill_below > 32)
-    return fail(ORION_ERR_INVALID, "launch configuration out of range");
-  if ((size_t)st * cfg->trace_block * 8 > 96 * 1024) return fail(ORION_ERR_INVALID, "traversal stack too large");
+  LaunchConfig c = ctx->cfg;
+  c.trace_block = cfg->trace_block;
+  c.shade_block = cfg->shade_block;
+  c.smem_stack = cfg->smem_stack;
+  c.blocks_per_sm = cfg->blocks_per_sm;
+  c.refill_below = cfg->refill_below;
+  std::string why = config_problem(ctx, c);
+  if (!why.empty()) return fail(ORION_ERR_INVALID, "launch configuration: " + why);
+  if (cfg->wave_paths < 1024 || cfg->batch_slots < 1024)
+    return fail(ORION_ERR_INVALID, "launch configuration: wave_paths and batch_slots must be >= 1024");
   std::lock_guard<std::mutex> g(ctx->mu);
-  ctx->cfg.trace_block = cfg->trace_block;
-  ctx->cfg.shade_block = cfg->shade_block;
-  ctx->cfg.smem_stack = st;
-  ctx->cfg.blocks_per_sm = cfg->blocks_per_sm;
+  ctx->cfg = c;
   ctx->default_wave = cfg->wave_paths;
   ctx->default_batch_slots = cfg->batch_slots;
-  ctx->cfg.refill_below = cfg->refill_below;
   return ORION_OK;
 }
 
@@ -840,6 +889,7 @@ extern "C" int orion_gpu_autotune(orion_gpu_ctx* ctx, orion_scene_id id, int32_t
       if (knob == 5) c.refill_below = refills[v];
       if (wave > 2 * paths && wave != best_wave) continue;
       if (std::memcmp(&c, &best, sizeof(c)) == 0 && wave == best_wave) continue;
+      if (!config_problem(ctx, c).empty()) continue;
       rc = trial(c, wave, &ms);
       if (rc == ORION_ERR_NOMEM) continue;
       if (rc != ORION_OK) return rc;
@@ -867,6 +917,92 @@ extern "C" int orion_gpu_autotune(orion_gpu_ctx* ctx, orion_scene_id id, int32_t
   return ORION_OK;
 }
 
+extern "C" int orion_gpu_autotune_batch(orion_gpu_ctx* ctx, int32_t njobs, const orion_job* jobs, int32_t spp_cap,
+                                        double budget_ms, orion_launch_config* best_out, double* best_mpaths) {
+  if (!ctx || njobs <= 0 || !jobs) return fail(ORION_ERR_INVALID, "bad argument");
+  std::lock_guard<std::mutex> g(ctx->mu);
+  CUDA_TRY(cudaSetDevice(ctx->device));
+  std::vector<DevJob> dj;
+  std::vector<size_t> film_off;
+  size_t film_bytes = 0;
+  unsigned long long total = 0;
+  int max_depth_all = 0;
+  RC(plan_batch(ctx, njobs, jobs, spp_cap, dj, film_off, &film_bytes, &total, &max_depth_all));
+  DevBuf films;  // trial films: accumulated into and discarded
+  RC(films.alloc(film_bytes));
+  char* fb = films.as<char>();
+  for (int i = 0; i < njobs; ++i) {
+    const long long wh = (long long)dj[i].width * dj[i].height;
+    dj[i].sum = reinterpret_cast<double*>(fb + film_off[i]);
+    dj[i].sumsq = dj[i].sum + 3 * wh;
+    dj[i].count = reinterpret_cast<unsigned int*>(dj[i].sumsq + 3 * wh);
+  }
+  CUDA_TRY(cudaMemsetAsync(films.p, 0, film_bytes, ctx->stream));
+  LaunchConfig best = ctx->cfg;
+  int best_slots = ctx->default_batch_slots;
+  double best_ms = 1e30, used = 0;
+  auto trial = [&](const LaunchConfig& c, int slots, double* ms) -> int {
+    LaunchConfig saved = ctx->cfg;
+    int saved_slots = ctx->default_batch_slots;
+    ctx->cfg = c;
+    ctx->default_batch_slots = slots;
+    BatchCtl out;
+    float fms = 0.f;
+    int rc = run_batch_locked(ctx, dj, total, max_depth_all, &out, &fms);
+    ctx->cfg = saved;
+    ctx->default_batch_slots = saved_slots;
+    *ms = fms;
+    used += fms;
+    return rc;
+  };
+  double ms;
+  RC(trial(best, best_slots, &ms));  // warm-up (graph instantiation)
+  RC(trial(best, best_slots, &best_ms));
+  const int trace_blocks[] = {64, 128, 256};
+  const int stacks[] = {8, 16, 32};
+  const int shade_blocks[] = {64, 128, 256};
+  const int bpsm[] = {4, 8, 16};
+  const int slot_counts[] = {1 << 20, 1 << 21, 1 << 22, 1 << 23};
+  const int refills[] = {8, 16, 24, 32};
+  for (int knob = 0; knob < 6 && used < budget_ms; ++knob) {
+    const int n = knob >= 4 ? 4 : 3;
+    for (int v = 0; v < n && used < budget_ms; ++v) {
+      LaunchConfig c = best;
+      int slots = best_slots;
+      if (knob == 0) c.trace_block = trace_blocks[v];
+      if (knob == 1) c.smem_stack = stacks[v];
+      if (knob == 2) c.shade_block = shade_blocks[v];
+      if (knob == 3) c.blocks_per_sm = bpsm[v];
+      if (knob == 4) slots = slot_counts[v];
+      if (knob == 5) c.refill_below = refills[v];
+      if (std::memcmp(&c, &best, sizeof(c)) == 0 && slots == best_slots) continue;
+      if (!config_problem(ctx, c).empty()) continue;
+      int rc = trial(c, slots, &ms);
+      if (rc == ORION_ERR_NOMEM) continue;
+      if (rc != ORION_OK) return rc;
+      if (ms < best_ms) {
+        best_ms = ms;
+        best = c;
+        best_slots = slots;
+      }
+    }
+  }
+  ctx->cfg = best;
+  ctx->default_batch_slots = best_slots;
+  if (best_out) {
+    best_out->trace_block = best.trace_block;
+    best_out->shade_block = best.shade_block;
+    best_out->smem_stack = best.smem_stack;
+    best_out->blocks_per_sm = best.blocks_per_sm;
+    best_out->wave_paths = ctx->default_wave;
+    best_out->batch_slots = best_slots;
+    best_out->refill_below = best.refill_below;
+    best_out->reserved = 0;
+  }
+  if (best_mpaths) *best_mpaths = (double)total / (best_ms * 1e-3) / 1e6;
+  return ORION_OK;
+}
+
 // --------------------------------------------------------- test hooks
 
 namespace {
@@ -884,11 +1020,6 @@ int to_host(T* host, const DevBuf& b, size_t n, cudaStream_t s) {
 }
 }  // namespace
 
-#define RC(x)                      \
-  do {                             \
-    int rc_ = (x);                 \
-    if (rc_ != ORION_OK) return rc_; \
-  } while (0)
 
 extern "C" int orion_gpu_sobol(orion_gpu_ctx* ctx, int64_t n, const uint64_t* index, const uint32_t* dim, float* out) {
   if (!ctx || n < 0 || (n > 0 && (!index || !dim || !out))) return fail(ORION_ERR_INVALID, "bad argument");

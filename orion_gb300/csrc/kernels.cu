@@ -328,6 +328,39 @@ void launch_trace(const SceneView& s, int64_t n, const float* rays, int any_hit,
   k_trace_rays<16><<<grid, block, (size_t)16 * block * sizeof(int2), stream>>>(s, n, rays, any_hit, t, u, v, prim);
 }
 
+namespace {
+
+cudaError_t limit_of(const void* f, int smem_bytes, int* max_block) {
+  if (smem_bytes > 0) {
+    cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
+    if (e != cudaSuccess) return e;
+  }
+  cudaFuncAttributes a;
+  cudaError_t e = cudaFuncGetAttributes(&a, f);
+  if (e != cudaSuccess) return e;
+  *max_block = std::min(*max_block, a.maxThreadsPerBlock);
+  return cudaSuccess;
+}
+
+}  // namespace
+
+cudaError_t configure_kernels(int smem_bytes, KernelLimits* lim) {
+  const void* trace[] = {(const void*)k_trace<0>,     (const void*)k_trace<8>,     (const void*)k_trace<16>,
+                         (const void*)k_trace<24>,    (const void*)k_trace<32>,    (const void*)k_trace_sh<0>,
+                         (const void*)k_trace_sh<8>,  (const void*)k_trace_sh<16>, (const void*)k_trace_sh<24>,
+                         (const void*)k_trace_sh<32>, (const void*)k_trace_rays<16>};
+  const void* shade[] = {(const void*)k_shade, (const void*)k_resolve};
+  for (const void* f : trace) {
+    cudaError_t e = limit_of(f, smem_bytes, &lim->max_trace_block);
+    if (e != cudaSuccess) return e;
+  }
+  for (const void* f : shade) {
+    cudaError_t e = limit_of(f, 0, &lim->max_shade_block);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
 void launch_camera_rays(const SceneView& s, const uint32_t* sobol, int64_t n, const int64_t* index, float* rays,
                         cudaStream_t stream) {
   k_camera_rays<<<grid_for(n, 256, 4096), 256, 0, stream>>>(s, sobol, n, index, rays);

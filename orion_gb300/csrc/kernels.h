@@ -152,6 +152,16 @@ struct StageTimer {
 void launch_wave(const SceneView& s, const WaveView& w, const WaveArgs& a, const FilmView& film,
                  const LaunchConfig& cfg, cudaStream_t stream, int* launches, StageTimer* timer = nullptr);
 
+// Launch limits of the kernel families, and the dynamic shared-memory
+// allowance of the traversal kernels (raised to `smem_bytes`, the device's
+// opt-in maximum, so any accepted stack depth x block size can launch).
+struct KernelLimits {
+  int max_trace_block;  // threads per block the traversal kernels can launch with
+  int max_shade_block;  // same for the shade / resolve / retire kernels
+};
+cudaError_t configure_kernels(int smem_bytes, KernelLimits* lim);
+cudaError_t configure_batch_kernels(int smem_bytes, KernelLimits* lim);
+
 // Batched mode: builds the body of the device-side loop (one iteration)
 // into `body` by stream capture on `stream`. The loop keeps running while
 // work or live paths remain; `cond` is the graph's while-condition handle.

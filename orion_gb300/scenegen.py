@@ -242,12 +242,16 @@ class Scene:
     def num_tris(self):
         return sum(m.num_tris for m in self.meshes)
 
-    def flat(self):
-        """De-indexed corner arrays in primitive order: (P Tx9, N Tx9, mesh index per tri)."""
+    def flat(self, text_rounding: bool = True):
+        """De-indexed corner arrays in primitive order: (P Tx9, N Tx9, mesh index per tri).
+
+        text_rounding: round to the 7 significant digits the OBJ writer emits (slow, exact
+        agreement with a written-and-loaded scene); else plain float32 of the generated values."""
+        rnd = _f32 if text_rounding else (lambda a: np.asarray(a, np.float32))
         ps, ns, ids = [], [], []
         for i, m in enumerate(self.meshes):
-            p = _f32(m.pos)[m.faces].reshape(-1, 9)
-            n = _f32(m.normals)[m.faces].reshape(-1, 9)
+            p = rnd(m.pos)[m.faces].reshape(-1, 9)
+            n = rnd(m.normals)[m.faces].reshape(-1, 9)
             ps.append(p)
             ns.append(n)
             ids.append(np.full(m.num_tris, i, dtype=np.int32))
@@ -566,13 +570,15 @@ def _basis_rows(d):
     return np.cross(y, d), y, d
 
 
-def to_host_scene(scene: Scene):
+def to_host_scene(scene: Scene, text_rounding: bool = False):
     """The scene as an orion_gb300.HostScene built from arrays.
 
-    Geometry, materials and light order are identical to writing the scene out and loading it;
-    light frames agree with the loader's to float rounding (computed here in float64)."""
+    Materials and light order are identical to writing the scene out and loading it. Geometry
+    is too with text_rounding (slow); without it, vertices are the generated values in float32
+    (within 1e-7 relative of the written text). Light frames agree with the loader's to float
+    rounding (computed here in float64)."""
     import orion_gb300 as og
-    P, N, mesh_of = scene.flat()
+    P, N, mesh_of = scene.flat(text_rounding)
     mats = [_material_record(m.material) for m in scene.meshes]
     lights, light_of = [], np.full(len(P), -1, np.int32)
     for i, m in enumerate(scene.meshes):
@@ -633,10 +639,9 @@ def to_host_scene(scene: Scene):
                                     light_of_prim=light_of)
 
 
-def job_views(seed: int, views: int = 16):
+def job_views(s: Scene, views: int = 16):
     """`views` cameras orbiting a job's scene (serving: one resident scene, many views)."""
     import orion_gb300 as og
-    s = job(seed)
     out = []
     for v in range(views):
         ang = 2 * math.pi * v / views

@@ -75,3 +75,41 @@ def test_small_pool_forces_regeneration(ctx, scenes):
     for (a, _, c1), (b, _, c2) in zip(outs, ref):
         assert np.array_equal(c1, c2)
         assert _close(a, b)
+
+
+def test_config_limits_and_large_stacks(ctx, scenes):
+    import orion_gb300 as og
+    cfg = ctx.get_config()
+    with pytest.raises(og.OrionError, match="shared memory"):
+        ctx.set_config(trace_block=1024, smem_stack=32)  # 256 KB of stack per block
+    with pytest.raises(og.OrionError, match="trace_block"):
+        ctx.set_config(trace_block=100)
+    assert ctx.get_config() == cfg
+    ref, _ = ctx.render_batch([_job(s) for s in scenes])
+    try:
+        ctx.set_config(trace_block=256, smem_stack=32)  # 64 KB: above the 48 KB default, allowed by opt-in
+        outs, _ = ctx.render_batch([_job(s) for s in scenes])
+        img, cnt = ctx.render(scenes[0]["sid"], scenes[0]["width"], scenes[0]["height"])
+    finally:
+        ctx.set_config(**cfg)
+    ref_img, ref_cnt = ctx.render(scenes[0]["sid"], scenes[0]["width"], scenes[0]["height"])
+    assert np.array_equal(cnt, ref_cnt) and np.allclose(img, ref_img, rtol=1e-5, atol=1e-6)
+    for (a, _, c1), (b, _, c2) in zip(outs, ref):
+        assert np.array_equal(c1, c2)
+        assert np.allclose(a, b, rtol=1e-5, atol=1e-9)
+
+
+def test_batch_autotuner(ctx, scenes):
+    cfg = ctx.get_config()
+    try:
+        best, mpaths = ctx.autotune_batch([_job(s) for s in scenes], spp_cap=2, budget_ms=300.0)
+        assert mpaths > 0 and best["batch_slots"] >= 1024
+        assert ctx.get_config()["trace_block"] == best["trace_block"]
+        outs, _ = ctx.render_batch([_job(s) for s in scenes])
+    finally:
+        ctx.set_config(**cfg)
+    ref, _ = ctx.render_batch([_job(s) for s in scenes])
+    for (a, _, c1), (b, _, c2) in zip(outs, ref):
+        assert np.array_equal(c1, c2)
+        assert np.allclose(a, b, rtol=1e-5, atol=1e-9)
+    print(f"batch autotuner: {best}, {mpaths:.1f} Mpaths/s")
