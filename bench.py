@@ -326,7 +326,7 @@ def run_batched(ctx, n_jobs: int, steps: int, tune_ms: float) -> dict:
 
     def batch_pass():
         t = time.perf_counter()
-        outs, st = ctx.render_batch(specs)
+        outs, st = ctx.render_batch(specs, sumsq=False)
         return (time.perf_counter() - t) * 1e3, st["device_ms"], [s / np.maximum(c, 1)[..., None]
                                                                   for s, _, c in outs[:4]], st
 
@@ -340,15 +340,27 @@ def run_batched(ctx, n_jobs: int, steps: int, tune_ms: float) -> dict:
     p_dev = float(np.median([p[1] for p in plain]))
     b_dev = float(np.median([b[1] for b in batched]))
     rmse = max(_rel_rmse(b, p.astype(np.float64)) for b, p in zip(batched[-1][2], plain[-1][2]))
+    # Per-stage device time of each arm (profiling: events around every kernel).
+    ctx.set_profiling(True)
+    ctx.render_batch(specs, sumsq=False)
+    b_stages = {k: round(v["ms"], 2) for k, v in ctx.stage_times().items()}
+    p_stages = dict.fromkeys(b_stages, 0.0)
+    for j in specs:
+        ctx.render(j["sid"], j["width"], j["height"], spp=j["spp"])
+        for k, v in ctx.stage_times().items():
+            p_stages[k] = round(p_stages[k] + v["ms"], 2)
+    ctx.set_profiling(False)
     for sid in sids:
         ctx.release(sid)
     return {
         "jobs": n_jobs, "seeds": [0, n_jobs - 1], "paths_per_step": int(paths), "triangles_total": int(sum(tris)),
         "plain": {"req_s": round(n_jobs / (p_wall * 1e-3), 2), "mpaths_s": round(paths / (p_wall * 1e-3) / 1e6, 2),
-                  "wall_ms": round(p_wall, 2), "device_ms": round(p_dev, 2), "launch_calls": n_jobs},
+                  "wall_ms": round(p_wall, 2), "device_ms": round(p_dev, 2), "launch_calls": n_jobs,
+                  "stages_ms": p_stages},
         "batched": {"req_s": round(n_jobs / (b_wall * 1e-3), 2), "mpaths_s": round(paths / (b_wall * 1e-3) / 1e6, 2),
                     "wall_ms": round(b_wall, 2), "device_ms": round(b_dev, 2), "launch_calls": 1,
-                    "loop_iterations": int(batched[-1][3]["iterations"]), "slots": int(batched[-1][3]["capacity"])},
+                    "loop_iterations": int(batched[-1][3]["iterations"]), "slots": int(batched[-1][3]["capacity"]),
+                    "stages_ms": b_stages},
         "req_s_ratio": round(p_wall / b_wall, 3),
         "rmse_batched_vs_plain": rmse,
         "autotuned": {**tuned, "tuning_mpaths_s": round(tuned_mp, 2), "budget_ms": tune_ms, "spp_cap": 4},

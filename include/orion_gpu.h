@@ -186,7 +186,10 @@ int orion_gpu_last_stats(orion_gpu_ctx* ctx, orion_render_stats* out);
 /* Per-stage device time of the last render, filled only while profiling is
  * on (CUDA events around every kernel; adds a little launch overhead).
  * Stages: 0 camera, 1 extension-ray trace, 2 shade, 3 shadow-ray trace,
- * 4 MIS-ray trace, 5 direct-light resolve, 6 film, 7 bookkeeping. */
+ * 4 MIS-ray trace, 5 direct-light resolve, 6 film, 7 bookkeeping.
+ * A batched render under profiling runs its loop from the host instead of a
+ * graph while-node (same kernels and results; stage 0 is then slot refill,
+ * stage 6 retirement into the films). */
 #define ORION_NUM_STAGES 8
 typedef struct orion_stage_times {
   double ms[ORION_NUM_STAGES];

@@ -321,19 +321,19 @@ class Context:
         _check(library().orion_gpu_stage_times(self._h, C.byref(t)))
         return {name: {"ms": t.ms[i], "launches": t.launches[i]} for i, name in enumerate(STAGES)}
 
-    def render_batch(self, jobs: list) -> tuple:
-        """jobs: dicts with sid, width, height and optional spp, max_depth, rr_depth, first_pass.
+    def render_batch(self, jobs: list, sumsq: bool = True) -> tuple:
+        """jobs: dicts with sid, width, height and optional spp, max_depth, rr_depth, first_pass, camera.
 
         Returns ([(sum, sumsq, count) per job], stats): FP64 (H, W, 3) sums and
-        sums of squares, (H, W) sample counts.
+        sums of squares (None when sumsq=False), (H, W) sample counts.
         """
-        arr, outs = self._job_array(jobs, films=True)
+        arr, outs = self._job_array(jobs, films=True, sumsq=sumsq)
         st = BatchStats()
         _check(library().orion_gpu_render_batch(self._h, len(jobs), C.cast(arr, C.c_void_p), C.byref(st)))
         return outs, {k: getattr(st, k) for k, _ in BatchStats._fields_}
 
     @staticmethod
-    def _job_array(jobs: list, films: bool):
+    def _job_array(jobs: list, films: bool, sumsq: bool = True):
         arr = (Job * max(1, len(jobs)))()
         outs = []
         for i, j in enumerate(jobs):
@@ -344,10 +344,12 @@ class Context:
                 arr[i].camera = C.addressof(j["camera"])
             if films:
                 h, w = j["height"], j["width"]
-                s, q = np.zeros((h, w, 3), np.float64), np.zeros((h, w, 3), np.float64)
+                s = np.zeros((h, w, 3), np.float64)
+                q = np.zeros((h, w, 3), np.float64) if sumsq else None
                 c = np.zeros((h, w), np.uint32)
                 outs.append((s, q, c))
-                arr[i].sum, arr[i].sumsq, arr[i].count = s.ctypes.data, q.ctypes.data, c.ctypes.data
+                arr[i].sum, arr[i].count = s.ctypes.data, c.ctypes.data
+                arr[i].sumsq = q.ctypes.data if sumsq else None
         return arr, outs
 
     def autotune_batch(self, jobs: list, spp_cap: int = 0, budget_ms: float = 4000.0) -> tuple:

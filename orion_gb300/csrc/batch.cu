@@ -49,6 +49,7 @@ __global__ void k_b_plan(BatchView b) {
   c.counters[CNT_FETCH_EXT] = 0;
   c.counters[CNT_FETCH_SH] = 0;
   c.counters[CNT_FETCH_MIS] = 0;
+  for (int k = 0; k < kShadeClasses; ++k) c.counters[CNT_CLS0 + k] = 0;
 }
 
 __device__ __forceinline__ int job_of_work(const DevJob* jobs, int njobs, unsigned long long work) {
@@ -93,7 +94,7 @@ __global__ void k_b_regen(WaveView w, BatchView b, const uint32_t* sobol) {
 
 // kind 0: extension rays (current queue), 1: shadow rays, 2: MIS rays.
 template <int SMEM>
-__global__ void k_b_trace(WaveView w, BatchView b, int kind, int refill_below) {
+__global__ void __launch_bounds__(512, 2) k_b_trace(WaveView w, BatchView b, int kind, int refill_below) {
   extern __shared__ int2 stack_smem[];
   BatchCtl& c = *b.ctl;
   JobScene js{b.jobs, b.job_of};
@@ -101,7 +102,7 @@ __global__ void k_b_trace(WaveView w, BatchView b, int kind, int refill_below) {
   if (kind == 0) {
     n = c.counters[CNT_EXT0 + c.cur];
     trace_persistent<false, SMEM>(js, w.q_ext[c.cur], n, &c.counters[CNT_FETCH_EXT], w.ray_o, w.ray_d, w.hit,
-                                  nullptr, stack_smem, refill_below);
+                                  nullptr, stack_smem, refill_below, &c.counters[CNT_CLS0], w.q_cls, w.capacity);
   } else if (kind == 1) {
     n = c.counters[CNT_SH];
     trace_persistent<true, SMEM>(js, w.q_sh, n, &c.counters[CNT_FETCH_SH], w.sh_o, w.sh_d, nullptr, w.occluded,
@@ -117,10 +118,11 @@ __global__ void k_b_trace(WaveView w, BatchView b, int kind, int refill_below) {
 __global__ void k_b_shade(WaveView w, BatchView b, const uint32_t* sobol_bitmajor) {
   BatchCtl& c = *b.ctl;
   const int cur = c.cur;
-  const int n = c.counters[CNT_EXT0 + cur];
-  const int* in_q = w.q_ext[cur];
+  ClassQueues cq;
+  cq.load(&c.counters[CNT_CLS0]);
+  const int n = cq.total();
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
-    const int pid = in_q[q];
+    const int pid = cq.slot(w.q_cls, w.capacity, q);
     const DevJob& J = b.jobs[b.job_of[pid]];
     const int bounce = b.bounce_of[pid];
     ShadeResult r = shade_one(J.scene, w, sobol_bitmajor, pid, (uint64_t)b.index_of[pid], bounce, J.max_depth,
@@ -153,16 +155,20 @@ __global__ void k_b_retire(WaveView w, BatchView b) {
     atomicAdd(&J.sum[3 * pix], (double)l.x);
     atomicAdd(&J.sum[3 * pix + 1], (double)l.y);
     atomicAdd(&J.sum[3 * pix + 2], (double)l.z);
-    atomicAdd(&J.sumsq[3 * pix], (double)l.x * l.x);
-    atomicAdd(&J.sumsq[3 * pix + 1], (double)l.y * l.y);
-    atomicAdd(&J.sumsq[3 * pix + 2], (double)l.z * l.z);
+    if (J.sumsq) {
+      atomicAdd(&J.sumsq[3 * pix], (double)l.x * l.x);
+      atomicAdd(&J.sumsq[3 * pix + 1], (double)l.y * l.y);
+      atomicAdd(&J.sumsq[3 * pix + 2], (double)l.z * l.z);
+    }
     atomicAdd(&J.count[pix], 1u);
     queue_append(&c.counters[CNT_FREE], b.q_free, pid, true);
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&c.paths_done, (unsigned long long)n);
 }
 
-__global__ void k_b_control(BatchView b, cudaGraphConditionalHandle cond) {
+// in_graph: sets the while-node's condition; otherwise leaves the decision in
+// ctl->more for a host-driven loop (profiling runs).
+__global__ void k_b_control(BatchView b, cudaGraphConditionalHandle cond, int in_graph) {
   if (blockIdx.x != 0 || threadIdx.x != 0) return;
   BatchCtl& c = *b.ctl;
   c.cur ^= 1;
@@ -172,7 +178,10 @@ __global__ void k_b_control(BatchView b, cudaGraphConditionalHandle cond) {
     c.error = 1;  // bounded loop: report instead of spinning on
     more = false;
   }
-  cudaGraphSetConditional(cond, more ? 1u : 0u);
+  if (in_graph)
+    cudaGraphSetConditional(cond, more ? 1u : 0u);
+  else
+    c.more = more ? 1 : 0;
 }
 
 template <int SMEM>
@@ -230,28 +239,67 @@ void launch_batch_init(const WaveView& w, const BatchView& b, int capacity, cuda
   k_b_init<<<grid_cap(capacity, 256, 4096), 256, 0, stream>>>(b, capacity);
 }
 
+namespace {
+
+// One loop iteration's kernels on `stream`, optionally timed per stage.
+void enqueue_iteration(const WaveView& w, const BatchView& b, const uint32_t* sobol, const uint32_t* sobol_bitmajor,
+                       const LaunchConfig& cfg, cudaGraphConditionalHandle cond, int in_graph, cudaStream_t stream,
+                       StageTimer* timer) {
+  const int cap = w.capacity;
+  const int persistent = cfg.num_sms * cfg.blocks_per_sm;
+  const int tgrid = grid_cap(cap, cfg.trace_block, persistent * 2);
+  const int sgrid = grid_cap(cap, cfg.shade_block, persistent * 2);
+  auto begin = [&](int st) {
+    if (timer) timer->begin(st, stream);
+  };
+  auto end = [&]() {
+    if (timer) timer->end(stream);
+  };
+  begin(ST_CAMERA);
+  k_b_plan<<<1, 32, 0, stream>>>(b);
+  k_b_regen<<<grid_cap(cap, 256, persistent * 4), 256, 0, stream>>>(w, b, sobol);
+  end();
+  begin(ST_TRACE_EXT);
+  b_trace(cfg, w, b, 0, tgrid, stream);
+  end();
+  begin(ST_SHADE);
+  k_b_shade<<<sgrid, cfg.shade_block, 0, stream>>>(w, b, sobol_bitmajor);
+  end();
+  begin(ST_TRACE_SHADOW);
+  b_trace(cfg, w, b, 1, tgrid, stream);
+  end();
+  begin(ST_TRACE_MIS);
+  b_trace(cfg, w, b, 2, tgrid, stream);
+  end();
+  begin(ST_RESOLVE);
+  k_b_resolve<<<sgrid, cfg.shade_block, 0, stream>>>(w, b);
+  end();
+  begin(ST_FILM);
+  k_b_retire<<<sgrid, cfg.shade_block, 0, stream>>>(w, b);
+  end();
+  begin(ST_OTHER);
+  k_b_control<<<1, 32, 0, stream>>>(b, cond, in_graph);
+  end();
+}
+
+}  // namespace
+
 cudaError_t capture_batch_iteration(const WaveView& w, const BatchView& b, const uint32_t* sobol,
                                     const uint32_t* sobol_bitmajor, const LaunchConfig& cfg,
                                     cudaGraphConditionalHandle cond, cudaStream_t stream, cudaGraph_t body) {
   cudaError_t e = cudaStreamBeginCaptureToGraph(stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
   if (e != cudaSuccess) return e;
-  const int cap = w.capacity;
-  const int persistent = cfg.num_sms * cfg.blocks_per_sm;
-  const int tgrid = grid_cap(cap, cfg.trace_block, persistent * 2);
-  const int sgrid = grid_cap(cap, cfg.shade_block, persistent * 2);
-  k_b_plan<<<1, 32, 0, stream>>>(b);
-  k_b_regen<<<grid_cap(cap, 256, persistent * 4), 256, 0, stream>>>(w, b, sobol);
-  b_trace(cfg, w, b, 0, tgrid, stream);
-  k_b_shade<<<sgrid, cfg.shade_block, 0, stream>>>(w, b, sobol_bitmajor);
-  b_trace(cfg, w, b, 1, tgrid, stream);
-  b_trace(cfg, w, b, 2, tgrid, stream);
-  k_b_resolve<<<sgrid, cfg.shade_block, 0, stream>>>(w, b);
-  k_b_retire<<<sgrid, cfg.shade_block, 0, stream>>>(w, b);
-  k_b_control<<<1, 32, 0, stream>>>(b, cond);
+  enqueue_iteration(w, b, sobol, sobol_bitmajor, cfg, cond, 1, stream, nullptr);
   cudaGraph_t out = body;
   cudaError_t e2 = cudaStreamEndCapture(stream, &out);
   cudaError_t e3 = cudaGetLastError();
   return e2 != cudaSuccess ? e2 : e3;
+}
+
+void launch_batch_iteration(const WaveView& w, const BatchView& b, const uint32_t* sobol,
+                            const uint32_t* sobol_bitmajor, const LaunchConfig& cfg, cudaStream_t stream,
+                            StageTimer* timer) {
+  enqueue_iteration(w, b, sobol, sobol_bitmajor, cfg, cudaGraphConditionalHandle{}, 0, stream, timer);
 }
 
 }  // namespace orion_gb300

@@ -138,145 +138,224 @@ __device__ __forceinline__ V3 md_sample_wh(int dist, float alpha, V3 wo, float u
 __device__ __forceinline__ float md_pdf(int dist, float alpha, V3 wh) { return md_D(dist, alpha, wh) * abs_cos_theta(wh); }
 
 // -------------------------------------------------------------- one lobe
+//
+// Every lobe and BSDF function is a template over KM, the set of lobe kinds
+// (bit k = LobeKind k) its material may contain. The shading kernel of a
+// shading class instantiates them with that class's kinds only, so its code
+// holds just those lobes' arithmetic; KM = kLobeAll is the general form,
+// whose lobe evaluators stay out of line (inlining every copy of every kind
+// overflows the instruction cache).
 
-// The lobe evaluators are out of line: the shading kernel calls them from
-// several places and inlining every copy overflows the instruction cache.
-static __device__ __noinline__ V3 lobe_f(const DevLobe& l, V3 wi, V3 wo) {
-  switch (l.kind) {
-    case LOBE_LAMBERT_R:
-      return ld3(l.c) * kInvPi;
-    case LOBE_OREN_NAYAR: {
-      float si = sin_theta(wi), so = sin_theta(wo);
-      float cos_term = 0.f;
-      if (si > 1e-4f && so > 1e-4f) {
-        float d = cos_phi(wi) * cos_phi(wo) + sin_phi(wi) * sin_phi(wo);
-        cos_term = fmaxf(0.f, d);
-      }
-      float sin_a, tan_b;
-      if (abs_cos_theta(wi) > abs_cos_theta(wo)) {
-        sin_a = so;
-        tan_b = si / abs_cos_theta(wi);
-      } else {
-        sin_a = si;
-        tan_b = so / abs_cos_theta(wo);
-      }
-      return (ld3(l.c) * kInvPi) * (l.on_a + l.on_b * cos_term * sin_a * tan_b);
-    }
-    case LOBE_MICROFACET_R: {
-      float co = abs_cos_theta(wo), ci = abs_cos_theta(wi);
-      if (ci == 0.f || co == 0.f) return V3{0, 0, 0};
-      V3 wh = wi + wo;
-      if (wh.x == 0.f && wh.y == 0.f && wh.z == 0.f) return V3{0, 0, 0};
-      wh = normalize(wh);
-      V3 F = fresnel_eval(l, dot(wi, wh));
-      float dg = md_D(l.dist, l.alpha, wh);
-      float g = md_G(l.dist, l.alpha, wi, wi);  // the reference passes wi twice
-      return sdiv(mul((ld3(l.c) * dg) * g, F), 4.f * ci * co);
-    }
-    case LOBE_MICROFACET_T: {
-      if (same_hemisphere(wi, wo)) return V3{0, 0, 0};
-      float co = cos_theta(wo), ci = cos_theta(wi);
-      if (ci == 0.f || co == 0.f) return V3{0, 0, 0};
-      float eta = cos_theta(wo) > 0.f ? (l.etaB / l.etaA) : (l.etaA / l.etaB);
-      V3 wh = normalize(wo + wi * eta);
-      if (wh.z < 0.f) wh = -wh;
-      float F = fr_dielectric(fabsf(dot(wo, wh)), l.etaA, l.etaB);
-      float sd = dot(wo, wh) + eta * dot(wi, wh);
-      float factor = 1.f / eta;
-      float v = fabsf(md_D(l.dist, l.alpha, wh) * md_G(l.dist, l.alpha, wi, wo) * eta * eta * absdot(wi, wh) *
-                      absdot(wo, wh) * factor * factor / (ci * co * sd * sd));
-      return mul(V3{1.f - F, 1.f - F, 1.f - F}, ld3(l.c)) * v;
-    }
-    default:  // specular lobes are delta distributions
-      return V3{0, 0, 0};
-  }
+constexpr unsigned kLobeAll = 0x7fu;
+
+template <unsigned KM>
+__device__ __forceinline__ constexpr bool has_kind(int kind) {
+  return ((KM >> kind) & 1u) != 0u;
 }
 
-static __device__ __noinline__ float lobe_pdf(const DevLobe& l, V3 wi, V3 wo) {
+template <unsigned KM>
+__device__ __forceinline__ V3 lobe_f_t(const DevLobe& l, V3 wi, V3 wo) {
+  switch (l.kind) {
+    case LOBE_LAMBERT_R:
+      if constexpr (has_kind<KM>(LOBE_LAMBERT_R)) return ld3(l.c) * kInvPi;
+      break;
+    case LOBE_OREN_NAYAR:
+      if constexpr (has_kind<KM>(LOBE_OREN_NAYAR)) {
+        float si = sin_theta(wi), so = sin_theta(wo);
+        float cos_term = 0.f;
+        if (si > 1e-4f && so > 1e-4f) {
+          float d = cos_phi(wi) * cos_phi(wo) + sin_phi(wi) * sin_phi(wo);
+          cos_term = fmaxf(0.f, d);
+        }
+        float sin_a, tan_b;
+        if (abs_cos_theta(wi) > abs_cos_theta(wo)) {
+          sin_a = so;
+          tan_b = si / abs_cos_theta(wi);
+        } else {
+          sin_a = si;
+          tan_b = so / abs_cos_theta(wo);
+        }
+        return (ld3(l.c) * kInvPi) * (l.on_a + l.on_b * cos_term * sin_a * tan_b);
+      }
+      break;
+    case LOBE_MICROFACET_R:
+      if constexpr (has_kind<KM>(LOBE_MICROFACET_R)) {
+        float co = abs_cos_theta(wo), ci = abs_cos_theta(wi);
+        if (ci == 0.f || co == 0.f) return V3{0, 0, 0};
+        V3 wh = wi + wo;
+        if (wh.x == 0.f && wh.y == 0.f && wh.z == 0.f) return V3{0, 0, 0};
+        wh = normalize(wh);
+        V3 F = fresnel_eval(l, dot(wi, wh));
+        float dg = md_D(l.dist, l.alpha, wh);
+        float g = md_G(l.dist, l.alpha, wi, wi);  // the reference passes wi twice
+        return sdiv(mul((ld3(l.c) * dg) * g, F), 4.f * ci * co);
+      }
+      break;
+    case LOBE_MICROFACET_T:
+      if constexpr (has_kind<KM>(LOBE_MICROFACET_T)) {
+        if (same_hemisphere(wi, wo)) return V3{0, 0, 0};
+        float co = cos_theta(wo), ci = cos_theta(wi);
+        if (ci == 0.f || co == 0.f) return V3{0, 0, 0};
+        float eta = cos_theta(wo) > 0.f ? (l.etaB / l.etaA) : (l.etaA / l.etaB);
+        V3 wh = normalize(wo + wi * eta);
+        if (wh.z < 0.f) wh = -wh;
+        float F = fr_dielectric(fabsf(dot(wo, wh)), l.etaA, l.etaB);
+        float sd = dot(wo, wh) + eta * dot(wi, wh);
+        float factor = 1.f / eta;
+        float v = fabsf(md_D(l.dist, l.alpha, wh) * md_G(l.dist, l.alpha, wi, wo) * eta * eta * absdot(wi, wh) *
+                        absdot(wo, wh) * factor * factor / (ci * co * sd * sd));
+        return mul(V3{1.f - F, 1.f - F, 1.f - F}, ld3(l.c)) * v;
+      }
+      break;
+    default:  // specular lobes are delta distributions
+      break;
+  }
+  return V3{0, 0, 0};
+}
+
+template <unsigned KM>
+__device__ __forceinline__ float lobe_pdf_t(const DevLobe& l, V3 wi, V3 wo) {
   switch (l.kind) {
     case LOBE_LAMBERT_R:
     case LOBE_OREN_NAYAR:
-      return same_hemisphere(wi, wo) ? abs_cos_theta(wi) * kInvPi : 0.f;
-    case LOBE_MICROFACET_R: {
-      if (!same_hemisphere(wi, wo)) return 0.f;
-      V3 wh = normalize(wi + wo);
-      return md_pdf(l.dist, l.alpha, wh) / (4.f * dot(wo, wh));
-    }
-    case LOBE_MICROFACET_T: {
-      if (same_hemisphere(wo, wi)) return 0.f;
-      float eta = cos_theta(wo) > 0.f ? (l.etaB / l.etaA) : (l.etaA / l.etaB);
-      V3 wh = normalize(wo + wi * eta);
-      float sd = dot(wo, wh) + eta * dot(wi, wh);
-      float dwh = fabsf((eta * eta * dot(wi, wh)) / (sd * sd));
-      return md_pdf(l.dist, l.alpha, wh) * dwh;
-    }
+      if constexpr (has_kind<KM>(LOBE_LAMBERT_R) || has_kind<KM>(LOBE_OREN_NAYAR))
+        return same_hemisphere(wi, wo) ? abs_cos_theta(wi) * kInvPi : 0.f;
+      break;
+    case LOBE_MICROFACET_R:
+      if constexpr (has_kind<KM>(LOBE_MICROFACET_R)) {
+        if (!same_hemisphere(wi, wo)) return 0.f;
+        V3 wh = normalize(wi + wo);
+        return md_pdf(l.dist, l.alpha, wh) / (4.f * dot(wo, wh));
+      }
+      break;
+    case LOBE_MICROFACET_T:
+      if constexpr (has_kind<KM>(LOBE_MICROFACET_T)) {
+        if (same_hemisphere(wo, wi)) return 0.f;
+        float eta = cos_theta(wo) > 0.f ? (l.etaB / l.etaA) : (l.etaA / l.etaB);
+        V3 wh = normalize(wo + wi * eta);
+        float sd = dot(wo, wh) + eta * dot(wi, wh);
+        float dwh = fabsf((eta * eta * dot(wi, wh)) / (sd * sd));
+        return md_pdf(l.dist, l.alpha, wh) * dwh;
+      }
+      break;
     default:
-      return 0.f;
+      break;
   }
+  return 0.f;
+}
+
+static __device__ __noinline__ V3 lobe_f_all(const DevLobe& l, V3 wi, V3 wo) { return lobe_f_t<kLobeAll>(l, wi, wo); }
+static __device__ __noinline__ float lobe_pdf_all(const DevLobe& l, V3 wi, V3 wo) {
+  return lobe_pdf_t<kLobeAll>(l, wi, wo);
+}
+
+template <unsigned KM>
+__device__ __forceinline__ V3 lobe_f(const DevLobe& l, V3 wi, V3 wo) {
+  if constexpr (KM == kLobeAll)
+    return lobe_f_all(l, wi, wo);
+  else
+    return lobe_f_t<KM>(l, wi, wo);
+}
+
+template <unsigned KM>
+__device__ __forceinline__ float lobe_pdf(const DevLobe& l, V3 wi, V3 wo) {
+  if constexpr (KM == kLobeAll)
+    return lobe_pdf_all(l, wi, wo);
+  else
+    return lobe_pdf_t<KM>(l, wi, wo);
 }
 
 // Samples one lobe; *pdf is left untouched (0) on the reference's early exits.
-static __device__ __noinline__ V3 lobe_sample_f(const DevLobe& l, V3 wo, float u0, float u1, V3* wi, float* pdf,
-                                            int* stype) {
+template <unsigned KM>
+__device__ __forceinline__ V3 lobe_sample_f_t(const DevLobe& l, V3 wo, float u0, float u1, V3* wi, float* pdf,
+                                              int* stype) {
   switch (l.kind) {
     case LOBE_LAMBERT_R:
-    case LOBE_OREN_NAYAR: {
-      *wi = cosine_sample_hemisphere(u0, u1);
-      if (wo.z < 0.f) wi->z *= -1.f;
-      *pdf = lobe_pdf(l, *wi, wo);
-      return lobe_f(l, *wi, wo);
-    }
-    case LOBE_MICROFACET_R: {
-      if (wo.z == 0.f) return V3{0, 0, 0};
-      V3 wh = md_sample_wh(l.dist, l.alpha, wo, u0, u1);
-      *wi = reflect(wo, wh);
-      if (!same_hemisphere(*wi, wo)) return V3{0, 0, 0};
-      *pdf = md_pdf(l.dist, l.alpha, wh) / (4.f * dot(wo, wh));
-      return lobe_f(l, *wi, wo);
-    }
-    case LOBE_MICROFACET_T: {
-      if (wo.z == 0.f) return V3{0, 0, 0};
-      V3 wh = md_sample_wh(l.dist, l.alpha, wo, u0, u1);
-      float eta = cos_theta(wo) > 0.f ? (l.etaA / l.etaB) : (l.etaB / l.etaA);
-      if (!refract(wo, wh, eta, wi)) return V3{0, 0, 0};
-      return lobe_f(l, *wi, wo);  // pdf is never set (src/bsdf/microfacet.cpp:76-85)
-    }
-    case LOBE_SPECULAR_R: {
-      *wi = V3{-wo.x, -wo.y, wo.z};
-      *pdf = 1.f;
-      return sdiv(mul(fresnel_eval(l, cos_theta(*wi)), ld3(l.c)), abs_cos_theta(*wi));
-    }
-    case LOBE_SPECULAR_T: {
-      bool entering = cos_theta(wo) > 0.f;
-      float ei = entering ? l.etaA : l.etaB;
-      float et = entering ? l.etaB : l.etaA;
-      if (!refract(wo, faceforward(V3{0, 0, 1}, wo), ei / et, wi)) return V3{0, 0, 0};
-      *pdf = 1.f;
-      float F = fr_dielectric(fabsf(cos_theta(*wi)), l.etaA, l.etaB);
-      V3 ft = mul(ld3(l.c), V3{1.f - F, 1.f - F, 1.f - F});
-      ft = ft * ((ei * ei) / (et * et));
-      return sdiv(ft, abs_cos_theta(*wi));
-    }
-    case LOBE_FRESNEL_SPECULAR: {
-      float F = fr_dielectric(cos_theta(wo), l.etaA, l.etaB);
-      if (u0 < F) {
-        *wi = V3{-wo.x, -wo.y, wo.z};
-        *stype = BXDF_SPECULAR | BXDF_REFLECTION;
-        *pdf = F;
-        return sdiv(ld3(l.c) * F, abs_cos_theta(*wi));
+    case LOBE_OREN_NAYAR:
+      if constexpr (has_kind<KM>(LOBE_LAMBERT_R) || has_kind<KM>(LOBE_OREN_NAYAR)) {
+        *wi = cosine_sample_hemisphere(u0, u1);
+        if (wo.z < 0.f) wi->z *= -1.f;
+        *pdf = lobe_pdf<KM>(l, *wi, wo);
+        return lobe_f<KM>(l, *wi, wo);
       }
-      bool entering = cos_theta(wo) > 0.f;
-      float ei = entering ? l.etaA : l.etaB;
-      float et = entering ? l.etaB : l.etaA;
-      if (!refract(wo, faceforward(V3{0, 0, 1}, wo), ei / et, wi)) return V3{0, 0, 0};
-      V3 ft = ld3(l.c2) * (1.f - F);
-      ft = ft * ((ei * ei) / (et * et));
-      *stype = BXDF_SPECULAR | BXDF_TRANSMISSION;
-      *pdf = 1.f - F;
-      return sdiv(ft, abs_cos_theta(*wi));
-    }
+      break;
+    case LOBE_MICROFACET_R:
+      if constexpr (has_kind<KM>(LOBE_MICROFACET_R)) {
+        if (wo.z == 0.f) return V3{0, 0, 0};
+        V3 wh = md_sample_wh(l.dist, l.alpha, wo, u0, u1);
+        *wi = reflect(wo, wh);
+        if (!same_hemisphere(*wi, wo)) return V3{0, 0, 0};
+        *pdf = md_pdf(l.dist, l.alpha, wh) / (4.f * dot(wo, wh));
+        return lobe_f<KM>(l, *wi, wo);
+      }
+      break;
+    case LOBE_MICROFACET_T:
+      if constexpr (has_kind<KM>(LOBE_MICROFACET_T)) {
+        if (wo.z == 0.f) return V3{0, 0, 0};
+        V3 wh = md_sample_wh(l.dist, l.alpha, wo, u0, u1);
+        float eta = cos_theta(wo) > 0.f ? (l.etaA / l.etaB) : (l.etaB / l.etaA);
+        if (!refract(wo, wh, eta, wi)) return V3{0, 0, 0};
+        return lobe_f<KM>(l, *wi, wo);  // pdf is never set (src/bsdf/microfacet.cpp:76-85)
+      }
+      break;
+    case LOBE_SPECULAR_R:
+      if constexpr (has_kind<KM>(LOBE_SPECULAR_R)) {
+        *wi = V3{-wo.x, -wo.y, wo.z};
+        *pdf = 1.f;
+        return sdiv(mul(fresnel_eval(l, cos_theta(*wi)), ld3(l.c)), abs_cos_theta(*wi));
+      }
+      break;
+    case LOBE_SPECULAR_T:
+      if constexpr (has_kind<KM>(LOBE_SPECULAR_T)) {
+        bool entering = cos_theta(wo) > 0.f;
+        float ei = entering ? l.etaA : l.etaB;
+        float et = entering ? l.etaB : l.etaA;
+        if (!refract(wo, faceforward(V3{0, 0, 1}, wo), ei / et, wi)) return V3{0, 0, 0};
+        *pdf = 1.f;
+        float F = fr_dielectric(fabsf(cos_theta(*wi)), l.etaA, l.etaB);
+        V3 ft = mul(ld3(l.c), V3{1.f - F, 1.f - F, 1.f - F});
+        ft = ft * ((ei * ei) / (et * et));
+        return sdiv(ft, abs_cos_theta(*wi));
+      }
+      break;
+    case LOBE_FRESNEL_SPECULAR:
+      if constexpr (has_kind<KM>(LOBE_FRESNEL_SPECULAR)) {
+        float F = fr_dielectric(cos_theta(wo), l.etaA, l.etaB);
+        if (u0 < F) {
+          *wi = V3{-wo.x, -wo.y, wo.z};
+          *stype = BXDF_SPECULAR | BXDF_REFLECTION;
+          *pdf = F;
+          return sdiv(ld3(l.c) * F, abs_cos_theta(*wi));
+        }
+        bool entering = cos_theta(wo) > 0.f;
+        float ei = entering ? l.etaA : l.etaB;
+        float et = entering ? l.etaB : l.etaA;
+        if (!refract(wo, faceforward(V3{0, 0, 1}, wo), ei / et, wi)) return V3{0, 0, 0};
+        V3 ft = ld3(l.c2) * (1.f - F);
+        ft = ft * ((ei * ei) / (et * et));
+        *stype = BXDF_SPECULAR | BXDF_TRANSMISSION;
+        *pdf = 1.f - F;
+        return sdiv(ft, abs_cos_theta(*wi));
+      }
+      break;
+    default:
+      break;
   }
   return V3{0, 0, 0};
+}
+
+static __device__ __noinline__ V3 lobe_sample_f_all(const DevLobe& l, V3 wo, float u0, float u1, V3* wi, float* pdf,
+                                                    int* stype) {
+  return lobe_sample_f_t<kLobeAll>(l, wo, u0, u1, wi, pdf, stype);
+}
+
+template <unsigned KM>
+__device__ __forceinline__ V3 lobe_sample_f(const DevLobe& l, V3 wo, float u0, float u1, V3* wi, float* pdf,
+                                            int* stype) {
+  if constexpr (KM == kLobeAll)
+    return lobe_sample_f_all(l, wo, u0, u1, wi, pdf, stype);
+  else
+    return lobe_sample_f_t<KM>(l, wo, u0, u1, wi, pdf, stype);
 }
 
 __device__ __forceinline__ bool lobe_matches(const DevLobe& l, int type) { return (l.type & type) == l.type; }
@@ -289,14 +368,16 @@ __device__ __forceinline__ int bsdf_num_matching(const DevMaterial& m, int type)
   return n;
 }
 
+template <unsigned KM = kLobeAll>
 __device__ __forceinline__ V3 bsdf_f(const DevMaterial& m, const Frame& fr, V3 wi_w, V3 wo_w, int type) {
   V3 wi = world_to_local(fr, wi_w), wo = world_to_local(fr, wo_w);
   V3 r{0, 0, 0};
   for (int i = 0; i < m.num_lobes; ++i)
-    if (lobe_matches(m.lobes[i], type)) r = r + lobe_f(m.lobes[i], wi, wo);
+    if (lobe_matches(m.lobes[i], type)) r = r + lobe_f<KM>(m.lobes[i], wi, wo);
   return r;
 }
 
+template <unsigned KM = kLobeAll>
 __device__ __forceinline__ float bsdf_pdf(const DevMaterial& m, const Frame& fr, V3 wi_w, V3 wo_w, int type) {
   if (m.num_lobes == 0) return 0.f;
   V3 wi = world_to_local(fr, wi_w), wo = world_to_local(fr, wo_w);
@@ -306,14 +387,15 @@ __device__ __forceinline__ float bsdf_pdf(const DevMaterial& m, const Frame& fr,
   for (int i = 0; i < m.num_lobes; ++i)
     if (lobe_matches(m.lobes[i], type)) {
       ++n;
-      pdf += lobe_pdf(m.lobes[i], wi, wo);
+      pdf += lobe_pdf<KM>(m.lobes[i], wi, wo);
     }
   return n > 0 ? pdf / n : 0.f;
 }
 
 // Returns f; *pdf = 0 and *stype = 0 on failure. *wi is written only on success.
-static __device__ __noinline__ V3 bsdf_sample_f(const DevMaterial& m, const Frame& fr, V3 wo_w, float u0, float u1,
-                                            int type, V3* wi_w, float* pdf, int* stype) {
+template <unsigned KM>
+__device__ __forceinline__ V3 bsdf_sample_f_t(const DevMaterial& m, const Frame& fr, V3 wo_w, float u0, float u1,
+                                              int type, V3* wi_w, float* pdf, int* stype) {
   int n = bsdf_num_matching(m, type);
   *pdf = 0.f;
   *stype = 0;
@@ -331,7 +413,7 @@ static __device__ __noinline__ V3 bsdf_sample_f(const DevMaterial& m, const Fram
   if (wo.z == 0.f) return V3{0, 0, 0};
   *stype = lb.type;
   V3 wi;
-  V3 f = lobe_sample_f(lb, wo, nu0, u1, &wi, pdf, stype);
+  V3 f = lobe_sample_f<KM>(lb, wo, nu0, u1, &wi, pdf, stype);
   if (*pdf == 0.f) {
     *stype = 0;
     return V3{0, 0, 0};
@@ -340,7 +422,7 @@ static __device__ __noinline__ V3 bsdf_sample_f(const DevMaterial& m, const Fram
   bool specular = (lb.type & BXDF_SPECULAR) != 0;
   if (!specular && n > 1)
     for (int i = 0; i < m.num_lobes; ++i)
-      if (i != sel && lobe_matches(m.lobes[i], type)) *pdf += lobe_pdf(m.lobes[i], wi, wo);
+      if (i != sel && lobe_matches(m.lobes[i], type)) *pdf += lobe_pdf<KM>(m.lobes[i], wi, wo);
   if (n > 1) *pdf /= n;
   if (!specular && n > 1) {
     bool refl = dot(*wi_w, fr.ng) * dot(wo_w, fr.ng) > 0.f;
@@ -348,10 +430,24 @@ static __device__ __noinline__ V3 bsdf_sample_f(const DevMaterial& m, const Fram
     for (int i = 0; i < m.num_lobes; ++i) {
       const DevLobe& l = m.lobes[i];
       bool has_r = (l.type & BXDF_REFLECTION) != 0, has_t = (l.type & BXDF_TRANSMISSION) != 0;
-      if (lobe_matches(l, type) && ((refl && has_r) || (!refl && has_t))) f = f + lobe_f(l, wi, wo);
+      if (lobe_matches(l, type) && ((refl && has_r) || (!refl && has_t))) f = f + lobe_f<KM>(l, wi, wo);
     }
   }
   return f;
+}
+
+static __device__ __noinline__ V3 bsdf_sample_f_all(const DevMaterial& m, const Frame& fr, V3 wo_w, float u0,
+                                                    float u1, int type, V3* wi_w, float* pdf, int* stype) {
+  return bsdf_sample_f_t<kLobeAll>(m, fr, wo_w, u0, u1, type, wi_w, pdf, stype);
+}
+
+template <unsigned KM = kLobeAll>
+__device__ __forceinline__ V3 bsdf_sample_f(const DevMaterial& m, const Frame& fr, V3 wo_w, float u0, float u1,
+                                            int type, V3* wi_w, float* pdf, int* stype) {
+  if constexpr (KM == kLobeAll)
+    return bsdf_sample_f_all(m, fr, wo_w, u0, u1, type, wi_w, pdf, stype);
+  else
+    return bsdf_sample_f_t<KM>(m, fr, wo_w, u0, u1, type, wi_w, pdf, stype);
 }
 
 }  // namespace orion_gb300

@@ -73,6 +73,7 @@ namespace {
 struct TmpNode {
   float lo[3], hi[3];
   int32_t begin = 0, count = 0;  // leaf range in `order`
+  int32_t first = 0, total = 0;  // the subtree's triangles: order[first, first + total)
   TmpNode* child[2] = {nullptr, nullptr};
   int depth = 0;
 };
@@ -126,6 +127,8 @@ struct Builder {
     n->depth = depth;
     bounds(begin, end, n->lo, n->hi);
     int count = end - begin;
+    n->first = begin;
+    n->total = count;
     int cur = max_depth.load();
     while (depth > cur && !max_depth.compare_exchange_weak(cur, depth)) {
     }
@@ -344,6 +347,189 @@ struct Flattener {
   }
 };
 
+// Collapses the binary tree into 8-wide nodes. Each wide node takes the
+// children of a binary node and keeps opening its internal child of largest
+// surface area until it has 8 children or only leaves; children are placed
+// in slots by the direction of their centre from the node's centre (the
+// slot order a ray visits depends on its octant); boxes are padded like the
+// binary nodes' and quantised outwards.
+struct WideCollapser {
+  const int32_t* order;            // binary leaf order -> primID
+  std::vector<WideNode>& out;
+  std::vector<int32_t>& tris;      // wide leaf order -> primID
+
+  static void padded(const TmpNode* n, double lo[3], double hi[3]) {
+    BvhNode b;
+    write_node(&b, n);
+    for (int k = 0; k < 3; ++k) {
+      lo[k] = b.lo[k];
+      hi[k] = b.hi[k];
+    }
+  }
+
+  static double area(const TmpNode* n) {
+    float dx = n->hi[0] - n->lo[0], dy = n->hi[1] - n->lo[1], dz = n->hi[2] - n->lo[2];
+    return (double)dx * dy + (double)dy * dz + (double)dz * dx;
+  }
+
+  // A child becomes a leaf slot when its subtree holds at most kWideLeaf triangles.
+  static constexpr int kWideLeaf = 3;
+  static bool is_leaf(const TmpNode* n) { return n->total <= kWideLeaf; }
+
+  void gather(const TmpNode* n, std::vector<const TmpNode*>& ch) const {
+    ch.clear();
+    if (is_leaf(n)) {  // a small root: one leaf child
+      ch.push_back(n);
+      return;
+    }
+    ch.push_back(n->child[0]);
+    ch.push_back(n->child[1]);
+    while (ch.size() < 8) {
+      int best = -1;
+      double best_a = -1.0;
+      for (int i = 0; i < (int)ch.size(); ++i)
+        if (!is_leaf(ch[i]) && area(ch[i]) > best_a) {
+          best_a = area(ch[i]);
+          best = i;
+        }
+      if (best < 0) break;
+      const TmpNode* c = ch[best];
+      ch[best] = c->child[0];
+      ch.push_back(c->child[1]);
+    }
+    // Slots left over: split leaf-sized subtrees too, for tighter leaf boxes.
+    while (ch.size() < 8) {
+      int best = -1;
+      double best_a = -1.0;
+      for (int i = 0; i < (int)ch.size(); ++i)
+        if (ch[i]->count == 0 && ch[i]->child[0] && area(ch[i]) > best_a) {
+          best_a = area(ch[i]);
+          best = i;
+        }
+      if (best < 0) break;
+      const TmpNode* c = ch[best];
+      ch[best] = c->child[0];
+      ch.push_back(c->child[1]);
+    }
+  }
+
+  // Slot of each child: greedy matching of child directions to the eight
+  // octant directions of the slots.
+  static void assign_slots(const std::vector<const TmpNode*>& ch, const double nlo[3], const double nhi[3],
+                           int slot_of[8]) {
+    const int m = (int)ch.size();
+    double score[8][8];
+    for (int c = 0; c < m; ++c) {
+      double off[3];
+      for (int k = 0; k < 3; ++k)
+        off[k] = 0.5 * ((double)ch[c]->lo[k] + ch[c]->hi[k]) - 0.5 * (nlo[k] + nhi[k]);
+      for (int s = 0; s < 8; ++s) {
+        double v = 0.0;
+        for (int k = 0; k < 3; ++k) v += ((s >> k) & 1) ? off[k] : -off[k];
+        score[c][s] = v;
+      }
+    }
+    bool used_c[8] = {}, used_s[8] = {};
+    for (int it = 0; it < m; ++it) {
+      int bc = -1, bs = -1;
+      double bv = -std::numeric_limits<double>::infinity();
+      for (int c = 0; c < m; ++c) {
+        if (used_c[c]) continue;
+        for (int s = 0; s < 8; ++s)
+          if (!used_s[s] && score[c][s] > bv) {
+            bv = score[c][s];
+            bc = c;
+            bs = s;
+          }
+      }
+      used_c[bc] = used_s[bs] = true;
+      slot_of[bc] = bs;
+    }
+  }
+
+  void fill(int idx, const TmpNode* n) {
+    std::vector<const TmpNode*> ch;
+    gather(n, ch);
+    const int m = (int)ch.size();
+    double clo[8][3], chi[8][3], nlo[3], nhi[3];
+    for (int k = 0; k < 3; ++k) {
+      nlo[k] = std::numeric_limits<double>::infinity();
+      nhi[k] = -std::numeric_limits<double>::infinity();
+    }
+    for (int c = 0; c < m; ++c) {
+      padded(ch[c], clo[c], chi[c]);
+      for (int k = 0; k < 3; ++k) {
+        nlo[k] = std::min(nlo[k], clo[c][k]);
+        nhi[k] = std::max(nhi[k], chi[c][k]);
+      }
+    }
+    int slot_of[8];
+    assign_slots(ch, nlo, nhi, slot_of);
+    const TmpNode* in_slot[8] = {};
+    int child_of_slot[8];
+    for (int c = 0; c < m; ++c) {
+      in_slot[slot_of[c]] = ch[c];
+      child_of_slot[slot_of[c]] = c;
+    }
+    WideNode w;
+    std::memset(&w, 0, sizeof(w));
+    // Empty slots get inverted boxes (lo = 255 > hi = 0 on every axis), which
+    // no ray hits whatever its direction.
+    std::memset(w.qlo, 0xff, sizeof(w.qlo));
+    // Quantisation grid per axis: the smallest power-of-two cell with 255 cells covering the node.
+    double cell[3];
+    for (int k = 0; k < 3; ++k) {
+      w.p[k] = (float)nlo[k];
+      if ((double)w.p[k] > nlo[k]) w.p[k] = std::nextafter(w.p[k], -std::numeric_limits<float>::infinity());
+      const double ext = nhi[k] - (double)w.p[k];
+      int e = -126;
+      while (e < 127 && std::ldexp(255.0, e) < ext) ++e;
+      w.e[k] = (uint8_t)(e + 127);
+      cell[k] = std::ldexp(1.0, e);
+    }
+    // Internal children first (their node slots), then leaf triangles.
+    int n_internal = 0;
+    for (int s = 0; s < 8; ++s)
+      if (in_slot[s] && !is_leaf(in_slot[s])) ++n_internal;
+    const int child_base = (int)out.size();
+    out.resize(out.size() + n_internal);
+    w.child_base = child_base;
+    w.tri_base = (int)tris.size();
+    for (int s = 0; s < 8; ++s) {
+      const TmpNode* c = in_slot[s];
+      if (!c) continue;
+      const int ci = child_of_slot[s];
+      for (int k = 0; k < 3; ++k) {
+        double ql = std::floor((clo[ci][k] - w.p[k]) / cell[k]);
+        double qh = std::ceil((chi[ci][k] - w.p[k]) / cell[k]);
+        ql = std::max(0.0, std::min(255.0, ql));
+        qh = std::max(0.0, std::min(255.0, qh));
+        while (ql > 0.0 && (double)w.p[k] + ql * cell[k] > clo[ci][k]) ql -= 1.0;
+        while (qh < 255.0 && (double)w.p[k] + qh * cell[k] < chi[ci][k]) qh += 1.0;
+        w.qlo[k][s] = (uint8_t)ql;
+        w.qhi[k][s] = (uint8_t)qh;
+      }
+      if (!is_leaf(c)) {
+        w.imask |= (uint8_t)(1u << s);
+        w.meta[s] = 0x80;
+      } else {
+        const int off = (int)tris.size() - w.tri_base;
+        w.meta[s] = (uint8_t)((c->total << 5) | off);
+        for (int i = 0; i < c->total; ++i) tris.push_back(order[c->first + i]);
+      }
+    }
+    out[idx] = w;
+    int r = 0;
+    for (int s = 0; s < 8; ++s)
+      if (in_slot[s] && !is_leaf(in_slot[s])) fill(child_base + r++, in_slot[s]);
+  }
+
+  void run(const TmpNode* root) {
+    out.assign(1, WideNode{});
+    fill(0, root);
+  }
+};
+
 }  // namespace
 
 void build_bvh(const float* positions, int64_t num_tris, const BvhBuildOptions& opt, BvhBuild* out) {
@@ -353,6 +539,15 @@ void build_bvh(const float* positions, int64_t num_tris, const BvhBuildOptions& 
   out->tri_prim.resize(T);
   out->depth = 0;
   out->leaves = 0;
+  out->wide.clear();
+  if (T == 0 && opt.wide) {
+    WideNode empty;
+    std::memset(&empty, 0, sizeof(empty));  // no slot in use, inverted boxes: nothing hits
+    std::memset(empty.qlo, 0xff, sizeof(empty.qlo));
+    for (int k = 0; k < 3; ++k) empty.e[k] = 127;
+    out->wide.push_back(empty);
+    return;
+  }
   if (T == 0) {
     BvhNode empty;
     std::memset(&empty, 0, sizeof(empty));
@@ -380,10 +575,21 @@ void build_bvh(const float* positions, int64_t num_tris, const BvhBuildOptions& 
   Builder b(opt, lo.data(), hi.data(), ce.data(), order.data(), threads);
   std::deque<TmpNode>* arena = b.new_arena();
   TmpNode* root = b.build(0, T, 0, arena);
-  Flattener fl(out->nodes);
-  fl.run(root, opt.top_bfs_nodes);
   out->depth = b.max_depth.load();
   out->leaves = b.leaves.load();
+  if (opt.wide) {
+    std::vector<int32_t> tris;
+    tris.reserve(T);
+    WideCollapser wc{order.data(), out->wide, tris};
+    wc.run(root);
+    for (int i = 0; i < T; ++i) {
+      out->tri_prim[i] = tris[i];
+      woop_record(positions + 9 * (size_t)tris[i], &out->woop[12 * (size_t)i]);
+    }
+    return;
+  }
+  Flattener fl(out->nodes);
+  fl.run(root, opt.top_bfs_nodes);
   for (int i = 0; i < T; ++i) {
     out->tri_prim[i] = order[i];
     woop_record(positions + 9 * (size_t)order[i], &out->woop[12 * (size_t)i]);

@@ -14,13 +14,15 @@ struct BvhBuildOptions {
   int bins = 32;           // SAH bins per axis
   int top_bfs_nodes = 0;   // the first N node slots hold the top levels in breadth-first order
   int threads = 0;         // build threads, 0 = hardware concurrency
+  bool wide = false;       // collapse into the 8-wide quantised BVH (needs max_leaf <= 3)
 };
 
 struct BvhBuild {
-  std::vector<BvhNode> nodes;    // node 0 is the root; children of an inner node are (a, a+1)
+  std::vector<BvhNode> nodes;    // binary: node 0 is the root; children of an inner node are (a, a+1)
+  std::vector<WideNode> wide;    // wide: node 0 is the root (binary `nodes` then left empty)
   std::vector<float> woop;       // 12 floats per triangle (3 x float4), leaf order
   std::vector<int32_t> tri_prim; // leaf order -> primID
-  int depth = 0;                 // levels below the root
+  int depth = 0;                 // levels below the root (of the binary tree; bounds the wide tree's)
   int leaves = 0;
   double sah_cost = 0.0;
 };

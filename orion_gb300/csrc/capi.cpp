@@ -84,7 +84,7 @@ struct DevBuf {
 };
 
 struct DeviceScene {
-  DevBuf nodes, woop, tri_prim, prims, mats, lights, lfunc, lcdf;
+  DevBuf nodes, woop, tri_prim, tri_class, prims, mats, lights, lfunc, lcdf;
   SceneView view{};
   int64_t bytes = 0;
   int64_t num_prims = 0;
@@ -216,7 +216,7 @@ static int ensure_wave(orion_gpu_ctx* c, int capacity) {
   if (c->wave.capacity >= capacity) return ORION_OK;
   const size_t n = (size_t)capacity;
   const size_t f4 = n * sizeof(float4), i4 = (n * sizeof(int) + 255) & ~(size_t)255;
-  const size_t bytes = 15 * f4 + 7 * i4 + 256 + 4096;
+  const size_t bytes = 15 * f4 + (7 + kShadeClasses) * i4 + 256 + 4096;
   int rc = c->wave.block.alloc(bytes);
   if (rc != ORION_OK) {
     c->wave.capacity = 0;
@@ -235,6 +235,8 @@ static int ensure_wave(orion_gpu_ctx* c, int capacity) {
     *q = reinterpret_cast<int*>(p);
     p += i4;
   }
+  w.q_cls = reinterpret_cast<int*>(p);  // class c at q_cls + c * capacity
+  p += kShadeClasses * i4;
   w.counters = reinterpret_cast<int*>(p);
   p += 128;
   w.ray_stats = reinterpret_cast<unsigned long long*>(p);
@@ -334,7 +336,10 @@ extern "C" int orion_gpu_scene_upload(orion_gpu_ctx* ctx, const orion_host_scene
     if (!hsm->bvh) {
       std::unique_ptr<BvhBuild> b(new BvhBuild());
       BvhBuildOptions bo;
+      bo.wide = true;
+      bo.max_leaf = 3;
       build_bvh(hs.positions.data(), hs.num_prims(), bo, b.get());
+      if (b->depth >= 48) return fail(ORION_ERR_UNSUPPORTED, "BVH deeper than the traversal stack bound");
       hsm->bvh = std::move(b);
     }
   }
@@ -343,9 +348,13 @@ extern "C" int orion_gpu_scene_upload(orion_gpu_ctx* ctx, const orion_host_scene
   std::unique_ptr<DeviceScene> d(new DeviceScene());
   int64_t bytes = 0;
   int rc;
-  if ((rc = upload(d->nodes, bvh.nodes, ctx->stream, &bytes)) != ORION_OK) return rc;
+  if ((rc = upload(d->nodes, bvh.wide, ctx->stream, &bytes)) != ORION_OK) return rc;
   if ((rc = upload(d->woop, bvh.woop, ctx->stream, &bytes)) != ORION_OK) return rc;
   if ((rc = upload(d->tri_prim, bvh.tri_prim, ctx->stream, &bytes)) != ORION_OK) return rc;
+  std::vector<uint8_t> tri_class(bvh.tri_prim.size());
+  for (size_t i = 0; i < tri_class.size(); ++i)
+    tri_class[i] = (uint8_t)ps.mats[ps.prims[bvh.tri_prim[i]].material].shade_class;
+  if ((rc = upload(d->tri_class, tri_class, ctx->stream, &bytes)) != ORION_OK) return rc;
   if ((rc = upload(d->prims, ps.prims, ctx->stream, &bytes)) != ORION_OK) return rc;
   if ((rc = upload(d->mats, ps.mats, ctx->stream, &bytes)) != ORION_OK) return rc;
   if ((rc = upload(d->lights, ps.lights, ctx->stream, &bytes)) != ORION_OK) return rc;
@@ -356,6 +365,7 @@ extern "C" int orion_gpu_scene_upload(orion_gpu_ctx* ctx, const orion_host_scene
   v.nodes = d->nodes.as<float4>();
   v.woop = d->woop.as<float4>();
   v.tri_prim = d->tri_prim.as<int>();
+  v.tri_class = d->tri_class.as<uint8_t>();
   v.prims = d->prims.as<PrimShade>();
   v.mats = d->mats.as<DevMaterial>();
   v.lights = d->lights.as<DevLight>();
@@ -601,7 +611,7 @@ static int run_batch_locked(orion_gpu_ctx* ctx, std::vector<DevJob>& dj, unsigne
   bv.index_of = ctx->b_index_of.as<long long>();
   bv.q_retire = ctx->b_retire.as<int>();
   bv.q_free = ctx->b_free.as<int>();
-  if ((rc = build_batch_graph(ctx, bv, cap)) != ORION_OK) return rc;
+  if (!ctx->profiling && (rc = build_batch_graph(ctx, bv, cap)) != ORION_OK) return rc;
 
   BatchCtl c;
   std::memset(&c, 0, sizeof(c));
@@ -616,9 +626,41 @@ static int run_batch_locked(orion_gpu_ctx* ctx, std::vector<DevJob>& dj, unsigne
   CUDA_TRY(cudaMemcpyAsync(bv.ctl, &c, sizeof(c), cudaMemcpyHostToDevice, s));
   launch_batch_init(ctx->wave.view, bv, cap, s);
   CUDA_TRY(cudaGetLastError());
-  CUDA_TRY(cudaEventRecord(ctx->ev0, s));
-  CUDA_TRY(cudaGraphLaunch(ctx->bexec, s));
-  CUDA_TRY(cudaEventRecord(ctx->ev1, s));
+  std::memset(&ctx->stage_times, 0, sizeof(ctx->stage_times));
+  if (ctx->profiling) {
+    // Profiling: the same iterations driven from the host, every stage timed
+    // (one host round trip per iteration, so device_ms includes those gaps).
+    const int per_iter = 8;
+    const int need = (int)std::min<int64_t>((int64_t)c.max_iterations * per_iter, 200000);
+    while ((int)ctx->prof_events.size() < 2 * need) {
+      cudaEvent_t e;
+      CUDA_TRY(cudaEventCreate(&e));
+      ctx->prof_events.push_back(e);
+    }
+    ctx->prof_stage.resize(need);
+    StageTimer timer{ctx->prof_events.data(), ctx->prof_stage.data(), need, 0};
+    CUDA_TRY(cudaEventRecord(ctx->ev0, s));
+    int more = 1;
+    for (int it = 0; more && it < c.max_iterations; ++it) {
+      launch_batch_iteration(ctx->wave.view, bv, ctx->sobol.as<uint32_t>(), ctx->sobol_bitmajor.as<uint32_t>(),
+                             ctx->cfg, s, &timer);
+      CUDA_TRY(cudaGetLastError());
+      CUDA_TRY(cudaMemcpyAsync(&more, &bv.ctl->more, sizeof(int), cudaMemcpyDeviceToHost, s));
+      CUDA_TRY(cudaStreamSynchronize(s));
+    }
+    CUDA_TRY(cudaEventRecord(ctx->ev1, s));
+    CUDA_TRY(cudaStreamSynchronize(s));
+    for (int i = 0; i < std::min(timer.used, timer.capacity); ++i) {
+      float e = 0.f;
+      CUDA_TRY(cudaEventElapsedTime(&e, timer.events[2 * i], timer.events[2 * i + 1]));
+      ctx->stage_times.ms[timer.stage[i]] += e;
+      ctx->stage_times.launches[timer.stage[i]] += 1;
+    }
+  } else {
+    CUDA_TRY(cudaEventRecord(ctx->ev0, s));
+    CUDA_TRY(cudaGraphLaunch(ctx->bexec, s));
+    CUDA_TRY(cudaEventRecord(ctx->ev1, s));
+  }
   CUDA_TRY(cudaMemcpyAsync(out_ctl, bv.ctl, sizeof(BatchCtl), cudaMemcpyDeviceToHost, s));
   CUDA_TRY(cudaStreamSynchronize(s));
   float ms = 0.f;
@@ -705,8 +747,9 @@ extern "C" int orion_gpu_render_batch(orion_gpu_ctx* ctx, int32_t njobs, const o
   for (int i = 0; i < njobs; ++i) {
     const long long wh = (long long)dj[i].width * dj[i].height;
     dj[i].sum = reinterpret_cast<double*>(fb + film_off[i]);
-    dj[i].sumsq = dj[i].sum + 3 * wh;
-    dj[i].count = reinterpret_cast<unsigned int*>(dj[i].sumsq + 3 * wh);
+    dj[i].count = reinterpret_cast<unsigned int*>(dj[i].sum + 6 * wh);
+    // Sums of squares only for callers that want them (they cost 3 FP64 atomics per path).
+    dj[i].sumsq = jobs[i].sumsq ? dj[i].sum + 3 * wh : nullptr;
   }
   cudaStream_t s = ctx->stream;
   CUDA_TRY(cudaMemsetAsync(ctx->b_films.p, 0, film_bytes, s));

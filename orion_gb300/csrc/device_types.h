@@ -62,10 +62,25 @@ struct DevLobe {       // 64 bytes
 
 constexpr int kMaxLobes = 5;
 
+// Shading classes: materials whose lobe lists run the same code. Paths are
+// sorted by the class of what they hit before shading, so a warp shades one
+// kind of material.
+enum ShadeClass : int32_t {
+  SC_DIFFUSE = 0,     // Lambert
+  SC_CONDUCTOR = 1,   // one microfacet reflection lobe (metal)
+  SC_SPECULAR = 2,    // delta lobes only (mirror, smooth glass)
+  SC_DIELECTRIC = 3,  // microfacet reflection + transmission (rough glass)
+  SC_PLASTIC = 4,     // Lambert + microfacet reflection
+  SC_GENERAL = 5,     // anything else (Oren-Nayar, uber, no lobes)
+  SC_MISS = 7,        // the ray left the scene
+  kShadeClasses = 8
+};
+
 struct DevMaterial {   // 16 + 5 * 64 = 336 bytes
   int32_t num_lobes;
   int32_t num_nonspecular;  // numBxDF(BxDF_ALL & ~BxDF_SPECULAR)
-  int32_t pad[2];
+  int32_t shade_class;      // ShadeClass
+  int32_t pad;
   DevLobe lobes[kMaxLobes];
 };
 
@@ -115,5 +130,28 @@ struct BvhNode {
   float hi[3];
   int32_t b;           // 0 = inner node, > 0 = leaf triangle count
 };
+
+// One node of the 8-wide BVH the kernels traverse: 80 bytes = 5 x float4.
+// Child boxes are quantised to 8 bits per bound on a per-axis grid of
+// power-of-two cells anchored at `p`: bound = p + q * 2^(e - 127).
+// Internal children are stored contiguously from child_base in slot order;
+// the triangles of all leaf children contiguously from tri_base.
+// meta[s]: 0 = empty slot; internal child: 0x80; leaf child:
+// (triangle count 1..3) << 5 | (first triangle - tri_base, 0..23).
+// An empty slot's box is inverted (qlo = 255, qhi = 0), so it is never hit.
+// Slots are assigned so that visiting them in order of (slot ^ octant),
+// octant bit a set when the ray direction is negative along axis a, is
+// roughly near to far.
+struct WideNode {
+  float p[3];
+  uint8_t e[3];        // biased exponent of the cell size per axis
+  uint8_t imask;       // bit s: slot s holds an internal child
+  int32_t child_base;
+  int32_t tri_base;
+  uint8_t meta[8];
+  uint8_t qlo[3][8];   // [axis][slot]
+  uint8_t qhi[3][8];
+};
+static_assert(sizeof(WideNode) == 80, "WideNode is five float4");
 
 }  // namespace orion_gb300

@@ -46,17 +46,18 @@ __global__ void k_camera(SceneView s, WaveView w, WaveArgs a) {
 }
 
 template <int SMEM>
-__global__ void k_trace(SceneView s, const int* queue, const int* count, int* fetch, const float4* ray_o,
-                        const float4* ray_d, float4* hit, unsigned long long* stat, int refill_below) {
+__global__ void __launch_bounds__(512, 2) k_trace(SceneView s, const int* queue, const int* count, int* fetch, const float4* ray_o,
+                        const float4* ray_d, float4* hit, unsigned long long* stat, int refill_below,
+                        int* cls_counters, int* q_cls, int cls_stride) {
   extern __shared__ int2 stack_smem[];
   const int n = *count;
   trace_persistent<false, SMEM>(SingleScene{&s}, queue, n, fetch, ray_o, ray_d, hit, nullptr, stack_smem,
-                                refill_below);
+                                refill_below, cls_counters, q_cls, cls_stride);
   if (stat && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(stat, (unsigned long long)n);
 }
 
 template <int SMEM>
-__global__ void k_trace_sh(SceneView s, const int* queue, const int* count, int* fetch, const float4* ray_o,
+__global__ void __launch_bounds__(512, 2) k_trace_sh(SceneView s, const int* queue, const int* count, int* fetch, const float4* ray_o,
                            const float4* ray_d, int* occluded, unsigned long long* stat, int refill_below) {
   extern __shared__ int2 stack_smem[];
   const int n = *count;
@@ -65,14 +66,16 @@ __global__ void k_trace_sh(SceneView s, const int* queue, const int* count, int*
   if (stat && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(stat, (unsigned long long)n);
 }
 
-// One bounce for every path in the current extension queue.
+// One bounce for every path traced this bounce, taken class by class from
+// the shading-class queues the extension trace filled.
 __global__ void k_shade(SceneView s, WaveView w, WaveArgs a, int bounce, int cur) {
-  const int* in_q = w.q_ext[cur];
   int* out_q = w.q_ext[cur ^ 1];
   int* out_cnt = w.counters + (cur ^ 1);
-  const int n = w.counters[cur];
+  ClassQueues cq;
+  cq.load(w.counters + CNT_CLS0);
+  const int n = cq.total();
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
-    const int pid = in_q[q];
+    const int pid = cq.slot(w.q_cls, w.capacity, q);
     ShadeResult r = shade_one(s, w, a.sobol_bitmajor, pid, (uint64_t)(a.base_index + pid), bounce, a.max_depth,
                               a.rr_depth);
     queue_append(w.counters + CNT_NEE, w.q_nee, pid, r.did_nee);
@@ -142,6 +145,7 @@ __global__ void k_reset_bounce_counters(int* counters, int next_ext) {
   if (i == 4) counters[CNT_FETCH_EXT] = 0;
   if (i == 5) counters[CNT_FETCH_SH] = 0;
   if (i == 6) counters[CNT_FETCH_MIS] = 0;
+  if (i >= CNT_CLS0 && i < CNT_CLS0 + kShadeClasses) counters[i] = 0;
 }
 
 // ------------------------------------------------------------ test hooks
@@ -231,6 +235,9 @@ struct TraceLaunch {
   float4* hit;
   int* occl;
   unsigned long long* stat;
+  int* cls_counters;  // closest hit: also sort slots by shading class (or null)
+  int* q_cls;
+  int cls_stride;
 };
 
 template <int SMEM>
@@ -242,7 +249,8 @@ void launch_trace_kernels(bool shadow, const SceneView& s, const TraceLaunch& t,
   if (shadow)
     k_trace_sh<SMEM><<<grid, block, smem, stream>>>(s, t.queue, t.count, t.fetch, t.o, t.d, t.occl, t.stat, refill);
   else
-    k_trace<SMEM><<<grid, block, smem, stream>>>(s, t.queue, t.count, t.fetch, t.o, t.d, t.hit, t.stat, refill);
+    k_trace<SMEM><<<grid, block, smem, stream>>>(s, t.queue, t.count, t.fetch, t.o, t.d, t.hit, t.stat, refill,
+                                                 t.cls_counters, t.q_cls, t.cls_stride);
 }
 
 void trace_dispatch(bool shadow, const SceneView& s, const TraceLaunch& t, const LaunchConfig& cfg, int grid,
@@ -285,7 +293,7 @@ void launch_wave(const SceneView& s, const WaveView& w, const WaveArgs& a, const
     begin(ST_TRACE_EXT);
     trace_dispatch(false, s,
                    TraceLaunch{w.q_ext[cur], w.counters + cur, w.counters + CNT_FETCH_EXT, w.ray_o, w.ray_d, w.hit,
-                               nullptr, w.ray_stats},
+                               nullptr, w.ray_stats, w.counters + CNT_CLS0, w.q_cls, w.capacity},
                    cfg, tgrid, stream);
     end();
     begin(ST_SHADE);
@@ -295,13 +303,13 @@ void launch_wave(const SceneView& s, const WaveView& w, const WaveArgs& a, const
       begin(ST_TRACE_SHADOW);
       trace_dispatch(true, s,
                      TraceLaunch{w.q_sh, w.counters + CNT_SH, w.counters + CNT_FETCH_SH, w.sh_o, w.sh_d, nullptr,
-                                 w.occluded, w.ray_stats + 1},
+                                 w.occluded, w.ray_stats + 1, nullptr, nullptr, 0},
                      cfg, tgrid, stream);
       end();
       begin(ST_TRACE_MIS);
       trace_dispatch(false, s,
                      TraceLaunch{w.q_mis, w.counters + CNT_MIS, w.counters + CNT_FETCH_MIS, w.mis_o, w.mis_d,
-                                 w.mis_hit, nullptr, w.ray_stats + 2},
+                                 w.mis_hit, nullptr, w.ray_stats + 2, nullptr, nullptr, 0},
                      cfg, tgrid, stream);
       end();
       begin(ST_RESOLVE);

@@ -12,6 +12,7 @@ struct SceneView {
   const float4* nodes;
   const float4* woop;
   const int* tri_prim;
+  const uint8_t* tri_class;  // leaf order -> ShadeClass of the triangle's material
   const PrimShade* prims;
   const DevMaterial* mats;
   const DevLight* lights;
@@ -47,6 +48,7 @@ struct WaveView {
   int* q_nee;        // paths that sampled a light this bounce
   int* q_sh;         // shadow rays
   int* q_mis;        // BSDF-sampled rays towards a non-delta light
+  int* q_cls;        // extension hits by shading class: kShadeClasses queues of `capacity`
   int* counters;     // kCounterSlots ints
   unsigned long long* ray_stats;  // ext, shadow, mis
   int* error_word;
@@ -54,7 +56,7 @@ struct WaveView {
 };
 
 enum CounterSlot { CNT_EXT0 = 0, CNT_EXT1 = 1, CNT_NEE = 2, CNT_SH = 3, CNT_MIS = 4, CNT_RETIRE = 5, CNT_FREE = 6,
-                   CNT_FETCH_EXT = 8, CNT_FETCH_SH = 9, CNT_FETCH_MIS = 10, kCounterSlots = 16 };
+                   CNT_FETCH_EXT = 8, CNT_FETCH_SH = 9, CNT_FETCH_MIS = 10, CNT_CLS0 = 16, kCounterSlots = 32 };
 
 // ------------------------------------------------------------ batched mode
 //
@@ -88,6 +90,7 @@ struct BatchCtl {
   int error;                     // 1: iteration cap reached
   unsigned long long rays[3];    // ext, shadow, mis
   unsigned long long paths_done;
+  int more;                      // host-driven loop: 1 while another iteration is needed
 };
 
 struct BatchView {
@@ -168,6 +171,11 @@ cudaError_t configure_batch_kernels(int smem_bytes, KernelLimits* lim);
 cudaError_t capture_batch_iteration(const WaveView& w, const BatchView& b, const uint32_t* sobol,
                                     const uint32_t* sobol_bitmajor, const LaunchConfig& cfg,
                                     cudaGraphConditionalHandle cond, cudaStream_t stream, cudaGraph_t body);
+// The same iteration launched directly (a host-driven loop reading ctl->more),
+// each stage timed by `timer`: the profiling path of the batched engine.
+void launch_batch_iteration(const WaveView& w, const BatchView& b, const uint32_t* sobol,
+                            const uint32_t* sobol_bitmajor, const LaunchConfig& cfg, cudaStream_t stream,
+                            StageTimer* timer);
 // Resets the batch control block and the free-slot list for `capacity` slots.
 void launch_batch_init(const WaveView& w, const BatchView& b, int capacity, cudaStream_t stream);
 

@@ -188,11 +188,26 @@ DevMaterial prepare_material(const orion_material& mt) {
       break;
     }
   }
+  unsigned kinds = 0;
   for (int i = 0; i < m.num_lobes; ++i) {
     int t = m.lobes[i].type;
     const int ns = BXDF_ALL & ~BXDF_SPECULAR;
     if ((t & ns) == t) ++m.num_nonspecular;
+    kinds |= 1u << m.lobes[i].kind;
   }
+  const unsigned spec = (1u << LOBE_SPECULAR_R) | (1u << LOBE_SPECULAR_T) | (1u << LOBE_FRESNEL_SPECULAR);
+  if (kinds == (1u << LOBE_LAMBERT_R))
+    m.shade_class = SC_DIFFUSE;
+  else if (kinds == (1u << LOBE_MICROFACET_R))
+    m.shade_class = SC_CONDUCTOR;
+  else if (kinds != 0 && (kinds & ~spec) == 0)
+    m.shade_class = SC_SPECULAR;
+  else if (kinds == ((1u << LOBE_MICROFACET_R) | (1u << LOBE_MICROFACET_T)))
+    m.shade_class = SC_DIELECTRIC;
+  else if (kinds == ((1u << LOBE_LAMBERT_R) | (1u << LOBE_MICROFACET_R)))
+    m.shade_class = SC_PLASTIC;
+  else
+    m.shade_class = SC_GENERAL;
   return m;
 }
 

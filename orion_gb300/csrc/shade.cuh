@@ -24,6 +24,36 @@ __device__ __forceinline__ void queue_append(int* counter, int* queue, int value
   queue[base + __popc(m & ((1u << lane) - 1u))] = value;
 }
 
+// Appends `value` to queue `cls` of `queues` (`stride` ints apart); the lanes
+// of a warp that append to the same queue share one atomicAdd.
+__device__ __forceinline__ void class_append(int* counters, int* queues, int stride, int cls, int value) {
+  const unsigned active = __activemask();
+  const unsigned peers = __match_any_sync(active, cls);
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(peers) - 1;
+  int base = 0;
+  if (lane == leader) base = atomicAdd(counters + cls, __popc(peers));
+  base = __shfl_sync(peers, base, leader);
+  queues[(size_t)cls * stride + base + __popc(peers & ((1u << lane) - 1u))] = value;
+}
+
+// The slot of entry q of the class queues taken in class order (q < total).
+struct ClassQueues {
+  int start[kShadeClasses + 1];
+  __device__ __forceinline__ void load(const int* counters) {
+    start[0] = 0;
+#pragma unroll
+    for (int c = 0; c < kShadeClasses; ++c) start[c + 1] = start[c] + counters[c];
+  }
+  __device__ __forceinline__ int total() const { return start[kShadeClasses]; }
+  __device__ __forceinline__ int slot(const int* queues, int stride, int q) const {
+    int c = 0;
+#pragma unroll
+    for (int k = 1; k < kShadeClasses; ++k) c += q >= start[k] ? 1 : 0;
+    return queues[(size_t)c * stride + (q - start[c])];
+  }
+};
+
 struct Hit {
   V3 p, ng, ns, su, sv;
 };
@@ -53,7 +83,7 @@ __device__ __forceinline__ V3 point_on(const PrimShade& sh, float u, float v) {
   return w * p0 + u * p1 + v * p2;
 }
 
-__device__ __forceinline__ TraceScene trace_scene(const SceneView& s) { return TraceScene{s.nodes, s.woop, s.tri_prim}; }
+__device__ __forceinline__ TraceScene trace_scene(const SceneView& s) { return TraceScene{s.nodes, s.woop, s.tri_prim, s.tri_class}; }
 
 // Pinhole::generateRay (src/camera/pinhole.cpp:8-33).
 // Sampler::next2() builds Point2f(next(), next()) (src/core/sampler.h:29); the
@@ -252,44 +282,24 @@ struct JobScene {
   __device__ __forceinline__ const SceneView& operator()(int pid) const { return jobs[job_of[pid]].scene; }
 };
 
-// Traces the rays of `n` queued path slots. ANY: occlusion within the ray's
-// tmax (origin.w), result in occluded[]; otherwise closest hit over
-// (0, FLT_MAX], result in hit[].
-template <bool ANY, int SMEM, class SceneOf>
-__device__ __forceinline__ void trace_list(const SceneOf& scene_of, const int* queue, int n, const float4* ray_o,
-                                           const float4* ray_d, float4* hit, int* occluded, int2* stack_smem) {
-  TraversalStack<SMEM> st;
-  st.smem = stack_smem + threadIdx.x;
-  st.stride = blockDim.x;
-  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
-    const int pid = queue[q];
-    const SceneView& s = scene_of(pid);
-    TraceScene ts{s.nodes, s.woop, s.tri_prim};
-    float4 o4 = ray_o[pid], d4 = ray_d[pid];
-    if (ANY) {
-      RayHit h = traverse<true, SMEM>(ts, xyz(o4), xyz(d4), 0.f, o4.w, st);
-      occluded[pid] = h.tri >= 0;
-    } else {
-      RayHit h = traverse<false, SMEM>(ts, xyz(o4), xyz(d4), 0.f, kFloatMax, st);
-      hit[pid] = make_float4(h.t, h.u, h.v, __int_as_float(h.tri));
-    }
-  }
-}
-
 // Persistent-warp tracing of `n` queued rays (see traverse.cuh): warps stay
 // in the kernel and refill idle lanes from the queue through `fetch`, a
 // counter that must be zero at launch. Block size must be a multiple of 32.
+// With `q_cls` (closest hit only), each finished ray's slot is also appended
+// to the queue of the shading class of what it hit (SC_MISS for a miss).
 template <bool ANY, int SMEM, class SceneOf>
 __device__ __forceinline__ void trace_persistent(const SceneOf& scene_of, const int* queue, int n, int* fetch,
                                                  const float4* ray_o, const float4* ray_d, float4* hit,
-                                                 int* occluded, int2* stack_smem, int refill_below) {
+                                                 int* occluded, int2* stack_smem, int refill_below,
+                                                 int* cls_counters = nullptr, int* q_cls = nullptr,
+                                                 int cls_stride = 0) {
   constexpr unsigned kFull = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   TraversalStack<SMEM> st;
   st.smem = stack_smem + threadIdx.x;
   st.stride = blockDim.x;
   LaneRay r;
-  TraceScene ts{nullptr, nullptr, nullptr};
+  TraceScene ts{nullptr, nullptr, nullptr, nullptr};
   int pid = -1;
   bool active = false, exhausted = false;
   while (true) {
@@ -306,10 +316,10 @@ __device__ __forceinline__ void trace_persistent(const SceneOf& scene_of, const 
         if (my < n) {
           pid = queue[my];
           const SceneView& s = scene_of(pid);
-          ts = TraceScene{s.nodes, s.woop, s.tri_prim};
+          ts = TraceScene{s.nodes, s.woop, s.tri_prim, s.tri_class};
           const float4 o4 = ray_o[pid], d4 = ray_d[pid];
           st.sp = 0;
-          lane_start(r, ts, o4, d4, ANY ? o4.w : kFloatMax);
+          lane_start(r, o4, d4, ANY ? o4.w : kFloatMax);
           active = true;
         }
       }
@@ -320,13 +330,15 @@ __device__ __forceinline__ void trace_persistent(const SceneOf& scene_of, const 
       continue;
     }
     if (active) {
-      lane_inner<SMEM>(r, ts, st);
-      bool found = lane_leaves<ANY, SMEM>(r, ts, st);
-      if (found || (r.na < 0 && r.lb == 0)) {
-        if (ANY)
+      if (lane_step<ANY, SMEM>(r, ts, st)) {
+        if (ANY) {
           occluded[pid] = r.tri >= 0;
-        else
+        } else {
           hit[pid] = make_float4(r.tri >= 0 ? r.tmax : kFloatMax, r.u, r.v, __int_as_float(r.tri));
+          if (q_cls)
+            class_append(cls_counters, q_cls, cls_stride, r.tri >= 0 ? (int)__ldg(ts.tri_class + r.tri) : SC_MISS,
+                         pid);
+        }
         active = false;
       }
     }

@@ -1,5 +1,5 @@
-// BVH traversal: closest hit and occlusion over the host-built BVH
-// (32-byte nodes with adjacent child pairs, Woop triangle records).
+// BVH traversal: closest hit and occlusion over the host-built 8-wide BVH
+// (80-byte nodes with quantised child boxes, Woop triangle records).
 //
 // Replaces rtcIntersect (src/core/kernel.cpp:111-125). Hit semantics match
 // the reference's use of Embree: accept tnear < t <= tfar, barycentrics
@@ -7,20 +7,21 @@
 //
 // The traversal stack is short and lives in shared memory, laid out
 // [entry][thread] so a warp's pushes hit 32 different banks; entries past the
-// shared part spill to a per-thread local array. Each entry is the (a, b)
-// pair of a postponed node, so popping needs no memory access.
+// shared part spill to a per-thread local array. Each entry is an 8-byte
+// node or triangle group, so popping needs no memory access.
 #pragma once
 #include "device_types.h"
 #include "dmath.cuh"
 
 namespace orion_gb300 {
 
-constexpr int kMaxStack = 64;  // >= BVH depth bound (the builder keeps depth < 64)
+constexpr int kMaxStack = 96;  // >= wide-tree depth (< 48) + postponed triangle groups (< 40) + 1
 
 struct TraceScene {
-  const float4* __restrict__ nodes;  // 2 float4 per node
+  const float4* __restrict__ nodes;  // 5 float4 per WideNode
   const float4* __restrict__ woop;   // 3 float4 per triangle, leaf order
   const int* __restrict__ tri_prim;  // leaf order -> primID
+  const uint8_t* __restrict__ tri_class;  // leaf order -> ShadeClass
 };
 
 struct RayHit {
@@ -84,6 +85,112 @@ __device__ __forceinline__ bool woop_hit(const float4* __restrict__ woop, int k,
   return true;
 }
 
+// ------------------------------------------------------- 8-wide traversal
+//
+// A node visit tests the ray against the eight quantised child boxes of one
+// WideNode (five 16-byte loads) and yields two groups:
+//   node group     (child_base, hits << 24 | imask): the hit internal
+//                  children, one bit per child at position slot ^ octant,
+//                  so taking the lowest bit first visits them roughly near
+//                  to far;
+//   triangle group (tri_base, mask): the triangles of the hit leaf children.
+// A stack entry is a node group (top byte non-zero) or a postponed triangle
+// group (top byte zero). The root is the single internal child of a virtual
+// group.
+
+constexpr int kPostponeLanes = 6;   // fewer lanes than this testing triangles: postpone them
+constexpr int kPostponeDepth = 40;  // postpone only while the stack is shallower than this
+
+// Octant of a ray from the signs of its reciprocal direction (never zero,
+// see safe_inv), so the near-plane choice agrees with the slab arithmetic
+// even for a -0 direction component.
+__device__ __forceinline__ uint32_t ray_octant(V3 idir) {
+  return (idir.x < 0.f ? 1u : 0u) | (idir.y < 0.f ? 2u : 0u) | (idir.z < 0.f ? 4u : 0u);
+}
+
+__device__ __forceinline__ uint2 root_group(uint32_t oct) { return make_uint2(0u, (1u << (24 + oct)) | 1u); }
+
+// Byte `b` of `w` as a float: the byte is placed in the mantissa of 2^23 with
+// one byte permute, and 2^23 subtracted (exact).
+__device__ __forceinline__ float q8(uint32_t w, int b) {
+  return __uint_as_float(__byte_perm(w, 0x4b000000u, 0x7440u + (uint32_t)b)) - 8388608.f;
+}
+
+__device__ __forceinline__ float max3f(float a, float b, float c) {
+  float d;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+  return d;
+}
+
+__device__ __forceinline__ float min3f(float a, float b, float c) {
+  float d;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+  return d;
+}
+
+// Moves bit s of an 8-bit mask to bit s ^ oct.
+__device__ __forceinline__ uint32_t octant_permute(uint32_t x, uint32_t oct) {
+  if (oct & 1u) x = ((x & 0x55u) << 1) | ((x >> 1) & 0x55u);
+  if (oct & 2u) x = ((x & 0x33u) << 2) | ((x >> 2) & 0x33u);
+  if (oct & 4u) x = ((x & 0x0fu) << 4) | ((x >> 4) & 0x0fu);
+  return x;
+}
+
+__device__ __forceinline__ void wide_node(const float4* __restrict__ nodes, int idx, V3 o, V3 idir, uint32_t oct,
+                                          float tnear, float tmax, uint2& ng, uint2& tg) {
+  const float4* n = nodes + 5 * (size_t)idx;
+  const float4 n0 = __ldg(n), n1 = __ldg(n + 1), n2 = __ldg(n + 2), n3 = __ldg(n + 3), n4 = __ldg(n + 4);
+  const uint32_t ew = __float_as_uint(n0.w);
+  const float sx = __uint_as_float((ew & 0xffu) << 23) * idir.x;
+  const float sy = __uint_as_float(((ew >> 8) & 0xffu) << 23) * idir.y;
+  const float sz = __uint_as_float(((ew >> 16) & 0xffu) << 23) * idir.z;
+  const uint32_t imask = ew >> 24;
+  const float ox = (n0.x - o.x) * idir.x, oy = (n0.y - o.y) * idir.y, oz = (n0.z - o.z) * idir.z;
+  // Quantised bounds: lo x = (n2.x, n2.y), lo y = (n2.z, n2.w), lo z = (n3.x, n3.y),
+  // hi x = (n3.z, n3.w), hi y = (n4.x, n4.y), hi z = (n4.z, n4.w); the near plane
+  // along a negative direction is the upper bound.
+  const uint32_t lx0 = __float_as_uint(n2.x), lx1 = __float_as_uint(n2.y);
+  const uint32_t ly0 = __float_as_uint(n2.z), ly1 = __float_as_uint(n2.w);
+  const uint32_t lz0 = __float_as_uint(n3.x), lz1 = __float_as_uint(n3.y);
+  const uint32_t hx0 = __float_as_uint(n3.z), hx1 = __float_as_uint(n3.w);
+  const uint32_t hy0 = __float_as_uint(n4.x), hy1 = __float_as_uint(n4.y);
+  const uint32_t hz0 = __float_as_uint(n4.z), hz1 = __float_as_uint(n4.w);
+  const bool fx = oct & 1u, fy = oct & 2u, fz = oct & 4u;
+  const uint32_t nx[2] = {fx ? hx0 : lx0, fx ? hx1 : lx1}, xf[2] = {fx ? lx0 : hx0, fx ? lx1 : hx1};
+  const uint32_t ny[2] = {fy ? hy0 : ly0, fy ? hy1 : ly1}, yf[2] = {fy ? ly0 : hy0, fy ? ly1 : hy1};
+  const uint32_t nz[2] = {fz ? hz0 : lz0, fz ? hz1 : lz1}, zf[2] = {fz ? lz0 : hz0, fz ? lz1 : hz1};
+  uint32_t hm = 0u;  // bit s: box of slot s hit (empty slots have inverted boxes)
+#pragma unroll
+  for (int s = 0; s < 8; ++s) {
+    const int h = s >> 2, b = s & 3;
+    const float tn = max3f(fmaf(q8(nx[h], b), sx, ox), fmaf(q8(ny[h], b), sy, oy),
+                           fmaxf(fmaf(q8(nz[h], b), sz, oz), tnear));
+    const float tf = min3f(fmaf(q8(xf[h], b), sx, ox), fmaf(q8(yf[h], b), sy, oy),
+                           fminf(fmaf(q8(zf[h], b), sz, oz), tmax));
+    hm |= (tn <= tf ? 1u : 0u) << s;
+  }
+  const uint32_t hits = octant_permute(hm & imask, oct);
+  uint32_t tris = 0u;
+  const uint32_t meta[2] = {__float_as_uint(n1.z), __float_as_uint(n1.w)};
+  for (uint32_t lh = hm & ~imask; lh; lh &= lh - 1u) {
+    const uint32_t s = (uint32_t)__ffs(lh) - 1u;
+    const uint32_t m = (meta[s >> 2] >> (8u * (s & 3u))) & 0xffu;
+    tris |= ((1u << (m >> 5)) - 1u) << (m & 31u);
+  }
+  ng = make_uint2(__float_as_uint(n1.x), hits ? (hits << 24) | imask : 0u);
+  tg = make_uint2(__float_as_uint(n1.y), tris);
+}
+
+// Takes the nearest-first remaining child of a node group; returns its node index.
+__device__ __forceinline__ int take_child(uint2& ng, uint32_t oct) {
+  const uint32_t k = (uint32_t)__ffs(ng.y >> 24) - 1u;
+  ng.y &= ~(1u << (24 + k));
+  const uint32_t slot = k ^ oct;
+  const int child = (int)ng.x + __popc((ng.y & 0xffu) & ((1u << slot) - 1u));
+  if (ng.y <= 0x00ffffffu) ng.y = 0u;
+  return child;
+}
+
 // ANY = false: closest hit over (tnear, tfar]. ANY = true: first hit found.
 template <bool ANY, int SMEM>
 __device__ __forceinline__ RayHit traverse(const TraceScene& s, V3 o, V3 d, float tnear, float tfar,
@@ -92,200 +199,129 @@ __device__ __forceinline__ RayHit traverse(const TraceScene& s, V3 o, V3 d, floa
   h.t = tfar;
   h.u = h.v = 0.f;
   h.tri = -1;
-  V3 idir = V3{safe_inv(d.x), safe_inv(d.y), safe_inv(d.z)};
-  V3 oid = V3{o.x * idir.x, o.y * idir.y, o.z * idir.z};
-  st.sp = 0;
-  float4 rlo = __ldg(s.nodes), rhi = __ldg(s.nodes + 1);
-  if (!(box_entry(rlo, rhi, idir, oid, tnear, tfar) < __int_as_float(0x7f800000))) return h;
-  int a = __float_as_int(rlo.w), b = __float_as_int(rhi.w);
+  const V3 idir = V3{safe_inv(d.x), safe_inv(d.y), safe_inv(d.z)};
+  const uint32_t oct = ray_octant(idir);
   int best_prim = 0x7fffffff;
+  st.sp = 0;
+  uint2 ng = root_group(oct), tg = make_uint2(0u, 0u);
   while (true) {
-    if (b == 0) {
-      float4 l0 = __ldg(s.nodes + 2 * a), h0 = __ldg(s.nodes + 2 * a + 1);
-      float4 l1 = __ldg(s.nodes + 2 * a + 2), h1 = __ldg(s.nodes + 2 * a + 3);
-      float t0 = box_entry(l0, h0, idir, oid, tnear, h.t);
-      float t1 = box_entry(l1, h1, idir, oid, tnear, h.t);
-      bool hit0 = t0 < __int_as_float(0x7f800000), hit1 = t1 < __int_as_float(0x7f800000);
-      if (hit0 && hit1) {
-        int2 n0 = make_int2(__float_as_int(l0.w), __float_as_int(h0.w));
-        int2 n1 = make_int2(__float_as_int(l1.w), __float_as_int(h1.w));
-        if (t1 < t0) {
-          int2 tmp = n0;
-          n0 = n1;
-          n1 = tmp;
-        }
-        st.push(n1);
-        a = n0.x;
-        b = n0.y;
-        continue;
-      }
-      if (hit0) {
-        a = __float_as_int(l0.w);
-        b = __float_as_int(h0.w);
-        continue;
-      }
-      if (hit1) {
-        a = __float_as_int(l1.w);
-        b = __float_as_int(h1.w);
-        continue;
-      }
+    if (ng.y > 0x00ffffffu) {
+      const int child = take_child(ng, oct);
+      if (ng.y) st.push(make_int2((int)ng.x, (int)ng.y));
+      wide_node(s.nodes, child, o, idir, oct, tnear, h.t, ng, tg);
     } else {
-      for (int k = a; k < a + b; ++k) {
-        float t, u, v;
-        if (woop_hit(s.woop, k, o, d, tnear, h.t, &t, &u, &v)) {
-          if (ANY) {
-            h.t = t;
-            h.u = u;
-            h.v = v;
-            h.tri = k;
-            return h;
-          }
-          int prim = __ldg(s.tri_prim + k);
-          if (t < h.t || h.tri < 0 || prim < best_prim) {
-            h.t = t;
-            h.u = u;
-            h.v = v;
-            h.tri = k;
-            best_prim = prim;
-          }
+      tg = ng;
+      ng = make_uint2(0u, 0u);
+    }
+    while (tg.y != 0u) {
+      const int k = (int)tg.x + __ffs(tg.y) - 1;
+      tg.y &= tg.y - 1u;
+      float t, u, v;
+      if (woop_hit(s.woop, k, o, d, tnear, h.t, &t, &u, &v)) {
+        if (ANY) {
+          h.t = t;
+          h.u = u;
+          h.v = v;
+          h.tri = k;
+          return h;
+        }
+        const int prim = __ldg(s.tri_prim + k);
+        if (t < h.t || h.tri < 0 || prim < best_prim) {
+          h.t = t;
+          h.u = u;
+          h.v = v;
+          h.tri = k;
+          best_prim = prim;
         }
       }
     }
-    if (st.sp == 0) break;
-    int2 e = st.pop();
-    a = e.x;
-    b = e.y;
+    if (ng.y == 0u) {
+      if (st.sp == 0) break;
+      const int2 e = st.pop();
+      ng = make_uint2((uint32_t)e.x, (uint32_t)e.y);
+    }
   }
   return h;
 }
 
 // ------------------------------------------------ persistent warp traversal
 //
-// The kernels below trace a queue of rays with warps that stay resident:
-//  * while-while: each lane walks inner nodes until every active lane of the
-//    warp has found a leaf (the first leaf a lane finds is postponed and the
-//    lane keeps traversing), then all lanes test triangles together, so the
-//    two phases do not interleave within a warp;
-//  * dynamic fetch: when fewer than `refill_below` lanes still hold a ray,
-//    the warp takes new rays for its idle lanes from the queue with one
-//    atomicAdd, instead of idling until its slowest ray ends.
-// Warp votes only steer scheduling; each ray's result does not depend on them.
+// The kernels below trace a queue of rays with warps that stay resident.
+// Each loop iteration visits one node per lane and then tests the triangles
+// it yielded; when fewer than kPostponeLanes lanes of the warp have triangles
+// to test, they push the triangle group and keep descending instead, so the
+// warp's lanes stay busy with node visits together. When fewer than
+// `refill_below` lanes still hold a ray, the warp takes new rays for its idle
+// lanes from the queue with one atomicAdd. Warp votes only steer scheduling;
+// each ray's result does not depend on them.
 
 struct LaneRay {
-  V3 o, d, idir, oid;
+  V3 o, d, idir;
   float tnear, tmax;  // tmax shrinks to the closest hit found so far
   float u, v;
   int tri, best_prim;
-  int na, nb;  // node to visit: (a, b) fields; na < 0 when the stack is empty
-  int la, lb;  // postponed leaf, lb == 0 when none
+  uint32_t oct;
+  uint2 ng, tg;
 };
 
-__device__ __forceinline__ void lane_start(LaneRay& r, const TraceScene& s, float4 o4, float4 d4, float tmax) {
+__device__ __forceinline__ void lane_start(LaneRay& r, float4 o4, float4 d4, float tmax) {
   r.o = xyz(o4);
   r.d = xyz(d4);
   r.idir = V3{safe_inv(r.d.x), safe_inv(r.d.y), safe_inv(r.d.z)};
-  r.oid = V3{r.o.x * r.idir.x, r.o.y * r.idir.y, r.o.z * r.idir.z};
+  r.oct = ray_octant(r.idir);
   r.tnear = 0.f;
   r.tmax = tmax;
   r.u = r.v = 0.f;
   r.tri = -1;
   r.best_prim = 0x7fffffff;
-  r.lb = 0;
-  r.la = 0;
-  float4 lo = __ldg(s.nodes), hi = __ldg(s.nodes + 1);
-  if (box_entry(lo, hi, r.idir, r.oid, r.tnear, r.tmax) < __int_as_float(0x7f800000)) {
-    r.na = __float_as_int(lo.w);
-    r.nb = __float_as_int(hi.w);
-  } else {
-    r.na = -1;
-    r.nb = 0;
-  }
+  r.ng = root_group(r.oct);
+  r.tg = make_uint2(0u, 0u);
 }
 
-template <int SMEM>
-__device__ __forceinline__ void lane_pop(LaneRay& r, TraversalStack<SMEM>& st) {
-  if (st.sp == 0) {
-    r.na = -1;
-    r.nb = 0;
-  } else {
-    int2 e = st.pop();
-    r.na = e.x;
-    r.nb = e.y;
-  }
-}
-
-// Inner nodes until this lane holds a postponed leaf and every active lane
-// in the warp does too (or has no inner node left).
-template <int SMEM>
-__device__ __forceinline__ void lane_inner(LaneRay& r, const TraceScene& s, TraversalStack<SMEM>& st) {
-  while (r.na >= 0 && r.nb == 0) {
-    const int a = r.na;
-    float4 l0 = __ldg(s.nodes + 2 * a), h0 = __ldg(s.nodes + 2 * a + 1);
-    float4 l1 = __ldg(s.nodes + 2 * a + 2), h1 = __ldg(s.nodes + 2 * a + 3);
-    float t0 = box_entry(l0, h0, r.idir, r.oid, r.tnear, r.tmax);
-    float t1 = box_entry(l1, h1, r.idir, r.oid, r.tnear, r.tmax);
-    bool hit0 = t0 < __int_as_float(0x7f800000), hit1 = t1 < __int_as_float(0x7f800000);
-    if (hit0 && hit1) {
-      int2 n0 = make_int2(__float_as_int(l0.w), __float_as_int(h0.w));
-      int2 n1 = make_int2(__float_as_int(l1.w), __float_as_int(h1.w));
-      if (t1 < t0) {
-        int2 tmp = n0;
-        n0 = n1;
-        n1 = tmp;
-      }
-      st.push(n1);
-      r.na = n0.x;
-      r.nb = n0.y;
-    } else if (hit0) {
-      r.na = __float_as_int(l0.w);
-      r.nb = __float_as_int(h0.w);
-    } else if (hit1) {
-      r.na = __float_as_int(l1.w);
-      r.nb = __float_as_int(h1.w);
-    } else {
-      lane_pop(r, st);
-    }
-    if (r.nb > 0 && r.lb == 0) {  // first leaf: postpone it, keep traversing
-      r.la = r.na;
-      r.lb = r.nb;
-      lane_pop(r, st);
-    }
-    if (!__any_sync(__activemask(), r.lb == 0)) break;
-  }
-}
-
-// Triangles of the postponed leaf, then of any leaves the lane is standing on.
-// Returns true when an occlusion query found its hit (ANY).
+// One node visit and its triangles. Returns true when the lane's ray is done:
+// its stack ran empty, or (ANY) a hit was found.
 template <bool ANY, int SMEM>
-__device__ __forceinline__ bool lane_leaves(LaneRay& r, const TraceScene& s, TraversalStack<SMEM>& st) {
-  while (r.lb > 0) {
-    for (int k = r.la; k < r.la + r.lb; ++k) {
-      float t, u, v;
-      if (woop_hit(s.woop, k, r.o, r.d, r.tnear, r.tmax, &t, &u, &v)) {
-        if (ANY) {
-          r.tmax = t;
-          r.tri = k;
-          return true;
-        }
-        int prim = __ldg(s.tri_prim + k);
-        if (t < r.tmax || r.tri < 0 || prim < r.best_prim) {
-          r.tmax = t;
-          r.u = u;
-          r.v = v;
-          r.tri = k;
-          r.best_prim = prim;
-        }
+__device__ __forceinline__ bool lane_step(LaneRay& r, const TraceScene& s, TraversalStack<SMEM>& st) {
+  if (r.ng.y > 0x00ffffffu) {
+    const int child = take_child(r.ng, r.oct);
+    if (r.ng.y) st.push(make_int2((int)r.ng.x, (int)r.ng.y));
+    wide_node(s.nodes, child, r.o, r.idir, r.oct, r.tnear, r.tmax, r.ng, r.tg);
+  } else {
+    r.tg = r.ng;
+    r.ng = make_uint2(0u, 0u);
+  }
+  while (r.tg.y != 0u) {
+    if (r.ng.y != 0u && st.sp < kPostponeDepth && __popc(__activemask()) < kPostponeLanes) {
+      st.push(make_int2((int)r.tg.x, (int)r.tg.y));
+      r.tg.y = 0u;
+      break;
+    }
+    const int k = (int)r.tg.x + __ffs(r.tg.y) - 1;
+    r.tg.y &= r.tg.y - 1u;
+    float t, u, v;
+    if (woop_hit(s.woop, k, r.o, r.d, r.tnear, r.tmax, &t, &u, &v)) {
+      if (ANY) {
+        r.tmax = t;
+        r.tri = k;
+        return true;
+      }
+      const int prim = __ldg(s.tri_prim + k);
+      if (t < r.tmax || r.tri < 0 || prim < r.best_prim) {
+        r.tmax = t;
+        r.u = u;
+        r.v = v;
+        r.tri = k;
+        r.best_prim = prim;
       }
     }
-    if (r.na >= 0 && r.nb > 0) {
-      r.la = r.na;
-      r.lb = r.nb;
-      lane_pop(r, st);
-    } else {
-      r.lb = 0;
-    }
+  }
+  if (r.ng.y == 0u) {
+    if (st.sp == 0) return true;
+    const int2 e = st.pop();
+    r.ng = make_uint2((uint32_t)e.x, (uint32_t)e.y);
   }
   return false;
 }
+
 
 }  // namespace orion_gb300

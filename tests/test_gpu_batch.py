@@ -80,8 +80,8 @@ def test_small_pool_forces_regeneration(ctx, scenes):
 def test_config_limits_and_large_stacks(ctx, scenes):
     import orion_gb300 as og
     cfg = ctx.get_config()
-    with pytest.raises(og.OrionError, match="shared memory"):
-        ctx.set_config(trace_block=1024, smem_stack=32)  # 256 KB of stack per block
+    with pytest.raises(og.OrionError, match="shared memory|trace_block"):
+        ctx.set_config(trace_block=1024, smem_stack=32)  # 256 KB of stack per block (or too many threads)
     with pytest.raises(og.OrionError, match="trace_block"):
         ctx.set_config(trace_block=100)
     assert ctx.get_config() == cfg
@@ -113,3 +113,17 @@ def test_batch_autotuner(ctx, scenes):
         assert np.array_equal(c1, c2)
         assert np.allclose(a, b, rtol=1e-5, atol=1e-9)
     print(f"batch autotuner: {best}, {mpaths:.1f} Mpaths/s")
+
+
+def test_profiled_batch_matches_graph_batch(ctx, scenes):
+    ref, _ = ctx.render_batch([_job(s) for s in scenes])
+    ctx.set_profiling(True)
+    try:
+        outs, st = ctx.render_batch([_job(s) for s in scenes])
+        stages = ctx.stage_times()
+    finally:
+        ctx.set_profiling(False)
+    for (a, q1, c1), (b, q2, c2) in zip(outs, ref):
+        assert np.array_equal(c1, c2)
+        assert _close(a, b) and _close(q1, q2)
+    assert stages["shade"]["launches"] == st["iterations"] and stages["trace_ext"]["ms"] > 0
