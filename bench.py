@@ -188,7 +188,8 @@ def run_ours(args) -> dict:
             torch.cuda.synchronize()
             dist.barrier()
 
-    first = rank * spp  # replicas render disjoint sample passes
+    from orion_gb300 import replicas
+    first, _ = replicas.pass_range(rank, world, spp)  # replicas render disjoint sample passes
     for _ in range(args.warmup):
         ctx.render(sid, W, H, spp=spp, first_pass=first)
 
@@ -244,8 +245,10 @@ def run_ours(args) -> dict:
     achieved = alg_bytes / (stages[top]["ms"] * 1e-3) / 1e9
     traffic = None
     prof_json = os.path.join(ROOT, "profiles", f"{top}_{args.workload}.json")
-    if os.path.exists(prof_json):
-        traffic = json.load(open(prof_json)).get("dram_bytes_per_launch")
+    if os.path.exists(prof_json):  # ncu DRAM bytes per unit, scaled to this run's average launch
+        bpu = json.load(open(prof_json)).get("dram_bytes_per_unit")
+        if bpu and stages[top]["launches"]:
+            traffic = int(bpu * units[top] / stages[top]["launches"])
     roofline = {"bound": "hbm", "kernel": top, "achieved": round(achieved, 2), "peak": peaks["hbm_gbs"],
                 "unit": "GB/s", "frac": round(achieved / peaks["hbm_gbs"], 5), "traffic": traffic,
                 "peak_source": peaks["source"],

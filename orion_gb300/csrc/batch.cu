@@ -115,18 +115,20 @@ __global__ void __launch_bounds__(512, 2) k_b_trace(WaveView w, BatchView b, int
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&c.rays[kind], (unsigned long long)n);
 }
 
+// Shading of the slots whose extension ray hit a material of class SC (or
+// missed, SC_MISS), each against its job's scene.
+template <int SC>
 __global__ void k_b_shade(WaveView w, BatchView b, const uint32_t* sobol_bitmajor) {
   BatchCtl& c = *b.ctl;
   const int cur = c.cur;
-  ClassQueues cq;
-  cq.load(&c.counters[CNT_CLS0]);
-  const int n = cq.total();
+  const int n = c.counters[CNT_CLS0 + SC];
+  const int* in_q = w.q_cls + (size_t)SC * w.capacity;
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
-    const int pid = cq.slot(w.q_cls, w.capacity, q);
+    const int pid = in_q[q];
     const DevJob& J = b.jobs[b.job_of[pid]];
     const int bounce = b.bounce_of[pid];
-    ShadeResult r = shade_one(J.scene, w, sobol_bitmajor, pid, (uint64_t)b.index_of[pid], bounce, J.max_depth,
-                              J.rr_depth);
+    ShadeResult r = shade_one<lobes_of_class(SC)>(J.scene, w, sobol_bitmajor, pid, (uint64_t)b.index_of[pid], bounce,
+                                                  J.max_depth, J.rr_depth);
     if (r.alive) b.bounce_of[pid] = bounce + 1;
     queue_append(&c.counters[CNT_NEE], w.q_nee, pid, r.did_nee);
     queue_append(&c.counters[CNT_SH], w.q_sh, pid, r.want_sh);
@@ -223,7 +225,11 @@ int grid_cap(int64_t n, int block, int cap) {
 cudaError_t configure_batch_kernels(int smem_bytes, KernelLimits* lim) {
   const void* trace[] = {(const void*)k_b_trace<0>, (const void*)k_b_trace<8>, (const void*)k_b_trace<16>,
                          (const void*)k_b_trace<24>, (const void*)k_b_trace<32>};
-  const void* shade[] = {(const void*)k_b_shade, (const void*)k_b_resolve, (const void*)k_b_retire};
+  const void* shade[] = {(const void*)k_b_shade<SC_DIFFUSE>,    (const void*)k_b_shade<SC_CONDUCTOR>,
+                         (const void*)k_b_shade<SC_SPECULAR>,   (const void*)k_b_shade<SC_DIELECTRIC>,
+                         (const void*)k_b_shade<SC_PLASTIC>,    (const void*)k_b_shade<SC_GENERAL>,
+                         (const void*)k_b_shade<SC_MISS>,       (const void*)k_b_resolve,
+                         (const void*)k_b_retire};
   for (const void* f : trace) {
     cudaError_t e = batch_limit_of(f, smem_bytes, &lim->max_trace_block);
     if (e != cudaSuccess) return e;
@@ -263,7 +269,13 @@ void enqueue_iteration(const WaveView& w, const BatchView& b, const uint32_t* so
   b_trace(cfg, w, b, 0, tgrid, stream);
   end();
   begin(ST_SHADE);
-  k_b_shade<<<sgrid, cfg.shade_block, 0, stream>>>(w, b, sobol_bitmajor);
+  k_b_shade<SC_DIFFUSE><<<sgrid, cfg.shade_block, 0, stream>>>(w, b, sobol_bitmajor);
+  k_b_shade<SC_CONDUCTOR><<<sgrid, cfg.shade_block, 0, stream>>>(w, b, sobol_bitmajor);
+  k_b_shade<SC_SPECULAR><<<sgrid, cfg.shade_block, 0, stream>>>(w, b, sobol_bitmajor);
+  k_b_shade<SC_DIELECTRIC><<<sgrid, cfg.shade_block, 0, stream>>>(w, b, sobol_bitmajor);
+  k_b_shade<SC_PLASTIC><<<sgrid, cfg.shade_block, 0, stream>>>(w, b, sobol_bitmajor);
+  k_b_shade<SC_GENERAL><<<sgrid, cfg.shade_block, 0, stream>>>(w, b, sobol_bitmajor);
+  k_b_shade<SC_MISS><<<sgrid, cfg.shade_block, 0, stream>>>(w, b, sobol_bitmajor);
   end();
   begin(ST_TRACE_SHADOW);
   b_trace(cfg, w, b, 1, tgrid, stream);

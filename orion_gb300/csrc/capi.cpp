@@ -33,8 +33,28 @@ struct orion_host_scene {
   // later uploads of the same scene (resident-scene serving, re-uploads).
   std::unique_ptr<BvhBuild> bvh;
   std::unique_ptr<PreparedScene> prep;
+  std::vector<uint8_t> tri_class;  // leaf order -> shading class
+  unsigned class_mask = 0;
+  // The upload arrays above are page-locked once (portable across contexts)
+  // so every upload copies at DMA speed; unlocked when the scene is freed.
+  std::vector<void*> pinned;
   std::mutex mu;
+  ~orion_host_scene() {
+    for (void* p : pinned) cudaHostUnregister(p);
+  }
 };
+
+namespace {
+template <class T>
+void pin(orion_host_scene* h, const std::vector<T>& v) {
+  if (v.empty()) return;
+  void* p = const_cast<T*>(v.data());
+  if (cudaHostRegister(p, v.size() * sizeof(T), cudaHostRegisterPortable) == cudaSuccess)
+    h->pinned.push_back(p);
+  else
+    cudaGetLastError();  // stays pageable: copies are slower, results the same
+}
+}  // namespace
 
 namespace {
 
@@ -90,6 +110,7 @@ struct DeviceScene {
   int64_t num_prims = 0;
   int width = 0, height = 0, spp = 1, max_depth = 5;
   int bvh_depth = 0;
+  unsigned class_mask = 1u << SC_MISS;  // shading classes of the scene's triangles, and misses
 };
 
 struct Wave {
@@ -340,7 +361,18 @@ extern "C" int orion_gpu_scene_upload(orion_gpu_ctx* ctx, const orion_host_scene
       bo.max_leaf = 3;
       build_bvh(hs.positions.data(), hs.num_prims(), bo, b.get());
       if (b->depth >= 48) return fail(ORION_ERR_UNSUPPORTED, "BVH deeper than the traversal stack bound");
+      hsm->tri_class.resize(b->tri_prim.size());
+      hsm->class_mask = 1u << SC_MISS;
+      for (size_t i = 0; i < hsm->tri_class.size(); ++i) {
+        hsm->tri_class[i] = (uint8_t)hsm->prep->mats[hsm->prep->prims[b->tri_prim[i]].material].shade_class;
+        hsm->class_mask |= 1u << hsm->tri_class[i];
+      }
       hsm->bvh = std::move(b);
+      pin(hsm, hsm->bvh->wide);
+      pin(hsm, hsm->bvh->woop);
+      pin(hsm, hsm->bvh->tri_prim);
+      pin(hsm, hsm->tri_class);
+      pin(hsm, hsm->prep->prims);
     }
   }
   const PreparedScene& ps = *hsm->prep;
@@ -351,10 +383,8 @@ extern "C" int orion_gpu_scene_upload(orion_gpu_ctx* ctx, const orion_host_scene
   if ((rc = upload(d->nodes, bvh.wide, ctx->stream, &bytes)) != ORION_OK) return rc;
   if ((rc = upload(d->woop, bvh.woop, ctx->stream, &bytes)) != ORION_OK) return rc;
   if ((rc = upload(d->tri_prim, bvh.tri_prim, ctx->stream, &bytes)) != ORION_OK) return rc;
-  std::vector<uint8_t> tri_class(bvh.tri_prim.size());
-  for (size_t i = 0; i < tri_class.size(); ++i)
-    tri_class[i] = (uint8_t)ps.mats[ps.prims[bvh.tri_prim[i]].material].shade_class;
-  if ((rc = upload(d->tri_class, tri_class, ctx->stream, &bytes)) != ORION_OK) return rc;
+  d->class_mask = hsm->class_mask;
+  if ((rc = upload(d->tri_class, hsm->tri_class, ctx->stream, &bytes)) != ORION_OK) return rc;
   if ((rc = upload(d->prims, ps.prims, ctx->stream, &bytes)) != ORION_OK) return rc;
   if ((rc = upload(d->mats, ps.mats, ctx->stream, &bytes)) != ORION_OK) return rc;
   if ((rc = upload(d->lights, ps.lights, ctx->stream, &bytes)) != ORION_OK) return rc;
@@ -470,6 +500,7 @@ static int render_impl(orion_gpu_ctx* ctx, orion_scene_id id, const orion_render
     a.height = d.height;
     a.max_depth = max_depth;
     a.rr_depth = rr_depth;
+    a.class_mask = d.class_mask;
     launch_wave(d.view, ctx->wave.view, a, film, ctx->cfg, s, &launches, ctx->profiling ? &timer : nullptr);
   }
   CUDA_TRY(cudaGetLastError());
@@ -672,7 +703,7 @@ static int run_batch_locked(orion_gpu_ctx* ctx, std::vector<DevJob>& dj, unsigne
   ctx->last.shadow_rays = (int64_t)out.rays[1];
   ctx->last.mis_rays = (int64_t)out.rays[2];
   ctx->last.rays = (int64_t)(out.rays[0] + out.rays[1] + out.rays[2]);
-  ctx->last.kernel_launches = 9LL * out.iterations + 1;
+  ctx->last.kernel_launches = 15LL * out.iterations + 1;  // plan, regen, 3 traces, 7 shades, resolve, retire, control
   ctx->last.device_ms = ms;
   if (out.error) return fail(ORION_ERR_DEVICE, "batch loop reached its iteration cap");
   if (out.paths_done != total)

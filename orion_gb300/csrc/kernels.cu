@@ -66,18 +66,18 @@ __global__ void __launch_bounds__(512, 2) k_trace_sh(SceneView s, const int* que
   if (stat && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(stat, (unsigned long long)n);
 }
 
-// One bounce for every path traced this bounce, taken class by class from
-// the shading-class queues the extension trace filled.
+// One bounce for every path whose extension ray hit a material of shading
+// class SC (or, for SC_MISS, left the scene), with that class's BSDF code only.
+template <int SC>
 __global__ void k_shade(SceneView s, WaveView w, WaveArgs a, int bounce, int cur) {
   int* out_q = w.q_ext[cur ^ 1];
   int* out_cnt = w.counters + (cur ^ 1);
-  ClassQueues cq;
-  cq.load(w.counters + CNT_CLS0);
-  const int n = cq.total();
+  const int n = w.counters[CNT_CLS0 + SC];
+  const int* in_q = w.q_cls + (size_t)SC * w.capacity;
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
-    const int pid = cq.slot(w.q_cls, w.capacity, q);
-    ShadeResult r = shade_one(s, w, a.sobol_bitmajor, pid, (uint64_t)(a.base_index + pid), bounce, a.max_depth,
-                              a.rr_depth);
+    const int pid = in_q[q];
+    ShadeResult r = shade_one<lobes_of_class(SC)>(s, w, a.sobol_bitmajor, pid, (uint64_t)(a.base_index + pid), bounce,
+                                                  a.max_depth, a.rr_depth);
     queue_append(w.counters + CNT_NEE, w.q_nee, pid, r.did_nee);
     queue_append(w.counters + CNT_SH, w.q_sh, pid, r.want_sh);
     queue_append(w.counters + CNT_MIS, w.q_mis, pid, r.want_mis);
@@ -297,7 +297,19 @@ void launch_wave(const SceneView& s, const WaveView& w, const WaveArgs& a, const
                    cfg, tgrid, stream);
     end();
     begin(ST_SHADE);
-    k_shade<<<sgrid, cfg.shade_block, 0, stream>>>(s, w, a, bounce, cur);
+    for (int sc = 0; sc < kShadeClasses; ++sc) {
+      if (!((a.class_mask >> sc) & 1u)) continue;
+      switch (sc) {
+        case SC_DIFFUSE: k_shade<SC_DIFFUSE><<<sgrid, cfg.shade_block, 0, stream>>>(s, w, a, bounce, cur); break;
+        case SC_CONDUCTOR: k_shade<SC_CONDUCTOR><<<sgrid, cfg.shade_block, 0, stream>>>(s, w, a, bounce, cur); break;
+        case SC_SPECULAR: k_shade<SC_SPECULAR><<<sgrid, cfg.shade_block, 0, stream>>>(s, w, a, bounce, cur); break;
+        case SC_DIELECTRIC: k_shade<SC_DIELECTRIC><<<sgrid, cfg.shade_block, 0, stream>>>(s, w, a, bounce, cur); break;
+        case SC_PLASTIC: k_shade<SC_PLASTIC><<<sgrid, cfg.shade_block, 0, stream>>>(s, w, a, bounce, cur); break;
+        case SC_GENERAL: k_shade<SC_GENERAL><<<sgrid, cfg.shade_block, 0, stream>>>(s, w, a, bounce, cur); break;
+        case SC_MISS: k_shade<SC_MISS><<<sgrid, cfg.shade_block, 0, stream>>>(s, w, a, bounce, cur); break;
+        default: break;
+      }
+    }
     end();
     if (bounce < a.max_depth) {
       begin(ST_TRACE_SHADOW);
@@ -357,7 +369,10 @@ cudaError_t configure_kernels(int smem_bytes, KernelLimits* lim) {
                          (const void*)k_trace<24>,    (const void*)k_trace<32>,    (const void*)k_trace_sh<0>,
                          (const void*)k_trace_sh<8>,  (const void*)k_trace_sh<16>, (const void*)k_trace_sh<24>,
                          (const void*)k_trace_sh<32>, (const void*)k_trace_rays<16>};
-  const void* shade[] = {(const void*)k_shade, (const void*)k_resolve};
+  const void* shade[] = {(const void*)k_shade<SC_DIFFUSE>, (const void*)k_shade<SC_CONDUCTOR>,
+                         (const void*)k_shade<SC_SPECULAR>, (const void*)k_shade<SC_DIELECTRIC>,
+                         (const void*)k_shade<SC_PLASTIC>, (const void*)k_shade<SC_GENERAL>,
+                         (const void*)k_shade<SC_MISS>, (const void*)k_resolve};
   for (const void* f : trace) {
     cudaError_t e = limit_of(f, smem_bytes, &lim->max_trace_block);
     if (e != cudaSuccess) return e;

@@ -111,6 +111,7 @@ struct WaveArgs {
   int width, height;
   int max_depth;
   int rr_depth;
+  unsigned class_mask;  // shading classes present in the scene (bit ShadeClass), SC_MISS always
 };
 
 struct FilmView {

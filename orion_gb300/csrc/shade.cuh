@@ -127,6 +127,20 @@ struct ShadeResult {
   bool alive, did_nee, want_sh, want_mis;
 };
 
+// Lobe kinds a shading class's materials can hold (see prepare_material).
+__host__ __device__ constexpr unsigned lobes_of_class(int sc) {
+  return sc == SC_DIFFUSE      ? (1u << LOBE_LAMBERT_R)
+         : sc == SC_CONDUCTOR  ? (1u << LOBE_MICROFACET_R)
+         : sc == SC_SPECULAR   ? ((1u << LOBE_SPECULAR_R) | (1u << LOBE_SPECULAR_T) | (1u << LOBE_FRESNEL_SPECULAR))
+         : sc == SC_DIELECTRIC ? ((1u << LOBE_MICROFACET_R) | (1u << LOBE_MICROFACET_T))
+         : sc == SC_PLASTIC    ? ((1u << LOBE_LAMBERT_R) | (1u << LOBE_MICROFACET_R))
+         : sc == SC_MISS       ? 0u
+                               : kLobeAll;
+}
+
+// One bounce of PathTracing::Li for the path in slot `pid`, whose material
+// (if it hit one) holds only lobe kinds in KM.
+template <unsigned KM = kLobeAll>
 __device__ __forceinline__ ShadeResult shade_one(const SceneView& s, const WaveView& w, const uint32_t* sobol_bitmajor,
                                                  int pid, uint64_t index, int bounce, int max_depth, int rr_depth) {
   LightDistrib distrib{s.light_func, s.light_cdf, s.light_func_int, s.num_lights};
@@ -182,8 +196,8 @@ __device__ __forceinline__ ShadeResult shade_one(const SceneView& s, const WaveV
           LightSample ls = sample_li(lt, s.prims, h.p, ul0, ul1, s.world_radius);
           V3 ld = V3{0, 0, 0};
           if (ls.pdf > 0.f && !is_black(ls.Li)) {
-            V3 f = bsdf_f(m, fr, ls.wi, wo, kNonSpecular) * absdot(ls.wi, h.ns);
-            float bpdf = bsdf_pdf(m, fr, ls.wi, wo, kNonSpecular);
+            V3 f = bsdf_f<KM>(m, fr, ls.wi, wo, kNonSpecular) * absdot(ls.wi, h.ns);
+            float bpdf = bsdf_pdf<KM>(m, fr, ls.wi, wo, kNonSpecular);
             if (!is_black(f)) {
               if (is_delta_light(lt.kind)) {
                 ld = sdiv(mul(f, ls.Li), ls.pdf);
@@ -205,7 +219,7 @@ __device__ __forceinline__ ShadeResult shade_one(const SceneView& s, const WaveV
           if (!is_delta_light(lt.kind)) {
             V3 wib;
             int st;
-            fb = bsdf_sample_f(m, fr, wo, ub0, ub1, kNonSpecular, &wib, &mis_pdf, &st);
+            fb = bsdf_sample_f<KM>(m, fr, wo, ub0, ub1, kNonSpecular, &wib, &mis_pdf, &st);
             fb = fb * absdot(wib, h.ns);
             if (!is_black(fb) && mis_pdf > 0.f) {
               bool ok = true;
@@ -242,7 +256,7 @@ __device__ __forceinline__ ShadeResult shade_one(const SceneView& s, const WaveV
       V3 wi;
       float pdf;
       int stype;
-      V3 f = bsdf_sample_f(m, fr, -rd, u0, u1, BXDF_ALL, &wi, &pdf, &stype);
+      V3 f = bsdf_sample_f<KM>(m, fr, -rd, u0, u1, BXDF_ALL, &wi, &pdf, &stype);
       if (is_black(f) || pdf == 0.f) {
         alive = false;
       } else {
