@@ -198,6 +198,13 @@ typedef struct orion_stage_times {
 int orion_gpu_set_profiling(orion_gpu_ctx* ctx, int32_t enable);
 int orion_gpu_stage_times(orion_gpu_ctx* ctx, orion_stage_times* out);
 
+/* ----------------------------------------------------------- film output */
+/* saveAsBmp (src/core/texture.cpp:77-136): the averaged film `rgb`
+ * (height x width x 3, row 0 at the top, as RenderTarget::getAveraged
+ * returns it) as a 32-bit BMP: rows bottom-up, bytes B, G, R, 255, each
+ * channel clamp(c, 0, 1) * 255 truncated (NaN -> 0), no tone mapping. */
+int orion_film_write_bmp(const char* path, int32_t width, int32_t height, const float* rgb);
+
 /* ------------------------------------------------------------- batches */
 /* Many render() calls in one launch. There is no single reference call for
  * this: it runs PathTracing::render (src/integrator/path.cpp:15-37) for every

@@ -149,6 +149,7 @@ def library() -> C.CDLL:
             "orion_gpu_last_stats": (i32, [vp, C.POINTER(RenderStats)]),
             "orion_gpu_set_profiling": (i32, [vp, i32]),
             "orion_gpu_stage_times": (i32, [vp, C.POINTER(StageTimes)]),
+            "orion_film_write_bmp": (i32, [C.c_char_p, i32, i32, vp]),
             "orion_gpu_render_batch": (i32, [vp, i32, vp, C.POINTER(BatchStats)]),
             "orion_gpu_get_config": (i32, [vp, C.POINTER(LaunchConfig)]),
             "orion_gpu_set_config": (i32, [vp, C.POINTER(LaunchConfig)]),
@@ -452,6 +453,15 @@ class RenderTarget:
     def getAveraged(self) -> np.ndarray:
         with np.errstate(invalid="ignore", divide="ignore"):
             return self.data / self.counter[..., None].astype(np.float32)
+
+
+def saveAsBmp(image: np.ndarray, path: str) -> None:
+    """saveAsBmp (src/core/texture.cpp:77-136) of an averaged (H, W, 3) film."""
+    img = np.ascontiguousarray(image, np.float32)
+    if img.ndim != 3 or img.shape[2] != 3:
+        raise ValueError("expected an (H, W, 3) image")
+    h, w = img.shape[:2]
+    _check(library().orion_film_write_bmp(os.fsencode(path), w, h, _ptr(img)))
 
 
 class CameraHandle:

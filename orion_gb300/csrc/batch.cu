@@ -80,14 +80,15 @@ __global__ void k_b_regen(WaveView w, BatchView b, const uint32_t* sobol) {
     PathSampler smp{sobol, (uint64_t)index, 5u};
     V3 o, d;
     camera_ray(J.scene.cam, smp, (int)(pix % J.width), (int)(pix / J.width), &o, &d);
-    w.ray_o[slot] = f4(o, 0.f);
-    w.ray_d[slot] = f4(d, 0.f);
-    w.beta[slot] = make_float4(1.f, 1.f, 1.f, 0.f);
-    w.L[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
-    w.dim[slot] = (int)smp.dim;
-    b.job_of[slot] = job;
-    b.bounce_of[slot] = 0;
-    b.index_of[slot] = index;
+    // The whole 96-byte record in one go: three full sectors at a scattered slot.
+    PathRec r;
+    r.o = f4(o, 0.f);
+    r.d = f4(d, 0.f);
+    r.beta = make_float4(1.f, 1.f, 1.f, 0.f);
+    r.L = make_float4(0.f, 0.f, 0.f, __uint_as_float((uint32_t)(unsigned long long)index));
+    r.hit = make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
+    r.meta = make_int4((int)smp.dim, job, 0, (int)((unsigned long long)index >> 32));
+    w.rec[slot] = r;
     queue_append(&c.counters[CNT_EXT0 + cur], w.q_ext[cur], slot, true);
   }
 }
@@ -97,7 +98,7 @@ template <int SMEM>
 __global__ void __launch_bounds__(512, 2) k_b_trace(WaveView w, BatchView b, int kind, int refill_below) {
   extern __shared__ int2 stack_smem[];
   BatchCtl& c = *b.ctl;
-  JobScene js{b.jobs, b.job_of};
+  JobScene js{b.jobs, w.job};
   int n;
   if (kind == 0) {
     n = c.counters[CNT_EXT0 + c.cur];
@@ -105,12 +106,12 @@ __global__ void __launch_bounds__(512, 2) k_b_trace(WaveView w, BatchView b, int
                                   nullptr, stack_smem, refill_below, &c.counters[CNT_CLS0], w.q_cls, w.capacity);
   } else if (kind == 1) {
     n = c.counters[CNT_SH];
-    trace_persistent<true, SMEM>(js, w.q_sh, n, &c.counters[CNT_FETCH_SH], w.sh_o, w.sh_d, nullptr, w.occluded,
-                                 stack_smem, refill_below);
+    trace_persistent<true, SMEM>(js, w.q_sh, n, &c.counters[CNT_FETCH_SH], w.sh_o, w.sh_d,
+                                 F4{nullptr}, w.occluded, stack_smem, refill_below);
   } else {
     n = c.counters[CNT_MIS];
-    trace_persistent<false, SMEM>(js, w.q_mis, n, &c.counters[CNT_FETCH_MIS], w.mis_o, w.mis_d, w.mis_hit, nullptr,
-                                  stack_smem, refill_below);
+    trace_persistent<false, SMEM>(js, w.q_mis, n, &c.counters[CNT_FETCH_MIS], w.mis_o, w.mis_d,
+                                  F4{w.mis_hit}, nullptr, stack_smem, refill_below);
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&c.rays[kind], (unsigned long long)n);
 }
@@ -118,18 +119,19 @@ __global__ void __launch_bounds__(512, 2) k_b_trace(WaveView w, BatchView b, int
 // Shading of the slots whose extension ray hit a material of class SC (or
 // missed, SC_MISS), each against its job's scene.
 template <int SC>
-__global__ void k_b_shade(WaveView w, BatchView b, const uint32_t* sobol_bitmajor) {
+__global__ void __launch_bounds__(128, 5) k_b_shade(WaveView w, BatchView b, const uint32_t* sobol_bitmajor) {
   BatchCtl& c = *b.ctl;
   const int cur = c.cur;
   const int n = c.counters[CNT_CLS0 + SC];
   const int* in_q = w.q_cls + (size_t)SC * w.capacity;
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
     const int pid = in_q[q];
-    const DevJob& J = b.jobs[b.job_of[pid]];
-    const int bounce = b.bounce_of[pid];
-    ShadeResult r = shade_one<lobes_of_class(SC)>(J.scene, w, sobol_bitmajor, pid, (uint64_t)b.index_of[pid], bounce,
-                                                  J.max_depth, J.rr_depth);
-    if (r.alive) b.bounce_of[pid] = bounce + 1;
+    const int4 meta = w.rec[pid].meta;
+    const DevJob& J = b.jobs[meta.y];
+    const int bounce = meta.z;
+    ShadeResult r = shade_one<lobes_of_class(SC)>(J.scene, w, sobol_bitmajor, pid, (uint64_t)slot_index(w, pid),
+                                                  bounce, J.max_depth, J.rr_depth);
+    if (r.alive) w.bounce[pid] = bounce + 1;
     queue_append(&c.counters[CNT_NEE], w.q_nee, pid, r.did_nee);
     queue_append(&c.counters[CNT_SH], w.q_sh, pid, r.want_sh);
     queue_append(&c.counters[CNT_MIS], w.q_mis, pid, r.want_mis);
@@ -142,7 +144,7 @@ __global__ void k_b_resolve(WaveView w, BatchView b) {
   const int n = b.ctl->counters[CNT_NEE];
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
     const int pid = w.q_nee[q];
-    resolve_one(b.jobs[b.job_of[pid]].scene, w, pid);
+    resolve_one(b.jobs[w.job[pid]].scene, w, pid);
   }
 }
 
@@ -151,9 +153,12 @@ __global__ void k_b_retire(WaveView w, BatchView b) {
   const int n = c.counters[CNT_RETIRE];
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
     const int pid = b.q_retire[q];
-    const DevJob& J = b.jobs[b.job_of[pid]];
-    const long long pix = b.index_of[pid] % ((long long)J.width * J.height);
     const float4 l = w.L[pid];
+    const int4 meta = w.rec[pid].meta;
+    const DevJob& J = b.jobs[meta.y];
+    const long long index =
+        (long long)(((unsigned long long)(unsigned)meta.w << 32) | (unsigned long long)__float_as_uint(l.w));
+    const long long pix = index % ((long long)J.width * J.height);
     atomicAdd(&J.sum[3 * pix], (double)l.x);
     atomicAdd(&J.sum[3 * pix + 1], (double)l.y);
     atomicAdd(&J.sum[3 * pix + 2], (double)l.z);
@@ -162,7 +167,7 @@ __global__ void k_b_retire(WaveView w, BatchView b) {
       atomicAdd(&J.sumsq[3 * pix + 1], (double)l.y * l.y);
       atomicAdd(&J.sumsq[3 * pix + 2], (double)l.z * l.z);
     }
-    atomicAdd(&J.count[pix], 1u);
+    if (J.count) atomicAdd(&J.count[pix], 1u);  // null: the caller knows every pixel gets spp samples
     queue_append(&c.counters[CNT_FREE], b.q_free, pid, true);
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&c.paths_done, (unsigned long long)n);

@@ -10,6 +10,7 @@
 #include <dlfcn.h>
 
 #include <algorithm>
+#include <cstddef>
 #include <cstdio>
 #include <cstring>
 #include <map>
@@ -141,7 +142,7 @@ struct orion_gpu_ctx {
   std::vector<int> prof_stage;
   orion_stage_times stage_times{};
   // batched mode
-  DevBuf b_job_of, b_bounce_of, b_index_of, b_retire, b_free, b_ctl, b_jobs, b_films;
+  DevBuf b_retire, b_free, b_ctl, b_jobs, b_films;
   int batch_slots_alloc = 0;
   int jobs_alloc = 0;
   int default_batch_slots = 1 << 22;
@@ -236,8 +237,10 @@ static int ensure_film(orion_gpu_ctx* c, int64_t pixels, bool fp64) {
 static int ensure_wave(orion_gpu_ctx* c, int capacity) {
   if (c->wave.capacity >= capacity) return ORION_OK;
   const size_t n = (size_t)capacity;
-  const size_t f4 = n * sizeof(float4), i4 = (n * sizeof(int) + 255) & ~(size_t)255;
-  const size_t bytes = 15 * f4 + (7 + kShadeClasses) * i4 + 256 + 4096;
+  auto round256 = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  const size_t recb = round256(n * sizeof(PathRec)), neeb = round256(n * sizeof(NeeRec));
+  const size_t f4 = round256(n * sizeof(float4)), i4 = round256(n * sizeof(int));
+  const size_t bytes = recb + neeb + f4 + (6 + kShadeClasses) * i4 + 256 + 4096;
   int rc = c->wave.block.alloc(bytes);
   if (rc != ORION_OK) {
     c->wave.capacity = 0;
@@ -245,13 +248,35 @@ static int ensure_wave(orion_gpu_ctx* c, int capacity) {
   }
   char* p = c->wave.block.as<char>();
   WaveView& w = c->wave.view;
-  float4** f4s[] = {&w.ray_o, &w.ray_d, &w.beta,  &w.L,    &w.hit,   &w.nee_p, &w.nee_beta, &w.nee_ld,
-                    &w.nee_f, &w.sh_o,  &w.sh_d,  &w.mis_o, &w.mis_d, &w.mis_hit};
-  for (float4** q : f4s) {
-    *q = reinterpret_cast<float4*>(p);
-    p += f4;
-  }
-  int** i4s[] = {&w.dim, &w.occluded, &w.q_ext[0], &w.q_ext[1], &w.q_nee, &w.q_sh, &w.q_mis};
+  w.rec = reinterpret_cast<PathRec*>(p);
+  p += recb;
+  w.nee = reinterpret_cast<NeeRec*>(p);
+  p += neeb;
+  w.mis_hit = reinterpret_cast<float4*>(p);
+  p += f4;
+  char* rb = reinterpret_cast<char*>(w.rec);
+  char* nb = reinterpret_cast<char*>(w.nee);
+  auto rec4 = [&](size_t off) { return RecF4{reinterpret_cast<float4*>(rb + off)}; };
+  auto reci = [&](size_t off) { return RecI{reinterpret_cast<int*>(rb + off)}; };
+  auto nee4 = [&](size_t off) { return NeeF4{reinterpret_cast<float4*>(nb + off)}; };
+  w.ray_o = rec4(offsetof(PathRec, o));
+  w.ray_d = rec4(offsetof(PathRec, d));
+  w.beta = rec4(offsetof(PathRec, beta));
+  w.L = rec4(offsetof(PathRec, L));
+  w.hit = rec4(offsetof(PathRec, hit));
+  w.dim = reci(offsetof(PathRec, meta));
+  w.job = reci(offsetof(PathRec, meta) + 4);
+  w.bounce = reci(offsetof(PathRec, meta) + 8);
+  w.index_hi = reci(offsetof(PathRec, meta) + 12);
+  w.nee_p = nee4(offsetof(NeeRec, p));
+  w.nee_beta = nee4(offsetof(NeeRec, beta));
+  w.nee_ld = nee4(offsetof(NeeRec, ld));
+  w.nee_f = nee4(offsetof(NeeRec, f));
+  w.sh_o = nee4(offsetof(NeeRec, sh_o));
+  w.sh_d = nee4(offsetof(NeeRec, sh_d));
+  w.mis_o = nee4(offsetof(NeeRec, mis_o));
+  w.mis_d = nee4(offsetof(NeeRec, mis_d));
+  int** i4s[] = {&w.occluded, &w.q_ext[0], &w.q_ext[1], &w.q_nee, &w.q_sh, &w.q_mis};
   for (int** q : i4s) {
     *q = reinterpret_cast<int*>(p);
     p += i4;
@@ -571,7 +596,7 @@ extern "C" int orion_gpu_stage_times(orion_gpu_ctx* ctx, orion_stage_times* out)
 // ------------------------------------------------------------ batches
 
 static int build_batch_graph(orion_gpu_ctx* ctx, const BatchView& bv, int slots) {
-  const void* key[4] = {ctx->wave.block.p, ctx->b_jobs.p, ctx->b_job_of.p, ctx->b_ctl.p};
+  const void* key[4] = {ctx->wave.block.p, ctx->b_jobs.p, ctx->b_retire.p, ctx->b_ctl.p};
   bool same = ctx->bexec && ctx->bgraph_slots == slots && std::memcmp(key, ctx->bgraph_key, sizeof(key)) == 0 &&
               std::memcmp(&ctx->bgraph_cfg, &ctx->cfg, sizeof(LaunchConfig)) == 0;
   if (same) return ORION_OK;
@@ -621,9 +646,6 @@ static int run_batch_locked(orion_gpu_ctx* ctx, std::vector<DevJob>& dj, unsigne
   if ((rc = ensure_wave(ctx, slots)) != ORION_OK) return rc;
   const int cap = ctx->wave.capacity;
   if (ctx->batch_slots_alloc < cap) {
-    if ((rc = ctx->b_job_of.alloc((size_t)cap * 4)) != ORION_OK) return rc;
-    if ((rc = ctx->b_bounce_of.alloc((size_t)cap * 4)) != ORION_OK) return rc;
-    if ((rc = ctx->b_index_of.alloc((size_t)cap * 8)) != ORION_OK) return rc;
     if ((rc = ctx->b_retire.alloc((size_t)cap * 4)) != ORION_OK) return rc;
     if ((rc = ctx->b_free.alloc((size_t)cap * 4)) != ORION_OK) return rc;
     ctx->batch_slots_alloc = cap;
@@ -637,9 +659,6 @@ static int run_batch_locked(orion_gpu_ctx* ctx, std::vector<DevJob>& dj, unsigne
   BatchView bv;
   bv.jobs = ctx->b_jobs.as<DevJob>();
   bv.ctl = ctx->b_ctl.as<BatchCtl>();
-  bv.job_of = ctx->b_job_of.as<int>();
-  bv.bounce_of = ctx->b_bounce_of.as<int>();
-  bv.index_of = ctx->b_index_of.as<long long>();
   bv.q_retire = ctx->b_retire.as<int>();
   bv.q_free = ctx->b_free.as<int>();
   if (!ctx->profiling && (rc = build_batch_graph(ctx, bv, cap)) != ORION_OK) return rc;
@@ -778,7 +797,9 @@ extern "C" int orion_gpu_render_batch(orion_gpu_ctx* ctx, int32_t njobs, const o
   for (int i = 0; i < njobs; ++i) {
     const long long wh = (long long)dj[i].width * dj[i].height;
     dj[i].sum = reinterpret_cast<double*>(fb + film_off[i]);
-    dj[i].count = reinterpret_cast<unsigned int*>(dj[i].sum + 6 * wh);
+    // Every pixel of a finished job has exactly its spp samples, so counts are
+    // written on the host, not counted on the device (one atomic per path less).
+    dj[i].count = nullptr;
     // Sums of squares only for callers that want them (they cost 3 FP64 atomics per path).
     dj[i].sumsq = jobs[i].sumsq ? dj[i].sum + 3 * wh : nullptr;
   }
@@ -792,8 +813,12 @@ extern "C" int orion_gpu_render_batch(orion_gpu_ctx* ctx, int32_t njobs, const o
     const size_t wh = (size_t)dj[i].width * dj[i].height;
     if (jobs[i].sum) CUDA_TRY(cudaMemcpyAsync(jobs[i].sum, dj[i].sum, wh * 24, cudaMemcpyDeviceToHost, s));
     if (jobs[i].sumsq) CUDA_TRY(cudaMemcpyAsync(jobs[i].sumsq, dj[i].sumsq, wh * 24, cudaMemcpyDeviceToHost, s));
-    if (jobs[i].count) CUDA_TRY(cudaMemcpyAsync(jobs[i].count, dj[i].count, wh * 4, cudaMemcpyDeviceToHost, s));
   }
+  for (int i = 0; i < njobs; ++i)
+    if (jobs[i].count) {
+      const size_t wh = (size_t)dj[i].width * dj[i].height;
+      std::fill(jobs[i].count, jobs[i].count + wh, (uint32_t)(dj[i].num_paths / (long long)wh));
+    }
   CUDA_TRY(cudaStreamSynchronize(s));
   if (stats) {
     stats->paths = (int64_t)out.paths_done;

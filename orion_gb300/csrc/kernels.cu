@@ -36,19 +36,24 @@ __global__ void k_camera(SceneView s, WaveView w, WaveArgs a) {
     PathSampler smp{a.sobol, (uint64_t)index, 5u};
     V3 o, d;
     camera_ray(s.cam, smp, i, j, &o, &d);
-    w.ray_o[pid] = f4(o, 0.f);
-    w.ray_d[pid] = f4(d, 0.f);
-    w.beta[pid] = make_float4(1.f, 1.f, 1.f, 0.f);
-    w.L[pid] = make_float4(0.f, 0.f, 0.f, 0.f);
-    w.dim[pid] = (int)smp.dim;
+    PathRec r;  // written whole: three full sectors
+    r.o = f4(o, 0.f);
+    r.d = f4(d, 0.f);
+    r.beta = make_float4(1.f, 1.f, 1.f, 0.f);
+    r.L = make_float4(0.f, 0.f, 0.f, 0.f);
+    r.hit = make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
+    r.meta = make_int4((int)smp.dim, 0, 0, 0);
+    w.rec[pid] = r;
     w.q_ext[0][pid] = pid;
   }
 }
 
-template <int SMEM>
-__global__ void __launch_bounds__(512, 2) k_trace(SceneView s, const int* queue, const int* count, int* fetch, const float4* ray_o,
-                        const float4* ray_d, float4* hit, unsigned long long* stat, int refill_below,
-                        int* cls_counters, int* q_cls, int cls_stride) {
+// Closest hit: extension rays (RayView = RecF4, hits into the path records,
+// slots sorted by shading class) or MIS rays (NeeF4, hits into mis_hit).
+template <int SMEM, class RayView, class HitView>
+__global__ void __launch_bounds__(512, 2)
+    k_trace(SceneView s, const int* queue, const int* count, int* fetch, RayView ray_o, RayView ray_d, HitView hit,
+            unsigned long long* stat, int refill_below, int* cls_counters, int* q_cls, int cls_stride) {
   extern __shared__ int2 stack_smem[];
   const int n = *count;
   trace_persistent<false, SMEM>(SingleScene{&s}, queue, n, fetch, ray_o, ray_d, hit, nullptr, stack_smem,
@@ -57,19 +62,21 @@ __global__ void __launch_bounds__(512, 2) k_trace(SceneView s, const int* queue,
 }
 
 template <int SMEM>
-__global__ void __launch_bounds__(512, 2) k_trace_sh(SceneView s, const int* queue, const int* count, int* fetch, const float4* ray_o,
-                           const float4* ray_d, int* occluded, unsigned long long* stat, int refill_below) {
+__global__ void __launch_bounds__(512, 2)
+    k_trace_sh(SceneView s, const int* queue, const int* count, int* fetch, NeeF4 ray_o, NeeF4 ray_d, int* occluded,
+               unsigned long long* stat, int refill_below) {
   extern __shared__ int2 stack_smem[];
   const int n = *count;
-  trace_persistent<true, SMEM>(SingleScene{&s}, queue, n, fetch, ray_o, ray_d, nullptr, occluded, stack_smem,
+  trace_persistent<true, SMEM>(SingleScene{&s}, queue, n, fetch, ray_o, ray_d, F4{nullptr}, occluded, stack_smem,
                                refill_below);
   if (stat && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(stat, (unsigned long long)n);
 }
 
 // One bounce for every path whose extension ray hit a material of shading
 // class SC (or, for SC_MISS, left the scene), with that class's BSDF code only.
+// Launch bounds: at most 96 registers (5 blocks of 128 threads per SM).
 template <int SC>
-__global__ void k_shade(SceneView s, WaveView w, WaveArgs a, int bounce, int cur) {
+__global__ void __launch_bounds__(128, 5) k_shade(SceneView s, WaveView w, WaveArgs a, int bounce, int cur) {
   int* out_q = w.q_ext[cur ^ 1];
   int* out_cnt = w.counters + (cur ^ 1);
   const int n = w.counters[CNT_CLS0 + SC];
@@ -226,41 +233,36 @@ int grid_for(int64_t n, int block, int max_blocks) {
   return (int)(g < 1 ? 1 : g);
 }
 
-struct TraceLaunch {
-  const int* queue;
-  const int* count;
-  int* fetch;
-  const float4* o;
-  const float4* d;
-  float4* hit;
-  int* occl;
-  unsigned long long* stat;
-  int* cls_counters;  // closest hit: also sort slots by shading class (or null)
-  int* q_cls;
-  int cls_stride;
-};
+enum TraceKind { TK_EXT = 0, TK_SHADOW = 1, TK_MIS = 2 };
 
 template <int SMEM>
-void launch_trace_kernels(bool shadow, const SceneView& s, const TraceLaunch& t, const LaunchConfig& cfg, int grid,
-                          cudaStream_t stream) {
+void launch_trace_kernels(int kind, const SceneView& s, const WaveView& w, int cur, const LaunchConfig& cfg,
+                          int grid, cudaStream_t stream) {
   const int block = cfg.trace_block;
   const int refill = cfg.refill_below < 1 ? 1 : (cfg.refill_below > 32 ? 32 : cfg.refill_below);
   size_t smem = (size_t)SMEM * block * sizeof(int2);
-  if (shadow)
-    k_trace_sh<SMEM><<<grid, block, smem, stream>>>(s, t.queue, t.count, t.fetch, t.o, t.d, t.occl, t.stat, refill);
+  if (kind == TK_EXT)
+    k_trace<SMEM, RecF4, RecF4><<<grid, block, smem, stream>>>(
+        s, w.q_ext[cur], w.counters + cur, w.counters + CNT_FETCH_EXT, w.ray_o, w.ray_d, w.hit, w.ray_stats, refill,
+        w.counters + CNT_CLS0, w.q_cls, w.capacity);
+  else if (kind == TK_SHADOW)
+    k_trace_sh<SMEM><<<grid, block, smem, stream>>>(s, w.q_sh, w.counters + CNT_SH, w.counters + CNT_FETCH_SH, w.sh_o,
+                                                    w.sh_d, w.occluded, w.ray_stats + 1, refill);
   else
-    k_trace<SMEM><<<grid, block, smem, stream>>>(s, t.queue, t.count, t.fetch, t.o, t.d, t.hit, t.stat, refill,
-                                                 t.cls_counters, t.q_cls, t.cls_stride);
+    k_trace<SMEM, NeeF4, F4><<<grid, block, smem, stream>>>(s, w.q_mis, w.counters + CNT_MIS,
+                                                            w.counters + CNT_FETCH_MIS, w.mis_o, w.mis_d,
+                                                            F4{w.mis_hit}, w.ray_stats + 2, refill, nullptr,
+                                                            nullptr, 0);
 }
 
-void trace_dispatch(bool shadow, const SceneView& s, const TraceLaunch& t, const LaunchConfig& cfg, int grid,
+void trace_dispatch(int kind, const SceneView& s, const WaveView& w, int cur, const LaunchConfig& cfg, int grid,
                     cudaStream_t stream) {
   switch (cfg.smem_stack) {
-    case 0: launch_trace_kernels<0>(shadow, s, t, cfg, grid, stream); break;
-    case 8: launch_trace_kernels<8>(shadow, s, t, cfg, grid, stream); break;
-    case 24: launch_trace_kernels<24>(shadow, s, t, cfg, grid, stream); break;
-    case 32: launch_trace_kernels<32>(shadow, s, t, cfg, grid, stream); break;
-    default: launch_trace_kernels<16>(shadow, s, t, cfg, grid, stream); break;
+    case 0: launch_trace_kernels<0>(kind, s, w, cur, cfg, grid, stream); break;
+    case 8: launch_trace_kernels<8>(kind, s, w, cur, cfg, grid, stream); break;
+    case 24: launch_trace_kernels<24>(kind, s, w, cur, cfg, grid, stream); break;
+    case 32: launch_trace_kernels<32>(kind, s, w, cur, cfg, grid, stream); break;
+    default: launch_trace_kernels<16>(kind, s, w, cur, cfg, grid, stream); break;
   }
 }
 
@@ -291,10 +293,7 @@ void launch_wave(const SceneView& s, const WaveView& w, const WaveArgs& a, const
     k_reset_bounce_counters<<<1, 32, 0, stream>>>(w.counters, cur ^ 1);
     end();
     begin(ST_TRACE_EXT);
-    trace_dispatch(false, s,
-                   TraceLaunch{w.q_ext[cur], w.counters + cur, w.counters + CNT_FETCH_EXT, w.ray_o, w.ray_d, w.hit,
-                               nullptr, w.ray_stats, w.counters + CNT_CLS0, w.q_cls, w.capacity},
-                   cfg, tgrid, stream);
+    trace_dispatch(TK_EXT, s, w, cur, cfg, tgrid, stream);
     end();
     begin(ST_SHADE);
     for (int sc = 0; sc < kShadeClasses; ++sc) {
@@ -313,16 +312,10 @@ void launch_wave(const SceneView& s, const WaveView& w, const WaveArgs& a, const
     end();
     if (bounce < a.max_depth) {
       begin(ST_TRACE_SHADOW);
-      trace_dispatch(true, s,
-                     TraceLaunch{w.q_sh, w.counters + CNT_SH, w.counters + CNT_FETCH_SH, w.sh_o, w.sh_d, nullptr,
-                                 w.occluded, w.ray_stats + 1, nullptr, nullptr, 0},
-                     cfg, tgrid, stream);
+      trace_dispatch(TK_SHADOW, s, w, cur, cfg, tgrid, stream);
       end();
       begin(ST_TRACE_MIS);
-      trace_dispatch(false, s,
-                     TraceLaunch{w.q_mis, w.counters + CNT_MIS, w.counters + CNT_FETCH_MIS, w.mis_o, w.mis_d,
-                                 w.mis_hit, nullptr, w.ray_stats + 2, nullptr, nullptr, 0},
-                     cfg, tgrid, stream);
+      trace_dispatch(TK_MIS, s, w, cur, cfg, tgrid, stream);
       end();
       begin(ST_RESOLVE);
       k_resolve<<<sgrid, cfg.shade_block, 0, stream>>>(s, w);
@@ -365,10 +358,15 @@ cudaError_t limit_of(const void* f, int smem_bytes, int* max_block) {
 }  // namespace
 
 cudaError_t configure_kernels(int smem_bytes, KernelLimits* lim) {
-  const void* trace[] = {(const void*)k_trace<0>,     (const void*)k_trace<8>,     (const void*)k_trace<16>,
-                         (const void*)k_trace<24>,    (const void*)k_trace<32>,    (const void*)k_trace_sh<0>,
-                         (const void*)k_trace_sh<8>,  (const void*)k_trace_sh<16>, (const void*)k_trace_sh<24>,
-                         (const void*)k_trace_sh<32>, (const void*)k_trace_rays<16>};
+  const void* trace[] = {
+      (const void*)k_trace<0, RecF4, RecF4>,  (const void*)k_trace<8, RecF4, RecF4>,
+      (const void*)k_trace<16, RecF4, RecF4>, (const void*)k_trace<24, RecF4, RecF4>,
+      (const void*)k_trace<32, RecF4, RecF4>, (const void*)k_trace<0, NeeF4, F4>,
+      (const void*)k_trace<8, NeeF4, F4>,     (const void*)k_trace<16, NeeF4, F4>,
+      (const void*)k_trace<24, NeeF4, F4>,    (const void*)k_trace<32, NeeF4, F4>,
+      (const void*)k_trace_sh<0>,             (const void*)k_trace_sh<8>,
+      (const void*)k_trace_sh<16>,            (const void*)k_trace_sh<24>,
+      (const void*)k_trace_sh<32>,            (const void*)k_trace_rays<16>};
   const void* shade[] = {(const void*)k_shade<SC_DIFFUSE>, (const void*)k_shade<SC_CONDUCTOR>,
                          (const void*)k_shade<SC_SPECULAR>, (const void*)k_shade<SC_DIELECTRIC>,
                          (const void*)k_shade<SC_PLASTIC>, (const void*)k_shade<SC_GENERAL>,

@@ -26,23 +26,55 @@ struct SceneView {
   DevCamera cam;
 };
 
-// Device path state for one wave of `capacity` paths (structure of arrays).
+// One field of an array of per-path records, seen as an array of its own
+// (STRIDE: record size in units of T).
+template <class T, int STRIDE>
+struct FieldView {
+  T* p;
+  ORION_HD inline T& operator[](int64_t i) const { return p[i * STRIDE]; }
+};
+
+// Per-path state, one 96-byte record (three 32-byte sectors) per path slot,
+// so a kernel that reaches a path through a scattered slot index moves whole
+// sectors: [o, d] (what a trace reads), [beta, L], [hit, meta].
+struct PathRec {
+  float4 o;     // ray origin; w unused
+  float4 d;     // ray direction; w unused
+  float4 beta;  // throughput; w = 1 after a specular bounce
+  float4 L;     // radiance so far; w = batched mode: sample index, low 32 bits
+  float4 hit;   // t, u, v, primitive (int bits; -1 miss)
+  int4 meta;    // Sobol dimension counter; batched mode: job, bounce, sample index high 32 bits
+};
+static_assert(sizeof(PathRec) == 96, "PathRec is three sectors");
+
+// Next-event-estimation record of a path, 128 bytes: written whole by the
+// shading kernel; the shadow trace reads [sh_o, sh_d], the MIS trace
+// [mis_o, mis_d], the resolve kernel the first two sectors.
+struct NeeRec {
+  float4 p;      // shading point xyz, light-selection pdf
+  float4 beta;   // beta before the bounce, w = flags | light << 8 (int bits)
+  float4 ld;     // light-sample contribution rgb, w = BSDF-sample pdf
+  float4 f;      // BSDF-sample f * |cos| rgb, w = MIS weight for environment lights
+  float4 sh_o;   // shadow ray origin, w = tmax
+  float4 sh_d;
+  float4 mis_o;
+  float4 mis_d;
+};
+static_assert(sizeof(NeeRec) == 128, "NeeRec is four sectors");
+
+using RecF4 = FieldView<float4, sizeof(PathRec) / sizeof(float4)>;
+using RecI = FieldView<int, sizeof(PathRec) / sizeof(int)>;
+using NeeF4 = FieldView<float4, sizeof(NeeRec) / sizeof(float4)>;
+using F4 = FieldView<float4, 1>;
+
+// Device path state for one wave of `capacity` paths.
 struct WaveView {
-  float4* ray_o;     // o.xyz
-  float4* ray_d;     // d.xyz
-  float4* beta;      // beta.rgb, w = 1 after a specular bounce
-  float4* L;         // radiance so far
-  int* dim;          // Sobol dimension counter
-  float4* hit;       // t, u, v, leaf triangle (int bits; -1 miss)
-  float4* nee_p;     // shading point xyz, light-selection pdf
-  float4* nee_beta;  // beta before the bounce, w = flags | light << 8 (int bits)
-  float4* nee_ld;    // light-sample contribution rgb, w = BSDF-sample pdf
-  float4* nee_f;     // BSDF-sample f * |cos| rgb, w = MIS weight for environment lights
-  float4* sh_o;      // shadow ray origin, w = tmax
-  float4* sh_d;
-  float4* mis_o;
-  float4* mis_d;
-  float4* mis_hit;
+  PathRec* rec;
+  NeeRec* nee;
+  RecF4 ray_o, ray_d, beta, L, hit;                          // fields of rec
+  RecI dim, job, bounce, index_hi;                           // rec.meta
+  NeeF4 nee_p, nee_beta, nee_ld, nee_f, sh_o, sh_d, mis_o, mis_d;  // fields of nee
+  float4* mis_hit;   // MIS ray hit: t, u, v, primitive
   int* occluded;
   int* q_ext[2];     // extension-ray queues (current / next bounce)
   int* q_nee;        // paths that sampled a light this bounce
@@ -96,12 +128,17 @@ struct BatchCtl {
 struct BatchView {
   DevJob* jobs;
   BatchCtl* ctl;
-  int* job_of;          // per slot
-  int* bounce_of;       // per slot
-  long long* index_of;  // per slot
   int* q_retire;
   int* q_free;
 };
+
+#ifdef __CUDACC__
+// Sample index of a batched path slot (kept in L.w and meta.w).
+__device__ __forceinline__ long long slot_index(const WaveView& w, int pid) {
+  return (long long)(((unsigned long long)(unsigned)w.index_hi[pid] << 32) |
+                     (unsigned long long)__float_as_uint(w.L[pid].w));
+}
+#endif
 
 struct WaveArgs {
   const uint32_t* sobol;          // dimension-major Sobol matrices (1024 x 52)

@@ -145,14 +145,14 @@ __device__ __forceinline__ ShadeResult shade_one(const SceneView& s, const WaveV
                                                  int pid, uint64_t index, int bounce, int max_depth, int rr_depth) {
   LightDistrib distrib{s.light_func, s.light_cdf, s.light_func_int, s.num_lights};
     const float4 hv = w.hit[pid];
-    const int tri = __float_as_int(hv.w);
+    const int prim = __float_as_int(hv.w);  // the trace stores the primitive, -1 for a miss
     const V3 ro = xyz(w.ray_o[pid]);
     const V3 rd = xyz(w.ray_d[pid]);
     float4 b4 = w.beta[pid];
     V3 beta = xyz(b4);
     const bool spec_prev = b4.w != 0.f;
-    V3 L = xyz(w.L[pid]);
-    const int prim = tri >= 0 ? __ldg(s.tri_prim + tri) : -1;
+    const float4 L4 = w.L[pid];
+    V3 L = xyz(L4);
 
     // Emission on the first hit or after a specular bounce (path.cpp:61-69).
     if (bounce == 0 || spec_prev) {
@@ -280,7 +280,7 @@ __device__ __forceinline__ ShadeResult shade_one(const SceneView& s, const WaveV
       }
       w.dim[pid] = (int)(d0 + used);
     }
-    w.L[pid] = f4(L, 0.f);
+    w.L[pid] = f4(L, L4.w);  // w holds batched mode's sample index bits
   return ShadeResult{alive, did_nee, want_sh, want_mis};
 }
 
@@ -292,8 +292,8 @@ struct SingleScene {
 };
 struct JobScene {
   const DevJob* jobs;
-  const int* job_of;
-  __device__ __forceinline__ const SceneView& operator()(int pid) const { return jobs[job_of[pid]].scene; }
+  RecI job;
+  __device__ __forceinline__ const SceneView& operator()(int pid) const { return jobs[job[pid]].scene; }
 };
 
 // Persistent-warp tracing of `n` queued rays (see traverse.cuh): warps stay
@@ -301,10 +301,10 @@ struct JobScene {
 // counter that must be zero at launch. Block size must be a multiple of 32.
 // With `q_cls` (closest hit only), each finished ray's slot is also appended
 // to the queue of the shading class of what it hit (SC_MISS for a miss).
-template <bool ANY, int SMEM, class SceneOf>
+template <bool ANY, int SMEM, class SceneOf, class RayView, class HitView>
 __device__ __forceinline__ void trace_persistent(const SceneOf& scene_of, const int* queue, int n, int* fetch,
-                                                 const float4* ray_o, const float4* ray_d, float4* hit,
-                                                 int* occluded, int2* stack_smem, int refill_below,
+                                                 RayView ray_o, RayView ray_d, HitView hit, int* occluded,
+                                                 int2* stack_smem, int refill_below,
                                                  int* cls_counters = nullptr, int* q_cls = nullptr,
                                                  int cls_stride = 0) {
   constexpr unsigned kFull = 0xffffffffu;
@@ -348,7 +348,8 @@ __device__ __forceinline__ void trace_persistent(const SceneOf& scene_of, const 
         if (ANY) {
           occluded[pid] = r.tri >= 0;
         } else {
-          hit[pid] = make_float4(r.tri >= 0 ? r.tmax : kFloatMax, r.u, r.v, __int_as_float(r.tri));
+          hit[pid] = make_float4(r.tri >= 0 ? r.tmax : kFloatMax, r.u, r.v,
+                                 __int_as_float(r.tri >= 0 ? __ldg(ts.tri_prim + r.tri) : -1));
           if (q_cls)
             class_append(cls_counters, q_cls, cls_stride, r.tri >= 0 ? (int)__ldg(ts.tri_class + r.tri) : SC_MISS,
                          pid);
@@ -375,12 +376,11 @@ __device__ __forceinline__ void resolve_one(const SceneView& s, const WaveView& 
       V3 fb = xyz(fv);
       float bpdf = ldv.w;
       float4 mh = w.mis_hit[pid];
-      int tri = __float_as_int(mh.w);
+      const int prim = __float_as_int(mh.w);  // primitive hit by the MIS ray, -1 for a miss
       V3 wi = xyz(w.mis_d[pid]);
       if (fl & kFlagEnv) {
-        if (tri < 0) Ld = Ld + sdiv(mul(fb, ld3(lt.L)) * fv.w, bpdf);
-      } else if (tri >= 0) {
-        int prim = __ldg(s.tri_prim + tri);
+        if (prim < 0) Ld = Ld + sdiv(mul(fb, ld3(lt.L)) * fv.w, bpdf);
+      } else if (prim >= 0) {
         if (prim == lt.prim) {
           // Triangle::pdf (src/core/triangle.cpp:123-135) on the traced hit.
           const PrimShade& sh = s.prims[prim];
@@ -396,9 +396,9 @@ __device__ __forceinline__ void resolve_one(const SceneView& s, const WaveView& 
         }
       }
     }
-    V3 L = xyz(w.L[pid]);
-    L = L + mul(xyz(pb), sdiv(Ld, np.w));
-    w.L[pid] = f4(L, 0.f);
+    const float4 L4 = w.L[pid];
+    const V3 L = xyz(L4) + mul(xyz(pb), sdiv(Ld, np.w));
+    w.L[pid] = f4(L, L4.w);
 }
 
 }  // namespace orion_gb300
