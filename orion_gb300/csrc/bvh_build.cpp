@@ -72,26 +72,35 @@ namespace {
 
 struct TmpNode {
   float lo[3], hi[3];
-  int32_t begin = 0, count = 0;  // leaf range in `order`
-  int32_t first = 0, total = 0;  // the subtree's triangles: order[first, first + total)
+  int32_t begin = 0, count = 0;  // leaf range in the reference array
+  int32_t first = 0, total = 0;  // the subtree's triangles: refs[first, first + total)
   TmpNode* child[2] = {nullptr, nullptr};
   int depth = 0;
 };
 
+// One triangle's box and id, 32 bytes. The build partitions these records
+// themselves (not indices into per-triangle arrays), so every scan of a
+// range reads memory in order.
+struct PrimRef {
+  float lo[3];
+  int32_t id;
+  float hi[3];
+  float pad;
+  float centroid(int k) const { return 0.5f * (lo[k] + hi[k]); }
+};
+
 struct Builder {
   const BvhBuildOptions& opt;
-  const float* lo;  // per prim, 3
-  const float* hi;
-  const float* ce;
-  int32_t* order;
+  PrimRef* refs;
   std::mutex arena_mu;
   std::vector<std::unique_ptr<std::deque<TmpNode>>> arenas;
   std::atomic<int> max_depth{0};
   std::atomic<int> leaves{0};
   int spawn_depth;
+  int threads;
+  std::atomic<int> running{0};  // subtrees building on threads of their own
 
-  Builder(const BvhBuildOptions& o, const float* l, const float* h, const float* c, int32_t* ord, int threads)
-      : opt(o), lo(l), hi(h), ce(c), order(ord) {
+  Builder(const BvhBuildOptions& o, PrimRef* r, int nthreads) : opt(o), refs(r), threads(nthreads) {
     spawn_depth = 0;
     while ((1 << spawn_depth) < 4 * threads) ++spawn_depth;
   }
@@ -107,19 +116,62 @@ struct Builder {
     return dx * dy + dy * dz + dz * dx;
   }
 
-  void bounds(int begin, int end, float* bl, float* bh) const {
+  // Ranges above this many primitives are scanned by several threads (the
+  // top levels of the tree, which would otherwise run on one thread).
+  static constexpr int kParallelScan = 1 << 16;
+
+  // Runs f(b, e, part) over `parts` contiguous pieces of [begin, end) in parallel.
+  template <class F>
+  static void parallel_parts(int begin, int end, int parts, F f) {
+    std::vector<std::thread> th;
+    const int64_t n = end - begin;
+    for (int t = 0; t < parts; ++t) {
+      const int b = begin + (int)(n * t / parts), e = begin + (int)(n * (t + 1) / parts);
+      th.emplace_back(f, b, e, t);
+    }
+    for (auto& x : th) x.join();
+  }
+
+  int scan_parts(int count) const {
+    if (count < kParallelScan) return 1;
+    return std::max(1, std::min(threads, count / (kParallelScan / 4)));
+  }
+
+  // Box of the primitives (centroids: the box of their centres) over [begin, end).
+  void bounds_range(bool centroids, int begin, int end, float* bl, float* bh) const {
     for (int k = 0; k < 3; ++k) {
       bl[k] = std::numeric_limits<float>::infinity();
       bh[k] = -std::numeric_limits<float>::infinity();
     }
     for (int i = begin; i < end; ++i) {
-      int p = order[i];
+      const PrimRef& r = refs[i];
       for (int k = 0; k < 3; ++k) {
-        bl[k] = std::min(bl[k], lo[3 * p + k]);
-        bh[k] = std::max(bh[k], hi[3 * p + k]);
+        const float a = centroids ? r.centroid(k) : r.lo[k], b = centroids ? a : r.hi[k];
+        bl[k] = std::min(bl[k], a);
+        bh[k] = std::max(bh[k], b);
       }
     }
   }
+
+  // bounds_range, in parallel for large ranges.
+  void box_of(bool centroids, int begin, int end, float* bl, float* bh) const {
+    const int parts = scan_parts(end - begin);
+    if (parts == 1) return bounds_range(centroids, begin, end, bl, bh);
+    std::vector<float> r(6 * (size_t)parts);
+    parallel_parts(begin, end, parts,
+                   [&](int s, int e, int t) { bounds_range(centroids, s, e, &r[6 * t], &r[6 * t + 3]); });
+    for (int k = 0; k < 3; ++k) {
+      bl[k] = std::numeric_limits<float>::infinity();
+      bh[k] = -std::numeric_limits<float>::infinity();
+    }
+    for (int t = 0; t < parts; ++t)
+      for (int k = 0; k < 3; ++k) {
+        bl[k] = std::min(bl[k], r[6 * t + k]);
+        bh[k] = std::max(bh[k], r[6 * t + 3 + k]);
+      }
+  }
+
+  void bounds(int begin, int end, float* bl, float* bh) const { box_of(false, begin, end, bl, bh); }
 
   TmpNode* build(int begin, int end, int depth, std::deque<TmpNode>* arena) {
     arena->emplace_back();
@@ -148,10 +200,20 @@ struct Builder {
       }
     }
     if (mid < 0) mid = median_split(begin, end);
-    if (depth < spawn_depth && count > 4096) {
+    // A subtree goes to a new thread while fewer than 2 x threads are busy, so
+    // uneven SAH splits still keep every core working.
+    bool spawn = false;
+    if (count > 8192) {
+      int live = running.load();
+      while (live < 2 * threads && !(spawn = running.compare_exchange_weak(live, live + 1))) {
+      }
+    }
+    if (spawn) {
       auto fut = std::async(std::launch::async, [=] {
         std::deque<TmpNode>* a2 = new_arena();
-        return build(begin, mid, depth + 1, a2);
+        TmpNode* r = build(begin, mid, depth + 1, a2);
+        running.fetch_sub(1);
+        return r;
       });
       n->child[1] = build(mid, end, depth + 1, arena);
       n->child[0] = fut.get();
@@ -176,59 +238,80 @@ struct Builder {
     for (int k = 1; k < 3; ++k)
       if (ch[k] - cl[k] > ch[axis] - cl[axis]) axis = k;
     int mid = begin + (end - begin) / 2;
-    std::nth_element(order + begin, order + mid, order + end,
-                     [&](int a, int b) { return ce[3 * a + axis] < ce[3 * b + axis]; });
+    std::nth_element(refs + begin, refs + mid, refs + end,
+                     [&](const PrimRef& a, const PrimRef& b) { return a.centroid(axis) < b.centroid(axis); });
     return mid;
   }
 
-  void centroid_bounds(int begin, int end, float* cl, float* ch) const {
-    for (int k = 0; k < 3; ++k) {
-      cl[k] = std::numeric_limits<float>::infinity();
-      ch[k] = -std::numeric_limits<float>::infinity();
+  void centroid_bounds(int begin, int end, float* cl, float* ch) const { box_of(true, begin, end, cl, ch); }
+
+  struct Bins {
+    int cnt[3][64];
+    float blo[3][64][3], bhi[3][64][3];
+    void clear(int B) {
+      for (int axis = 0; axis < 3; ++axis)
+        for (int b = 0; b < B; ++b) {
+          cnt[axis][b] = 0;
+          for (int k = 0; k < 3; ++k) {
+            blo[axis][b][k] = std::numeric_limits<float>::infinity();
+            bhi[axis][b][k] = -std::numeric_limits<float>::infinity();
+          }
+        }
     }
+  };
+
+  void bin_range(int begin, int end, int B, const float* cl, const float* scale, Bins& bins) const {
+    bins.clear(B);
     for (int i = begin; i < end; ++i) {
-      int p = order[i];
-      for (int k = 0; k < 3; ++k) {
-        cl[k] = std::min(cl[k], ce[3 * p + k]);
-        ch[k] = std::max(ch[k], ce[3 * p + k]);
+      const PrimRef& r = refs[i];
+      for (int axis = 0; axis < 3; ++axis) {
+        if (scale[axis] == 0.f) continue;
+        int b = std::min(B - 1, (int)((r.centroid(axis) - cl[axis]) * scale[axis]));
+        bins.cnt[axis][b]++;
+        for (int k = 0; k < 3; ++k) {
+          bins.blo[axis][b][k] = std::min(bins.blo[axis][b][k], r.lo[k]);
+          bins.bhi[axis][b][k] = std::max(bins.bhi[axis][b][k], r.hi[k]);
+        }
       }
     }
   }
 
   // Returns the partition point of the best binned SAH split, or -1.
   int sah_split(int begin, int end, const TmpNode* n, float* best_cost_out) {
-    const int B = std::max(2, std::min(opt.bins, 64));
+    // Small ranges get as many bins as primitives (at least 4): the per-bin
+    // clear and sweep would otherwise dominate near the leaves.
+    const int B = std::max(2, std::min(std::min(opt.bins, 64), std::max(4, end - begin)));
     float cl[3], ch[3];
     centroid_bounds(begin, end, cl, ch);
     float parent_area = half_area(n->lo, n->hi);
     int best_axis = -1, best_bin = -1;
     float best_cost = std::numeric_limits<float>::infinity();
-    int cnt[3][64];
-    float blo[3][64][3], bhi[3][64][3];
     float scale[3];
     for (int axis = 0; axis < 3; ++axis) {
       float ext = ch[axis] - cl[axis];
       scale[axis] = ext > 0.f ? B / ext : 0.f;
-      for (int b = 0; b < B; ++b) {
-        cnt[axis][b] = 0;
-        for (int k = 0; k < 3; ++k) {
-          blo[axis][b][k] = std::numeric_limits<float>::infinity();
-          bhi[axis][b][k] = -std::numeric_limits<float>::infinity();
-        }
-      }
     }
-    for (int i = begin; i < end; ++i) {
-      int p = order[i];
-      for (int axis = 0; axis < 3; ++axis) {
-        if (scale[axis] == 0.f) continue;
-        int b = std::min(B - 1, (int)((ce[3 * p + axis] - cl[axis]) * scale[axis]));
-        cnt[axis][b]++;
-        for (int k = 0; k < 3; ++k) {
-          blo[axis][b][k] = std::min(blo[axis][b][k], lo[3 * p + k]);
-          bhi[axis][b][k] = std::max(bhi[axis][b][k], hi[3 * p + k]);
-        }
-      }
+    Bins all;
+    const int parts = scan_parts(end - begin);
+    if (parts == 1) {
+      bin_range(begin, end, B, cl, scale, all);
+    } else {  // per-thread bins, merged (counts add, boxes union: independent of timing)
+      std::vector<Bins> part(parts);
+      parallel_parts(begin, end, parts, [&](int s, int e, int t) { bin_range(s, e, B, cl, scale, part[t]); });
+      all.clear(B);
+      for (const Bins& pb : part)
+        for (int axis = 0; axis < 3; ++axis)
+          for (int b = 0; b < B; ++b) {
+            all.cnt[axis][b] += pb.cnt[axis][b];
+            for (int k = 0; k < 3; ++k) {
+              all.blo[axis][b][k] = std::min(all.blo[axis][b][k], pb.blo[axis][b][k]);
+              all.bhi[axis][b][k] = std::max(all.bhi[axis][b][k], pb.bhi[axis][b][k]);
+            }
+          }
     }
+    auto& cnt = all.cnt;
+    auto& blo = all.blo;
+    auto& bhi = all.bhi;
     for (int axis = 0; axis < 3; ++axis) {
       if (scale[axis] == 0.f) continue;
       float rarea[64];
@@ -271,11 +354,11 @@ struct Builder {
     if (best_axis < 0) return -1;
     *best_cost_out = parent_area > 0.f ? 1.f + best_cost / parent_area : 1.f;
     float s = scale[best_axis], c0 = cl[best_axis];
-    int32_t* it = std::partition(order + begin, order + end, [&](int p) {
-      int b = std::min(B - 1, (int)((ce[3 * p + best_axis] - c0) * s));
+    PrimRef* it = std::partition(refs + begin, refs + end, [&](const PrimRef& r) {
+      int b = std::min(B - 1, (int)((r.centroid(best_axis) - c0) * s));
       return b <= best_bin;
     });
-    int mid = (int)(it - order);
+    int mid = (int)(it - refs);
     if (mid == begin || mid == end) return -1;
     return mid;
   }
@@ -447,8 +530,13 @@ struct WideCollapser {
     }
   }
 
-  void fill(int idx, const TmpNode* n) {
+  // Builds the wide node of binary node `n` into `w`: its internal children
+  // get placeholder slots appended to `nodes` (from w.child_base) and are
+  // returned in `kids` in slot order; its leaf triangles are appended to `tris`.
+  void fill_node(const TmpNode* n, WideNode& w, std::vector<WideNode>& nodes, std::vector<int32_t>& tris,
+                 const TmpNode* kids[8], int* nkids) const {
     std::vector<const TmpNode*> ch;
+    ch.reserve(8);
     gather(n, ch);
     const int m = (int)ch.size();
     double clo[8][3], chi[8][3], nlo[3], nhi[3];
@@ -471,7 +559,6 @@ struct WideCollapser {
       in_slot[slot_of[c]] = ch[c];
       child_of_slot[slot_of[c]] = c;
     }
-    WideNode w;
     std::memset(&w, 0, sizeof(w));
     // Empty slots get inverted boxes (lo = 255 > hi = 0 on every axis), which
     // no ray hits whatever its direction.
@@ -483,7 +570,12 @@ struct WideCollapser {
       if ((double)w.p[k] > nlo[k]) w.p[k] = std::nextafter(w.p[k], -std::numeric_limits<float>::infinity());
       const double ext = nhi[k] - (double)w.p[k];
       int e = -126;
-      while (e < 127 && std::ldexp(255.0, e) < ext) ++e;
+      if (ext > 0.0) {
+        int ex;
+        const double m = std::frexp(ext / 255.0, &ex);  // ext / 255 = m * 2^ex, m in [0.5, 1)
+        e = std::max(-126, std::min(127, m == 0.5 ? ex - 1 : ex));
+      }
+      while (e < 127 && std::ldexp(255.0, e) < ext) ++e;  // guards the rounding of ext / 255
       w.e[k] = (uint8_t)(e + 127);
       cell[k] = std::ldexp(1.0, e);
     }
@@ -491,8 +583,8 @@ struct WideCollapser {
     int n_internal = 0;
     for (int s = 0; s < 8; ++s)
       if (in_slot[s] && !is_leaf(in_slot[s])) ++n_internal;
-    const int child_base = (int)out.size();
-    out.resize(out.size() + n_internal);
+    const int child_base = (int)nodes.size();
+    nodes.resize(nodes.size() + n_internal);
     w.child_base = child_base;
     w.tri_base = (int)tris.size();
     for (int s = 0; s < 8; ++s) {
@@ -518,15 +610,72 @@ struct WideCollapser {
         for (int i = 0; i < c->total; ++i) tris.push_back(order[c->first + i]);
       }
     }
-    out[idx] = w;
-    int r = 0;
+    *nkids = 0;
     for (int s = 0; s < 8; ++s)
-      if (in_slot[s] && !is_leaf(in_slot[s])) fill(child_base + r++, in_slot[s]);
+      if (in_slot[s] && !is_leaf(in_slot[s])) kids[(*nkids)++] = in_slot[s];
   }
 
-  void run(const TmpNode* root) {
+  // The wide subtree of `n` into nodes[idx] and below, depth first.
+  void fill(int idx, const TmpNode* n, std::vector<WideNode>& nodes, std::vector<int32_t>& tris) const {
+    WideNode w;
+    const TmpNode* kids[8];
+    int nk;
+    fill_node(n, w, nodes, tris, kids, &nk);
+    nodes[idx] = w;
+    for (int r = 0; r < nk; ++r) fill(w.child_base + r, kids[r], nodes, tris);
+  }
+
+  // The top levels breadth first on this thread until there are enough
+  // subtrees for every core, then the subtrees in parallel, each into arrays
+  // of its own, appended in order with their child and triangle bases shifted.
+  void run(const TmpNode* root, int threads) {
     out.assign(1, WideNode{});
-    fill(0, root);
+    std::vector<std::pair<int, const TmpNode*>> frontier{{0, root}}, next;
+    for (int level = 0; level < 6 && !frontier.empty() && (int)frontier.size() < 4 * threads; ++level) {
+      next.clear();
+      for (auto& f : frontier) {
+        WideNode w;
+        const TmpNode* kids[8];
+        int nk;
+        fill_node(f.second, w, out, tris, kids, &nk);
+        out[f.first] = w;
+        for (int r = 0; r < nk; ++r) next.push_back({w.child_base + r, kids[r]});
+      }
+      frontier.swap(next);
+    }
+    struct Task {
+      int idx;
+      const TmpNode* n;
+      WideNode root;
+      std::vector<WideNode> nodes;
+      std::vector<int32_t> tris;
+    };
+    std::vector<Task> tasks(frontier.size());
+    std::atomic<int> next_task{0};
+    auto worker = [&](int, int, int) {
+      for (int t; (t = next_task.fetch_add(1)) < (int)tasks.size();) {
+        Task& tk = tasks[t];
+        tk.idx = frontier[t].first;
+        tk.n = frontier[t].second;
+        const TmpNode* kids[8];
+        int nk;
+        fill_node(tk.n, tk.root, tk.nodes, tk.tris, kids, &nk);
+        for (int r = 0; r < nk; ++r) fill(tk.root.child_base + r, kids[r], tk.nodes, tk.tris);
+      }
+    };
+    if (!tasks.empty()) Builder::parallel_parts(0, threads, std::max(1, std::min(threads, (int)tasks.size())), worker);
+    for (Task& tk : tasks) {
+      const int node_off = (int)out.size(), tri_off = (int)tris.size();
+      for (WideNode& w : tk.nodes) {
+        w.child_base += node_off;
+        w.tri_base += tri_off;
+      }
+      tk.root.child_base += node_off;
+      tk.root.tri_base += tri_off;
+      out[tk.idx] = tk.root;
+      out.insert(out.end(), tk.nodes.begin(), tk.nodes.end());
+      tris.insert(tris.end(), tk.tris.begin(), tk.tris.end());
+    }
   }
 };
 
@@ -558,42 +707,47 @@ void build_bvh(const float* positions, int64_t num_tris, const BvhBuildOptions& 
     out->nodes.push_back(empty);
     return;
   }
-  std::vector<float> lo(3 * (size_t)T), hi(3 * (size_t)T), ce(3 * (size_t)T);
-  for (int i = 0; i < T; ++i) {
-    const float* p = positions + 9 * (size_t)i;
-    for (int k = 0; k < 3; ++k) {
-      float a = std::min(std::min(p[k], p[3 + k]), p[6 + k]);
-      float b = std::max(std::max(p[k], p[3 + k]), p[6 + k]);
-      lo[3 * (size_t)i + k] = a;
-      hi[3 * (size_t)i + k] = b;
-      ce[3 * (size_t)i + k] = 0.5f * (a + b);
-    }
-  }
-  std::vector<int32_t> order(T);
-  for (int i = 0; i < T; ++i) order[i] = i;
   int threads = opt.threads > 0 ? opt.threads : (int)std::max(1u, std::thread::hardware_concurrency());
-  Builder b(opt, lo.data(), hi.data(), ce.data(), order.data(), threads);
+  std::vector<PrimRef> refs(T);
+  Builder::parallel_parts(0, T, std::max(1, std::min(threads, T / 4096)), [&](int s, int e, int) {
+    for (int i = s; i < e; ++i) {
+      const float* p = positions + 9 * (size_t)i;
+      PrimRef& r = refs[i];
+      for (int k = 0; k < 3; ++k) {
+        r.lo[k] = std::min(std::min(p[k], p[3 + k]), p[6 + k]);
+        r.hi[k] = std::max(std::max(p[k], p[3 + k]), p[6 + k]);
+      }
+      r.id = i;
+      r.pad = 0.f;
+    }
+  });
+  Builder b(opt, refs.data(), threads);
   std::deque<TmpNode>* arena = b.new_arena();
   TmpNode* root = b.build(0, T, 0, arena);
   out->depth = b.max_depth.load();
   out->leaves = b.leaves.load();
+  std::vector<int32_t> order(T);  // binary leaf order -> primID
+  for (int i = 0; i < T; ++i) order[i] = refs[i].id;
+  // Woop records of triangles in `ids` order, in parallel.
+  auto records = [&](const std::vector<int32_t>& ids) {
+    Builder::parallel_parts(0, T, std::max(1, std::min(threads, T / 4096)), [&](int s, int e, int) {
+      for (int i = s; i < e; ++i) {
+        out->tri_prim[i] = ids[i];
+        woop_record(positions + 9 * (size_t)ids[i], &out->woop[12 * (size_t)i]);
+      }
+    });
+  };
   if (opt.wide) {
     std::vector<int32_t> tris;
     tris.reserve(T);
     WideCollapser wc{order.data(), out->wide, tris};
-    wc.run(root);
-    for (int i = 0; i < T; ++i) {
-      out->tri_prim[i] = tris[i];
-      woop_record(positions + 9 * (size_t)tris[i], &out->woop[12 * (size_t)i]);
-    }
+    wc.run(root, threads);
+    records(tris);
     return;
   }
   Flattener fl(out->nodes);
   fl.run(root, opt.top_bfs_nodes);
-  for (int i = 0; i < T; ++i) {
-    out->tri_prim[i] = order[i];
-    woop_record(positions + 9 * (size_t)order[i], &out->woop[12 * (size_t)i]);
-  }
+  records(order);
   // SAH cost of the result (traversal + intersection, relative to the root).
   double root_area = Builder::half_area(out->nodes[0].lo, out->nodes[0].hi);
   double cost = 0.0;

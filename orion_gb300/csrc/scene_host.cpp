@@ -18,6 +18,8 @@
 // samplers) are reported as ORION_ERR_UNSUPPORTED instead of being loaded.
 #include "scene_host.h"
 
+#include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -26,7 +28,9 @@
 #include <map>
 #include <memory>
 #include <sstream>
+#include <thread>
 #include <utility>
+#include <vector>
 
 namespace orion_gb300 {
 
@@ -503,37 +507,50 @@ struct CornerMesh {  // de-indexed: 3 corners per triangle
 };
 
 bool read_file(const std::string& path, std::string* out) {
-  std::ifstream f(path, std::ios::binary);
+  FILE* f = std::fopen(path.c_str(), "rb");
   if (!f) return false;
-  std::ostringstream ss;
-  ss << f.rdbuf();
-  *out = ss.str();
-  return true;
+  std::fseek(f, 0, SEEK_END);
+  const long n = std::ftell(f);
+  std::fseek(f, 0, SEEK_SET);
+  out->resize(n > 0 ? (size_t)n : 0);
+  const bool ok = n >= 0 && std::fread(&(*out)[0], 1, out->size(), f) == out->size();
+  std::fclose(f);
+  return ok;
 }
 
 // Wavefront OBJ as the reference reads it through tiny_obj_loader
 // (src/core/triangle.cpp:8-58): polygons fan-triangulated, positions and
 // normals required per corner, texture coordinates optional (0 if absent).
-void load_obj(const std::string& path, CornerMesh* out) {
-  std::string text;
-  if (!read_file(path, &text)) raise(ORION_ERR_IO, "cannot read mesh " + path);
+//
+// The file is parsed in line-aligned pieces on several threads; each piece
+// keeps its own vertex arrays and face corners, which are then joined in file
+// order (relative indices resolved against the vertices read before them), so
+// the triangles and their order are those of a sequential read.
+namespace obj {
+
+struct Corner {
+  long v, t, n;  // as written: 1-based, negative = relative, 0 = absent
+};
+
+struct Piece {
+  const char* begin;
+  const char* end;
   std::vector<float> v, vn, vt;
-  const char* s = text.c_str();
-  const char* end = s + text.size();
-  int line_no = 0;
-  struct Idx {
-    int v, t, n;
-  };
-  std::vector<Idx> face;
-  auto resolve = [](long i, size_t count) -> int {
-    if (i > 0) return (int)(i - 1);
-    if (i < 0) return (int)((long)count + i);
-    return -1;
-  };
-  while (s < end) {
-    const char* eol = (const char*)std::memchr(s, '\n', end - s);
-    if (!eol) eol = end;
-    ++line_no;
+  std::vector<Corner> corners;
+  std::vector<int> face_first;   // first corner of each face
+  std::vector<int> face_line;    // line of each face within the piece
+  std::vector<int> face_counts;  // v, vt, vn counts in the piece when the face was read
+  int lines = 0;
+  int64_t tris = 0;
+  std::string error;  // "line: message"
+};
+
+void parse_piece(Piece& pc) {
+  const char* s = pc.begin;
+  while (s < pc.end) {
+    const char* eol = (const char*)std::memchr(s, '\n', pc.end - s);
+    if (!eol) eol = pc.end;
+    ++pc.lines;
     const char* p = s;
     while (p < eol && (*p == ' ' || *p == '\t')) ++p;
     if (p + 1 < eol && p[0] == 'v' && (p[1] == ' ' || p[1] == '\t')) {
@@ -541,25 +558,20 @@ void load_obj(const std::string& path, CornerMesh* out) {
       float x = std::strtof(p + 2, &q);
       float y = std::strtof(q, &q);
       float z = std::strtof(q, &q);
-      v.push_back(x);
-      v.push_back(y);
-      v.push_back(z);
+      pc.v.insert(pc.v.end(), {x, y, z});
     } else if (p + 2 < eol && p[0] == 'v' && p[1] == 'n' && (p[2] == ' ' || p[2] == '\t')) {
       char* q;
       float x = std::strtof(p + 3, &q);
       float y = std::strtof(q, &q);
       float z = std::strtof(q, &q);
-      vn.push_back(x);
-      vn.push_back(y);
-      vn.push_back(z);
+      pc.vn.insert(pc.vn.end(), {x, y, z});
     } else if (p + 2 < eol && p[0] == 'v' && p[1] == 't' && (p[2] == ' ' || p[2] == '\t')) {
       char* q;
       float x = std::strtof(p + 3, &q);
       float y = std::strtof(q, &q);
-      vt.push_back(x);
-      vt.push_back(y);
+      pc.vt.insert(pc.vt.end(), {x, y});
     } else if (p + 1 < eol && p[0] == 'f' && (p[1] == ' ' || p[1] == '\t')) {
-      face.clear();
+      const int first = (int)pc.corners.size();
       const char* q = p + 2;
       while (q < eol) {
         while (q < eol && (*q == ' ' || *q == '\t' || *q == '\r')) ++q;
@@ -567,7 +579,10 @@ void load_obj(const std::string& path, CornerMesh* out) {
         char* r;
         long a = std::strtol(q, &r, 10);
         long b = 0, c = 0;
-        if (r == q) raise(ORION_ERR_PARSE, path + ":" + std::to_string(line_no) + ": bad face");
+        if (r == q) {
+          pc.error = std::to_string(pc.lines) + ": bad face";
+          return;
+        }
         q = r;
         if (q < eol && *q == '/') {
           ++q;
@@ -581,35 +596,126 @@ void load_obj(const std::string& path, CornerMesh* out) {
             q = r;
           }
         }
-        face.push_back(Idx{resolve(a, v.size() / 3), resolve(b, vt.size() / 2), resolve(c, vn.size() / 3)});
+        pc.corners.push_back(Corner{a, b, c});
         while (q < eol && *q != ' ' && *q != '\t') ++q;
       }
-      if (face.size() < 3) raise(ORION_ERR_PARSE, path + ":" + std::to_string(line_no) + ": face with < 3 corners");
-      for (size_t k = 1; k + 1 < face.size(); ++k) {
-        const Idx tri[3] = {face[0], face[k], face[k + 1]};
-        for (const Idx& c : tri) {
-          if (c.v < 0 || (size_t)c.v * 3 + 2 >= v.size() + 0 || (size_t)c.v >= v.size() / 3)
-            raise(ORION_ERR_PARSE, path + ":" + std::to_string(line_no) + ": vertex index out of range");
-          if (c.n < 0 || (size_t)c.n >= vn.size() / 3)
-            raise(ORION_ERR_PARSE,
-                  path + ":" + std::to_string(line_no) + ": face corner without a normal (vn is required)");
-          for (int d = 0; d < 3; ++d) {
-            out->p.push_back(v[3 * c.v + d]);
-            out->n.push_back(vn[3 * c.n + d]);
-          }
-          if (c.t >= 0 && (size_t)c.t < vt.size() / 2) {
-            out->uv.push_back(vt[2 * c.t]);
-            out->uv.push_back(vt[2 * c.t + 1]);
-          } else {
-            out->uv.push_back(0.f);
-            out->uv.push_back(0.f);
-          }
-        }
-        ++out->num_tris;
+      const int nc = (int)pc.corners.size() - first;
+      if (nc < 3) {
+        pc.error = std::to_string(pc.lines) + ": face with < 3 corners";
+        return;
       }
+      pc.face_first.push_back(first);
+      pc.face_line.push_back(pc.lines);
+      pc.face_counts.insert(pc.face_counts.end(),
+                            {(int)(pc.v.size() / 3), (int)(pc.vt.size() / 2), (int)(pc.vn.size() / 3)});
+      pc.tris += nc - 2;
     }
     s = eol + 1;
   }
+}
+
+}  // namespace obj
+
+void load_obj(const std::string& path, CornerMesh* out) {
+  std::string text;
+  if (!read_file(path, &text)) raise(ORION_ERR_IO, "cannot read mesh " + path);
+  const char* s = text.data();
+  const char* end = s + text.size();
+  const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
+  const int npieces = text.size() < (1u << 20) ? 1 : std::min(4 * hw, (int)(text.size() >> 18));
+  std::vector<obj::Piece> pcs(npieces);
+  const char* cut = s;
+  for (int i = 0; i < npieces; ++i) {  // line-aligned pieces
+    const char* e = i + 1 == npieces ? end : s + (text.size() * (size_t)(i + 1)) / npieces;
+    if (e < cut) e = cut;
+    const char* nl = e < end ? (const char*)std::memchr(e, '\n', end - e) : nullptr;
+    e = (i + 1 == npieces || !nl) ? end : nl + 1;
+    pcs[i].begin = cut;
+    pcs[i].end = e;
+    cut = e;
+  }
+  auto for_pieces = [&](auto f) {
+    std::vector<std::thread> th;
+    std::atomic<int> next{0};
+    const int nt = std::min(hw, npieces);
+    for (int t = 0; t < nt; ++t)
+      th.emplace_back([&] {
+        for (int i; (i = next.fetch_add(1)) < npieces;) f(i);
+      });
+    for (auto& x : th) x.join();
+  };
+  for_pieces([&](int i) { obj::parse_piece(pcs[i]); });
+  // Join: vertex arrays in file order, global line numbers, triangle offsets.
+  std::vector<int64_t> v0(npieces), t0(npieces), n0(npieces), line0(npieces), tri0(npieces);
+  std::vector<float> v, vn, vt;
+  int64_t lines = 0, tris = 0;
+  for (int i = 0; i < npieces; ++i) {
+    const obj::Piece& pc = pcs[i];
+    if (!pc.error.empty()) {
+      const size_t colon = pc.error.find(':');
+      raise(ORION_ERR_PARSE, path + ":" + std::to_string(lines + std::stol(pc.error.substr(0, colon))) +
+                                 pc.error.substr(colon));
+    }
+    v0[i] = (int64_t)v.size() / 3;
+    t0[i] = (int64_t)vt.size() / 2;
+    n0[i] = (int64_t)vn.size() / 3;
+    line0[i] = lines;
+    tri0[i] = tris;
+    v.insert(v.end(), pc.v.begin(), pc.v.end());
+    vt.insert(vt.end(), pc.vt.begin(), pc.vt.end());
+    vn.insert(vn.end(), pc.vn.begin(), pc.vn.end());
+    lines += pc.lines;
+    tris += pc.tris;
+  }
+  out->num_tris = (int)tris;
+  out->p.assign(9 * (size_t)tris, 0.f);
+  out->n.assign(9 * (size_t)tris, 0.f);
+  out->uv.assign(6 * (size_t)tris, 0.f);
+  const size_t nv = v.size() / 3, nt = vt.size() / 2, nn = vn.size() / 3;
+  std::vector<std::string> errors(npieces);
+  for_pieces([&](int i) {
+    const obj::Piece& pc = pcs[i];
+    int64_t tri = tri0[i];
+    // Index as written -> 0-based, -1 when absent; relative indices count back
+    // from the vertices read so far (earlier pieces + this one up to the face).
+    auto resolve = [](long idx, int64_t before) -> int64_t {
+      if (idx > 0) return idx - 1;
+      if (idx < 0) return before + idx;
+      return -1;
+    };
+    for (size_t f = 0; f < pc.face_first.size(); ++f) {
+      const int first = pc.face_first[f];
+      const int last = f + 1 < pc.face_first.size() ? pc.face_first[f + 1] : (int)pc.corners.size();
+      const int64_t vb = v0[i] + pc.face_counts[3 * f], tb = t0[i] + pc.face_counts[3 * f + 1],
+                    nb = n0[i] + pc.face_counts[3 * f + 2];
+      for (int k = first + 1; k + 1 < last; ++k) {
+        const int cs[3] = {first, k, k + 1};
+        for (int c = 0; c < 3; ++c) {
+          const obj::Corner& cr = pc.corners[cs[c]];
+          const int64_t iv = resolve(cr.v, vb), it = resolve(cr.t, tb), in = resolve(cr.n, nb);
+          if (iv < 0 || (size_t)iv >= nv || in < 0 || (size_t)in >= nn) {
+            errors[i] = path + ":" + std::to_string(line0[i] + pc.face_line[f]) +
+                        ((iv < 0 || (size_t)iv >= nv) ? ": vertex index out of range"
+                                                      : ": face corner without a normal (vn is required)");
+            return;
+          }
+          float* P = &out->p[9 * (size_t)tri + 3 * c];
+          float* N = &out->n[9 * (size_t)tri + 3 * c];
+          for (int d = 0; d < 3; ++d) {
+            P[d] = v[3 * iv + d];
+            N[d] = vn[3 * in + d];
+          }
+          if (it >= 0 && (size_t)it < nt) {
+            out->uv[6 * (size_t)tri + 2 * c] = vt[2 * it];
+            out->uv[6 * (size_t)tri + 2 * c + 1] = vt[2 * it + 1];
+          }
+        }
+        ++tri;
+      }
+    }
+  });
+  for (const std::string& e : errors)
+    if (!e.empty()) raise(ORION_ERR_PARSE, e);
 }
 
 // meshHandy: inline comma-separated corner data (src/util/strutil.cpp:100-160).
@@ -864,18 +970,28 @@ class Loader {
         parse_spectrum(ap.get("Le"), le);
       }
       // createTriangleMesh (src/core/triangle.cpp:137-151): bake the model
-      // transform into corner positions and (un-normalised) normals.
+      // transform into corner positions and (un-normalised) normals, in
+      // parallel slices of the mesh (each corner's result is independent).
+      const size_t base = out_->positions.size();
+      out_->positions.resize(base + 9 * (size_t)mesh.num_tris);
+      out_->normals.resize(base + 9 * (size_t)mesh.num_tris);
+      out_->uvs.insert(out_->uvs.end(), mesh.uv.begin(), mesh.uv.begin() + 6 * (size_t)mesh.num_tris);
+      {
+        const int hw = (int)std::max(1u, std::thread::hardware_concurrency());
+        const int parts = mesh.num_tris < 65536 ? 1 : hw;
+        std::vector<std::thread> th;
+        for (int pt = 0; pt < parts; ++pt)
+          th.emplace_back([&, pt] {
+            const int64_t b = (int64_t)mesh.num_tris * pt / parts, e = (int64_t)mesh.num_tris * (pt + 1) / parts;
+            for (int64_t c = 3 * b; c < 3 * e; ++c) {
+              t.point(&mesh.p[3 * c], &out_->positions[base + 3 * c]);
+              t.normal(&mesh.n[3 * c], &out_->normals[base + 3 * c]);
+            }
+          });
+        for (auto& x : th) x.join();
+      }
       for (int tri = 0; tri < mesh.num_tris; ++tri) {
         int32_t prim = (int32_t)out_->material_of_prim.size();
-        for (int k = 0; k < 3; ++k) {
-          float p[3], n[3];
-          t.point(&mesh.p[9 * (size_t)tri + 3 * k], p);
-          t.normal(&mesh.n[9 * (size_t)tri + 3 * k], n);
-          out_->positions.insert(out_->positions.end(), p, p + 3);
-          out_->normals.insert(out_->normals.end(), n, n + 3);
-          out_->uvs.push_back(mesh.uv[6 * (size_t)tri + 2 * k]);
-          out_->uvs.push_back(mesh.uv[6 * (size_t)tri + 2 * k + 1]);
-        }
         out_->material_of_prim.push_back(mat);
         if (al) {
           orion_light l;

@@ -141,3 +141,59 @@ def test_scene_from_desc_validates(built):
         og.HostScene.from_arrays(pos, pos, [3], [m], [], cam, 1, 2)        # material index out of range
     s = og.HostScene.from_arrays(pos, pos, [0], [m], [], cam, 1, 2)
     assert s.desc().num_prims == 1
+
+
+def _reference_obj(text):
+    """Straight sequential reading of an OBJ (the rules of the loader): fan triangulation,
+    1-based or relative indices, corners (p, n, uv)."""
+    v, vn, vt, tris = [], [], [], []
+    for line in text.splitlines():
+        f = line.split()
+        if not f:
+            continue
+        if f[0] == "v":
+            v.append([np.float32(x) for x in f[1:4]])
+        elif f[0] == "vn":
+            vn.append([np.float32(x) for x in f[1:4]])
+        elif f[0] == "vt":
+            vt.append([np.float32(x) for x in f[1:3]])
+        elif f[0] == "f":
+            cs = []
+            for c in f[1:]:
+                a = (c.split("/") + ["", ""])[:3]
+                res = lambda s, n: (int(s) - 1 if int(s) > 0 else n + int(s)) if s else -1
+                cs.append((res(a[0], len(v)), res(a[1], len(vt)), res(a[2], len(vn))))
+            for k in range(1, len(cs) - 1):
+                tris.append([cs[0], cs[k], cs[k + 1]])
+    P = np.array([[v[c[0]] for c in t] for t in tris], np.float32).reshape(-1, 9)
+    N = np.array([[vn[c[2]] for c in t] for t in tris], np.float32).reshape(-1, 9)
+    return P, N
+
+
+def test_large_obj_parsed_in_pieces_equals_sequential_reading(built, tmp_path):
+    """A multi-megabyte OBJ (read in parallel pieces) with relative indices and polygons."""
+    import orion_gb300 as og
+    rng = np.random.default_rng(3)
+    lines, nv = [], 0
+    for blk in range(1500):  # blocks of 40 vertices, faces referring back with negative indices
+        pts = rng.uniform(-1, 1, size=(40, 3))
+        lines += ["v %.6f %.6f %.6f" % tuple(p) for p in pts]
+        lines += ["vn %.6f %.6f %.6f" % tuple(p) for p in pts]
+        nv += 40
+        for k in range(30):
+            a, b, c, d = rng.choice(40, 4, replace=False)
+            if k % 3 == 0:  # absolute quad
+                base = nv - 40 + 1
+                lines.append("f %d//%d %d//%d %d//%d %d//%d" % (base + a, base + a, base + b, base + b, base + c,
+                                                              base + c, base + d, base + d))
+            else:  # relative triangle
+                lines.append("f %d//%d %d//%d %d//%d" % (a - 40, a - 40, b - 40, b - 40, c - 40, c - 40))
+    text = "\n".join(lines) + "\n"
+    assert len(text) > (1 << 21)
+    (tmp_path / "big.obj").write_text(text)
+    p = tmp_path / "s.ori"
+    p.write_text(GOOD.replace('type="meshHandy"', 'type="mesh" filename="big.obj"'))
+    a = og.HostScene.load(str(p)).arrays()
+    P, N = _reference_obj(text)
+    assert a["positions"].shape == P.shape
+    assert np.array_equal(a["positions"], P) and np.array_equal(a["normals"], N)
