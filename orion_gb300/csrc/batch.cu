@@ -49,6 +49,8 @@ __global__ void k_b_plan(BatchView b) {
   c.counters[CNT_FETCH_EXT] = 0;
   c.counters[CNT_FETCH_SH] = 0;
   c.counters[CNT_FETCH_MIS] = 0;
+  c.counters[CNT_MIS_ENV] = 0;
+  c.counters[CNT_FETCH_MIS_ENV] = 0;
   for (int k = 0; k < kShadeClasses; ++k) c.counters[CNT_CLS0 + k] = 0;
 }
 
@@ -93,7 +95,8 @@ __global__ void k_b_regen(WaveView w, BatchView b, const uint32_t* sobol) {
   }
 }
 
-// kind 0: extension rays (current queue), 1: shadow rays, 2: MIS rays.
+// kind 0: extension rays (current queue), 1: shadow rays, 2: MIS rays towards
+// area lights, 3: MIS rays towards environment lights (occlusion).
 template <int SMEM>
 __global__ void __launch_bounds__(512, 2) k_b_trace(WaveView w, BatchView b, int kind, int refill_below) {
   extern __shared__ int2 stack_smem[];
@@ -108,12 +111,16 @@ __global__ void __launch_bounds__(512, 2) k_b_trace(WaveView w, BatchView b, int
     n = c.counters[CNT_SH];
     trace_persistent<true, SMEM>(js, w.q_sh, n, &c.counters[CNT_FETCH_SH], w.sh_o, w.sh_d,
                                  F4{nullptr}, w.occluded, stack_smem, refill_below);
-  } else {
+  } else if (kind == 2) {
     n = c.counters[CNT_MIS];
     trace_persistent<false, SMEM>(js, w.q_mis, n, &c.counters[CNT_FETCH_MIS], w.mis_o, w.mis_d,
                                   F4{w.mis_hit}, nullptr, stack_smem, refill_below);
+  } else {  // 3: MIS rays towards environment lights, occlusion only
+    n = c.counters[CNT_MIS_ENV];
+    trace_persistent<true, SMEM>(js, w.q_mis_env, n, &c.counters[CNT_FETCH_MIS_ENV], w.mis_o, w.mis_d,
+                                 F4{nullptr}, w.mis_occluded, stack_smem, refill_below);
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&c.rays[kind], (unsigned long long)n);
+  if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&c.rays[kind < 3 ? kind : 2], (unsigned long long)n);
 }
 
 // Shading of the slots whose extension ray hit a material of class SC (or
@@ -135,6 +142,7 @@ __global__ void __launch_bounds__(128, 5) k_b_shade(WaveView w, BatchView b, con
     queue_append(&c.counters[CNT_NEE], w.q_nee, pid, r.did_nee);
     queue_append(&c.counters[CNT_SH], w.q_sh, pid, r.want_sh);
     queue_append(&c.counters[CNT_MIS], w.q_mis, pid, r.want_mis);
+    queue_append(&c.counters[CNT_MIS_ENV], w.q_mis_env, pid, r.want_mis_env);
     queue_append(&c.counters[CNT_EXT0 + (cur ^ 1)], w.q_ext[cur ^ 1], pid, r.alive);
     queue_append(&c.counters[CNT_RETIRE], b.q_retire, pid, !r.alive);
   }
@@ -287,6 +295,7 @@ void enqueue_iteration(const WaveView& w, const BatchView& b, const uint32_t* so
   end();
   begin(ST_TRACE_MIS);
   b_trace(cfg, w, b, 2, tgrid, stream);
+  b_trace(cfg, w, b, 3, tgrid, stream);
   end();
   begin(ST_RESOLVE);
   k_b_resolve<<<sgrid, cfg.shade_block, 0, stream>>>(w, b);

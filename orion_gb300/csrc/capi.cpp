@@ -240,7 +240,7 @@ static int ensure_wave(orion_gpu_ctx* c, int capacity) {
   auto round256 = [](size_t b) { return (b + 255) & ~(size_t)255; };
   const size_t recb = round256(n * sizeof(PathRec)), neeb = round256(n * sizeof(NeeRec));
   const size_t f4 = round256(n * sizeof(float4)), i4 = round256(n * sizeof(int));
-  const size_t bytes = recb + neeb + f4 + (6 + kShadeClasses) * i4 + 256 + 4096;
+  const size_t bytes = recb + neeb + f4 + (8 + kShadeClasses) * i4 + 256 + 4096;
   int rc = c->wave.block.alloc(bytes);
   if (rc != ORION_OK) {
     c->wave.capacity = 0;
@@ -276,7 +276,8 @@ static int ensure_wave(orion_gpu_ctx* c, int capacity) {
   w.sh_d = nee4(offsetof(NeeRec, sh_d));
   w.mis_o = nee4(offsetof(NeeRec, mis_o));
   w.mis_d = nee4(offsetof(NeeRec, mis_d));
-  int** i4s[] = {&w.occluded, &w.q_ext[0], &w.q_ext[1], &w.q_nee, &w.q_sh, &w.q_mis};
+  int** i4s[] = {&w.occluded, &w.mis_occluded, &w.q_ext[0], &w.q_ext[1],
+                 &w.q_nee,    &w.q_sh,         &w.q_mis,    &w.q_mis_env};
   for (int** q : i4s) {
     *q = reinterpret_cast<int*>(p);
     p += i4;
@@ -722,7 +723,7 @@ static int run_batch_locked(orion_gpu_ctx* ctx, std::vector<DevJob>& dj, unsigne
   ctx->last.shadow_rays = (int64_t)out.rays[1];
   ctx->last.mis_rays = (int64_t)out.rays[2];
   ctx->last.rays = (int64_t)(out.rays[0] + out.rays[1] + out.rays[2]);
-  ctx->last.kernel_launches = 15LL * out.iterations + 1;  // plan, regen, 3 traces, 7 shades, resolve, retire, control
+  ctx->last.kernel_launches = 16LL * out.iterations + 1;  // plan, regen, 4 traces, 7 shades, resolve, retire, control
   ctx->last.device_ms = ms;
   if (out.error) return fail(ORION_ERR_DEVICE, "batch loop reached its iteration cap");
   if (out.paths_done != total)

@@ -88,6 +88,7 @@ __global__ void __launch_bounds__(128, 5) k_shade(SceneView s, WaveView w, WaveA
     queue_append(w.counters + CNT_NEE, w.q_nee, pid, r.did_nee);
     queue_append(w.counters + CNT_SH, w.q_sh, pid, r.want_sh);
     queue_append(w.counters + CNT_MIS, w.q_mis, pid, r.want_mis);
+    queue_append(w.counters + CNT_MIS_ENV, w.q_mis_env, pid, r.want_mis_env);
     queue_append(out_cnt, out_q, pid, r.alive);
   }
 }
@@ -152,6 +153,7 @@ __global__ void k_reset_bounce_counters(int* counters, int next_ext) {
   if (i == 4) counters[CNT_FETCH_EXT] = 0;
   if (i == 5) counters[CNT_FETCH_SH] = 0;
   if (i == 6) counters[CNT_FETCH_MIS] = 0;
+  if (i == CNT_MIS_ENV || i == CNT_FETCH_MIS_ENV) counters[i] = 0;
   if (i >= CNT_CLS0 && i < CNT_CLS0 + kShadeClasses) counters[i] = 0;
 }
 
@@ -233,7 +235,7 @@ int grid_for(int64_t n, int block, int max_blocks) {
   return (int)(g < 1 ? 1 : g);
 }
 
-enum TraceKind { TK_EXT = 0, TK_SHADOW = 1, TK_MIS = 2 };
+enum TraceKind { TK_EXT = 0, TK_SHADOW = 1, TK_MIS = 2, TK_MIS_ENV = 3 };
 
 template <int SMEM>
 void launch_trace_kernels(int kind, const SceneView& s, const WaveView& w, int cur, const LaunchConfig& cfg,
@@ -248,6 +250,10 @@ void launch_trace_kernels(int kind, const SceneView& s, const WaveView& w, int c
   else if (kind == TK_SHADOW)
     k_trace_sh<SMEM><<<grid, block, smem, stream>>>(s, w.q_sh, w.counters + CNT_SH, w.counters + CNT_FETCH_SH, w.sh_o,
                                                     w.sh_d, w.occluded, w.ray_stats + 1, refill);
+  else if (kind == TK_MIS_ENV)
+    k_trace_sh<SMEM><<<grid, block, smem, stream>>>(s, w.q_mis_env, w.counters + CNT_MIS_ENV,
+                                                    w.counters + CNT_FETCH_MIS_ENV, w.mis_o, w.mis_d,
+                                                    w.mis_occluded, w.ray_stats + 2, refill);
   else
     k_trace<SMEM, NeeF4, F4><<<grid, block, smem, stream>>>(s, w.q_mis, w.counters + CNT_MIS,
                                                             w.counters + CNT_FETCH_MIS, w.mis_o, w.mis_d,
@@ -308,7 +314,9 @@ void launch_wave(const SceneView& s, const WaveView& w, const WaveArgs& a, const
         case SC_MISS: k_shade<SC_MISS><<<sgrid, cfg.shade_block, 0, stream>>>(s, w, a, bounce, cur); break;
         default: break;
       }
+      ++nl;  // one launch per class present
     }
+    --nl;  // end() counts one of them
     end();
     if (bounce < a.max_depth) {
       begin(ST_TRACE_SHADOW);
@@ -316,6 +324,10 @@ void launch_wave(const SceneView& s, const WaveView& w, const WaveArgs& a, const
       end();
       begin(ST_TRACE_MIS);
       trace_dispatch(TK_MIS, s, w, cur, cfg, tgrid, stream);
+      if (s.num_env > 0) {
+        trace_dispatch(TK_MIS_ENV, s, w, cur, cfg, tgrid, stream);
+        ++nl;
+      }
       end();
       begin(ST_RESOLVE);
       k_resolve<<<sgrid, cfg.shade_block, 0, stream>>>(s, w);

@@ -76,6 +76,8 @@ struct WaveView {
   NeeF4 nee_p, nee_beta, nee_ld, nee_f, sh_o, sh_d, mis_o, mis_d;  // fields of nee
   float4* mis_hit;   // MIS ray hit: t, u, v, primitive
   int* occluded;
+  int* mis_occluded;  // MIS ray towards an environment light: anything hit
+  int* q_mis_env;     // MIS rays towards an environment light (occlusion queries)
   int* q_ext[2];     // extension-ray queues (current / next bounce)
   int* q_nee;        // paths that sampled a light this bounce
   int* q_sh;         // shadow rays
@@ -88,7 +90,8 @@ struct WaveView {
 };
 
 enum CounterSlot { CNT_EXT0 = 0, CNT_EXT1 = 1, CNT_NEE = 2, CNT_SH = 3, CNT_MIS = 4, CNT_RETIRE = 5, CNT_FREE = 6,
-                   CNT_FETCH_EXT = 8, CNT_FETCH_SH = 9, CNT_FETCH_MIS = 10, CNT_CLS0 = 16, kCounterSlots = 32 };
+                   CNT_FETCH_EXT = 8, CNT_FETCH_SH = 9, CNT_FETCH_MIS = 10, CNT_MIS_ENV = 11,
+                   CNT_FETCH_MIS_ENV = 12, CNT_CLS0 = 16, kCounterSlots = 32 };
 
 // ------------------------------------------------------------ batched mode
 //

@@ -124,7 +124,7 @@ __device__ __forceinline__ void camera_ray(const DevCamera& c, PathSampler& smp,
 // Writes the path state and NEE records; the caller appends the slot to the
 // queues the result asks for.
 struct ShadeResult {
-  bool alive, did_nee, want_sh, want_mis;
+  bool alive, did_nee, want_sh, want_mis, want_mis_env;
 };
 
 // Lobe kinds a shading class's materials can hold (see prepare_material).
@@ -167,7 +167,7 @@ __device__ __forceinline__ ShadeResult shade_one(const SceneView& s, const WaveV
       }
     }
     bool alive = prim >= 0 && bounce < max_depth;
-    bool did_nee = false, want_sh = false, want_mis = false;
+    bool did_nee = false, want_sh = false, want_mis = false, want_mis_env = false;
     if (alive) {
       const PrimShade& sh = s.prims[prim];
       Hit h = reconstruct(sh, hv.y, hv.z);
@@ -233,10 +233,15 @@ __device__ __forceinline__ ShadeResult shade_one(const SceneView& s, const WaveV
                 }
               }
               if (ok) {
+                // Towards an environment light only an escape counts, so that
+                // ray is an occlusion query over (0, FLT_MAX] (tmax in o.w);
+                // towards an area light the closest hit is needed.
                 V3 mo = offset_ray_origin(h.p, h.ng, wib);
-                w.mis_o[pid] = f4(mo, 0.f);
+                const bool env = (flags & kFlagEnv) != 0;
+                w.mis_o[pid] = f4(mo, env ? kFloatMax : 0.f);
                 w.mis_d[pid] = f4(wib, 0.f);
-                want_mis = true;
+                want_mis = !env;
+                want_mis_env = env;
                 flags |= kFlagMis;
               }
             }
@@ -281,7 +286,7 @@ __device__ __forceinline__ ShadeResult shade_one(const SceneView& s, const WaveV
       w.dim[pid] = (int)(d0 + used);
     }
     w.L[pid] = f4(L, L4.w);  // w holds batched mode's sample index bits
-  return ShadeResult{alive, did_nee, want_sh, want_mis};
+  return ShadeResult{alive, did_nee, want_sh, want_mis, want_mis_env};
 }
 
 // The scene a path slot traces against: one scene for a plain wave, the
@@ -375,12 +380,12 @@ __device__ __forceinline__ void resolve_one(const SceneView& s, const WaveView& 
       float4 fv = w.nee_f[pid];
       V3 fb = xyz(fv);
       float bpdf = ldv.w;
-      float4 mh = w.mis_hit[pid];
-      const int prim = __float_as_int(mh.w);  // primitive hit by the MIS ray, -1 for a miss
-      V3 wi = xyz(w.mis_d[pid]);
       if (fl & kFlagEnv) {
-        if (prim < 0) Ld = Ld + sdiv(mul(fb, ld3(lt.L)) * fv.w, bpdf);
-      } else if (prim >= 0) {
+        if (!w.mis_occluded[pid]) Ld = Ld + sdiv(mul(fb, ld3(lt.L)) * fv.w, bpdf);
+      } else {
+        const float4 mh = w.mis_hit[pid];
+        const int prim = __float_as_int(mh.w);  // primitive hit by the MIS ray, -1 for a miss
+        const V3 wi = xyz(w.mis_d[pid]);
         if (prim == lt.prim) {
           // Triangle::pdf (src/core/triangle.cpp:123-135) on the traced hit.
           const PrimShade& sh = s.prims[prim];
