@@ -87,7 +87,17 @@ typedef struct orion_light {
   float dir[3];            /* distant: unit direction towards which light travels from `from` */
   float l2w[12], w2l[12];  /* spot/env: light<->world, 3x4 row-major */
   float cos_total, cos_falloff; /* spot */
+  int32_t image;           /* env: 0 = constant map, k = the scene's image k - 1 (times L) */
+  int32_t reserved;
 } orion_light;
+
+/* An image of a scene (environment map texels): linear RGB floats, row 0 at
+ * the top, as the reference's ImageMemory holds them (8-bit files: byte / 255,
+ * src/texture/imagetexture.cpp:16-52). */
+typedef struct orion_image {
+  int32_t width, height;
+  const float* rgb;        /* width x height x 3 */
+} orion_image;
 
 /* ---------------------------------------------------------------- camera */
 typedef struct orion_camera {
@@ -115,6 +125,9 @@ typedef struct orion_scene_desc {
   orion_camera camera;
   int32_t spp;                   /* <Integrator> nSamplesPerPixel */
   int32_t max_depth;             /* <Integrator> maxDepth */
+  int32_t num_images;
+  int32_t reserved;
+  const orion_image* images;     /* referenced by orion_light.image */
 } orion_scene_desc;
 
 typedef struct orion_host_scene orion_host_scene;

@@ -29,6 +29,7 @@ namespace port {
 
 constexpr float kPi = 3.14159265358979323846f;     // src/orion.h:52-58
 constexpr float kInvPi = 0.31830988618379067154f;
+constexpr float kInv2Pi = 0.15915494309189533577f;
 constexpr float kPiOver2 = 1.57079632679489661923f;
 constexpr float kPiOver4 = 0.78539816339744830961f;
 constexpr float kEpsilon = 0.000001f;
@@ -663,6 +664,95 @@ Mat makeMat(const orion_material& m) {
 
 // ------------------------------------------------------------------ scene
 
+// findInterval (geometry.h:877-889) over a cdf of `size` entries.
+int findIntervalCdf(const float* cdf, int size, float u) {
+  int first = 0, len = size;
+  while (len > 0) {
+    int half = len >> 1, mid = first + half;
+    if (cdf[mid] <= u) {
+      first = mid + 1;
+      len -= half + 1;
+    } else {
+      len = half;
+    }
+  }
+  return std::max(0, std::min(first - 1, size - 2));
+}
+
+// Distribution1D (sampling.h:71-110).
+struct Distribution1D {
+  std::vector<float> func, cdf;
+  float funcInt = 0;
+  Distribution1D(const float* f, int n) : func(f, f + n), cdf(n + 1) {
+    cdf[0] = 0;
+    for (int i = 1; i < n + 1; ++i) cdf[i] = cdf[i - 1] + func[i - 1] / n;
+    funcInt = cdf[n];
+    if (funcInt == 0)
+      for (int i = 1; i < n + 1; ++i) cdf[i] = float(i) / float(n);
+    else
+      for (int i = 1; i < n + 1; ++i) cdf[i] /= funcInt;
+  }
+  int count() const { return (int)func.size(); }
+  float sampleContinuous(float u, float* pdf, int* off) const {
+    int offset = findIntervalCdf(cdf.data(), (int)cdf.size(), u);
+    if (off) *off = offset;
+    float du = u - cdf[offset];
+    if ((cdf[offset + 1] - cdf[offset]) > 0) du /= (cdf[offset + 1] - cdf[offset]);
+    if (pdf) *pdf = (funcInt > 0) ? func[offset] / funcInt : 0;
+    return (offset + du) / count();
+  }
+};
+
+// Envmap with an image (envmap.cpp:9-44): texels times L, ImageTexture
+// lookups with the default wrap filter (texture.cpp:3-27), Distribution2D
+// (sampling.h:127-151, sampling.cpp:63-76) over intensity x sin(theta).
+struct EnvImage {
+  int w = 0, h = 0;
+  std::vector<V> tex;
+  std::vector<std::unique_ptr<Distribution1D>> cond;
+  std::unique_ptr<Distribution1D> marg;
+  V ave{0.f};
+  V sample(int x, int y) const {
+    x = x >= 0 ? x % w : w - (-x) % w;
+    y = y >= 0 ? y % h : h - (-y) % h;
+    return tex[(size_t)y * w + x];
+  }
+  V sample(float u, float v) const { return sample((int)(u * w), (int)(v * h)); }
+  void build(const orion_image& im, V L) {
+    w = im.width;
+    h = im.height;
+    tex.resize((size_t)w * h);
+    for (size_t i = 0; i < tex.size(); ++i) tex[i] = mul(V(im.rgb[3 * i], im.rgb[3 * i + 1], im.rgb[3 * i + 2]), L);
+    std::vector<float> img((size_t)w * h);
+    for (int j = 0; j < h; ++j) {
+      float v = (j + 0.5f) / (float)h;
+      float sinTheta = std::sin(kPi * v);
+      for (int i = 0; i < w; ++i) {
+        V sp = sample(i, j);
+        img[i + (size_t)j * w] = intensity(sp) * sinTheta;
+        ave = ave + sp;
+      }
+    }
+    ave = V(ave.x / (w * h), ave.y / (w * h), ave.z / (w * h));
+    for (int v = 0; v < h; ++v) cond.emplace_back(new Distribution1D(&img[(size_t)v * w], w));
+    std::vector<float> mf;
+    for (int v = 0; v < h; ++v) mf.push_back(cond[v]->funcInt);
+    marg.reset(new Distribution1D(mf.data(), h));
+  }
+  void sampleContinuous(float u0, float u1, float* su, float* sv, float* pdf) const {
+    float p0, p1;
+    int v;
+    *sv = marg->sampleContinuous(u1, &p1, &v);
+    *su = cond[v]->sampleContinuous(u0, &p0, nullptr);
+    *pdf = p0 * p1;
+  }
+  float pdf(float pu, float pv) const {
+    int iu = std::max(0, std::min(int(pu * cond[0]->count()), cond[0]->count() - 1));
+    int iv = std::max(0, std::min(int(pv * marg->count()), marg->count() - 1));
+    return cond[iv]->func[iu] / marg->funcInt;
+  }
+};
+
 struct Light {
   int type;
   int prim;
@@ -671,6 +761,7 @@ struct Light {
   float l2w[12], w2l[12];
   float cosTotal = 0, cosFalloff = 0;
   float envInt = 0;
+  std::shared_ptr<EnvImage> image;  // image environment map, or null (constant map)
 };
 
 struct Isect {
@@ -721,6 +812,20 @@ struct Scene {
 V mat3(const float* m, V v) {  // Transform applied to a vector (rows of a 3x4)
   return V(m[0] * v.x + m[1] * v.y + m[2] * v.z, m[4] * v.x + m[5] * v.y + m[6] * v.z,
            m[8] * v.x + m[9] * v.y + m[10] * v.z);
+}
+
+// sphericalTheta / sphericalPhi (sampling.h:61-69)
+float sphericalTheta(V v) { return std::acos(clampf(v.z, -1.0f, 1.0f)); }
+float sphericalPhi(V v) {
+  float p = std::atan2(v.y, v.x);
+  return (p < 0) ? (p + 2 * kPi) : p;
+}
+
+// Envmap::Le (envmap.cpp:44-49)
+V envLe(const Light& L, V d) {
+  if (!L.image) return L.L;
+  V w = normalize(mat3(L.w2l, d));
+  return L.image->sample(sphericalPhi(w) * kInv2Pi, sphericalTheta(w) * kInvPi);
 }
 
 // Distribution1D::sampleDiscrete with findInterval (sampling.h:113-121, geometry.h:877-889)
@@ -809,7 +914,21 @@ LS sampleLi(const Scene& s, const Light& L, const Isect& it, float u0, float u1)
       r.pLight = it.p + L.dir * (2 * s.worldRadius);
       r.Li = L.L;
       return r;
-    case ORION_LIGHT_ENV: {  // envmap.cpp:45-60, constant map (1x1 distribution: uv = u, mapPdf = 1)
+    case ORION_LIGHT_ENV: {  // envmap.cpp:50-68
+      if (L.image) {
+        float su, sv, mapPdf;
+        L.image->sampleContinuous(u0, u1, &su, &sv, &mapPdf);
+        if (mapPdf == 0) return r;
+        float theta = sv * kPi, phi = su * 2 * kPi;
+        float ct = std::cos(theta), st = std::sin(theta), sp = std::sin(phi), cp = std::cos(phi);
+        r.wi = mat3(L.l2w, V(st * cp, st * sp, ct));
+        r.pdf = mapPdf / (2 * kPi * kPi * st);
+        if (st == 0) r.pdf = 0;
+        r.pLight = it.p + r.wi * (2 * s.worldRadius);
+        r.Li = L.image->sample(su, sv);
+        return r;
+      }
+      // constant map (1x1 distribution: uv = u, mapPdf = 1)
       if (L.envInt == 0) return r;
       float theta = u1 * kPi, phi = u0 * 2 * kPi;
       float ct = std::cos(theta), st = std::sin(theta), sp = std::sin(phi), cp = std::cos(phi);
@@ -868,9 +987,11 @@ V estimateDirect(const Scene& s, V rayD, const Isect& it, const Mat& m, const Fr
         lightPdf = len_sq(it.p - in.p) / (absdot(in.ng, -wi) * L.area);
         if (std::isinf(lightPdf)) lightPdf = 0;
       } else {  // Envmap::pdf_Li (envmap.cpp:70-80)
+        // v = theta / (2 pi) and no early return at sin(theta) == 0, as written there.
         V w = mat3(L.w2l, wi);
         float theta = std::acos(clampf(w.z, -1.0f, 1.0f));
-        lightPdf = 1 / (2 * kPi * kPi * std::sin(theta));
+        float mapPdf = L.image ? L.image->pdf(sphericalPhi(w) * kInv2Pi, theta * kInv2Pi) : 1.0f;
+        lightPdf = mapPdf / (2 * kPi * kPi * std::sin(theta));
       }
       if (lightPdf == 0) return Ld;
       float weight = powerHeuristic(bsdfPdfv, lightPdf);
@@ -880,7 +1001,7 @@ V estimateDirect(const Scene& s, V rayD, const Isect& it, const Mat& m, const Fr
       if (hit) {
         if (s.lightOf[in.prim] == li) Li = dot(in.ng, -wi) > 0 ? L.L : V(0.f);
       } else {
-        if (L.type == ORION_LIGHT_ENV) Li = L.L;
+        if (L.type == ORION_LIGHT_ENV) Li = envLe(L, wi);
       }
       if (!black(Li)) Ld = Ld + sdiv(mul(f, Li) * weight, bsdfPdfv);
     }
@@ -935,7 +1056,7 @@ V Li(const Scene& s, V ro, V rd, Sampler& smp, int maxDepth, int rrDepth, int64_
         int li = s.lightOf[it.prim];
         if (li >= 0 && dot(it.ng, -rd) > 0) L = L + mul(beta, s.lights[li].L);
       } else {
-        for (int e : s.envs) L = L + mul(beta, s.lights[e].L);
+        for (int e : s.envs) L = L + mul(beta, envLe(s.lights[e], rd));
       }
     }
     if (!found || bounces >= maxDepth) break;
@@ -1025,7 +1146,13 @@ Scene* makeScene(const orion_scene_desc* d) {
         break;
       case ORION_LIGHT_ENV:
         L.envInt = intensity(L.L) * std::sin(kPi * 0.5f);
-        pw = L.L * (kPi * r * r);
+        if (o.image > 0) {
+          L.image = std::make_shared<EnvImage>();
+          L.image->build(d->images[o.image - 1], L.L);
+          pw = L.image->ave * (kPi * r * r);
+        } else {
+          pw = L.L * (kPi * r * r);
+        }
         s->envs.push_back(i);
         break;
     }

@@ -53,7 +53,11 @@ class Material(C.Structure):
 class Light(C.Structure):
     _fields_ = [("type", C.c_int32), ("prim", C.c_int32), ("L", C.c_float * 3), ("p", C.c_float * 3),
                 ("dir", C.c_float * 3), ("l2w", C.c_float * 12), ("w2l", C.c_float * 12),
-                ("cos_total", C.c_float), ("cos_falloff", C.c_float)]
+                ("cos_total", C.c_float), ("cos_falloff", C.c_float), ("image", C.c_int32), ("reserved", C.c_int32)]
+
+
+class Image(C.Structure):
+    _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("rgb", C.c_void_p)]
 
 
 class Camera(C.Structure):
@@ -65,7 +69,8 @@ class SceneDesc(C.Structure):
     _fields_ = [("num_prims", C.c_int64), ("positions", C.c_void_p), ("normals", C.c_void_p), ("uvs", C.c_void_p),
                 ("material_of_prim", C.c_void_p), ("light_of_prim", C.c_void_p), ("num_materials", C.c_int32),
                 ("num_lights", C.c_int32), ("materials", C.c_void_p), ("lights", C.c_void_p), ("camera", Camera),
-                ("spp", C.c_int32), ("max_depth", C.c_int32)]
+                ("spp", C.c_int32), ("max_depth", C.c_int32), ("num_images", C.c_int32), ("reserved", C.c_int32),
+                ("images", C.c_void_p)]
 
 
 class GpuOpts(C.Structure):
@@ -207,7 +212,8 @@ class HostScene:
 
     @classmethod
     def from_arrays(cls, positions, normals, material_of_prim, materials, lights, camera: Camera, spp: int,
-                    max_depth: int, light_of_prim=None, uvs=None) -> "HostScene":
+                    max_depth: int, light_of_prim=None, uvs=None, images=None) -> "HostScene":
+        """images: list of (H, W, 3) float arrays, referenced 1-based by Light.image."""
         pos = np.ascontiguousarray(positions, dtype=np.float32).reshape(-1, 9)
         nrm = np.ascontiguousarray(normals, dtype=np.float32).reshape(-1, 9)
         mop = np.ascontiguousarray(material_of_prim, dtype=np.int32)
@@ -222,6 +228,9 @@ class HostScene:
         d.num_materials, d.num_lights = len(materials), len(lights)
         d.materials, d.lights = C.addressof(mats), C.addressof(lts)
         d.camera, d.spp, d.max_depth = camera, spp, max_depth
+        imgs = [np.ascontiguousarray(im, np.float32) for im in (images or [])]
+        recs = (Image * max(1, len(imgs)))(*[Image(im.shape[1], im.shape[0], im.ctypes.data) for im in imgs])
+        d.num_images, d.images = len(imgs), C.addressof(recs)
         h = C.c_void_p()
         _check(library().orion_scene_from_desc(C.byref(d), C.byref(h)))
         return cls(h.value)
@@ -250,6 +259,8 @@ class HostScene:
                           for i in range(d.num_materials)],
             "lights": [Light.from_buffer_copy(C.cast(d.lights, C.POINTER(Light))[i]) for i in range(d.num_lights)],
             "camera": d.camera, "spp": d.spp, "max_depth": d.max_depth,
+            "images": [arr(im.rgb, 3 * im.width * im.height, np.float32).reshape(im.height, im.width, 3)
+                       for im in (C.cast(d.images, C.POINTER(Image))[i] for i in range(d.num_images))],
         }
 
     def __del__(self):

@@ -105,7 +105,7 @@ struct DevBuf {
 };
 
 struct DeviceScene {
-  DevBuf nodes, woop, tri_prim, tri_class, prims, mats, lights, lfunc, lcdf;
+  DevBuf nodes, woop, tri_prim, tri_class, prims, mats, lights, lfunc, lcdf, env_data, envmaps;
   SceneView view{};
   int64_t bytes = 0;
   int64_t num_prims = 0;
@@ -416,6 +416,14 @@ extern "C" int orion_gpu_scene_upload(orion_gpu_ctx* ctx, const orion_host_scene
   if ((rc = upload(d->lights, ps.lights, ctx->stream, &bytes)) != ORION_OK) return rc;
   if ((rc = upload(d->lfunc, ps.light_func, ctx->stream, &bytes)) != ORION_OK) return rc;
   if ((rc = upload(d->lcdf, ps.light_cdf, ctx->stream, &bytes)) != ORION_OK) return rc;
+  // Image environment maps: the float block, then their records pointing into it.
+  if ((rc = upload(d->env_data, ps.env_data, ctx->stream, &bytes)) != ORION_OK) return rc;
+  std::vector<DevEnvMap> envs;
+  const float* eb = d->env_data.as<float>();
+  for (const PreparedScene::EnvMapLayout& e : ps.envmaps)
+    envs.push_back(DevEnvMap{e.width, e.height, e.marg_int, 0, eb + e.texels, eb + e.cond_func, eb + e.cond_cdf,
+                             eb + e.cond_int, eb + e.marg_func, eb + e.marg_cdf});
+  if ((rc = upload(d->envmaps, envs, ctx->stream, &bytes)) != ORION_OK) return rc;
   CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   SceneView& v = d->view;
   v.nodes = d->nodes.as<float4>();
@@ -427,6 +435,7 @@ extern "C" int orion_gpu_scene_upload(orion_gpu_ctx* ctx, const orion_host_scene
   v.lights = d->lights.as<DevLight>();
   v.light_func = d->lfunc.as<float>();
   v.light_cdf = d->lcdf.as<float>();
+  v.envmaps = d->envmaps.as<DevEnvMap>();
   v.light_func_int = ps.light_func_int;
   v.num_lights = (int)ps.lights.size();
   v.num_env = (int)ps.env_idx.size();

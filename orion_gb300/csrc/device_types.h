@@ -91,7 +91,7 @@ struct DevLight {      // 128 bytes
   int32_t prim;        // area: emissive primitive
   float area;          // area: triangle area (src/core/triangle.cpp:77-83);
                        // env: intensity of the constant map (0 disables sampling)
-  float pad0;
+  int32_t image;       // env: index of its DevEnvMap, -1 for a constant map
   float L[3];          // Le / I / L
   float pad1;
   float p[3];          // point/spot position; distant: direction
@@ -100,6 +100,22 @@ struct DevLight {      // 128 bytes
   float minv[9];       // env: world->light 3x3
   float cos_total, cos_falloff;
   float pad3[2];
+};
+
+// An image environment map (src/light/envmap.cpp:9-44): texels already
+// scaled by L, and the Distribution2D (src/sampler/sampling.h:127-151,
+// sampling.cpp:63-76) over intensity x sin(theta) of each texel: one
+// conditional Distribution1D per row and the marginal over the rows.
+struct DevEnvMap {
+  int32_t width, height;
+  float marg_int;          // marginal funcInt
+  int32_t pad;
+  const float* texels;     // width x height x 3, row 0 at the top
+  const float* cond_func;  // height rows of width
+  const float* cond_cdf;   // height rows of width + 1
+  const float* cond_int;   // height
+  const float* marg_func;  // height
+  const float* marg_cdf;   // height + 1
 };
 
 struct DevCamera {

@@ -16,6 +16,7 @@ struct SceneView {
   const PrimShade* prims;
   const DevMaterial* mats;
   const DevLight* lights;
+  const DevEnvMap* envmaps;  // image environment maps (DevLight::image)
   const float* light_func;
   const float* light_cdf;
   float light_func_int;

@@ -49,11 +49,62 @@ __device__ __forceinline__ V3 mat3_mul(const float* m, V3 v) {
             m[6] * v.x + m[7] * v.y + m[8] * v.z};
 }
 
+// ------------------------------------------------ image environment maps
+
+// Distribution1D::sampleContinuous (src/sampler/sampling.h:93-109).
+__device__ __forceinline__ float dist1d_sample(const float* func, const float* cdf, int n, float func_int, float u,
+                                               float* pdf, int* off) {
+  const int offset = find_interval(cdf, n + 1, u);
+  if (off) *off = offset;
+  const float c0 = __ldg(cdf + offset), c1 = __ldg(cdf + offset + 1);
+  float du = u - c0;
+  if (c1 - c0 > 0.f) du /= (c1 - c0);
+  *pdf = func_int > 0.f ? __ldg(func + offset) / func_int : 0.f;
+  return (offset + du) / n;
+}
+
+// Distribution2D::SampleContinuous (src/sampler/sampling.h:131-138): the
+// marginal picks the row with u1, the row's conditional the column with u0.
+__device__ __forceinline__ void dist2d_sample(const DevEnvMap& e, float u0, float u1, float* su, float* sv,
+                                              float* pdf) {
+  float p0, p1;
+  int v;
+  *sv = dist1d_sample(e.marg_func, e.marg_cdf, e.height, e.marg_int, u1, &p1, &v);
+  *su = dist1d_sample(e.cond_func + (size_t)v * e.width, e.cond_cdf + (size_t)v * (e.width + 1), e.width,
+                      __ldg(e.cond_int + v), u0, &p0, nullptr);
+  *pdf = p0 * p1;
+}
+
+// Distribution2D::Pdf (src/sampler/sampling.h:139-145).
+__device__ __forceinline__ float dist2d_pdf(const DevEnvMap& e, float pu, float pv) {
+  const int iu = min(max((int)(pu * e.width), 0), e.width - 1);
+  const int iv = min(max((int)(pv * e.height), 0), e.height - 1);
+  return __ldg(e.cond_func + (size_t)iv * e.width + iu) / e.marg_int;
+}
+
+// Texture::sample(u, v) with the default wrap filter (src/core/texture.cpp:3-7,
+// 12-27) on an ImageTexture (src/texture/imagetexture.cpp:4-11).
+__device__ __forceinline__ V3 env_texel(const DevEnvMap& e, float u, float v) {
+  int x = (int)(u * e.width), y = (int)(v * e.height);
+  x = x >= 0 ? x % e.width : e.width - (-x) % e.width;
+  y = y >= 0 ? y % e.height : e.height - (-y) % e.height;
+  const float* t = e.texels + 3 * ((size_t)y * e.width + x);
+  return V3{__ldg(t), __ldg(t + 1), __ldg(t + 2)};
+}
+
+// Envmap::Le (src/light/envmap.cpp:44-49): the map in the direction of `d`.
+__device__ __forceinline__ V3 env_le(const DevLight& L, const DevEnvMap* envmaps, V3 d) {
+  if (L.image < 0) return ld3(L.L);
+  const V3 w = normalize(mat3_mul(L.minv, d));
+  return env_texel(envmaps[L.image], spherical_phi(w) * kInv2Pi, spherical_theta(w) * kInvPi);
+}
+
 // Light::sample_Li for every light type. `prims` gives the emissive
 // triangle of an area light; `world_radius` bounds the scene for distant and
 // environment lights (Bounds3::boundingSphere, src/core/geometry.h:551-554).
-static __device__ __noinline__ LightSample sample_li(const DevLight& L, const PrimShade* __restrict__ prims, V3 ref_p,
-                                                 float u0, float u1, float world_radius) {
+static __device__ __noinline__ LightSample sample_li(const DevLight& L, const PrimShade* __restrict__ prims,
+                                                    const DevEnvMap* envmaps, V3 ref_p, float u0, float u1,
+                                                    float world_radius) {
   LightSample s;
   s.valid = false;
   s.pdf = 0.f;
@@ -126,7 +177,23 @@ static __device__ __noinline__ LightSample sample_li(const DevLight& L, const Pr
       s.valid = true;
       return s;
     }
-    case DL_ENV: {  // constant map: src/light/envmap.cpp:45-60 with a 1x1 Distribution2D
+    case DL_ENV: {  // src/light/envmap.cpp:50-68
+      if (L.image >= 0) {
+        const DevEnvMap& e = envmaps[L.image];
+        float su, sv, map_pdf;
+        dist2d_sample(e, u0, u1, &su, &sv, &map_pdf);
+        if (map_pdf == 0.f) return s;
+        const float theta = sv * kPi, phi = su * 2.f * kPi;
+        const float ct = cosf(theta), st = sinf(theta), sp = sinf(phi), cp = cosf(phi);
+        s.wi = mat3_mul(L.m, V3{st * cp, st * sp, ct});
+        s.pdf = map_pdf / (2.f * kPi * kPi * st);
+        if (st == 0.f) s.pdf = 0.f;
+        s.p_light = ref_p + s.wi * (2.f * world_radius);
+        s.Li = env_texel(e, su, sv);
+        s.valid = true;
+        return s;
+      }
+      // Constant map: a 1x1 Distribution2D (uv = u, mapPdf = 1).
       if (L.area == 0.f) return s;  // zero-intensity map: the distribution's pdf is 0
       float theta = u1 * kPi, phi = u0 * 2.f * kPi;
       float ct = cosf(theta), st = sinf(theta), sp = sinf(phi), cp = cosf(phi);
@@ -142,12 +209,16 @@ static __device__ __noinline__ LightSample sample_li(const DevLight& L, const Pr
   return s;
 }
 
-// Envmap::pdf_Li for the constant map (src/light/envmap.cpp:70-80).
-__device__ __forceinline__ float env_pdf_li(const DevLight& L, V3 wi) {
+// Envmap::pdf_Li (src/light/envmap.cpp:70-80). As written there, the map's
+// v coordinate is theta / (2 pi) (not theta / pi), and its sin(theta) == 0
+// test compares a function with 0, so it never returns early.
+__device__ __forceinline__ float env_pdf_li(const DevLight& L, const DevEnvMap* envmaps, V3 wi) {
   V3 w = mat3_mul(L.minv, wi);
   float theta = spherical_theta(w);
   float st = sinf(theta);
-  return 1.f / (2.f * kPi * kPi * st);
+  if (L.image < 0) return 1.f / (2.f * kPi * kPi * st);  // constant map: Pdf = 1
+  const float phi = spherical_phi(w);
+  return dist2d_pdf(envmaps[L.image], phi * kInv2Pi, theta * kInv2Pi) / (2.f * kPi * kPi * st);
 }
 
 __device__ __forceinline__ bool is_delta_light(int kind) { return kind == DL_POINT || kind == DL_SPOT || kind == DL_DISTANT; }

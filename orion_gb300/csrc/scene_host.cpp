@@ -17,6 +17,7 @@
 // (image textures and envmaps, SPD files, named metals, sppm and pseudo
 // samplers) are reported as ORION_ERR_UNSUPPORTED instead of being loaded.
 #include "scene_host.h"
+#include "image_io.h"
 
 #include <algorithm>
 #include <atomic>
@@ -1094,10 +1095,27 @@ class Loader {
     for (const XmlNode* en : root_->all("Envmap")) {
       Xform transform = transform_of(en);
       ParamMap ps = params_of(en);
-      if (ps.has("name")) raise(ORION_ERR_UNSUPPORTED, "image environment maps are not supported");
       orion_light l;
       std::memset(&l, 0, sizeof(l));
       l.type = ORION_LIGHT_ENV;
+      if (ps.has("name")) {
+        // Envmap(...) reads the image from the resource directory
+        // (src/light/envmap.cpp:120, :14-22; src/texture/imagetexture.cpp:28-52).
+        const std::string file = res_dir_ + trim(ps.get("name"));
+        Image8 im8;
+        std::string ierr;
+        if (!load_image8(file, &im8, &ierr)) raise(ORION_ERR_IO, ierr);
+        if (im8.channels != 3 && im8.channels != 4)
+          raise(ORION_ERR_UNSUPPORTED, file + ": only 3- or 4-channel images are read by the reference");
+        HostImage hi;
+        hi.width = im8.width;
+        hi.height = im8.height;
+        hi.rgb.resize(im8.rgb.size());
+        const float inv255 = 0.0039215686274509803921568627451f;  // color_CharToFloat
+        for (size_t i = 0; i < im8.rgb.size(); ++i) hi.rgb[i] = im8.rgb[i] * inv255;
+        out_->images.push_back(std::move(hi));
+        l.image = (int32_t)out_->images.size();
+      }
       if (ps.has("L"))
         parse_spectrum(ps.get("L"), l.L);
       else
@@ -1142,11 +1160,19 @@ void HostScene::desc(orion_scene_desc* d) const {
   d->camera = camera;
   d->spp = spp;
   d->max_depth = max_depth;
+  d->num_images = (int32_t)image_desc.size();
+  d->images = image_desc.empty() ? nullptr : image_desc.data();
+}
+
+void HostScene::index_images() {
+  image_desc.clear();
+  for (const HostImage& im : images) image_desc.push_back(orion_image{im.width, im.height, im.rgb.data()});
 }
 
 int load_ori(const std::string& path, HostScene* out, std::string* err) {
   try {
     Loader(path, out).run();
+    out->index_images();
   } catch (const LoadError& e) {
     *err = e.msg;
     return e.code;
@@ -1188,6 +1214,29 @@ int scene_from_desc(const orion_scene_desc& d, HostScene* out, std::string* err)
     out->light_of_prim.assign(T, -1);
   out->materials.assign(d.materials, d.materials + d.num_materials);
   out->lights.assign(d.lights, d.lights + d.num_lights);
+  if (d.num_images < 0 || (d.num_images > 0 && !d.images)) {
+    *err = "scene description: bad image array";
+    return ORION_ERR_INVALID;
+  }
+  out->images.clear();
+  for (int i = 0; i < d.num_images; ++i) {
+    const orion_image& im = d.images[i];
+    if (im.width <= 0 || im.height <= 0 || !im.rgb || (int64_t)im.width * im.height > (1LL << 28)) {
+      *err = "scene description: bad image " + std::to_string(i);
+      return ORION_ERR_INVALID;
+    }
+    HostImage hi;
+    hi.width = im.width;
+    hi.height = im.height;
+    hi.rgb.assign(im.rgb, im.rgb + 3 * (size_t)im.width * im.height);
+    out->images.push_back(std::move(hi));
+  }
+  out->index_images();
+  for (const orion_light& l : out->lights)
+    if (l.image < 0 || l.image > d.num_images || (l.image > 0 && l.type != ORION_LIGHT_ENV)) {
+      *err = "scene description: light image index out of range";
+      return ORION_ERR_INVALID;
+    }
   for (size_t i = 0; i < T; ++i) {
     if (out->material_of_prim[i] < 0 || out->material_of_prim[i] >= d.num_materials) {
       *err = "scene description: material index out of range at primitive " + std::to_string(i);

@@ -40,6 +40,11 @@ struct Xform {
   static Xform look_at(const float pos[3], const float look[3], const float up[3]);
 };
 
+struct HostImage {
+  int32_t width = 0, height = 0;
+  std::vector<float> rgb;         // width x height x 3, row 0 at the top
+};
+
 struct HostScene {
   std::vector<float> positions;   // T x 9
   std::vector<float> normals;     // T x 9
@@ -48,6 +53,8 @@ struct HostScene {
   std::vector<int32_t> light_of_prim;
   std::vector<orion_material> materials;
   std::vector<orion_light> lights;
+  std::vector<HostImage> images;   // environment map texels (orion_light.image = index + 1)
+  std::vector<orion_image> image_desc;  // views of `images` for desc()
   orion_camera camera{};
   int32_t spp = 1;
   int32_t max_depth = 5;
@@ -55,6 +62,7 @@ struct HostScene {
 
   int64_t num_prims() const { return (int64_t)material_of_prim.size(); }
   void desc(orion_scene_desc* out) const;
+  void index_images();  // refresh image_desc after `images` changes
 };
 
 // Returns ORION_OK or an error code; `err` receives a message.

@@ -211,6 +211,68 @@ DevMaterial prepare_material(const orion_material& mt) {
   return m;
 }
 
+namespace {
+
+// Distribution1D (src/sampler/sampling.h:71-90): func, cdf (n + 1), funcInt.
+float dist1d(const float* f, int n, float* func, float* cdf) {
+  for (int i = 0; i < n; ++i) func[i] = f[i];
+  cdf[0] = 0.f;
+  for (int i = 1; i < n + 1; ++i) cdf[i] = cdf[i - 1] + func[i - 1] / n;
+  const float func_int = cdf[n];
+  if (func_int == 0.f) {
+    for (int i = 1; i < n + 1; ++i) cdf[i] = float(i) / float(n);
+  } else {
+    for (int i = 1; i < n + 1; ++i) cdf[i] /= func_int;
+  }
+  return func_int;
+}
+
+// Envmap::Envmap for an image (src/light/envmap.cpp:9-44): texels times L,
+// the sampling function intensity(texel) * sin(theta) per texel, and the
+// Distribution2D over it (sampling.cpp:63-76). Returns the average texel.
+void prepare_envmap(const HostImage& im, const float L[3], PreparedScene* out, float ave[3]) {
+  const int w = im.width, h = im.height;
+  const size_t n = (size_t)w * h;
+  PreparedScene::EnvMapLayout lay;
+  lay.width = w;
+  lay.height = h;
+  std::vector<float>& d = out->env_data;
+  lay.texels = d.size();
+  d.resize(d.size() + 3 * n);
+  for (size_t i = 0; i < n; ++i)
+    for (int k = 0; k < 3; ++k) d[lay.texels + 3 * i + k] = im.rgb[3 * i + k] * L[k];
+  std::vector<float> img(n);
+  float sum[3] = {0.f, 0.f, 0.f};
+  for (int j = 0; j < h; ++j) {
+    const float v = (j + 0.5f) / (float)h;
+    const float sin_theta = std::sin(kPiF * v);
+    for (int i = 0; i < w; ++i) {
+      const float* t = &d[lay.texels + 3 * ((size_t)j * w + i)];
+      img[i + (size_t)j * w] = spectrum_intensity(t) * sin_theta;
+      for (int k = 0; k < 3; ++k) sum[k] += t[k];
+    }
+  }
+  for (int k = 0; k < 3; ++k) ave[k] = sum[k] / (float)(w * h);
+  lay.cond_func = d.size();
+  d.resize(d.size() + n);
+  lay.cond_cdf = d.size();
+  d.resize(d.size() + (size_t)h * (w + 1));
+  lay.cond_int = d.size();
+  d.resize(d.size() + h);
+  for (int j = 0; j < h; ++j)
+    d[lay.cond_int + j] = dist1d(&img[(size_t)j * w], w, &d[lay.cond_func + (size_t)j * w],
+                                 &d[lay.cond_cdf + (size_t)j * (w + 1)]);
+  std::vector<float> marginal(d.begin() + lay.cond_int, d.begin() + lay.cond_int + h);
+  lay.marg_func = d.size();
+  d.resize(d.size() + h);
+  lay.marg_cdf = d.size();
+  d.resize(d.size() + h + 1);
+  lay.marg_int = dist1d(marginal.data(), h, &d[lay.marg_func], &d[lay.marg_cdf]);
+  out->envmaps.push_back(lay);
+}
+
+}  // namespace
+
 bool prepare_scene(const HostScene& s, PreparedScene* out, std::string* err) {
   const int64_t T = s.num_prims();
   out->prims.resize(T);
@@ -248,6 +310,8 @@ bool prepare_scene(const HostScene& s, PreparedScene* out, std::string* err) {
   const float pi = kPiF, r = out->world_radius;
   out->lights.clear();
   out->env_idx.clear();
+  out->env_data.clear();
+  out->envmaps.clear();
   std::vector<float> power;
   for (size_t i = 0; i < s.lights.size(); ++i) {
     const orion_light& l = s.lights[i];
@@ -295,16 +359,26 @@ bool prepare_scene(const HostScene& s, PreparedScene* out, std::string* err) {
         for (int k = 0; k < 3; ++k) pw[k] = l.L[k] * pi * r * r;
         break;
       }
-      case ORION_LIGHT_ENV: {  // src/light/envmap.cpp:9-44, 62-65 (constant map)
+      case ORION_LIGHT_ENV: {  // src/light/envmap.cpp:9-44, 62-65
         d.kind = DL_ENV;
         for (int rr = 0; rr < 3; ++rr)
           for (int c = 0; c < 3; ++c) {
             d.m[3 * rr + c] = l.l2w[4 * rr + c];
             d.minv[3 * rr + c] = l.w2l[4 * rr + c];
           }
+        float ave[3] = {l.L[0], l.L[1], l.L[2]};  // constant map: the one texel is L
+        d.image = -1;
+        if (l.image > 0) {
+          if (l.image > (int)s.images.size()) {
+            *err = "environment light references a missing image";
+            return false;
+          }
+          d.image = (int)out->envmaps.size();
+          prepare_envmap(s.images[l.image - 1], l.L, out, ave);
+        }
         d.area = spectrum_intensity(l.L) * std::sin(pi * 0.5f);
         float f = pi * r * r;
-        for (int k = 0; k < 3; ++k) pw[k] = l.L[k] * f;
+        for (int k = 0; k < 3; ++k) pw[k] = ave[k] * f;
         out->env_idx.push_back((int)i);
         break;
       }

@@ -17,6 +17,15 @@ struct PreparedScene {
   float world_center[3] = {0, 0, 0};
   float world_radius = 0.f;
   DevCamera cam{};
+  // Image environment maps: every array in one float block; DevEnvMap
+  // pointers are these offsets until the block is uploaded.
+  std::vector<float> env_data;
+  struct EnvMapLayout {
+    int width, height;
+    float marg_int;
+    size_t texels, cond_func, cond_cdf, cond_int, marg_func, marg_cdf;
+  };
+  std::vector<EnvMapLayout> envmaps;
 };
 
 // Materials -> lobe lists (Material::getBSDF, src/material/*.cpp).

@@ -163,7 +163,7 @@ __device__ __forceinline__ ShadeResult shade_one(const SceneView& s, const WaveV
           if (dot(ng, -rd) > 0.f) L = L + mul(beta, ld3(s.lights[li].L));
         }
       } else {
-        for (int e = 0; e < s.num_env; ++e) L = L + mul(beta, ld3(s.lights[s.env_idx[e]].L));
+        for (int e = 0; e < s.num_env; ++e) L = L + mul(beta, env_le(s.lights[s.env_idx[e]], s.envmaps, rd));
       }
     }
     bool alive = prim >= 0 && bounce < max_depth;
@@ -193,7 +193,7 @@ __device__ __forceinline__ ShadeResult shade_one(const SceneView& s, const WaveV
           const DevLight& lt = s.lights[li];
           V3 wo = normalize(-rd);
           // estimateDirect, light-sampling half (integrator.cpp:39-60).
-          LightSample ls = sample_li(lt, s.prims, h.p, ul0, ul1, s.world_radius);
+          LightSample ls = sample_li(lt, s.prims, s.envmaps, h.p, ul0, ul1, s.world_radius);
           V3 ld = V3{0, 0, 0};
           if (ls.pdf > 0.f && !is_black(ls.Li)) {
             V3 f = bsdf_f<KM>(m, fr, ls.wi, wo, kNonSpecular) * absdot(ls.wi, h.ns);
@@ -224,7 +224,7 @@ __device__ __forceinline__ ShadeResult shade_one(const SceneView& s, const WaveV
             if (!is_black(fb) && mis_pdf > 0.f) {
               bool ok = true;
               if (lt.kind == DL_ENV) {
-                float lpdf = env_pdf_li(lt, wib);
+                float lpdf = env_pdf_li(lt, s.envmaps, wib);
                 if (lpdf == 0.f)
                   ok = false;
                 else {
@@ -381,7 +381,7 @@ __device__ __forceinline__ void resolve_one(const SceneView& s, const WaveView& 
       V3 fb = xyz(fv);
       float bpdf = ldv.w;
       if (fl & kFlagEnv) {
-        if (!w.mis_occluded[pid]) Ld = Ld + sdiv(mul(fb, ld3(lt.L)) * fv.w, bpdf);
+        if (!w.mis_occluded[pid]) Ld = Ld + sdiv(mul(fb, env_le(lt, s.envmaps, xyz(w.mis_d[pid]))) * fv.w, bpdf);
       } else {
         const float4 mh = w.mis_hit[pid];
         const int prim = __float_as_int(mh.w);  // primitive hit by the MIS ray, -1 for a miss

@@ -490,8 +490,13 @@ def write_ori(scene: Scene, directory: str, mesh_prefix: str | None = None) -> s
         elif l["type"] == "distant":
             out.append(f'  <Light type="distant">\n    <Param L="{_fmt(l["L"])}"/>\n'
                        f'    <Param from="{_fmt(l["from"])}"/>\n    <Param to="{_fmt(l["to"])}"/>\n  </Light>\n')
-    for e in scene.envmaps:
-        out.append(f'  <Envmap>\n    <Param L="{_fmt(e["L"])}"/>\n    <Param nLightSamples="1"/>\n'
+    for k, e in enumerate(scene.envmaps):
+        name = ""
+        if e.get("image") is not None:  # an image map: written as PNG beside the scene
+            fn = f"{scene.name}_env{k}.png"
+            write_png(os.path.join(directory, fn), e["image"])
+            name = f'    <Param name="{fn}"/>\n'
+        out.append(f'  <Envmap>\n    <Param L="{_fmt(e["L"])}"/>\n    <Param nLightSamples="1"/>\n{name}'
                    f'    <Param worldUp="{_fmt(e["worldUp"])}"/>\n  </Envmap>\n')
     out.append(f'  <Integrator type="path">\n    <Param maxDepth="{scene.max_depth}"/>\n'
                f'    <Param nSamplesPerPixel="{scene.spp}"/>\n  </Integrator>\n')
@@ -500,6 +505,51 @@ def write_ori(scene: Scene, directory: str, mesh_prefix: str | None = None) -> s
     with open(path, "w") as fh:
         fh.write("".join(out))
     return path
+
+
+def write_png(path: str, rgb8) -> None:
+    """An 8-bit RGB image as a PNG file (filter 0 rows, one zlib stream)."""
+    import struct
+    import zlib
+    img = np.ascontiguousarray(rgb8, np.uint8)
+    h, w = img.shape[:2]
+    raw = b"".join(b"\x00" + img[j].tobytes() for j in range(h))
+
+    def chunk(kind: bytes, data: bytes) -> bytes:
+        return struct.pack(">I", len(data)) + kind + data + struct.pack(">I", zlib.crc32(kind + data) & 0xFFFFFFFF)
+
+    with open(path, "wb") as f:
+        f.write(b"\x89PNG\r\n\x1a\n" + chunk(b"IHDR", struct.pack(">IIBBBBB", w, h, 8, 2, 0, 0, 0))
+                + chunk(b"IDAT", zlib.compress(raw, 9)) + chunk(b"IEND", b""))
+
+
+def sky_image(width: int = 64, height: int = 32, seed: int = 11) -> np.ndarray:
+    """A procedural 8-bit sky: a vertical gradient, value noise and one bright sun disc."""
+    rng = Rng(seed)
+    v = (np.arange(height) + 0.5)[:, None] / height
+    u = (np.arange(width) + 0.5)[None, :] / width
+    base = np.stack([60 + 120 * (1 - v) + 0 * u, 90 + 110 * (1 - v) + 0 * u, 140 + 90 * (1 - v) + 0 * u], -1)
+    noise = np.array([[rng.uniform(-18, 18) for _ in range(width)] for _ in range(height)])[..., None]
+    su, sv = rng.uniform(0.2, 0.8), rng.uniform(0.2, 0.4)
+    d2 = ((u - su) * 2.0) ** 2 + (v - sv) ** 2
+    sun = np.where(d2 < 0.004, 255.0, 0.0)[..., None]
+    return np.clip(np.maximum(base + noise, sun), 0, 255).astype(np.uint8)
+
+
+def envlit(res: int = 64, spp: int = 16, max_depth: int = 6, subdiv: int = 3) -> Scene:
+    """Spheres of several materials on a ground quad, lit only by an image environment map."""
+    s = Scene("envlit", res, res, spp, max_depth, (0.0, 1.2, 5.0), (0.0, 0.3, 0.0), (0, 1, 0), 40.0,
+              meta={"config": "envlit"})
+    mats = [matte((0.7, 0.7, 0.7)), metal((0.2, 0.42, 1.37), (3.91, 2.45, 2.14), 0.3), glass(1.5, 0.0),
+            plastic((0.2, 0.5, 0.3), (0.5, 0.5, 0.5), 0.15)]
+    for i, m in enumerate(mats):
+        v, f = icosphere(subdiv)
+        x = -1.8 + 1.2 * i
+        s.meshes.append(Mesh(f"ball{i}", v * 0.5 + np.array([x, -0.5, 0.0]), f, v.copy(), m))
+    p, f, nn = quad([(-6, -1, -6), (6, -1, -6), (6, -1, 6), (-6, -1, 6)], (0, 1, 0))
+    s.meshes.append(Mesh("ground", p, f, nn, matte((0.5, 0.45, 0.4))))
+    s.envmaps.append({"L": (1.5, 1.5, 1.5), "worldUp": (0, 1, 0), "image": sky_image()})
+    return s
 
 
 def zoo(res: int = 64, spp: int = 16, max_depth: int = 6, subdiv: int = 2, beckmann: bool = False) -> Scene:
@@ -615,10 +665,14 @@ def to_host_scene(scene: Scene, text_rounding: bool = False):
             d = np.asarray(l["to"], np.float64) - np.asarray(l["from"], np.float64)
             L.dir[:] = list(d / np.linalg.norm(d))
         lights.append(L)
+    images = []
     for e in scene.envmaps:
         L = og.Light()
         L.type = og.LIGHT_ENV
         L.L[:] = list(e["L"])
+        if e.get("image") is not None:  # 8-bit texels as the loader converts them (byte * 1/255 in float)
+            images.append(np.asarray(e["image"], np.uint8).astype(np.float32) * np.float32(1.0 / 255.0))
+            L.image = len(images)
         up = np.asarray(e["worldUp"], np.float64)
         up /= np.linalg.norm(up)
         z = np.array([0.0, 0.0, 1.0])
@@ -636,7 +690,7 @@ def to_host_scene(scene: Scene, text_rounding: bool = False):
     cam = og.look_at_camera(scene.eye, scene.look, scene.up, scene.fov, scene.width, scene.height,
                             scene.lens_radius, scene.focal_distance)
     return og.HostScene.from_arrays(P, N, mesh_of, mats, lights, cam, scene.spp, scene.max_depth,
-                                    light_of_prim=light_of)
+                                    light_of_prim=light_of, images=images)
 
 
 def job_views(s: Scene, views: int = 16):

@@ -9,7 +9,8 @@ records its outputs on fixed inputs:
   bsdf.npz     BSDF f/pdf/sample_f per material            (src/core/bsdf.cpp, src/bsdf/*)
   camera.npz   Pinhole::generateRay, pinhole + thin lens    (src/camera/pinhole.cpp:8-33)
   trace.npz    Scene::intersect hits on the Cornell box     (project CPU kernel in Embree's place)
-  image_*.npz  PathTracing::render film sums                (src/integrator/path.cpp:15-37)
+  image_*.npz  PathTracing::render film sums                (src/integrator/path.cpp:15-37);
+               image_envlit lit by an image environment map (src/light/envmap.cpp)
   stats_*.npz  FP64 per-pixel mean and variance at high spp (for 3-sigma checks)
   geometry.npz loader output digests
 
@@ -154,7 +155,8 @@ def main():
         print("trace", time.time() - t0)
 
         # Images through the reference's own PathTracing::render
-        for name, kw in [("cornell", dict(res=64, spp=16)), ("zoo", dict(res=48, spp=16))]:
+        for name, kw in [("cornell", dict(res=64, spp=16)), ("zoo", dict(res=48, spp=16)),
+                         ("envlit", dict(res=48, spp=16))]:
             path = helpers.write_scene(name, os.path.join(tmp, "img_" + name), **kw)
             h, info = ref.load(path)
             W, H = int(info[0]), int(info[1])

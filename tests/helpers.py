@@ -73,12 +73,13 @@ def write_scene(name: str, directory: str, **kw) -> str:
 
 
 def scene_hash(ori_path: str) -> str:
-    """SHA-256 over the scene file and the meshes it names."""
+    """SHA-256 over the scene file and the meshes and images it names."""
     d = os.path.dirname(ori_path)
     h = hashlib.sha256()
     h.update(open(ori_path, "rb").read())
     import re
-    for fn in re.findall(r'filename="([^"]+\.obj)"', open(ori_path).read()):
+    text = open(ori_path).read()
+    for fn in re.findall(r'filename="([^"]+\.obj)"', text) + re.findall(r'name="([^"]+\.(?:png|bmp|tga|ppm))"', text):
         h.update(open(os.path.join(d, fn), "rb").read())
     return h.hexdigest()
 

@@ -75,7 +75,8 @@ def test_port_trace_matches_reference_and_brute_force(port, tmp_path):
     assert np.array_equal(prim, pb) and np.array_equal(t, tb), "BVH must equal the brute-force loop"
 
 
-@pytest.mark.parametrize("name,kw", [("cornell", dict(res=64, spp=16)), ("zoo", dict(res=48, spp=16))])
+@pytest.mark.parametrize("name,kw", [("cornell", dict(res=64, spp=16)), ("zoo", dict(res=48, spp=16)),
+                                     ("envlit", dict(res=48, spp=16))])
 def test_port_image_matches_reference_render(port, tmp_path, name, kw):
     g = helpers.golden(f"image_{name}.npz")
     path = helpers.write_scene(name, str(tmp_path / name), **kw)

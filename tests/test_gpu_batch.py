@@ -1,10 +1,13 @@
 """Batched rendering (many jobs, one graph launch) against the plain path.
 
-Each path's arithmetic is the plain render's; only the film accumulation
-order differs (FP64 atomics), so per-pixel FP64 sums must agree with the
-plain FP64 render to 1e-12 relative, counts exactly. The same job must give
-the same result alone and in a mix of other jobs, and with a pool of slots
-far smaller than its path count (heavy slot regeneration).
+Each path runs the plain render's device functions on the same samples; the
+batched and plain shading kernels are compiled separately, so the compiler
+may contract different multiply-adds, and a path's FP32 radiance can differ
+in its last bits. Per-pixel FP64 sums must agree with the plain FP64 render
+to 1e-5 relative (FP32 rounding), counts exactly. Within the batched engine
+(same kernels), the same job must give the same result to 1e-12 alone and in
+a mix of other jobs, and with a pool of slots far smaller than its path
+count (heavy slot regeneration).
 """
 from __future__ import annotations
 
@@ -49,8 +52,8 @@ def test_batch_matches_plain_fp64(ctx, scenes):
     for s, (sm, sq, cnt) in zip(scenes, outs):
         ps, pq = ctx.render(s["sid"], s["width"], s["height"], fp64=True)
         assert (cnt == s["spp"]).all(), s["name"]
-        assert _close(sm, ps), f"{s['name']}: max diff {np.abs(sm - ps).max()}"
-        assert _close(sq, pq), s["name"]
+        assert np.allclose(sm, ps, rtol=1e-5, atol=1e-7), f"{s['name']}: max diff {np.abs(sm - ps).max()}"
+        assert np.allclose(sq, pq, rtol=1e-5, atol=1e-7), s["name"]
     print(f"batch of {len(scenes)} jobs: {st['iterations']} loop iterations, {st['paths']} paths, "
           f"{st['device_ms']:.2f} ms in one graph launch")
 
