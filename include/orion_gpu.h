@@ -57,6 +57,20 @@ enum {
  * Beckmann is an extension selected by <Param distribution="beckmann"/>. */
 enum { ORION_DIST_GGX = 0, ORION_DIST_BECKMANN = 1 };
 
+/* Spectrum inputs a material can take from an image texture
+ * (<Kd><Param type="image"/><Param filename="..."/></Kd>, src/util/parser.cpp:433-461):
+ * index into orion_material.tex. */
+enum {
+  ORION_TEX_KD = 0,
+  ORION_TEX_KS = 1,
+  ORION_TEX_KR = 2,
+  ORION_TEX_KT = 3,
+  ORION_TEX_OPACITY = 4,
+  ORION_TEX_ETA = 5, /* metal eta_rgb */
+  ORION_TEX_K = 6,   /* metal k */
+  ORION_TEX_SLOTS = 7
+};
+
 typedef struct orion_material {
   int32_t type;
   int32_t distribution;
@@ -65,6 +79,10 @@ typedef struct orion_material {
   float Kd[3], Ks[3], Kr[3], Kt[3], opacity[3];
   float eta_rgb[3], k[3]; /* metal */
   float sigma, roughness, eta;
+  /* tex[ORION_TEX_*]: 0 = the constant above; k = the scene's image k - 1,
+   * looked up at the hit's texture coordinates (Texture::evaluate,
+   * src/core/texture.cpp:8-11, wrap filter). tex[7] is reserved (0). */
+  int32_t tex[8];
 } orion_material;
 
 /* ---------------------------------------------------------------- lights */
@@ -91,9 +109,9 @@ typedef struct orion_light {
   int32_t reserved;
 } orion_light;
 
-/* An image of a scene (environment map texels): linear RGB floats, row 0 at
- * the top, as the reference's ImageMemory holds them (8-bit files: byte / 255,
- * src/texture/imagetexture.cpp:16-52). */
+/* An image of a scene (environment map or material texture texels): linear
+ * RGB floats, row 0 at the top, as the reference's ImageMemory holds them
+ * (8-bit files: byte / 255, src/texture/imagetexture.cpp:16-52). */
 typedef struct orion_image {
   int32_t width, height;
   const float* rgb;        /* width x height x 3 */

@@ -768,6 +768,26 @@ struct Isect {
   V p, ng, ns, u, v;
   int prim = -1;
   float t = 0;
+  float uvx = 0, uvy = 0;  // texture coordinates (kernel.cpp:138-142)
+};
+
+// ImageTexture with the wrap filter (src/core/texture.cpp:8-29,
+// src/texture/imagetexture.cpp:4-12).
+struct Tex {
+  int w = 0, h = 0;
+  std::vector<float> rgb;
+  V eval(float u, float v) const {
+    int x = (int)(u * w), y = (int)(v * h);
+    // _coordFilter, FILTER_WRAP; a negative multiple of the size wraps to the
+    // size itself, which reads the texel that follows in memory; past the
+    // last texel (undefined in the reference) the last texel is read.
+    x = x >= 0 ? x % w : w - (int)((0u - (unsigned)x) % (unsigned)w);
+    y = y >= 0 ? y % h : h - (int)((0u - (unsigned)y) % (unsigned)h);
+    int64_t off = (int64_t)y * w + x;
+    const int64_t last = (int64_t)w * h - 1;
+    if (off > last) off = last;
+    return ld(&rgb[3 * off]);
+  }
 };
 
 struct Scene {
@@ -783,6 +803,24 @@ struct Scene {
   orion_camera cam;
   float tanHalf = 0, aspect = 1;
   int spp = 1, maxDepth = 5;
+  // Image textures: per material its record and whether an input is an
+  // image; per primitive its corner texture coordinates.
+  std::vector<orion_material> matSrc;
+  std::vector<char> textured;
+  std::vector<Tex> images;
+  std::vector<float> uv;
+
+  // Material::getBSDF of material `mi` at the hit (textures evaluated there).
+  Mat material(int mi, const Isect& it) const {
+    orion_material m = matSrc[mi];
+    float* dst[ORION_TEX_SLOTS] = {m.Kd, m.Ks, m.Kr, m.Kt, m.opacity, m.eta_rgb, m.k};
+    for (int t = 0; t < ORION_TEX_SLOTS; ++t) {
+      if (m.tex[t] == 0) continue;
+      V c = images[m.tex[t] - 1].eval(it.uvx, it.uvy);
+      dst[t][0] = c.x, dst[t][1] = c.y, dst[t][2] = c.z;
+    }
+    return makeMat(m);
+  }
 
   // Scene::intersect -> EmbreeKernel::intersect post-hit (kernel.cpp:127-169)
   bool intersect(V o, V d, float tnear, float tfar, Isect* is) const {
@@ -801,6 +839,11 @@ struct Scene {
     is->v = normalize(cross(is->ns, su));
     is->u = normalize(cross(is->v, is->ns));
     is->prim = h.prim;
+    if (!uv.empty()) {
+      const float* q2 = &uv[6 * (size_t)h.prim];
+      is->uvx = w * q2[0] + h.u * q2[2] + h.v * q2[4];
+      is->uvy = w * q2[1] + h.u * q2[3] + h.v * q2[5];
+    }
     return true;
   }
   bool occluded(V o, V d, float tmax) const {  // ShadowTester::unoccluded, light.h:26-29 (closest hit)
@@ -1060,7 +1103,10 @@ V Li(const Scene& s, V ro, V rd, Sampler& smp, int maxDepth, int rrDepth, int64_
       }
     }
     if (!found || bounces >= maxDepth) break;
-    const Mat& m = s.mats[s.matOf[it.prim]];
+    const int mi = s.matOf[it.prim];
+    Mat tm;
+    if (s.textured[mi]) tm = s.material(mi, it);
+    const Mat& m = s.textured[mi] ? tm : s.mats[mi];
     Frame fr{it.ng, it.ns, it.u, it.v};
     if (numMatching(m, NONSPEC) > 0 && !s.lights.empty()) {  // uniformSampleOneLight, integrator.cpp:8-27
       float sel;
@@ -1102,7 +1148,28 @@ Scene* makeScene(const orion_scene_desc* d) {
   else
     s->lightOf.assign(T, -1);
   s->bvh.build(s->pos.data(), (int)T);
-  for (int i = 0; i < d->num_materials; ++i) s->mats.push_back(makeMat(d->materials[i]));
+  for (int i = 0; i < d->num_materials; ++i) {
+    const orion_material& m = d->materials[i];
+    s->mats.push_back(makeMat(m));
+    s->matSrc.push_back(m);
+    bool tex = false;
+    for (int t = 0; t < ORION_TEX_SLOTS; ++t) {
+      if (m.tex[t] < 0 || m.tex[t] > d->num_images) {
+        delete s;
+        return nullptr;
+      }
+      tex = tex || m.tex[t] != 0;
+    }
+    s->textured.push_back(tex);
+    if (tex && s->uv.empty() && d->uvs) s->uv.assign(d->uvs, d->uvs + 6 * T);
+  }
+  for (int i = 0; i < d->num_images; ++i) {
+    Tex t;
+    t.w = d->images[i].width;
+    t.h = d->images[i].height;
+    t.rgb.assign(d->images[i].rgb, d->images[i].rgb + 3 * (size_t)t.w * t.h);
+    s->images.push_back(std::move(t));
+  }
   // worldbound + boundingSphere (kernel.cpp:44-50, geometry.h:551-554)
   float lo[3] = {kInfinity, kInfinity, kInfinity}, hi[3] = {-kInfinity, -kInfinity, -kInfinity};
   for (size_t i = 0; i < 9 * T; ++i) {

@@ -47,7 +47,8 @@ class Material(C.Structure):
     _fields_ = [("type", C.c_int32), ("distribution", C.c_int32), ("has_sigma", C.c_int32), ("reserved", C.c_int32),
                 ("Kd", C.c_float * 3), ("Ks", C.c_float * 3), ("Kr", C.c_float * 3), ("Kt", C.c_float * 3),
                 ("opacity", C.c_float * 3), ("eta_rgb", C.c_float * 3), ("k", C.c_float * 3),
-                ("sigma", C.c_float), ("roughness", C.c_float), ("eta", C.c_float)]
+                ("sigma", C.c_float), ("roughness", C.c_float), ("eta", C.c_float),
+                ("tex", C.c_int32 * 8)]  # per ORION_TEX_* input: 0 = constant, k = image k - 1
 
 
 class Light(C.Structure):
@@ -213,7 +214,8 @@ class HostScene:
     @classmethod
     def from_arrays(cls, positions, normals, material_of_prim, materials, lights, camera: Camera, spp: int,
                     max_depth: int, light_of_prim=None, uvs=None, images=None) -> "HostScene":
-        """images: list of (H, W, 3) float arrays, referenced 1-based by Light.image."""
+        """images: list of (H, W, 3) float arrays, referenced 1-based by Light.image and Material.tex;
+        uvs: texture coordinates per primitive corner (T x 6) or None."""
         pos = np.ascontiguousarray(positions, dtype=np.float32).reshape(-1, 9)
         nrm = np.ascontiguousarray(normals, dtype=np.float32).reshape(-1, 9)
         mop = np.ascontiguousarray(material_of_prim, dtype=np.int32)
@@ -223,7 +225,10 @@ class HostScene:
         d = SceneDesc()
         d.num_prims = len(pos)
         d.positions, d.normals = pos.ctypes.data, nrm.ctypes.data
-        d.uvs = np.ascontiguousarray(uvs, np.float32).ctypes.data if uvs is not None else None
+        uva = np.ascontiguousarray(uvs, np.float32).reshape(-1, 6) if uvs is not None else None  # kept alive below
+        if uva is not None and len(uva) != len(pos):
+            raise ValueError("uvs must hold 6 floats per primitive")
+        d.uvs = uva.ctypes.data if uva is not None else None
         d.material_of_prim, d.light_of_prim = mop.ctypes.data, lop.ctypes.data
         d.num_materials, d.num_lights = len(materials), len(lights)
         d.materials, d.lights = C.addressof(mats), C.addressof(lts)

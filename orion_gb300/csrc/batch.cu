@@ -136,8 +136,8 @@ __global__ void __launch_bounds__(128, 5) k_b_shade(WaveView w, BatchView b, con
     const int4 meta = w.rec[pid].meta;
     const DevJob& J = b.jobs[meta.y];
     const int bounce = meta.z;
-    ShadeResult r = shade_one<lobes_of_class(SC)>(J.scene, w, sobol_bitmajor, pid, (uint64_t)slot_index(w, pid),
-                                                  bounce, J.max_depth, J.rr_depth);
+    ShadeResult r = shade_one<lobes_of_class(SC), SC == SC_TEXTURED>(
+        J.scene, w, sobol_bitmajor, pid, (uint64_t)slot_index(w, pid), bounce, J.max_depth, J.rr_depth);
     if (r.alive) w.bounce[pid] = bounce + 1;
     queue_append(&c.counters[CNT_NEE], w.q_nee, pid, r.did_nee);
     queue_append(&c.counters[CNT_SH], w.q_sh, pid, r.want_sh);
@@ -241,6 +241,7 @@ cudaError_t configure_batch_kernels(int smem_bytes, KernelLimits* lim) {
   const void* shade[] = {(const void*)k_b_shade<SC_DIFFUSE>,    (const void*)k_b_shade<SC_CONDUCTOR>,
                          (const void*)k_b_shade<SC_SPECULAR>,   (const void*)k_b_shade<SC_DIELECTRIC>,
                          (const void*)k_b_shade<SC_PLASTIC>,    (const void*)k_b_shade<SC_GENERAL>,
+                         (const void*)k_b_shade<SC_TEXTURED>,
                          (const void*)k_b_shade<SC_MISS>,       (const void*)k_b_resolve,
                          (const void*)k_b_retire};
   for (const void* f : trace) {
@@ -262,8 +263,8 @@ namespace {
 
 // One loop iteration's kernels on `stream`, optionally timed per stage.
 void enqueue_iteration(const WaveView& w, const BatchView& b, const uint32_t* sobol, const uint32_t* sobol_bitmajor,
-                       const LaunchConfig& cfg, cudaGraphConditionalHandle cond, int in_graph, cudaStream_t stream,
-                       StageTimer* timer) {
+                       const LaunchConfig& cfg, unsigned class_mask, cudaGraphConditionalHandle cond, int in_graph,
+                       cudaStream_t stream, StageTimer* timer) {
   const int cap = w.capacity;
   const int persistent = cfg.num_sms * cfg.blocks_per_sm;
   const int tgrid = grid_cap(cap, cfg.trace_block, persistent * 2);
@@ -282,13 +283,19 @@ void enqueue_iteration(const WaveView& w, const BatchView& b, const uint32_t* so
   b_trace(cfg, w, b, 0, tgrid, stream);
   end();
   begin(ST_SHADE);
-  k_b_shade<SC_DIFFUSE><<<sgrid, cfg.shade_block, 0, stream>>>(w, b, sobol_bitmajor);
-  k_b_shade<SC_CONDUCTOR><<<sgrid, cfg.shade_block, 0, stream>>>(w, b, sobol_bitmajor);
-  k_b_shade<SC_SPECULAR><<<sgrid, cfg.shade_block, 0, stream>>>(w, b, sobol_bitmajor);
-  k_b_shade<SC_DIELECTRIC><<<sgrid, cfg.shade_block, 0, stream>>>(w, b, sobol_bitmajor);
-  k_b_shade<SC_PLASTIC><<<sgrid, cfg.shade_block, 0, stream>>>(w, b, sobol_bitmajor);
-  k_b_shade<SC_GENERAL><<<sgrid, cfg.shade_block, 0, stream>>>(w, b, sobol_bitmajor);
-  k_b_shade<SC_MISS><<<sgrid, cfg.shade_block, 0, stream>>>(w, b, sobol_bitmajor);
+  for (int sc = 0; sc < kShadeClasses; ++sc) {
+    if (!((class_mask >> sc) & 1u)) continue;
+    switch (sc) {
+      case SC_DIFFUSE: k_b_shade<SC_DIFFUSE><<<sgrid, cfg.shade_block, 0, stream>>>(w, b, sobol_bitmajor); break;
+      case SC_CONDUCTOR: k_b_shade<SC_CONDUCTOR><<<sgrid, cfg.shade_block, 0, stream>>>(w, b, sobol_bitmajor); break;
+      case SC_SPECULAR: k_b_shade<SC_SPECULAR><<<sgrid, cfg.shade_block, 0, stream>>>(w, b, sobol_bitmajor); break;
+      case SC_DIELECTRIC: k_b_shade<SC_DIELECTRIC><<<sgrid, cfg.shade_block, 0, stream>>>(w, b, sobol_bitmajor); break;
+      case SC_PLASTIC: k_b_shade<SC_PLASTIC><<<sgrid, cfg.shade_block, 0, stream>>>(w, b, sobol_bitmajor); break;
+      case SC_GENERAL: k_b_shade<SC_GENERAL><<<sgrid, cfg.shade_block, 0, stream>>>(w, b, sobol_bitmajor); break;
+      case SC_TEXTURED: k_b_shade<SC_TEXTURED><<<sgrid, cfg.shade_block, 0, stream>>>(w, b, sobol_bitmajor); break;
+      case SC_MISS: k_b_shade<SC_MISS><<<sgrid, cfg.shade_block, 0, stream>>>(w, b, sobol_bitmajor); break;
+    }
+  }
   end();
   begin(ST_TRACE_SHADOW);
   b_trace(cfg, w, b, 1, tgrid, stream);
@@ -311,11 +318,11 @@ void enqueue_iteration(const WaveView& w, const BatchView& b, const uint32_t* so
 }  // namespace
 
 cudaError_t capture_batch_iteration(const WaveView& w, const BatchView& b, const uint32_t* sobol,
-                                    const uint32_t* sobol_bitmajor, const LaunchConfig& cfg,
+                                    const uint32_t* sobol_bitmajor, const LaunchConfig& cfg, unsigned class_mask,
                                     cudaGraphConditionalHandle cond, cudaStream_t stream, cudaGraph_t body) {
   cudaError_t e = cudaStreamBeginCaptureToGraph(stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
   if (e != cudaSuccess) return e;
-  enqueue_iteration(w, b, sobol, sobol_bitmajor, cfg, cond, 1, stream, nullptr);
+  enqueue_iteration(w, b, sobol, sobol_bitmajor, cfg, class_mask, cond, 1, stream, nullptr);
   cudaGraph_t out = body;
   cudaError_t e2 = cudaStreamEndCapture(stream, &out);
   cudaError_t e3 = cudaGetLastError();
@@ -323,9 +330,9 @@ cudaError_t capture_batch_iteration(const WaveView& w, const BatchView& b, const
 }
 
 void launch_batch_iteration(const WaveView& w, const BatchView& b, const uint32_t* sobol,
-                            const uint32_t* sobol_bitmajor, const LaunchConfig& cfg, cudaStream_t stream,
-                            StageTimer* timer) {
-  enqueue_iteration(w, b, sobol, sobol_bitmajor, cfg, cudaGraphConditionalHandle{}, 0, stream, timer);
+                            const uint32_t* sobol_bitmajor, const LaunchConfig& cfg, unsigned class_mask,
+                            cudaStream_t stream, StageTimer* timer) {
+  enqueue_iteration(w, b, sobol, sobol_bitmajor, cfg, class_mask, cudaGraphConditionalHandle{}, 0, stream, timer);
 }
 
 }  // namespace orion_gb300

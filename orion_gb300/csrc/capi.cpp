@@ -106,6 +106,7 @@ struct DevBuf {
 
 struct DeviceScene {
   DevBuf nodes, woop, tri_prim, tri_class, prims, mats, lights, lfunc, lcdf, env_data, envmaps;
+  DevBuf mat_src, textures, prim_uv;  // image textures (empty when no material is textured)
   SceneView view{};
   int64_t bytes = 0;
   int64_t num_prims = 0;
@@ -151,6 +152,7 @@ struct orion_gpu_ctx {
   const void* bgraph_key[4] = {nullptr, nullptr, nullptr, nullptr};
   LaunchConfig bgraph_cfg{};
   int bgraph_slots = 0;
+  unsigned bgraph_mask = 0;  // shading classes the captured loop launches
   int smem_limit = 48 * 1024;  // opt-in dynamic shared memory per block
   KernelLimits limits{1024, 1024};
   std::mutex mu;
@@ -424,6 +426,15 @@ extern "C" int orion_gpu_scene_upload(orion_gpu_ctx* ctx, const orion_host_scene
     envs.push_back(DevEnvMap{e.width, e.height, e.marg_int, 0, eb + e.texels, eb + e.cond_func, eb + e.cond_cdf,
                              eb + e.cond_int, eb + e.marg_func, eb + e.marg_cdf});
   if ((rc = upload(d->envmaps, envs, ctx->stream, &bytes)) != ORION_OK) return rc;
+  // Image textures: records pointing into the same block, the materials'
+  // builder inputs, and per-primitive texture coordinates.
+  std::vector<DevTexture> texs;
+  for (const PreparedScene::TextureLayout& t : ps.textures) texs.push_back(DevTexture{t.width, t.height, eb + t.texels});
+  if (!texs.empty()) {
+    if ((rc = upload(d->textures, texs, ctx->stream, &bytes)) != ORION_OK) return rc;
+    if ((rc = upload(d->mat_src, ps.mat_src, ctx->stream, &bytes)) != ORION_OK) return rc;
+    if ((rc = upload(d->prim_uv, ps.prim_uv, ctx->stream, &bytes)) != ORION_OK) return rc;
+  }
   CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   SceneView& v = d->view;
   v.nodes = d->nodes.as<float4>();
@@ -436,6 +447,10 @@ extern "C" int orion_gpu_scene_upload(orion_gpu_ctx* ctx, const orion_host_scene
   v.light_func = d->lfunc.as<float>();
   v.light_cdf = d->lcdf.as<float>();
   v.envmaps = d->envmaps.as<DevEnvMap>();
+  v.textures = d->textures.as<DevTexture>();
+  v.mat_src = d->mat_src.as<DevMaterialSrc>();
+  v.prim_uv = d->prim_uv.as<float>();
+  v.class_mask = d->class_mask;
   v.light_func_int = ps.light_func_int;
   v.num_lights = (int)ps.lights.size();
   v.num_env = (int)ps.env_idx.size();
@@ -605,11 +620,16 @@ extern "C" int orion_gpu_stage_times(orion_gpu_ctx* ctx, orion_stage_times* out)
 
 // ------------------------------------------------------------ batches
 
-static int build_batch_graph(orion_gpu_ctx* ctx, const BatchView& bv, int slots) {
+// The captured loop launches the shading kernels of the classes in `mask`;
+// a graph that launches a superset is reused (an absent class's kernel
+// finds an empty queue), so the mask of a long-lived context only grows.
+static int build_batch_graph(orion_gpu_ctx* ctx, const BatchView& bv, int slots, unsigned mask) {
   const void* key[4] = {ctx->wave.block.p, ctx->b_jobs.p, ctx->b_retire.p, ctx->b_ctl.p};
   bool same = ctx->bexec && ctx->bgraph_slots == slots && std::memcmp(key, ctx->bgraph_key, sizeof(key)) == 0 &&
-              std::memcmp(&ctx->bgraph_cfg, &ctx->cfg, sizeof(LaunchConfig)) == 0;
+              std::memcmp(&ctx->bgraph_cfg, &ctx->cfg, sizeof(LaunchConfig)) == 0 &&
+              (mask & ~ctx->bgraph_mask) == 0;
   if (same) return ORION_OK;
+  if (ctx->bexec) mask |= ctx->bgraph_mask;
   if (ctx->bexec) cudaGraphExecDestroy(ctx->bexec);
   if (ctx->bgraph) cudaGraphDestroy(ctx->bgraph);
   ctx->bexec = nullptr;
@@ -629,7 +649,7 @@ static int build_batch_graph(orion_gpu_ctx* ctx, const BatchView& bv, int slots)
   CUDA_TRY(cudaGraphAddNode(&node, ctx->bgraph, nullptr, nullptr, 0, &np));
   cudaGraph_t body = np.conditional.phGraph_out[0];
   cudaError_t ce = capture_batch_iteration(ctx->wave.view, bv, ctx->sobol.as<uint32_t>(),
-                                           ctx->sobol_bitmajor.as<uint32_t>(), ctx->cfg, cond, ctx->stream, body);
+                                           ctx->sobol_bitmajor.as<uint32_t>(), ctx->cfg, mask, cond, ctx->stream, body);
   if (ce != cudaSuccess) {
     // A graph whose loop-body capture was invalidated is dropped, not
     // destroyed: nothing is assumed about its state after the failure.
@@ -641,6 +661,7 @@ static int build_batch_graph(orion_gpu_ctx* ctx, const BatchView& bv, int slots)
   std::memcpy(ctx->bgraph_key, key, sizeof(key));
   ctx->bgraph_cfg = ctx->cfg;
   ctx->bgraph_slots = slots;
+  ctx->bgraph_mask = mask;
   return ORION_OK;
 }
 
@@ -671,7 +692,9 @@ static int run_batch_locked(orion_gpu_ctx* ctx, std::vector<DevJob>& dj, unsigne
   bv.ctl = ctx->b_ctl.as<BatchCtl>();
   bv.q_retire = ctx->b_retire.as<int>();
   bv.q_free = ctx->b_free.as<int>();
-  if (!ctx->profiling && (rc = build_batch_graph(ctx, bv, cap)) != ORION_OK) return rc;
+  unsigned mask = 1u << SC_MISS;
+  for (const DevJob& J : dj) mask |= J.scene.class_mask;
+  if (!ctx->profiling && (rc = build_batch_graph(ctx, bv, cap, mask)) != ORION_OK) return rc;
 
   BatchCtl c;
   std::memset(&c, 0, sizeof(c));
@@ -703,7 +726,7 @@ static int run_batch_locked(orion_gpu_ctx* ctx, std::vector<DevJob>& dj, unsigne
     int more = 1;
     for (int it = 0; more && it < c.max_iterations; ++it) {
       launch_batch_iteration(ctx->wave.view, bv, ctx->sobol.as<uint32_t>(), ctx->sobol_bitmajor.as<uint32_t>(),
-                             ctx->cfg, s, &timer);
+                             ctx->cfg, mask, s, &timer);
       CUDA_TRY(cudaGetLastError());
       CUDA_TRY(cudaMemcpyAsync(&more, &bv.ctl->more, sizeof(int), cudaMemcpyDeviceToHost, s));
       CUDA_TRY(cudaStreamSynchronize(s));
@@ -732,7 +755,9 @@ static int run_batch_locked(orion_gpu_ctx* ctx, std::vector<DevJob>& dj, unsigne
   ctx->last.shadow_rays = (int64_t)out.rays[1];
   ctx->last.mis_rays = (int64_t)out.rays[2];
   ctx->last.rays = (int64_t)(out.rays[0] + out.rays[1] + out.rays[2]);
-  ctx->last.kernel_launches = 16LL * out.iterations + 1;  // plan, regen, 4 traces, 7 shades, resolve, retire, control
+  // Per iteration: plan, regen, 4 traces, one shade per class, resolve, retire, control; plus the init.
+  const unsigned launched = ctx->profiling ? mask : ctx->bgraph_mask;
+  ctx->last.kernel_launches = (9LL + __builtin_popcount(launched)) * out.iterations + 1;
   ctx->last.device_ms = ms;
   if (out.error) return fail(ORION_ERR_DEVICE, "batch loop reached its iteration cap");
   if (out.paths_done != total)

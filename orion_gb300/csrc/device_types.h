@@ -72,6 +72,7 @@ enum ShadeClass : int32_t {
   SC_DIELECTRIC = 3,  // microfacet reflection + transmission (rough glass)
   SC_PLASTIC = 4,     // Lambert + microfacet reflection
   SC_GENERAL = 5,     // anything else (Oren-Nayar, uber, no lobes)
+  SC_TEXTURED = 6,    // an input comes from an image texture: lobes built per hit
   SC_MISS = 7,        // the ray left the scene
   kShadeClasses = 8
 };
@@ -82,6 +83,38 @@ struct DevMaterial {   // 16 + 5 * 64 = 336 bytes
   int32_t shade_class;      // ShadeClass
   int32_t pad;
   DevLobe lobes[kMaxLobes];
+};
+
+// What Material::getBSDF reads (src/material/*.cpp), with every texture
+// already evaluated: constants on the host, image texels at the hit in the
+// textured shading kernel. Transcendental constants (alpha, Oren-Nayar A, B)
+// are derived once on the host so both sides build identical lobes.
+struct MaterialInputs {  // 128 bytes
+  int32_t type;          // ORION_MAT_*
+  int32_t dist;          // DistKind
+  float Kd[3], Ks[3], Kr[3], Kt[3], opacity[3], eta_rgb[3], k[3];
+  float sigma;           // matte: clamped at 0; 0 selects Lambert
+  float roughness, eta;
+  float alpha;           // roughnessToAlpha(roughness)
+  float on_a, on_b;      // Oren-Nayar A, B for sigma
+  float pad[3];
+};
+static_assert(sizeof(MaterialInputs) == 128, "MaterialInputs is 128 bytes");
+
+constexpr int kTexSlots = 7;  // Kd, Ks, Kr, Kt, opacity, eta, k (ORION_TEX_*)
+
+// A material with image-textured inputs: its constant inputs and, per
+// input, the DevTexture it reads (-1: the constant).
+struct DevMaterialSrc {  // 160 bytes
+  MaterialInputs in;
+  int32_t tex[8];
+};
+static_assert(sizeof(DevMaterialSrc) == 160, "DevMaterialSrc is 160 bytes");
+
+// An image texture (ImageTexture, src/texture/imagetexture.cpp:4-12).
+struct DevTexture {
+  int32_t width, height;
+  const float* texels;   // width x height x 3, row 0 at the top
 };
 
 enum DevLightKind : int32_t { DL_AREA = 0, DL_POINT = 1, DL_SPOT = 2, DL_DISTANT = 3, DL_ENV = 4 };

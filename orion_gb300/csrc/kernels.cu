@@ -83,8 +83,8 @@ __global__ void __launch_bounds__(128, 5) k_shade(SceneView s, WaveView w, WaveA
   const int* in_q = w.q_cls + (size_t)SC * w.capacity;
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
     const int pid = in_q[q];
-    ShadeResult r = shade_one<lobes_of_class(SC)>(s, w, a.sobol_bitmajor, pid, (uint64_t)(a.base_index + pid), bounce,
-                                                  a.max_depth, a.rr_depth);
+    ShadeResult r = shade_one<lobes_of_class(SC), SC == SC_TEXTURED>(
+        s, w, a.sobol_bitmajor, pid, (uint64_t)(a.base_index + pid), bounce, a.max_depth, a.rr_depth);
     queue_append(w.counters + CNT_NEE, w.q_nee, pid, r.did_nee);
     queue_append(w.counters + CNT_SH, w.q_sh, pid, r.want_sh);
     queue_append(w.counters + CNT_MIS, w.q_mis, pid, r.want_mis);
@@ -311,6 +311,7 @@ void launch_wave(const SceneView& s, const WaveView& w, const WaveArgs& a, const
         case SC_DIELECTRIC: k_shade<SC_DIELECTRIC><<<sgrid, cfg.shade_block, 0, stream>>>(s, w, a, bounce, cur); break;
         case SC_PLASTIC: k_shade<SC_PLASTIC><<<sgrid, cfg.shade_block, 0, stream>>>(s, w, a, bounce, cur); break;
         case SC_GENERAL: k_shade<SC_GENERAL><<<sgrid, cfg.shade_block, 0, stream>>>(s, w, a, bounce, cur); break;
+        case SC_TEXTURED: k_shade<SC_TEXTURED><<<sgrid, cfg.shade_block, 0, stream>>>(s, w, a, bounce, cur); break;
         case SC_MISS: k_shade<SC_MISS><<<sgrid, cfg.shade_block, 0, stream>>>(s, w, a, bounce, cur); break;
         default: break;
       }
@@ -381,7 +382,7 @@ cudaError_t configure_kernels(int smem_bytes, KernelLimits* lim) {
       (const void*)k_trace_sh<32>,            (const void*)k_trace_rays<16>};
   const void* shade[] = {(const void*)k_shade<SC_DIFFUSE>, (const void*)k_shade<SC_CONDUCTOR>,
                          (const void*)k_shade<SC_SPECULAR>, (const void*)k_shade<SC_DIELECTRIC>,
-                         (const void*)k_shade<SC_PLASTIC>, (const void*)k_shade<SC_GENERAL>,
+                         (const void*)k_shade<SC_PLASTIC>, (const void*)k_shade<SC_GENERAL>, (const void*)k_shade<SC_TEXTURED>,
                          (const void*)k_shade<SC_MISS>, (const void*)k_resolve};
   for (const void* f : trace) {
     cudaError_t e = limit_of(f, smem_bytes, &lim->max_trace_block);

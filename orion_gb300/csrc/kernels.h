@@ -17,6 +17,9 @@ struct SceneView {
   const DevMaterial* mats;
   const DevLight* lights;
   const DevEnvMap* envmaps;  // image environment maps (DevLight::image)
+  const DevTexture* textures;      // image textures (DevMaterialSrc::tex)
+  const DevMaterialSrc* mat_src;   // builder inputs per material (null when nothing is textured)
+  const float* prim_uv;            // texture coordinates, 6 per primitive (null when nothing is textured)
   const float* light_func;
   const float* light_cdf;
   float light_func_int;
@@ -24,6 +27,7 @@ struct SceneView {
   int env_idx[8];
   int num_env;
   float world_radius;
+  unsigned class_mask;  // shading classes of the scene's triangles (bit ShadeClass), SC_MISS always
   DevCamera cam;
 };
 
@@ -210,14 +214,15 @@ cudaError_t configure_batch_kernels(int smem_bytes, KernelLimits* lim);
 // Batched mode: builds the body of the device-side loop (one iteration)
 // into `body` by stream capture on `stream`. The loop keeps running while
 // work or live paths remain; `cond` is the graph's while-condition handle.
+// Shading kernels are launched for the classes in `class_mask` only.
 cudaError_t capture_batch_iteration(const WaveView& w, const BatchView& b, const uint32_t* sobol,
-                                    const uint32_t* sobol_bitmajor, const LaunchConfig& cfg,
+                                    const uint32_t* sobol_bitmajor, const LaunchConfig& cfg, unsigned class_mask,
                                     cudaGraphConditionalHandle cond, cudaStream_t stream, cudaGraph_t body);
 // The same iteration launched directly (a host-driven loop reading ctl->more),
 // each stage timed by `timer`: the profiling path of the batched engine.
 void launch_batch_iteration(const WaveView& w, const BatchView& b, const uint32_t* sobol,
-                            const uint32_t* sobol_bitmajor, const LaunchConfig& cfg, cudaStream_t stream,
-                            StageTimer* timer);
+                            const uint32_t* sobol_bitmajor, const LaunchConfig& cfg, unsigned class_mask,
+                            cudaStream_t stream, StageTimer* timer);
 // Resets the batch control block and the free-slot list for `capacity` slots.
 void launch_batch_init(const WaveView& w, const BatchView& b, int capacity, cudaStream_t stream);
 

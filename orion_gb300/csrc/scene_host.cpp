@@ -13,9 +13,12 @@
 // Differences, all deliberate: the resource directory is resolved against
 // the scene file's directory (the reference prefixes the executable path,
 // src/util/envvariable.cpp:37-40); named materials and stored transforms
-// are per file rather than process-wide; features outside the path tracer
-// (image textures and envmaps, SPD files, named metals, sppm and pseudo
-// samplers) are reported as ORION_ERR_UNSUPPORTED instead of being loaded.
+// are per file rather than process-wide; an image texture's file name, which
+// the reference opens relative to the working directory
+// (src/util/parser.cpp:438-443), is looked up in the resource directory, then
+// the scene's directory, then the working directory; features outside the
+// path tracer (SPD files, named metals, sppm and pseudo samplers) are
+// reported as ORION_ERR_UNSUPPORTED instead of being loaded.
 #include "scene_host.h"
 #include "image_io.h"
 
@@ -26,6 +29,7 @@
 #include <cstdlib>
 #include <cstring>
 #include <fstream>
+#include <functional>
 #include <map>
 #include <memory>
 #include <sstream>
@@ -745,9 +749,14 @@ struct TexValue {
   bool present = false;
   bool is_float = false;  // a FloatTexture (usable where the reference casts to one)
   float rgb[3] = {0, 0, 0};
+  int32_t image = 0;      // an ImageTexture: the scene's image image - 1
 };
 
-TexValue texture_of(const XmlNode* mat, const char* tag) {
+// Loads an image file named in the scene and returns its 1-based index in
+// the scene's image list (the same file is loaded once).
+using ImageLoader = std::function<int32_t(const std::string& name)>;
+
+TexValue texture_of(const XmlNode* mat, const char* tag, const ImageLoader& images) {
   TexValue t;
   const XmlNode* n = mat->child(tag);
   if (!n) return t;
@@ -762,8 +771,11 @@ TexValue texture_of(const XmlNode* mat, const char* tag) {
     float v = parse_float(ps.get("value"));
     t.rgb[0] = t.rgb[1] = t.rgb[2] = v;
     t.present = t.is_float = true;
-  } else if (type == "image") {
-    raise(ORION_ERR_UNSUPPORTED, std::string("image texture for <") + tag + "> is not supported");
+  } else if (type == "image") {  // src/util/parser.cpp:438-443
+    const std::string fn = trim(ps.get("filename"));
+    if (fn.empty()) return t;
+    t.image = images(fn);
+    t.present = true;
   }
   return t;
 }
@@ -776,8 +788,13 @@ void need_float(const TexValue& t, const char* mat, const char* tag) {
     raise(ORION_ERR_PARSE, std::string(mat) + " material needs a float texture <" + tag + ">");
 }
 void copy3(float* d, const float* s) { d[0] = s[0], d[1] = s[1], d[2] = s[2]; }
+// A Spectrum input: its constant, or the image it is looked up in.
+void take(const TexValue& t, float* d, int32_t* tex) {
+  copy3(d, t.rgb);
+  *tex = t.image;
+}
 
-orion_material make_material(const XmlNode* mn) {
+orion_material make_material(const XmlNode* mn, const ImageLoader& images) {
   orion_material m;
   std::memset(&m, 0, sizeof(m));
   std::string type = mn->attr("type") ? mn->attr("type") : "";
@@ -790,53 +807,53 @@ orion_material make_material(const XmlNode* mn) {
       raise(ORION_ERR_UNSUPPORTED, "unknown microfacet distribution '" + d + "'");
   }
   if (type == "matte") {
-    TexValue kd = texture_of(mn, "Kd"), sg = texture_of(mn, "sigma");
+    TexValue kd = texture_of(mn, "Kd", images), sg = texture_of(mn, "sigma", images);
     need(kd, "matte", "Kd");
     m.type = ORION_MAT_MATTE;
-    copy3(m.Kd, kd.rgb);
+    take(kd, m.Kd, &m.tex[ORION_TEX_KD]);
     if (sg.present && sg.is_float) {
       m.has_sigma = 1;
       m.sigma = sg.rgb[0];
     }
   } else if (type == "mirror") {
-    TexValue kr = texture_of(mn, "Kr");
+    TexValue kr = texture_of(mn, "Kr", images);
     need(kr, "mirror", "Kr");
     m.type = ORION_MAT_MIRROR;
-    copy3(m.Kr, kr.rgb);
+    take(kr, m.Kr, &m.tex[ORION_TEX_KR]);
   } else if (type == "glass") {
-    TexValue kr = texture_of(mn, "Kr"), kt = texture_of(mn, "Kt"), eta = texture_of(mn, "eta"),
-             rough = texture_of(mn, "roughness");
+    TexValue kr = texture_of(mn, "Kr", images), kt = texture_of(mn, "Kt", images), eta = texture_of(mn, "eta", images),
+             rough = texture_of(mn, "roughness", images);
     need(kr, "glass", "Kr");
     need(kt, "glass", "Kt");
     need_float(eta, "glass", "eta");
     need_float(rough, "glass", "roughness");
     m.type = ORION_MAT_GLASS;
-    copy3(m.Kr, kr.rgb);
-    copy3(m.Kt, kt.rgb);
+    take(kr, m.Kr, &m.tex[ORION_TEX_KR]);
+    take(kt, m.Kt, &m.tex[ORION_TEX_KT]);
     m.eta = eta.rgb[0];
     m.roughness = rough.rgb[0];
   } else if (type == "plastic") {
-    TexValue kd = texture_of(mn, "Kd"), ks = texture_of(mn, "Ks"), rough = texture_of(mn, "roughness");
+    TexValue kd = texture_of(mn, "Kd", images), ks = texture_of(mn, "Ks", images), rough = texture_of(mn, "roughness", images);
     need(kd, "plastic", "Kd");
     need(ks, "plastic", "Ks");
     need_float(rough, "plastic", "roughness");
     m.type = ORION_MAT_PLASTIC;
-    copy3(m.Kd, kd.rgb);
-    copy3(m.Ks, ks.rgb);
+    take(kd, m.Kd, &m.tex[ORION_TEX_KD]);
+    take(ks, m.Ks, &m.tex[ORION_TEX_KS]);
     m.roughness = rough.rgb[0];
   } else if (type == "metal") {
     const XmlNode* en = mn->child("eta");
     const XmlNode* kn = mn->child("k");
     if ((en && params_of(en).has("SPD")) || (kn && params_of(kn).has("SPD")))
       raise(ORION_ERR_UNSUPPORTED, "metal SPD files are not supported");
-    TexValue eta = texture_of(mn, "eta"), k = texture_of(mn, "k"), rough = texture_of(mn, "roughness");
+    TexValue eta = texture_of(mn, "eta", images), k = texture_of(mn, "k", images), rough = texture_of(mn, "roughness", images);
     m.type = ORION_MAT_METAL;
     // src/material/metal.cpp:98-140: explicit eta, k and roughness are used
     // only when all three are given; otherwise the named-metal branch runs,
     // which leaves eta = k = 0 unless a metalName is set.
     if (eta.present && k.present && rough.present && rough.is_float) {
-      copy3(m.eta_rgb, eta.rgb);
-      copy3(m.k, k.rgb);
+      take(eta, m.eta_rgb, &m.tex[ORION_TEX_ETA]);
+      take(k, m.k, &m.tex[ORION_TEX_K]);
       m.roughness = rough.rgb[0];
     } else {
       if (mp.has("metalName")) raise(ORION_ERR_UNSUPPORTED, "named metals are not supported");
@@ -845,12 +862,13 @@ orion_material make_material(const XmlNode* mn) {
   } else if (type == "uber") {
     const char* tags[5] = {"Kd", "Ks", "Kr", "Kt", "opacity"};
     float* dst[5] = {m.Kd, m.Ks, m.Kr, m.Kt, m.opacity};
+    const int slot[5] = {ORION_TEX_KD, ORION_TEX_KS, ORION_TEX_KR, ORION_TEX_KT, ORION_TEX_OPACITY};
     for (int i = 0; i < 5; ++i) {
-      TexValue t = texture_of(mn, tags[i]);
+      TexValue t = texture_of(mn, tags[i], images);
       need(t, "uber", tags[i]);
-      copy3(dst[i], t.rgb);
+      take(t, dst[i], &m.tex[slot[i]]);
     }
-    TexValue rough = texture_of(mn, "roughness"), eta = texture_of(mn, "eta");
+    TexValue rough = texture_of(mn, "roughness", images), eta = texture_of(mn, "eta", images);
     need_float(rough, "uber", "roughness");
     need_float(eta, "uber", "eta");
     m.type = ORION_MAT_UBER;
@@ -903,6 +921,7 @@ class Loader {
   std::unique_ptr<XmlNode> root_;
   std::vector<Xform> reuse_;
   std::map<std::string, int> named_;
+  std::map<std::string, int32_t> image_index_;
 
   Xform transform_of(const XmlNode* n) {
     const XmlNode* t = n->child("Transform");
@@ -941,7 +960,7 @@ class Loader {
       if (it == named_.end()) raise(ORION_ERR_PARSE, std::string("no material named '") + named + "'");
       return it->second;
     }
-    out_->materials.push_back(make_material(mn));
+    out_->materials.push_back(make_material(mn, [this](const std::string& fn) { return texture_image(fn); }));
     int idx = (int)out_->materials.size() - 1;
     const char* name = mn->attr("name");
     if (name && *name) named_.insert(std::make_pair(std::string(name), idx));
@@ -1090,6 +1109,42 @@ class Loader {
     out_->spp = parse_int(ps.get("nSamplesPerPixel"));
   }
 
+  // loadImage (src/texture/imagetexture.cpp:28-52): 8-bit texels times
+  // 1/255; returns the image's 1-based index in the scene (a file is loaded once).
+  int32_t load_image(const std::string& file) {
+    auto it = image_index_.find(file);
+    if (it != image_index_.end()) return it->second;
+    Image8 im8;
+    std::string ierr;
+    if (!load_image8(file, &im8, &ierr)) raise(ORION_ERR_IO, ierr);
+    if (im8.channels != 3 && im8.channels != 4)
+      raise(ORION_ERR_UNSUPPORTED, file + ": only 3- or 4-channel images are read by the reference");
+    HostImage hi;
+    hi.width = im8.width;
+    hi.height = im8.height;
+    hi.rgb.resize(im8.rgb.size());
+    const float inv255 = 0.0039215686274509803921568627451f;  // color_CharToFloat
+    for (size_t i = 0; i < im8.rgb.size(); ++i) hi.rgb[i] = im8.rgb[i] * inv255;
+    out_->images.push_back(std::move(hi));
+    const int32_t idx = (int32_t)out_->images.size();
+    image_index_[file] = idx;
+    return idx;
+  }
+
+  // An image texture's file: absolute, or found in the resource directory,
+  // the scene's directory or the working directory, in that order.
+  int32_t texture_image(const std::string& name) {
+    if (name[0] == '/') return load_image(name);
+    for (const std::string& dir : {res_dir_, scene_dir_}) {
+      std::FILE* f = std::fopen((dir + name).c_str(), "rb");
+      if (f) {
+        std::fclose(f);
+        return load_image(dir + name);
+      }
+    }
+    return load_image(name);
+  }
+
   void envmaps() {
     // src/light/envmap.cpp:116-135
     for (const XmlNode* en : root_->all("Envmap")) {
@@ -1100,21 +1155,8 @@ class Loader {
       l.type = ORION_LIGHT_ENV;
       if (ps.has("name")) {
         // Envmap(...) reads the image from the resource directory
-        // (src/light/envmap.cpp:120, :14-22; src/texture/imagetexture.cpp:28-52).
-        const std::string file = res_dir_ + trim(ps.get("name"));
-        Image8 im8;
-        std::string ierr;
-        if (!load_image8(file, &im8, &ierr)) raise(ORION_ERR_IO, ierr);
-        if (im8.channels != 3 && im8.channels != 4)
-          raise(ORION_ERR_UNSUPPORTED, file + ": only 3- or 4-channel images are read by the reference");
-        HostImage hi;
-        hi.width = im8.width;
-        hi.height = im8.height;
-        hi.rgb.resize(im8.rgb.size());
-        const float inv255 = 0.0039215686274509803921568627451f;  // color_CharToFloat
-        for (size_t i = 0; i < im8.rgb.size(); ++i) hi.rgb[i] = im8.rgb[i] * inv255;
-        out_->images.push_back(std::move(hi));
-        l.image = (int32_t)out_->images.size();
+        // (src/light/envmap.cpp:120, :14-22).
+        l.image = load_image(res_dir_ + trim(ps.get("name")));
       }
       if (ps.has("L"))
         parse_spectrum(ps.get("L"), l.L);

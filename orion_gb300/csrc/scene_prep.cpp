@@ -6,6 +6,8 @@
 // computes per hit or at preprocess time.
 #include "scene_prep.h"
 
+#include "material_build.h"
+
 #include <cmath>
 #include <cstring>
 #include <limits>
@@ -15,43 +17,10 @@ namespace orion_gb300 {
 namespace {
 constexpr float kPiF = 3.14159265358979323846f;
 
-bool black3(const float* c) { return c[0] == 0.f && c[1] == 0.f && c[2] == 0.f; }
-void clamp0(const float* in, float* out) {
-  for (int k = 0; k < 3; ++k) out[k] = in[k] < 0.f ? 0.f : in[k];
-}
 void set3(float* d, const float* s) {
   d[0] = s[0];
   d[1] = s[1];
   d[2] = s[2];
-}
-
-DevLobe lobe(int kind, int type) {
-  DevLobe l;
-  std::memset(&l, 0, sizeof(l));
-  l.kind = kind;
-  l.type = type;
-  l.fresnel = FRESNEL_NOOP;
-  l.dist = DIST_GGX;
-  return l;
-}
-
-void add(DevMaterial* m, const DevLobe& l) {
-  if (m->num_lobes < kMaxLobes) m->lobes[m->num_lobes++] = l;
-}
-
-DevLobe microfacet_r(const float* R, int dist, float alpha) {
-  DevLobe l = lobe(LOBE_MICROFACET_R, BXDF_REFLECTION | BXDF_GLOSSY);
-  set3(l.c, R);
-  l.dist = dist;
-  l.alpha = alpha;
-  return l;
-}
-
-DevLobe dielectric_fresnel(DevLobe l, float eta_i, float eta_t) {
-  l.fresnel = FRESNEL_DIELECTRIC;
-  l.etaA = eta_i;
-  l.etaB = eta_t;
-  return l;
 }
 }  // namespace
 
@@ -63,131 +32,41 @@ float roughness_to_alpha(float roughness) {
 
 float spectrum_intensity(const float c[3]) { return 0.212671f * c[0] + 0.715160f * c[1] + 0.072169f * c[2]; }
 
+MaterialInputs material_inputs(const orion_material& mt) {
+  MaterialInputs in;
+  std::memset(&in, 0, sizeof(in));
+  in.type = mt.type;
+  in.dist = mt.distribution == ORION_DIST_BECKMANN ? DIST_BECKMANN : DIST_GGX;
+  set3(in.Kd, mt.Kd);
+  set3(in.Ks, mt.Ks);
+  set3(in.Kr, mt.Kr);
+  set3(in.Kt, mt.Kt);
+  set3(in.opacity, mt.opacity);
+  set3(in.eta_rgb, mt.eta_rgb);
+  set3(in.k, mt.k);
+  in.sigma = mt.has_sigma ? (mt.sigma < 0.f ? 0.f : mt.sigma) : 0.f;
+  in.roughness = mt.roughness;
+  in.eta = mt.eta;
+  in.alpha = roughness_to_alpha(mt.roughness);
+  if (in.sigma != 0.f) {  // src/bsdf/orennayar.cpp:5-12
+    float s = in.sigma * static_cast<float>(0.01745329251994329576923690768489);
+    float s2 = s * s;
+    in.on_a = 1.f - (s2 / (2.f * (s2 + 0.33f)));
+    in.on_b = 0.45f * s2 / (s2 + 0.09f);
+  }
+  return in;
+}
+
+bool material_textured(const orion_material& mt) {
+  for (int t = 0; t < kTexSlots; ++t)
+    if (mt.tex[t] != 0) return true;
+  return false;
+}
+
 DevMaterial prepare_material(const orion_material& mt) {
   DevMaterial m;
   std::memset(&m, 0, sizeof(m));
-  const int dist = mt.distribution == ORION_DIST_BECKMANN ? DIST_BECKMANN : DIST_GGX;
-  switch (mt.type) {
-    case ORION_MAT_MATTE: {  // src/material/matte.cpp:9-21
-      float r[3];
-      clamp0(mt.Kd, r);
-      float sig = mt.has_sigma ? (mt.sigma < 0.f ? 0.f : mt.sigma) : 0.f;
-      if (!black3(r)) {
-        if (sig == 0.f) {
-          DevLobe l = lobe(LOBE_LAMBERT_R, BXDF_REFLECTION | BXDF_DIFFUSE);
-          set3(l.c, r);
-          add(&m, l);
-        } else {  // src/bsdf/orennayar.cpp:5-12
-          DevLobe l = lobe(LOBE_OREN_NAYAR, BXDF_REFLECTION | BXDF_DIFFUSE);
-          set3(l.c, r);
-          float s = sig * static_cast<float>(0.01745329251994329576923690768489);
-          float s2 = s * s;
-          l.on_a = 1.f - (s2 / (2.f * (s2 + 0.33f)));
-          l.on_b = 0.45f * s2 / (s2 + 0.09f);
-          add(&m, l);
-        }
-      }
-      break;
-    }
-    case ORION_MAT_METAL: {  // src/material/metal.cpp:8-17
-      const float one[3] = {1.f, 1.f, 1.f};
-      DevLobe l = microfacet_r(one, dist, roughness_to_alpha(mt.roughness));
-      l.fresnel = FRESNEL_CONDUCTOR;
-      set3(l.fr_eta, mt.eta_rgb);
-      set3(l.fr_k, mt.k);
-      add(&m, l);
-      break;
-    }
-    case ORION_MAT_MIRROR: {  // src/material/mirror.cpp:6-13
-      float r[3];
-      clamp0(mt.Kr, r);
-      if (!black3(r)) {
-        DevLobe l = lobe(LOBE_SPECULAR_R, BXDF_REFLECTION | BXDF_SPECULAR);
-        set3(l.c, r);
-        add(&m, l);
-      }
-      break;
-    }
-    case ORION_MAT_GLASS: {  // src/material/glass.cpp:9-37
-      float e = mt.eta, rough = mt.roughness;
-      if (black3(mt.Kr) && black3(mt.Kt)) break;
-      float alpha = roughness_to_alpha(rough);
-      if (rough == 0.f) {
-        DevLobe l = lobe(LOBE_FRESNEL_SPECULAR, BXDF_REFLECTION | BXDF_TRANSMISSION | BXDF_SPECULAR);
-        set3(l.c, mt.Kr);
-        set3(l.c2, mt.Kt);
-        l.etaA = 1.f;
-        l.etaB = e;
-        add(&m, l);
-      } else {
-        if (!black3(mt.Kr)) add(&m, dielectric_fresnel(microfacet_r(mt.Kr, dist, alpha), 1.f, e));
-        if (!black3(mt.Kt)) {
-          DevLobe l = lobe(LOBE_MICROFACET_T, BXDF_TRANSMISSION | BXDF_GLOSSY);
-          set3(l.c, mt.Kt);
-          l.dist = dist;
-          l.alpha = alpha;
-          l.etaA = 1.f;
-          l.etaB = e;
-          add(&m, l);
-        }
-      }
-      break;
-    }
-    case ORION_MAT_PLASTIC: {  // src/material/plastic.cpp:8-24
-      float kd[3], ks[3];
-      clamp0(mt.Kd, kd);
-      if (!black3(kd)) {
-        DevLobe l = lobe(LOBE_LAMBERT_R, BXDF_REFLECTION | BXDF_DIFFUSE);
-        set3(l.c, kd);
-        add(&m, l);
-      }
-      clamp0(mt.Ks, ks);
-      if (!black3(ks))  // the reference's fixed Fresnel has the etas reversed (plastic.cpp:17)
-        add(&m, dielectric_fresnel(microfacet_r(ks, dist, roughness_to_alpha(mt.roughness)), 1.5f, 1.0f));
-      break;
-    }
-    case ORION_MAT_UBER: {  // src/material/uber.cpp:9-42
-      const float* op = mt.opacity;
-      float e = mt.eta;
-      float one_minus[3] = {1.f - op[0], 1.f - op[1], 1.f - op[2]}, t[3];
-      clamp0(one_minus, t);
-      if (!black3(t)) {
-        DevLobe l = lobe(LOBE_SPECULAR_T, BXDF_TRANSMISSION | BXDF_SPECULAR);
-        set3(l.c, t);
-        l.etaA = 1.f;
-        l.etaB = 1.f;
-        add(&m, l);
-      }
-      float tmp[3], c[3];
-      clamp0(mt.Kd, tmp);
-      for (int k = 0; k < 3; ++k) c[k] = tmp[k] * op[k];
-      if (!black3(c)) {
-        DevLobe l = lobe(LOBE_LAMBERT_R, BXDF_REFLECTION | BXDF_DIFFUSE);
-        set3(l.c, c);
-        add(&m, l);
-      }
-      clamp0(mt.Ks, tmp);
-      for (int k = 0; k < 3; ++k) c[k] = tmp[k] * op[k];
-      if (!black3(c)) add(&m, dielectric_fresnel(microfacet_r(c, dist, roughness_to_alpha(mt.roughness)), 1.f, e));
-      clamp0(mt.Kr, tmp);
-      for (int k = 0; k < 3; ++k) c[k] = tmp[k] * op[k];
-      if (!black3(c)) {
-        DevLobe l = lobe(LOBE_SPECULAR_R, BXDF_REFLECTION | BXDF_SPECULAR);
-        set3(l.c, c);
-        add(&m, dielectric_fresnel(l, 1.f, e));
-      }
-      clamp0(mt.Kt, tmp);
-      for (int k = 0; k < 3; ++k) c[k] = tmp[k] * op[k];
-      if (!black3(c)) {
-        DevLobe l = lobe(LOBE_SPECULAR_T, BXDF_TRANSMISSION | BXDF_SPECULAR);
-        set3(l.c, c);
-        l.etaA = 1.f;
-        l.etaB = e;
-        add(&m, l);
-      }
-      break;
-    }
-  }
+  build_material(material_inputs(mt), &m);
   unsigned kinds = 0;
   for (int i = 0; i < m.num_lobes; ++i) {
     int t = m.lobes[i].type;
@@ -208,6 +87,7 @@ DevMaterial prepare_material(const orion_material& mt) {
     m.shade_class = SC_PLASTIC;
   else
     m.shade_class = SC_GENERAL;
+  if (material_textured(mt)) m.shade_class = SC_TEXTURED;
   return m;
 }
 
@@ -312,6 +192,44 @@ bool prepare_scene(const HostScene& s, PreparedScene* out, std::string* err) {
   out->env_idx.clear();
   out->env_data.clear();
   out->envmaps.clear();
+  out->textures.clear();
+  out->mat_src.clear();
+  out->prim_uv.clear();
+  // Image textures (src/util/parser.cpp:433-461): one DevTexture per image
+  // that a material input reads, texels as loaded (no scaling).
+  std::vector<int> tex_of_image(s.images.size(), -1);
+  bool any_textured = false;
+  for (const orion_material& m : s.materials) {
+    DevMaterialSrc src;
+    std::memset(&src, 0, sizeof(src));
+    src.in = material_inputs(m);
+    for (int t = 0; t < 8; ++t) src.tex[t] = -1;
+    for (int t = 0; t < kTexSlots; ++t) {
+      if (m.tex[t] == 0) continue;
+      if (m.tex[t] < 0 || m.tex[t] > (int)s.images.size()) {
+        *err = "material references a missing image";
+        return false;
+      }
+      const int ii = m.tex[t] - 1;
+      if (tex_of_image[ii] < 0) {
+        const HostImage& im = s.images[ii];
+        PreparedScene::TextureLayout lay{im.width, im.height, out->env_data.size()};
+        out->env_data.insert(out->env_data.end(), im.rgb.begin(), im.rgb.begin() + 3 * (size_t)im.width * im.height);
+        tex_of_image[ii] = (int)out->textures.size();
+        out->textures.push_back(lay);
+      }
+      src.tex[t] = tex_of_image[ii];
+      any_textured = true;
+    }
+    out->mat_src.push_back(src);
+  }
+  if (any_textured) {
+    if (s.uvs.size() != 6 * (size_t)T) {
+      *err = "textured materials need texture coordinates for every primitive";
+      return false;
+    }
+    out->prim_uv = s.uvs;
+  }
   std::vector<float> power;
   for (size_t i = 0; i < s.lights.size(); ++i) {
     const orion_light& l = s.lights[i];

@@ -26,10 +26,24 @@ struct PreparedScene {
     size_t texels, cond_func, cond_cdf, cond_int, marg_func, marg_cdf;
   };
   std::vector<EnvMapLayout> envmaps;
+  // Image textures: texels in env_data too; per material its builder inputs
+  // and texture slots; per primitive its three texture coordinates (only
+  // when a material is textured).
+  struct TextureLayout {
+    int width, height;
+    size_t texels;
+  };
+  std::vector<TextureLayout> textures;
+  std::vector<DevMaterialSrc> mat_src;
+  std::vector<float> prim_uv;  // T x 6, or empty
 };
 
 // Materials -> lobe lists (Material::getBSDF, src/material/*.cpp).
 DevMaterial prepare_material(const orion_material& m);
+// The builder inputs of a material: its constants and derived constants.
+MaterialInputs material_inputs(const orion_material& m);
+// True when an input of the material comes from an image texture.
+bool material_textured(const orion_material& m);
 // Everything else; returns false with `err` set on inconsistent input.
 bool prepare_scene(const HostScene& s, PreparedScene* out, std::string* err);
 DevCamera prepare_camera(const orion_camera& cam);

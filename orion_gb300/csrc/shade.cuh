@@ -5,6 +5,7 @@
 #include "dmath.cuh"
 #include "kernels.h"
 #include "light.cuh"
+#include "material_build.h"
 #include "traverse.cuh"
 
 namespace orion_gb300 {
@@ -37,23 +38,6 @@ __device__ __forceinline__ void class_append(int* counters, int* queues, int str
   queues[(size_t)cls * stride + base + __popc(peers & ((1u << lane) - 1u))] = value;
 }
 
-// The slot of entry q of the class queues taken in class order (q < total).
-struct ClassQueues {
-  int start[kShadeClasses + 1];
-  __device__ __forceinline__ void load(const int* counters) {
-    start[0] = 0;
-#pragma unroll
-    for (int c = 0; c < kShadeClasses; ++c) start[c + 1] = start[c] + counters[c];
-  }
-  __device__ __forceinline__ int total() const { return start[kShadeClasses]; }
-  __device__ __forceinline__ int slot(const int* queues, int stride, int q) const {
-    int c = 0;
-#pragma unroll
-    for (int k = 1; k < kShadeClasses; ++k) c += q >= start[k] ? 1 : 0;
-    return queues[(size_t)c * stride + (q - start[c])];
-  }
-};
-
 struct Hit {
   V3 p, ng, ns, su, sv;
 };
@@ -81,6 +65,57 @@ __device__ __forceinline__ V3 point_on(const PrimShade& sh, float u, float v) {
   V3 p0 = ld3(sh.p), p1 = ld3(sh.p + 3), p2 = ld3(sh.p + 6);
   float w = 1.f - u - v;
   return w * p0 + u * p1 + v * p2;
+}
+
+// Texture coordinates at barycentrics (u, v) (src/core/kernel.cpp:138-142),
+// rounded without contraction: the texel choice is discontinuous in them.
+__device__ __forceinline__ void hit_uv(const float* uv, float u, float v, float* x, float* y) {
+  const float w = __fsub_rn(__fsub_rn(1.f, u), v);
+  *x = __fadd_rn(__fadd_rn(__fmul_rn(w, __ldg(uv + 0)), __fmul_rn(u, __ldg(uv + 2))), __fmul_rn(v, __ldg(uv + 4)));
+  *y = __fadd_rn(__fadd_rn(__fmul_rn(w, __ldg(uv + 1)), __fmul_rn(u, __ldg(uv + 3))), __fmul_rn(v, __ldg(uv + 5)));
+}
+
+// Texture::evaluate -> ImageTexture::sample(int, int) with the wrap filter
+// (src/core/texture.cpp:8-29, src/texture/imagetexture.cpp:4-12): texel
+// (int)(u * width), (int)(v * height), wrapped. The reference wraps a
+// negative multiple of the size to the size itself and reads the texel that
+// follows in memory (the next row's first); past the last texel, undefined
+// there, the last texel is read here.
+__device__ __forceinline__ V3 texture_eval(const DevTexture& t, float x, float y) {
+  const int w = t.width, h = t.height;
+  int ix = __float2int_rz(__fmul_rn(x, (float)w)), iy = __float2int_rz(__fmul_rn(y, (float)h));
+  ix = ix >= 0 ? ix % w : w - (int)((0u - (unsigned)ix) % (unsigned)w);
+  iy = iy >= 0 ? iy % h : h - (int)((0u - (unsigned)iy) % (unsigned)h);
+  int64_t off = (int64_t)iy * w + ix;
+  const int64_t last = (int64_t)w * h - 1;
+  off = off > last ? last : off;
+  const float* p = t.texels + 3 * off;
+  return V3{__ldg(p), __ldg(p + 1), __ldg(p + 2)};
+}
+
+// Material::getBSDF of a textured material at texture coordinates (x, y):
+// its image inputs looked up, then the lobe list built as the host builds
+// constant materials.
+static __device__ __noinline__ void textured_material(const SceneView& s, int mi, float x, float y, DevMaterial* m) {
+  const DevMaterialSrc& src = s.mat_src[mi];
+  MaterialInputs in = src.in;
+#pragma unroll
+  for (int t = 0; t < kTexSlots; ++t) {
+    const int ti = src.tex[t];
+    if (ti < 0) continue;
+    const V3 c = texture_eval(s.textures[ti], x, y);
+    float* d = t == ORION_TEX_KD ? in.Kd
+               : t == ORION_TEX_KS ? in.Ks
+               : t == ORION_TEX_KR ? in.Kr
+               : t == ORION_TEX_KT ? in.Kt
+               : t == ORION_TEX_OPACITY ? in.opacity
+               : t == ORION_TEX_ETA ? in.eta_rgb
+                                    : in.k;
+    d[0] = c.x;
+    d[1] = c.y;
+    d[2] = c.z;
+  }
+  build_material(in, m);
 }
 
 __device__ __forceinline__ TraceScene trace_scene(const SceneView& s) { return TraceScene{s.nodes, s.woop, s.tri_prim, s.tri_class}; }
@@ -139,8 +174,8 @@ __host__ __device__ constexpr unsigned lobes_of_class(int sc) {
 }
 
 // One bounce of PathTracing::Li for the path in slot `pid`, whose material
-// (if it hit one) holds only lobe kinds in KM.
-template <unsigned KM = kLobeAll>
+// (if it hit one) holds only lobe kinds in KM; TEX: the material is textured.
+template <unsigned KM = kLobeAll, bool TEX = false>
 __device__ __forceinline__ ShadeResult shade_one(const SceneView& s, const WaveView& w, const uint32_t* sobol_bitmajor,
                                                  int pid, uint64_t index, int bounce, int max_depth, int rr_depth) {
   LightDistrib distrib{s.light_func, s.light_cdf, s.light_func_int, s.num_lights};
@@ -171,7 +206,15 @@ __device__ __forceinline__ ShadeResult shade_one(const SceneView& s, const WaveV
     if (alive) {
       const PrimShade& sh = s.prims[prim];
       Hit h = reconstruct(sh, hv.y, hv.z);
-      const DevMaterial& m = s.mats[sh.material];
+      DevMaterial tm;  // a textured material's lobes at this hit
+      const DevMaterial* mp = &s.mats[sh.material];
+      if constexpr (TEX) {
+        float x, y;
+        hit_uv(s.prim_uv + 6 * (size_t)prim, hv.y, hv.z, &x, &y);
+        textured_material(s, sh.material, x, y, &tm);
+        mp = &tm;
+      }
+      const DevMaterial& m = *mp;
       Frame fr{h.ng, h.ns, h.su, h.sv};
       // This bounce consumes at most 8 sample dimensions (light choice 1,
       // light point 2, BSDF for MIS 2, continuation 2, roulette 1), all from

@@ -214,6 +214,7 @@ class Mesh:
     normals: np.ndarray  # V x 3
     material: dict
     area_le: tuple | None = None  # emitted radiance if this mesh is an area light
+    uvs: np.ndarray | None = None  # V x 2 texture coordinates (written as OBJ vt), or none (0, 0)
 
     @property
     def num_tris(self):
@@ -256,6 +257,12 @@ class Scene:
             ns.append(n)
             ids.append(np.full(m.num_tris, i, dtype=np.int32))
         return np.concatenate(ps), np.concatenate(ns), np.concatenate(ids)
+
+    def flat_uvs(self, text_rounding: bool = True) -> np.ndarray:
+        """Texture coordinates per primitive corner (T x 6); (0, 0) where a mesh has none."""
+        rnd = _f32 if text_rounding else (lambda a: np.asarray(a, np.float32))
+        return np.concatenate([rnd(m.uvs)[m.faces].reshape(-1, 6) if m.uvs is not None
+                               else np.zeros((m.num_tris, 6), np.float32) for m in self.meshes])
 
 
 def _f32(a):
@@ -404,7 +411,14 @@ def _fmt(v):
     return ",".join("%.7g" % float(x) for x in np.ravel(v))
 
 
-def _tex_color(tag, rgb):
+def _is_image(v) -> bool:
+    return isinstance(v, np.ndarray) and v.ndim == 3
+
+
+def _tex_color(tag, rgb, image_file=None):
+    if _is_image(rgb):  # an image texture: written as PNG beside the scene
+        return (f'      <{tag}>\n        <Param type="image"/>\n        <Param filename="{image_file(rgb)}"/>\n'
+                f'      </{tag}>\n')
     return f'      <{tag}>\n        <Param type="constant"/>\n        <Param color="{_fmt(rgb)}"/>\n      </{tag}>\n'
 
 
@@ -412,43 +426,53 @@ def _tex_float(tag, v):
     return f'      <{tag}>\n        <Param type="float"/>\n        <Param value="{_fmt([v])}"/>\n      </{tag}>\n'
 
 
-def material_xml(m: dict, name: str) -> str:
+def material_xml(m: dict, name: str, image_file=None) -> str:
+    """image_file(rgb8) -> file name: writes an image texture and names it."""
     t = m["type"]
     out = f'    <Material type="{t}" name="{name}">\n'
     if "distribution" in m:
         out += f'      <Param distribution="{m["distribution"]}"/>\n'
+
+    def col(tag):
+        return _tex_color(tag, m[tag], image_file)
     if t == "matte":
-        out += _tex_color("Kd", m["Kd"])
+        out += col("Kd")
         if "sigma" in m:
             out += _tex_float("sigma", m["sigma"])
     elif t == "metal":
-        out += _tex_color("eta", m["eta"]) + _tex_color("k", m["k"]) + _tex_float("roughness", m["roughness"])
+        out += col("eta") + col("k") + _tex_float("roughness", m["roughness"])
     elif t == "mirror":
-        out += _tex_color("Kr", m["Kr"])
+        out += col("Kr")
     elif t == "glass":
-        out += (_tex_color("Kr", m["Kr"]) + _tex_color("Kt", m["Kt"]) + _tex_float("eta", m["eta"])
-                + _tex_float("roughness", m["roughness"]))
+        out += col("Kr") + col("Kt") + _tex_float("eta", m["eta"]) + _tex_float("roughness", m["roughness"])
     elif t == "plastic":
-        out += _tex_color("Kd", m["Kd"]) + _tex_color("Ks", m["Ks"]) + _tex_float("roughness", m["roughness"])
+        out += col("Kd") + col("Ks") + _tex_float("roughness", m["roughness"])
     elif t == "uber":
         for k in ("Kd", "Ks", "Kr", "Kt", "opacity"):
-            out += _tex_color(k, m[k])
+            out += col(k)
         out += _tex_float("roughness", m["roughness"]) + _tex_float("eta", m["eta"])
     else:
         raise ValueError(t)
     return out + "    </Material>\n"
 
 
-def write_obj(path: str, pos: np.ndarray, faces: np.ndarray, normals: np.ndarray) -> None:
+def write_obj(path: str, pos: np.ndarray, faces: np.ndarray, normals: np.ndarray, uvs=None) -> None:
     p = np.char.mod("%.7g", np.asarray(pos, dtype=np.float64))
     n = np.char.mod("%.7g", np.asarray(normals, dtype=np.float64))
     f = (np.asarray(faces) + 1).astype(str)
     with open(path, "w") as fh:
         fh.write("\n".join("v " + " ".join(r) for r in p))
         fh.write("\n")
+        if uvs is not None:
+            t = np.char.mod("%.7g", np.asarray(uvs, dtype=np.float64))
+            fh.write("\n".join("vt " + " ".join(r) for r in t))
+            fh.write("\n")
         fh.write("\n".join("vn " + " ".join(r) for r in n))
         fh.write("\n")
-        fh.write("\n".join(f"f {a}//{a} {b}//{b} {c}//{c}" for a, b, c in f))
+        if uvs is not None:
+            fh.write("\n".join(f"f {a}/{a}/{a} {b}/{b}/{b} {c}/{c}/{c}" for a, b, c in f))
+        else:
+            fh.write("\n".join(f"f {a}//{a} {b}//{b} {c}//{c}" for a, b, c in f))
         fh.write("\n")
 
 
@@ -470,11 +494,19 @@ def write_ori(scene: Scene, directory: str, mesh_prefix: str | None = None) -> s
         out.append(f'    <Param lensRadius="{_fmt([scene.lens_radius])}"/>\n')
         out.append(f'    <Param focalDistance="{_fmt([scene.focal_distance])}"/>\n')
     out.append("  </Camera>\n")
+    written = {}
+
+    def image_file(rgb8):  # each texture image once, as PNG beside the scene
+        if id(rgb8) not in written:
+            fn = f"{scene.name}_tex{len(written)}.png"
+            write_png(os.path.join(directory, fn), rgb8)
+            written[id(rgb8)] = fn
+        return written[id(rgb8)]
     for i, m in enumerate(scene.meshes):
         fn = f"{prefix}_{m.name}.obj"
-        write_obj(os.path.join(directory, fn), m.pos, m.faces, m.normals)
+        write_obj(os.path.join(directory, fn), m.pos, m.faces, m.normals, m.uvs)
         out.append(f'  <Model type="mesh" filename="{fn}">\n')
-        out.append(material_xml(m.material, f"{scene.name}_m{i}"))
+        out.append(material_xml(m.material, f"{scene.name}_m{i}", image_file))
         if m.area_le is not None:
             out.append(f'    <AreaLight>\n      <Param Le="{_fmt(m.area_le)}"/>\n'
                        f'      <Param nLightSamples="1"/>\n    </AreaLight>\n')
@@ -552,6 +584,61 @@ def envlit(res: int = 64, spp: int = 16, max_depth: int = 6, subdiv: int = 3) ->
     return s
 
 
+def pattern_image(kind: str, width: int, height: int, seed: int) -> np.ndarray:
+    """A procedural 8-bit RGB texture: "checker" (8 x 8 cells of two seeded colours), "stripes"
+    (vertical bands of seeded colours) or "noise" (per-texel seeded values)."""
+    rng = Rng(seed)
+    if kind == "noise":
+        return np.array([[[int(rng.integers(0, 256)) for _ in range(3)] for _ in range(width)]
+                         for _ in range(height)], np.uint8)
+    cols = np.array([[int(rng.integers(20, 256)) for _ in range(3)] for _ in range(8)], np.uint8)
+    x = np.arange(width)[None, :]
+    y = np.arange(height)[:, None]
+    if kind == "checker":
+        idx = ((x * 8 // width) + (y * 8 // height)) % 2 + 0 * y
+    else:
+        idx = (x * 8 // width) % len(cols) + 0 * y
+    return cols[idx]
+
+
+def sphere_uvs(v: np.ndarray) -> np.ndarray:
+    """Longitude / latitude texture coordinates of unit-sphere vertices."""
+    u = 0.5 + np.arctan2(v[:, 2], v[:, 0]) / (2 * np.pi)
+    w = np.arccos(np.clip(v[:, 1], -1.0, 1.0)) / np.pi
+    return np.stack([u, w], 1)
+
+
+def textured(res: int = 64, spp: int = 16, max_depth: int = 6, subdiv: int = 3) -> Scene:
+    """Image textures on every kind of material input: a checkered matte ground whose texture
+    coordinates run past [0, 1) on both sides (wrap filter), and spheres with a textured plastic
+    Kd, metal eta, rough-glass Kt, mirror Kr and uber Kd + opacity; area light and a constant
+    environment."""
+    s = Scene("textured", res, res, spp, max_depth, (0.0, 1.4, 5.0), (0.0, 0.0, 0.0), (0, 1, 0), 45.0,
+              meta={"config": "image textures"})
+    checker = pattern_image("checker", 32, 32, 3)
+    stripes = pattern_image("stripes", 24, 12, 4)
+    noise = pattern_image("noise", 16, 8, 5)
+    p, f, nn = quad([(-6, -1, -6), (6, -1, -6), (6, -1, 6), (-6, -1, 6)], (0, 1, 0))
+    # u in [-0.65, 0.85], v in [-0.35, 1.15]: negative coordinates wrap, but none reaches -1, where the
+    # reference's wrap reads past the texel array (src/core/texture.cpp:16-24)
+    s.meshes.append(Mesh("ground", p, f, nn, {"type": "matte", "Kd": checker},
+                         uvs=np.stack([p[:, 0] / 8.0 + 0.1, p[:, 2] / 8.0 + 0.4], 1)))
+    mats = [{"type": "plastic", "Kd": stripes, "Ks": (0.4, 0.4, 0.4), "roughness": 0.2},
+            {"type": "metal", "eta": noise, "k": (3.9, 2.4, 2.1), "roughness": 0.25},
+            {"type": "glass", "Kr": (1.0, 1.0, 1.0), "Kt": stripes, "eta": 1.5, "roughness": 0.2},
+            {"type": "mirror", "Kr": checker},
+            {"type": "uber", "Kd": noise, "Ks": (0.3, 0.3, 0.3), "Kr": (0.1, 0.1, 0.1), "Kt": (0.2, 0.2, 0.2),
+             "opacity": checker, "roughness": 0.3, "eta": 1.4}]
+    for i, m in enumerate(mats):
+        v, fc = icosphere(subdiv)
+        c = np.array([-2.0 + 1.0 * i, -0.55, -0.3 + 0.25 * (i % 2)])
+        s.meshes.append(Mesh(f"ball{i}", v * 0.42 + c, fc, v.copy(), m, uvs=sphere_uvs(v)))
+    p, f, nn = quad([(-0.6, 2.8, -0.6), (0.6, 2.8, -0.6), (0.6, 2.8, 0.6), (-0.6, 2.8, 0.6)], (0, -1, 0))
+    s.meshes.append(Mesh("panel", p, f, nn, matte((0, 0, 0)), area_le=(8.0, 7.5, 7.0)))
+    s.envmaps.append({"L": (0.2, 0.22, 0.25), "worldUp": (0, 1, 0)})
+    return s
+
+
 def zoo(res: int = 64, spp: int = 16, max_depth: int = 6, subdiv: int = 2, beckmann: bool = False) -> Scene:
     """Every material and light type of the path tracer in one small scene.
 
@@ -591,16 +678,23 @@ def zoo(res: int = 64, spp: int = 16, max_depth: int = 6, subdiv: int = 2, beckm
 # in-memory host scenes (no OBJ text): for the batched and served workloads
 
 
-def _material_record(m: dict):
+TEX_INPUTS = ("Kd", "Ks", "Kr", "Kt", "opacity", "eta", "k")  # ORION_TEX_* order
+
+
+def _material_record(m: dict, image_index=None):
+    """image_index(rgb8) -> 1-based index of a texture image in the scene's image list."""
     from orion_gb300 import Material
     r = Material()
     kinds = {"matte": 0, "metal": 1, "mirror": 2, "glass": 3, "plastic": 4, "uber": 5}
     r.type = kinds[m["type"]]
     r.distribution = 1 if m.get("distribution") == "beckmann" else 0
-    for src, dst in [("Kd", "Kd"), ("Ks", "Ks"), ("Kr", "Kr"), ("Kt", "Kt"), ("opacity", "opacity"),
-                     ("eta", "eta_rgb" if m["type"] == "metal" else None), ("k", "k")]:
+    for slot, (src, dst) in enumerate([("Kd", "Kd"), ("Ks", "Ks"), ("Kr", "Kr"), ("Kt", "Kt"), ("opacity", "opacity"),
+                                       ("eta", "eta_rgb" if m["type"] == "metal" else None), ("k", "k")]):
         if src in m and dst is not None:
-            getattr(r, dst)[:] = [float(np.float32(x)) for x in m[src]]
+            if _is_image(m[src]):
+                r.tex[slot] = image_index(m[src])
+            else:
+                getattr(r, dst)[:] = [float(np.float32(x)) for x in m[src]]
     if m["type"] == "matte" and "sigma" in m:
         r.has_sigma, r.sigma = 1, m["sigma"]
     if "roughness" in m:
@@ -629,7 +723,15 @@ def to_host_scene(scene: Scene, text_rounding: bool = False):
     rounding (computed here in float64)."""
     import orion_gb300 as og
     P, N, mesh_of = scene.flat(text_rounding)
-    mats = [_material_record(m.material) for m in scene.meshes]
+    images, image_ids = [], {}
+
+    def image_index(rgb8):  # 8-bit texels as the loader converts them (byte * 1/255 in float)
+        if id(rgb8) not in image_ids:
+            images.append(np.asarray(rgb8, np.uint8).astype(np.float32) * np.float32(1.0 / 255.0))
+            image_ids[id(rgb8)] = len(images)
+        return image_ids[id(rgb8)]
+    mats = [_material_record(m.material, image_index) for m in scene.meshes]
+    uvs = scene.flat_uvs(text_rounding) if any(m.uvs is not None for m in scene.meshes) else None
     lights, light_of = [], np.full(len(P), -1, np.int32)
     for i, m in enumerate(scene.meshes):
         if m.area_le is None:
@@ -665,7 +767,6 @@ def to_host_scene(scene: Scene, text_rounding: bool = False):
             d = np.asarray(l["to"], np.float64) - np.asarray(l["from"], np.float64)
             L.dir[:] = list(d / np.linalg.norm(d))
         lights.append(L)
-    images = []
     for e in scene.envmaps:
         L = og.Light()
         L.type = og.LIGHT_ENV
@@ -690,7 +791,7 @@ def to_host_scene(scene: Scene, text_rounding: bool = False):
     cam = og.look_at_camera(scene.eye, scene.look, scene.up, scene.fov, scene.width, scene.height,
                             scene.lens_radius, scene.focal_distance)
     return og.HostScene.from_arrays(P, N, mesh_of, mats, lights, cam, scene.spp, scene.max_depth,
-                                    light_of_prim=light_of, images=images)
+                                    light_of_prim=light_of, uvs=uvs, images=images)
 
 
 def job_views(s: Scene, views: int = 16):

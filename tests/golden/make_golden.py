@@ -10,7 +10,8 @@ records its outputs on fixed inputs:
   camera.npz   Pinhole::generateRay, pinhole + thin lens    (src/camera/pinhole.cpp:8-33)
   trace.npz    Scene::intersect hits on the Cornell box     (project CPU kernel in Embree's place)
   image_*.npz  PathTracing::render film sums                (src/integrator/path.cpp:15-37);
-               image_envlit lit by an image environment map (src/light/envmap.cpp)
+               image_envlit lit by an image environment map (src/light/envmap.cpp),
+               image_textured with image textures on every material input (src/core/texture.cpp)
   stats_*.npz  FP64 per-pixel mean and variance at high spp (for 3-sigma checks)
   geometry.npz loader output digests
 
@@ -54,6 +55,16 @@ class Ref:
         info = np.zeros(5, np.int32)
         self.lib.ref_scene_info(h, vp(info))
         return h, info
+
+    def load_in_scene_dir(self, path):
+        """load() from the scene's directory: the reference opens image-texture file names
+        relative to the working directory (src/util/parser.cpp:438-443)."""
+        cwd = os.getcwd()
+        os.chdir(os.path.dirname(os.path.abspath(path)))
+        try:
+            return self.load(os.path.abspath(path))
+        finally:
+            os.chdir(cwd)
 
     def sobol(self, idx, dim):
         out = np.zeros(len(idx), np.float32)
@@ -156,9 +167,9 @@ def main():
 
         # Images through the reference's own PathTracing::render
         for name, kw in [("cornell", dict(res=64, spp=16)), ("zoo", dict(res=48, spp=16)),
-                         ("envlit", dict(res=48, spp=16))]:
+                         ("envlit", dict(res=48, spp=16)), ("textured", dict(res=48, spp=16))]:
             path = helpers.write_scene(name, os.path.join(tmp, "img_" + name), **kw)
-            h, info = ref.load(path)
+            h, info = ref.load_in_scene_dir(path)
             W, H = int(info[0]), int(info[1])
             img = np.zeros((H, W, 3), np.float32)
             ref.lib.ref_scene_render(h, vp(img))

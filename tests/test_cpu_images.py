@@ -1,4 +1,4 @@
-"""Environment-map image files as the scene loader reads them.
+"""Image files as the scene loader reads them: environment maps and textures.
 
 The reference loads `<Envmap><Param name=.../>` through stb_image and accepts
 3- or 4-channel images only (src/texture/imagetexture.cpp:20-36); texels are
@@ -175,3 +175,43 @@ def test_rejected_images_raise(scene_dir):
     open(d / "junk.tga", "wb").write(os.urandom(11))
     with pytest.raises(og.OrionError):
         _load(scene_dir, "junk.tga")
+
+
+def test_image_textures_load_into_material_slots(tmp_path):
+    """<Kd><Param type="image"/><Param filename=.../></Kd> (src/util/parser.cpp:433-461): the loaded scene
+    equals the in-memory one, with each image loaded once and referenced from its material inputs."""
+    import orion_gb300 as og
+    sc = scenegen.textured(res=16, spp=1, subdiv=1)
+    path = scenegen.write_ori(sc, str(tmp_path))
+    host = og.HostScene.load(path)
+    a = host.arrays()
+    b = scenegen.to_host_scene(sc, text_rounding=True).arrays()
+    assert len(a["images"]) == 3 and all(np.array_equal(x, y) for x, y in zip(a["images"], b["images"]))
+    assert np.array_equal(a["uvs"], b["uvs"])
+    tex = [list(m.tex) for m in a["materials"]]
+    assert tex == [list(m.tex) for m in b["materials"]]
+    slots = dict(zip(scenegen.TEX_INPUTS, range(7)))
+    # ground Kd, plastic Kd, metal eta, glass Kt, mirror Kr, uber Kd + opacity; the light panel is constant
+    expect = [{"Kd": 1}, {"Kd": 2}, {"eta": 3}, {"Kt": 2}, {"Kr": 1}, {"Kd": 3, "opacity": 1}, {}]
+    for t, e in zip(tex, expect):
+        want = [0] * 8
+        for k, v in e.items():
+            want[slots[k]] = v
+        assert t == want
+
+
+def test_texture_files_resolve_from_the_scene_directory(tmp_path, monkeypatch):
+    import orion_gb300 as og
+    sc = scenegen.textured(res=16, spp=1, subdiv=1)
+    path = scenegen.write_ori(sc, str(tmp_path / "s"))
+    monkeypatch.chdir(tmp_path)  # not the scene's directory
+    assert len(og.HostScene.load(path).arrays()["images"]) == 3
+    text = open(path).read()
+    absolute = re.sub(r'filename="(textured_tex\d\.png)"', lambda m: f'filename="{tmp_path / "s" / m.group(1)}"', text)
+    p2 = tmp_path / "s" / "abs.ori"
+    p2.write_text(absolute)
+    assert len(og.HostScene.load(str(p2)).arrays()["images"]) == 3
+    missing = tmp_path / "s" / "missing.ori"
+    missing.write_text(text.replace("textured_tex1.png", "nothing_here.png"))
+    with pytest.raises(og.OrionError, match="nothing_here"):
+        og.HostScene.load(str(missing))

@@ -76,7 +76,7 @@ def test_port_trace_matches_reference_and_brute_force(port, tmp_path):
 
 
 @pytest.mark.parametrize("name,kw", [("cornell", dict(res=64, spp=16)), ("zoo", dict(res=48, spp=16)),
-                                     ("envlit", dict(res=48, spp=16))])
+                                     ("envlit", dict(res=48, spp=16)), ("textured", dict(res=48, spp=16))])
 def test_port_image_matches_reference_render(port, tmp_path, name, kw):
     g = helpers.golden(f"image_{name}.npz")
     path = helpers.write_scene(name, str(tmp_path / name), **kw)

@@ -20,7 +20,7 @@ pytestmark = pytest.mark.gpu
 
 SCENES = [("cornell", dict(res=48, spp=8)), ("zoo", dict(res=40, spp=4, beckmann=True)),
           ("mixed", dict(width=64, height=36, spp=4, subdivs=(2, 2, 2, 2, 2, 2, 2, 2))),
-          ("displaced", dict(res=32, spp=6, subdiv=4))]
+          ("displaced", dict(res=32, spp=6, subdiv=4)), ("textured", dict(res=32, spp=4, subdiv=2))]
 
 
 @pytest.fixture(scope="module")

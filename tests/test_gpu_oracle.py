@@ -67,6 +67,7 @@ def test_million_rays_match_oracle(ctx, port, tmp_path, name, kw):
     ("mixed", dict(width=96, height=54, spp=8, subdivs=(2, 2, 2, 2, 2, 2, 2, 2))),
     ("displaced", dict(res=64, spp=8, subdiv=5)),
     ("envlit", dict(res=64, spp=8)),
+    ("textured", dict(res=64, spp=8)),
 ])
 def test_image_matches_oracle_path_for_path(ctx, port, tmp_path, name, kw):
     import orion_gb300 as og
