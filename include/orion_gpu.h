@@ -126,6 +126,18 @@ typedef struct orion_camera {
   int32_t width, height;   /* film size */
 } orion_camera;
 
+/* ------------------------------------------------------------ integrator */
+/* <Integrator type=...> (src/util/parser.cpp:123-137). */
+enum { ORION_INTEGRATOR_PATH = 0, ORION_INTEGRATOR_SPPM = 1 };
+
+/* SPPM parameters (createSPPMIntegrator, src/integrator/sppm.cpp:324-333). */
+typedef struct orion_sppm_params {
+  int32_t iterations;        /* numIterations */
+  int32_t photons_per_iter;  /* photonsPerIteration; < 0 = film width x height */
+  float initial_radius;      /* initRadius */
+  int32_t max_depth;         /* maxDepth */
+} orion_sppm_params;
+
 /* ----------------------------------------------------------------- scene */
 /* Flat, de-indexed scene in primitive (primID) order: the data the
  * reference hands to Embree plus what shading needs per primitive. */
@@ -145,7 +157,10 @@ typedef struct orion_scene_desc {
   int32_t max_depth;             /* <Integrator> maxDepth */
   int32_t num_images;
   int32_t reserved;
-  const orion_image* images;     /* referenced by orion_light.image */
+  const orion_image* images;     /* referenced by orion_light.image and orion_material.tex */
+  int32_t integrator;            /* ORION_INTEGRATOR_*; spp and max_depth above are the path tracer's */
+  int32_t reserved2;
+  orion_sppm_params sppm;        /* ORION_INTEGRATOR_SPPM: its parameters */
 } orion_scene_desc;
 
 typedef struct orion_host_scene orion_host_scene;
@@ -193,6 +208,15 @@ typedef struct orion_render_params {
 enum {
   ORION_RENDER_FP64 = 1      /* also accumulate FP64 sums and sums of squares */
 };
+
+/* SPPM::render (src/integrator/sppm.cpp:58-322) of a resident scene with
+ * its camera: `params` NULL = the scene's <Integrator type="sppm">
+ * parameters. film_rgb_sum: W*H*3 floats, the sum over iterations of each
+ * iteration's estimate (the reference accumulates one per iteration into
+ * its film); film_count: W*H (each = iterations) or NULL. Stats: paths =
+ * camera paths + photons, rays = all rays traced. */
+int orion_gpu_render_sppm(orion_gpu_ctx* ctx, orion_scene_id id, const orion_sppm_params* params,
+                          float* film_rgb_sum, uint32_t* film_count);
 
 /* Render statistics of the last orion_gpu_render on a context. */
 typedef struct orion_render_stats {

@@ -33,6 +33,7 @@ def lib() -> C.CDLL:
             ("port_render", i64, [vp, i32, i64, i32, i32, i32, i32, vp, i32]),
             ("port_render_pixels", i32, [vp, i64, vp, i64, i32, i32, i32, vp, vp, i32]),
             ("port_scene_info", i32, [vp, vp]),
+            ("port_render_sppm", i64, [vp, i32, i32, C.c_float, i32, vp]),
         ]:
             f = getattr(l, name)
             f.restype, f.argtypes = res, args
@@ -71,6 +72,9 @@ class Scene:
         info = np.zeros(5, np.int32)
         lib().port_scene_info(self._h, _p(info))
         self.width, self.height, self.spp, self.max_depth, self.num_lights = (int(x) for x in info)
+        self.integrator = int(d.integrator)
+        self.sppm = (int(d.sppm.iterations), int(d.sppm.photons_per_iter), float(d.sppm.initial_radius),
+                     int(d.sppm.max_depth))
         self._og = og
 
     @classmethod
@@ -103,6 +107,19 @@ class Scene:
         rays = lib().port_render(self._h, spp or self.spp, first_pass,
                                  self.max_depth if max_depth is None else max_depth, rr_depth, r0, r1, _p(film),
                                  threads)
+        return film, int(rays)
+
+    def render_sppm(self, iterations=None, photons=None, radius=None, max_depth=None):
+        """FP32 film sums (H, W, 3) of SPPM::render: one estimate per iteration added to the film.
+        Defaults: the scene's sppm parameters (photons < 0: W x H)."""
+        it0, ph0, r0, md0 = self.sppm
+        it = it0 if iterations is None else iterations
+        ph = ph0 if photons is None else photons
+        if ph < 0:
+            ph = self.width * self.height
+        film = np.zeros((self.height, self.width, 3), np.float32)
+        rays = lib().port_render_sppm(self._h, it, ph, r0 if radius is None else radius,
+                                      md0 if max_depth is None else max_depth, _p(film))
         return film, int(rays)
 
     def render_pixels(self, pix, spp, first_pass=0, max_depth=None, rr_depth=3, threads=0):

@@ -30,6 +30,7 @@ namespace port {
 constexpr float kPi = 3.14159265358979323846f;     // src/orion.h:52-58
 constexpr float kInvPi = 0.31830988618379067154f;
 constexpr float kInv2Pi = 0.15915494309189533577f;
+constexpr float kInv4Pi = 0.07957747154594766788f;
 constexpr float kPiOver2 = 1.57079632679489661923f;
 constexpr float kPiOver4 = 0.78539816339744830961f;
 constexpr float kEpsilon = 0.000001f;
@@ -193,6 +194,7 @@ struct Lobe {
   V c, c2;
   float alpha = 0, etaA = 1, etaB = 1, A = 0, B = 0;
   V fr_eta, fr_k;
+  bool photon = false;  // TransportMode::Photon: no radiance scaling on transmission
 };
 
 struct Mat {
@@ -335,7 +337,7 @@ V lobeF(const Lobe& l, V wi, V wo) {
       if (wh.z < 0) wh = -wh;
       float F = frDielectric(std::abs(dot(wo, wh)), l.etaA, l.etaB);
       float sd = dot(wo, wh) + eta * dot(wi, wh);
-      float factor = 1 / eta;
+      float factor = l.photon ? 1 : 1 / eta;  // microfacet.cpp:102
       return mul(V(1.f - F), l.c) * std::abs(mfD(l, wh) * mfG(l, wi, wo) * eta * eta * absdot(wi, wh) *
                                              absdot(wo, wh) * factor * factor / (ci * co * sd * sd));
     }
@@ -400,7 +402,7 @@ V lobeSample(const Lobe& l, V wo, float u0, float u1, V* wi, float* pdf, int* st
       if (!refract(wo, faceforward(V(0, 0, 1), wo), ei / et, wi)) return V(0.f);
       *pdf = 1.0f;
       V ft = mul(l.c, V(1.0f) - V(frDielectric(std::abs(cosT(*wi)), l.etaA, l.etaB)));
-      ft = mul(ft, V((ei * ei) / (et * et)));
+      if (!l.photon) ft = mul(ft, V((ei * ei) / (et * et)));
       return sdiv(ft, absCosT(*wi));
     }
     case FRES_SPEC: {  // src/bsdf/specular.cpp:28-54
@@ -415,7 +417,7 @@ V lobeSample(const Lobe& l, V wo, float u0, float u1, V* wi, float* pdf, int* st
       float ei = entering ? l.etaA : l.etaB, et = entering ? l.etaB : l.etaA;
       if (!refract(wo, faceforward(V(0, 0, 1), wo), ei / et, wi)) return V(0.f);
       V ft = l.c2 * (1 - F);
-      ft = mul(ft, V((ei * ei) / (et * et)));
+      if (!l.photon) ft = mul(ft, V((ei * ei) / (et * et)));
       *st = SPEC | TRANS;
       *pdf = 1 - F;
       return sdiv(ft, absCosT(*wi));
@@ -800,6 +802,7 @@ struct Scene {
   std::vector<float> func, cdf;
   float funcInt = 0;
   float worldRadius = 0;
+  V worldCenter{0.f};
   orion_camera cam;
   float tanHalf = 0, aspect = 1;
   int spp = 1, maxDepth = 5;
@@ -1136,6 +1139,349 @@ V Li(const Scene& s, V ro, V rd, Sampler& smp, int maxDepth, int rrDepth, int64_
   return L;
 }
 
+// ------------------------------------------------------------------ SPPM
+// SPPM::render (src/integrator/sppm.cpp:58-322), restated one thread at a
+// time: the photon contributions add in photon order and each grid cell
+// lists its visible points most recent first, as the reference's
+// single-threaded run builds and walks them.
+
+// coordinateSystem (src/core/geometry.h:902-909)
+inline void coordinateSystem(V z, V* x, V* y) {
+  if (std::abs(z.x) > std::abs(z.y))
+    *y = vdiv(V(-z.z, 0, z.x), std::sqrt(z.x * z.x + z.z * z.z));
+  else
+    *y = vdiv(V(0, z.z, -z.y), std::sqrt(z.y * z.y + z.z * z.z));
+  *x = cross(*y, z);
+}
+
+// Material at a hit in the given transport mode (Intersection::calculateBSDF).
+Mat materialAt(const Scene& s, const Isect& it, bool photon) {
+  const int mi = s.matOf[it.prim];
+  Mat m = s.textured[mi] ? s.material(mi, it) : s.mats[mi];
+  if (photon)
+    for (Lobe& l : m.lobes) l.photon = true;
+  return m;
+}
+
+// Light::sample_Le (src/light/{diffuse,point,spot,distant,envmap}.cpp);
+// rand0 / rand1 as the reference's Point2f (x = the later dimension).
+V sampleLe(const Scene& s, const Light& L, float r0x, float r0y, float r1x, float r1y, V* ro, V* rd, V* nLight,
+           float* pdfPos, float* pdfDir) {
+  *pdfPos = *pdfDir = 0;
+  switch (L.type) {
+    case ORION_LIGHT_AREA: {  // diffuse.cpp:32-44, triangle.cpp:85-106
+      const float* q = &s.pos[9 * (size_t)L.prim];
+      const float* n = &s.nrm[9 * (size_t)L.prim];
+      float su0 = std::sqrt(r0x);
+      float b0 = 1 - su0, b1 = r0y * su0;
+      V p0 = ld(q), p1 = ld(q + 3), p2 = ld(q + 6);
+      V p = b0 * p0 + b1 * p1 + (1 - b0 - b1) * p2;
+      V ng = normalize(cross(p1 - p0, p2 - p0));
+      V ns = ld(n) * b0 + ld(n + 3) * b1 + ld(n + 6) * (1.0f - b0 - b1);
+      ng = faceforward(ng, ns);
+      *pdfPos = 1.0f / L.area;
+      *nLight = ng;
+      V w = cosineSampleHemisphere(r1x, r1y);
+      *pdfDir = w.z * kInvPi;
+      V x, y;
+      coordinateSystem(ng, &x, &y);
+      w = w.x * x + w.y * y + w.z * ng;
+      *ro = offsetRayOrigin(p, ng, w);
+      *rd = w;
+      return dot(ng, w) > 0 ? L.L : V(0.f);
+    }
+    case ORION_LIGHT_POINT: {  // point.cpp:20-27
+      float z = 1 - 2 * r0x;
+      float r = std::sqrt(std::max((float)0, (float)1 - z * z));
+      float phi = 2 * kPi * r0y;
+      *ro = L.p;
+      *rd = V(r * std::cos(phi), r * std::sin(phi), z);
+      *nLight = *rd;
+      *pdfPos = 1;
+      *pdfDir = kInv4Pi;
+      return L.L;
+    }
+    case ORION_LIGHT_SPOT: {  // spot.cpp:30-38
+      float cosTheta = ((float)1 - r0x) + r0x * L.cosTotal;
+      float sinTheta = std::sqrt((float)1 - cosTheta * cosTheta);
+      float phi = r0y * 2 * kPi;
+      V w(std::cos(phi) * sinTheta, std::sin(phi) * sinTheta, cosTheta);
+      *ro = L.p;
+      *rd = mat3(L.l2w, w);
+      *nLight = *rd;
+      *pdfPos = 1;
+      *pdfDir = 1 / (2 * kPi * (1 - L.cosTotal));
+      V wl = normalize(mat3(L.w2l, *rd));
+      float c = wl.z, f;
+      if (c < L.cosTotal)
+        f = 0;
+      else if (c > L.cosFalloff)
+        f = 1;
+      else {
+        float d = (c - L.cosTotal) / (L.cosFalloff - L.cosTotal);
+        f = (d * d) * (d * d);
+      }
+      return L.L * f;
+    }
+    case ORION_LIGHT_DISTANT: {  // distant.cpp:28-41
+      V v1, v2;
+      coordinateSystem(L.dir, &v1, &v2);
+      float cx, cy;
+      concentricSampleDisk(r0x, r0y, &cx, &cy);
+      V pDisk = s.worldCenter + s.worldRadius * (cx * v1 + cy * v2);
+      *ro = pDisk + s.worldRadius * L.dir;
+      *rd = -L.dir;
+      *nLight = *rd;
+      *pdfPos = 1 / (kPi * s.worldRadius * s.worldRadius);
+      *pdfDir = 1;
+      return L.L;
+    }
+    case ORION_LIGHT_ENV: {  // envmap.cpp:82-104
+      float su, sv, mapPdf;
+      if (L.image) {
+        L.image->sampleContinuous(r0x, r0y, &su, &sv, &mapPdf);
+      } else {  // 1x1 distribution: uv = u, mapPdf = 1 (0 for a black map)
+        su = r0x, sv = r0y;
+        mapPdf = L.envInt == 0 ? 0.f : 1.f;
+      }
+      if (mapPdf == 0) return V(0.f);
+      float theta = sv * kPi, phi = su * 2.f * kPi;
+      float ct = std::cos(theta), st = std::sin(theta), sp = std::sin(phi), cp = std::cos(phi);
+      V d = -mat3(L.l2w, V(st * cp, st * sp, ct));
+      *nLight = d;
+      V v1, v2;
+      coordinateSystem(-d, &v1, &v2);
+      float cx, cy;
+      concentricSampleDisk(r1x, r1y, &cx, &cy);
+      V pDisk = s.worldCenter + s.worldRadius * (cx * v1 + cy * v2);
+      *ro = pDisk + s.worldRadius * -d;
+      *rd = d;
+      *pdfDir = st == 0 ? 0 : mapPdf / (2 * kPi * kPi * st);
+      *pdfPos = 1 / (kPi * s.worldRadius * s.worldRadius);
+      return L.image ? L.image->sample(su, sv) : L.L;
+    }
+  }
+  return V(0.f);
+}
+
+struct SppmPixel {
+  float radius = 0;
+  V Ld{0.f};
+  bool vp = false;  // a visible point this iteration (the reference: vp.beta non-black)
+  V vpP{0.f}, vpWo{0.f}, vpBeta{0.f};
+  Mat vpMat;
+  Frame vpFr;
+  V phi{0.f};
+  int M = 0;
+  float N = 0;
+  V tau{0.f};
+};
+
+struct SppmGrid {
+  V lo{kInfinity}, hi{-kInfinity};  // Bounds3f(): pMin = max, pMax = lowest
+  int res[3] = {1, 1, 1};
+  // offset() then the truncated cell index, clamped (sppm.cpp:41-51)
+  bool toGrid(V p, int* c) const {
+    V o = p - lo;
+    if (hi.x > lo.x) o.x = o.x / (hi.x - lo.x);
+    if (hi.y > lo.y) o.y = o.y / (hi.y - lo.y);
+    if (hi.z > lo.z) o.z = o.z / (hi.z - lo.z);
+    float pg[3] = {o.x, o.y, o.z};
+    bool in = true;
+    for (int i = 0; i < 3; ++i) {
+      c[i] = (int)(res[i] * pg[i]);
+      in &= c[i] >= 0 && c[i] < res[i];
+      c[i] = std::min(std::max(c[i], 0), res[i] - 1);
+    }
+    return in;
+  }
+};
+
+// hash (sppm.cpp:53-57), products taken modulo 2^32
+inline unsigned sppmHash(const int* c, int size) {
+  return (((unsigned)c[0] * 73856093u) ^ ((unsigned)c[1] * 19349663u) ^ ((unsigned)c[2] * 83492791u)) %
+         (unsigned)size;
+}
+
+// film: W*H*3 sums of each iteration's estimate (RenderTarget::acumulate).
+void renderSppm(const Scene& s, int nIter, int photons, float radius0, int maxDepth, float* film, int64_t* rays) {
+  const int W = s.cam.width, H = s.cam.height, nPix = W * H;
+  std::vector<SppmPixel> px(nPix);
+  for (SppmPixel& p : px) p.radius = radius0;
+  const int nL = (int)s.lights.size();
+  for (int iter = 0; iter < nIter; ++iter) {
+    // Visible points (sppm.cpp:78-140).
+    for (int j = 0; j < H; ++j)
+      for (int i = 0; i < W; ++i) {
+        Sampler smp{(uint64_t)iter * nPix + (uint64_t)W * j + i};
+        V ro, rd;
+        cameraRay(s, smp, i, j, &ro, &rd);
+        V beta(1.0f);
+        SppmPixel& pixel = px[(size_t)W * j + i];
+        bool specular = false;
+        for (int depth = 0; depth < maxDepth; ++depth) {
+          Isect it;
+          ++*rays;
+          if (!s.intersect(ro, rd, 0, kInfinity, &it)) {
+            for (int e : s.envs) pixel.Ld = pixel.Ld + mul(beta, envLe(s.lights[e], rd));
+            break;
+          }
+          Mat m = materialAt(s, it, false);
+          Frame fr{it.ng, it.ns, it.u, it.v};
+          V wo = -rd;
+          if (depth == 0 || specular) {
+            int li = s.lightOf[it.prim];
+            V Le = (li >= 0 && dot(it.ng, wo) > 0) ? s.lights[li].L : V(0.f);
+            pixel.Ld = pixel.Ld + mul(beta, Le);
+          }
+          V direct(0.f);  // uniformSampleOneLight without a light distribution (integrator.cpp:8-27)
+          if (nL > 0) {
+            int li = std::min((int)(smp.next() * nL), nL - 1);
+            float lightPdf = 1.0f / nL;
+            float a = smp.next(), b = smp.next(), c = smp.next(), d = smp.next();
+            direct = sdiv(estimateDirect(s, rd, it, m, fr, d, c, s.lights[li], li, b, a, rays), lightPdf);
+          }
+          pixel.Ld = pixel.Ld + mul(beta, direct);
+          bool isDiffuse = numMatching(m, DIFF | REFL | TRANS) > 0;
+          bool isGlossy = numMatching(m, GLOSSY | REFL | TRANS) > 0;
+          if (isDiffuse || (isGlossy && depth == maxDepth - 1)) {
+            pixel.vp = !black(beta);
+            pixel.vpP = it.p;
+            pixel.vpWo = wo;
+            pixel.vpBeta = beta;
+            pixel.vpMat = m;
+            pixel.vpFr = fr;
+            break;
+          }
+          if (depth < maxDepth - 1) {
+            float u0 = smp.next(), u1 = smp.next();
+            V wi;
+            float pdf;
+            int st;
+            V f = bsdfSample(m, fr, wo, u1, u0, ALL, &wi, &pdf, &st);
+            if (pdf == 0 || black(f)) break;
+            specular = (st & SPEC) != 0;
+            beta = mul(beta, sdiv(f * absdot(wi, it.ns), pdf));
+            if (intensity(beta) < 0.25f) {
+              float continueProb = std::min((float)1, intensity(beta));
+              if (smp.next() > continueProb) break;
+              beta = sdiv(beta, continueProb);
+            }
+            ro = offsetRayOrigin(it.p, it.ng, wi);
+            rd = wi;
+          }
+        }
+      }
+    // Visible-point grid (sppm.cpp:142-195).
+    SppmGrid g;
+    float maxRadius = 0;
+    bool any = false;
+    for (const SppmPixel& p : px) {
+      if (!p.vp) continue;
+      any = true;
+      V r(p.radius);
+      V lo = p.vpP - r, hi = p.vpP + r;
+      g.lo = V(std::min(g.lo.x, lo.x), std::min(g.lo.y, lo.y), std::min(g.lo.z, lo.z));
+      g.hi = V(std::max(g.hi.x, hi.x), std::max(g.hi.y, hi.y), std::max(g.hi.z, hi.z));
+      maxRadius = std::max(maxRadius, p.radius);
+    }
+    std::vector<std::vector<int>> cells(nPix);  // each list most recent first
+    if (any) {
+      V diag = g.hi - g.lo;
+      float maxDiag = maxc(diag);
+      int base = (int)(maxDiag / maxRadius);
+      float dg[3] = {diag.x, diag.y, diag.z};
+      for (int i = 0; i < 3; ++i) g.res[i] = std::max((int)(base * dg[i] / maxDiag), 1);
+      for (int pi = 0; pi < nPix; ++pi) {
+        const SppmPixel& p = px[pi];
+        if (!p.vp) continue;
+        V r(p.radius);
+        int lo[3], hi[3];
+        g.toGrid(p.vpP - r, lo);
+        g.toGrid(p.vpP + r, hi);
+        for (int z = lo[2]; z <= hi[2]; ++z)
+          for (int y = lo[1]; y <= hi[1]; ++y)
+            for (int x = lo[0]; x <= hi[0]; ++x) {
+              int c[3] = {x, y, z};
+              cells[sppmHash(c, nPix)].push_back(pi);
+            }
+      }
+    }
+    // Photons (sppm.cpp:197-270).
+    for (int k = 0; any && k < photons; ++k) {
+      Sampler smp{(uint64_t)nIter * nPix + (uint64_t)iter * photons + k};
+      float lightPdf;
+      int ln = sampleDiscrete(s, smp.next(), &lightPdf);
+      const Light& L = s.lights[ln];
+      float a = smp.next(), b = smp.next(), c = smp.next(), d = smp.next();
+      V ro, rd, nLight;
+      float pdfPos, pdfDir;
+      V Le = sampleLe(s, L, b, a, d, c, &ro, &rd, &nLight, &pdfPos, &pdfDir);
+      if (pdfPos == 0 || pdfDir == 0 || black(Le)) continue;
+      V beta = sdiv(absdot(nLight, rd) * Le, lightPdf * pdfPos * pdfDir);
+      if (black(beta)) continue;
+      for (int depth = 0; depth < maxDepth; ++depth) {
+        Isect it;
+        ++*rays;
+        if (!s.intersect(ro, rd, 0, kInfinity, &it)) break;
+        if (depth > 0) {
+          int cell[3];
+          if (g.toGrid(it.p, cell)) {
+            const std::vector<int>& list = cells[sppmHash(cell, nPix)];
+            for (size_t e = list.size(); e-- > 0;) {
+              SppmPixel& p = px[list[e]];
+              if (len_sq(p.vpP - it.p) > p.radius * p.radius) continue;
+              V wi = -rd;
+              V Phi = mul(beta, bsdfF(p.vpMat, p.vpFr, wi, p.vpWo, ALL));
+              p.phi = p.phi + Phi;
+              ++p.M;
+            }
+          }
+        }
+        Mat m = materialAt(s, it, true);
+        Frame fr{it.ng, it.ns, it.u, it.v};
+        V wo = -rd, wi;
+        float pdf;
+        int st;
+        float u0 = smp.next(), u1 = smp.next();
+        V f = bsdfSample(m, fr, wo, u1, u0, ALL, &wi, &pdf, &st);
+        if (black(f) || pdf == 0) break;
+        V bnew = sdiv(mul(beta, f) * absdot(wi, it.ns), pdf);
+        float q = std::max((float)0, 1 - intensity(bnew) / intensity(beta));
+        if (smp.next() < q) break;
+        beta = sdiv(bnew, 1 - q);
+        ro = offsetRayOrigin(it.p, it.ng, wi);
+        rd = wi;
+      }
+    }
+    // Pixel update (sppm.cpp:285-312).
+    for (SppmPixel& p : px) {
+      if (p.M > 0) {
+        float gamma = (float)2 / (float)3;
+        float Nnew = p.N + gamma * p.M;
+        float Rnew = p.radius * std::sqrt(Nnew / (p.N + p.M));
+        p.tau = sdiv((p.tau + mul(p.vpBeta, p.phi)) * (Rnew * Rnew), p.radius * p.radius);
+        p.N = Nnew;
+        p.radius = Rnew;
+        p.M = 0;
+        p.phi = V(0.f);
+      }
+      p.vp = false;
+      p.vpBeta = V(0.f);
+    }
+    // Film (sppm.cpp:314-320).
+    const uint64_t Np = (uint64_t)nIter * (uint64_t)photons;
+    for (int pi = 0; pi < nPix; ++pi) {
+      const SppmPixel& p = px[pi];
+      V L = sdiv(p.Ld, (float)nIter);
+      L = L + sdiv(p.tau, Np * kPi * p.radius * p.radius);
+      film[3 * pi] += L.x;
+      film[3 * pi + 1] += L.y;
+      film[3 * pi + 2] += L.z;
+    }
+  }
+}
+
 // Scene setup: Scene::Scene + light preprocess + PathTracing::preprocess.
 Scene* makeScene(const orion_scene_desc* d) {
   Scene* s = new Scene();
@@ -1180,6 +1526,7 @@ Scene* makeScene(const orion_scene_desc* d) {
   V c = (V(lo[0], lo[1], lo[2]) + V(hi[0], hi[1], hi[2])) * 0.5f;
   bool in = T > 0 && c.x >= lo[0] && c.x <= hi[0] && c.y >= lo[1] && c.y <= hi[1] && c.z >= lo[2] && c.z <= hi[2];
   s->worldRadius = in ? std::sqrt(len_sq(c - V(hi[0], hi[1], hi[2]))) : 0;
+  s->worldCenter = c;
   const float r = s->worldRadius;
   std::vector<float> power;
   for (int i = 0; i < d->num_lights; ++i) {
@@ -1388,6 +1735,13 @@ int port_render_pixels(void* h, int64_t npix, const int32_t* pix, int64_t k0, in
     }
   }
   return 0;
+}
+
+// SPPM::render with the given parameters; film: W*H*3 floats, zeroed by the caller.
+int64_t port_render_sppm(void* h, int32_t iterations, int32_t photons, float radius, int32_t max_depth, float* film) {
+  int64_t rays = 0;
+  renderSppm(*static_cast<Scene*>(h), iterations, photons, radius, max_depth, film, &rays);
+  return rays;
 }
 
 int port_scene_info(void* h, int32_t* info) {

@@ -147,6 +147,10 @@ void* ref_scene_load(const char* path) {
 
 void ref_scene_free(void* h) { delete static_cast<RefScene*>(h); }
 
+// OpenMP threads of the reference's own parallel loops (1: SPPM's photon
+// sums and cell lists in their single-thread order).
+void ref_set_threads(int32_t n) { omp_set_num_threads(n > 0 ? n : omp_get_num_procs()); }
+
 // info: width, height, num_prims, num_lights, num_envmaps
 int ref_scene_info(void* h, int32_t* info) {
   RefScene* s = static_cast<RefScene*>(h);

@@ -30,6 +30,7 @@ ERRORS = {-1: "invalid", -2: "io", -3: "parse", -4: "cuda", -5: "nomem", -6: "un
           -8: "not_ready", -9: "cancelled"}
 
 MAT_MATTE, MAT_METAL, MAT_MIRROR, MAT_GLASS, MAT_PLASTIC, MAT_UBER = range(6)
+INTEGRATOR_PATH, INTEGRATOR_SPPM = 0, 1
 DIST_GGX, DIST_BECKMANN = 0, 1
 LIGHT_AREA, LIGHT_POINT, LIGHT_SPOT, LIGHT_DISTANT, LIGHT_ENV = range(5)
 NOALLOC_MAX_RAYS = 65536  # ORION_NOALLOC_MAX_RAYS
@@ -57,6 +58,11 @@ class Light(C.Structure):
                 ("cos_total", C.c_float), ("cos_falloff", C.c_float), ("image", C.c_int32), ("reserved", C.c_int32)]
 
 
+class SppmParams(C.Structure):
+    _fields_ = [("iterations", C.c_int32), ("photons_per_iter", C.c_int32), ("initial_radius", C.c_float),
+                ("max_depth", C.c_int32)]
+
+
 class Image(C.Structure):
     _fields_ = [("width", C.c_int32), ("height", C.c_int32), ("rgb", C.c_void_p)]
 
@@ -71,7 +77,8 @@ class SceneDesc(C.Structure):
                 ("material_of_prim", C.c_void_p), ("light_of_prim", C.c_void_p), ("num_materials", C.c_int32),
                 ("num_lights", C.c_int32), ("materials", C.c_void_p), ("lights", C.c_void_p), ("camera", Camera),
                 ("spp", C.c_int32), ("max_depth", C.c_int32), ("num_images", C.c_int32), ("reserved", C.c_int32),
-                ("images", C.c_void_p)]
+                ("images", C.c_void_p), ("integrator", C.c_int32), ("reserved2", C.c_int32),
+                ("sppm", SppmParams)]
 
 
 class GpuOpts(C.Structure):
@@ -152,6 +159,7 @@ def library() -> C.CDLL:
             "orion_gpu_scene_bytes": (i32, [vp, i32, C.POINTER(i64)]),
             "orion_gpu_render": (i32, [vp, i32, C.POINTER(RenderParams), vp, vp]),
             "orion_gpu_render_fp64": (i32, [vp, i32, C.POINTER(RenderParams), vp, vp]),
+            "orion_gpu_render_sppm": (i32, [vp, i32, C.POINTER(SppmParams), vp, vp]),
             "orion_gpu_last_stats": (i32, [vp, C.POINTER(RenderStats)]),
             "orion_gpu_set_profiling": (i32, [vp, i32]),
             "orion_gpu_stage_times": (i32, [vp, C.POINTER(StageTimes)]),
@@ -213,9 +221,10 @@ class HostScene:
 
     @classmethod
     def from_arrays(cls, positions, normals, material_of_prim, materials, lights, camera: Camera, spp: int,
-                    max_depth: int, light_of_prim=None, uvs=None, images=None) -> "HostScene":
+                    max_depth: int, light_of_prim=None, uvs=None, images=None, sppm=None) -> "HostScene":
         """images: list of (H, W, 3) float arrays, referenced 1-based by Light.image and Material.tex;
-        uvs: texture coordinates per primitive corner (T x 6) or None."""
+        uvs: texture coordinates per primitive corner (T x 6) or None; sppm: dict (iterations, photons,
+        radius, max_depth) for an <Integrator type="sppm"> scene."""
         pos = np.ascontiguousarray(positions, dtype=np.float32).reshape(-1, 9)
         nrm = np.ascontiguousarray(normals, dtype=np.float32).reshape(-1, 9)
         mop = np.ascontiguousarray(material_of_prim, dtype=np.int32)
@@ -236,6 +245,10 @@ class HostScene:
         imgs = [np.ascontiguousarray(im, np.float32) for im in (images or [])]
         recs = (Image * max(1, len(imgs)))(*[Image(im.shape[1], im.shape[0], im.ctypes.data) for im in imgs])
         d.num_images, d.images = len(imgs), C.addressof(recs)
+        if sppm is not None:
+            d.integrator = INTEGRATOR_SPPM
+            d.sppm = SppmParams(sppm["iterations"], sppm["photons"], sppm["radius"], sppm["max_depth"])
+            d.spp, d.max_depth = sppm["iterations"], sppm["max_depth"]
         h = C.c_void_p()
         _check(library().orion_scene_from_desc(C.byref(d), C.byref(h)))
         return cls(h.value)
@@ -285,6 +298,7 @@ class Context:
         h = C.c_void_p()
         _check(library().orion_gpu_create(C.byref(opts), C.byref(h)))
         self._h = h
+        self._scene_sppm = {}  # scene id -> its sppm parameters
 
     def close(self):
         if self._h and self._h.value:
@@ -300,6 +314,8 @@ class Context:
     def upload(self, scene: HostScene) -> int:
         sid = C.c_int32()
         _check(library().orion_gpu_scene_upload(self._h, scene._h, C.byref(sid)))
+        p = scene.desc().sppm
+        self._scene_sppm[sid.value] = (p.iterations, p.photons_per_iter, p.initial_radius, p.max_depth)
         return sid.value
 
     def release(self, sid: int) -> None:
@@ -323,6 +339,23 @@ class Context:
         img = np.zeros((height, width, 3), np.float32)
         cnt = np.zeros((height, width), np.uint32)
         _check(library().orion_gpu_render(self._h, sid, C.byref(p), _ptr(img), _ptr(cnt)))
+        return img, cnt
+
+    def render_sppm(self, sid: int, width: int, height: int, iterations: int | None = None,
+                    photons: int | None = None, radius: float | None = None, max_depth: int | None = None):
+        """SPPM::render: FP32 (H, W, 3) film sums (one estimate per iteration) and (H, W) counts.
+        Parameters left None come from the scene's <Integrator type="sppm">."""
+        p = None
+        if any(x is not None for x in (iterations, photons, radius, max_depth)):
+            d = self._scene_sppm.get(sid)
+            if d is None:
+                raise OrionError(-1, "sppm parameters of this scene are unknown: pass all four")
+            p = SppmParams(iterations if iterations is not None else d[0], photons if photons is not None else d[1],
+                           radius if radius is not None else d[2], max_depth if max_depth is not None else d[3])
+        img = np.zeros((height, width, 3), np.float32)
+        cnt = np.zeros((height, width), np.uint32)
+        _check(library().orion_gpu_render_sppm(self._h, sid, C.byref(p) if p is not None else None, _ptr(img),
+                                               _ptr(cnt)))
         return img, cnt
 
     def last_stats(self) -> dict:
@@ -510,11 +543,29 @@ class PathTracing:
         self.stats = scene.ctx.last_stats()
 
 
+class SPPM:
+    """GPU stand-in for SPPM (src/integrator/sppm.h:16-29): render() fills the camera's film."""
+
+    def __init__(self, camera: CameraHandle, max_depth: int, n_iterations: int, photons_per_iter: int,
+                 radius: float):
+        self.camera, self.maxDepth, self.nIterations = camera, max_depth, n_iterations
+        self.photonPerIteration, self.initialSearchRadius = photons_per_iter, radius
+        self.stats = None
+
+    def render(self, scene: SceneHandle) -> None:
+        film = self.camera.getFilm()
+        img, cnt = scene.ctx.render_sppm(scene.sid, film.width, film.height, iterations=self.nIterations,
+                                         photons=self.photonPerIteration, radius=self.initialSearchRadius,
+                                         max_depth=self.maxDepth)
+        film.data, film.counter = img, cnt
+        self.stats = scene.ctx.last_stats()
+
+
 @dataclass
 class RenderOption:
     scene: SceneHandle
     camera: CameraHandle
-    integrator: PathTracing
+    integrator: PathTracing | SPPM
 
 
 class Parser:
@@ -527,7 +578,12 @@ class Parser:
         sid = self.ctx.upload(self.host)
         film = RenderTarget(d.camera.width, d.camera.height)
         cam = CameraHandle(film)
-        self._ro = RenderOption(SceneHandle(self.ctx, sid, self.host), cam, PathTracing(cam, d.max_depth, d.spp))
+        if d.integrator == INTEGRATOR_SPPM:
+            p = d.sppm
+            integ = SPPM(cam, p.max_depth, p.iterations, p.photons_per_iter, p.initial_radius)
+        else:
+            integ = PathTracing(cam, d.max_depth, d.spp)
+        self._ro = RenderOption(SceneHandle(self.ctx, sid, self.host), cam, integ)
 
     def getRenderOption(self) -> RenderOption:
         return self._ro

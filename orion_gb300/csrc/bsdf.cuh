@@ -201,7 +201,7 @@ __device__ __forceinline__ V3 lobe_f_t(const DevLobe& l, V3 wi, V3 wo) {
         if (wh.z < 0.f) wh = -wh;
         float F = fr_dielectric(fabsf(dot(wo, wh)), l.etaA, l.etaB);
         float sd = dot(wo, wh) + eta * dot(wi, wh);
-        float factor = 1.f / eta;
+        float factor = l.photon ? 1.f : 1.f / eta;  // TransportMode (microfacet.cpp:102)
         float v = fabsf(md_D(l.dist, l.alpha, wh) * md_G(l.dist, l.alpha, wi, wo) * eta * eta * absdot(wi, wh) *
                         absdot(wo, wh) * factor * factor / (ci * co * sd * sd));
         return mul(V3{1.f - F, 1.f - F, 1.f - F}, ld3(l.c)) * v;
@@ -314,7 +314,7 @@ __device__ __forceinline__ V3 lobe_sample_f_t(const DevLobe& l, V3 wo, float u0,
         *pdf = 1.f;
         float F = fr_dielectric(fabsf(cos_theta(*wi)), l.etaA, l.etaB);
         V3 ft = mul(ld3(l.c), V3{1.f - F, 1.f - F, 1.f - F});
-        ft = ft * ((ei * ei) / (et * et));
+        if (!l.photon) ft = ft * ((ei * ei) / (et * et));
         return sdiv(ft, abs_cos_theta(*wi));
       }
       break;
@@ -332,7 +332,7 @@ __device__ __forceinline__ V3 lobe_sample_f_t(const DevLobe& l, V3 wo, float u0,
         float et = entering ? l.etaB : l.etaA;
         if (!refract(wo, faceforward(V3{0, 0, 1}, wo), ei / et, wi)) return V3{0, 0, 0};
         V3 ft = ld3(l.c2) * (1.f - F);
-        ft = ft * ((ei * ei) / (et * et));
+        if (!l.photon) ft = ft * ((ei * ei) / (et * et));
         *stype = BXDF_SPECULAR | BXDF_TRANSMISSION;
         *pdf = 1.f - F;
         return sdiv(ft, abs_cos_theta(*wi));

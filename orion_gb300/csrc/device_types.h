@@ -57,7 +57,7 @@ struct DevLobe {       // 64 bytes
   float on_a, on_b;    // Oren-Nayar A, B
   float fr_eta[3];     // conductor etaT
   float fr_k[3];       // conductor k
-  float pad;
+  int32_t photon;      // TransportMode::Photon: transmission without radiance scaling (SPPM photon pass)
 };
 
 constexpr int kMaxLobes = 5;
@@ -130,7 +130,7 @@ struct DevLight {      // 128 bytes
   float p[3];          // point/spot position; distant: direction
   float pad2;
   float m[9];          // spot: world->light 3x3; env: light->world 3x3
-  float minv[9];       // env: world->light 3x3
+  float minv[9];       // spot: light->world 3x3; env: world->light 3x3
   float cos_total, cos_falloff;
   float pad3[2];
 };

@@ -15,6 +15,7 @@ namespace orion_gb300 {
 constexpr float kPi = 3.14159265358979323846f;
 constexpr float kInvPi = 0.31830988618379067154f;
 constexpr float kInv2Pi = 0.15915494309189533577f;
+constexpr float kInv4Pi = 0.07957747154594766788f;
 constexpr float kPiOver2 = 1.57079632679489661923f;
 constexpr float kPiOver4 = 0.78539816339744830961f;
 constexpr float kEpsilon = 0.000001f;        // src/orion.h:48
@@ -118,6 +119,34 @@ __device__ __forceinline__ void uniform_sample_triangle(float u0, float u1, floa
   *b0 = 1.f - su0;
   *b1 = u1 * su0;
 }
+
+// src/sampler/sampling.cpp:5-11
+__device__ __forceinline__ V3 uniform_sample_sphere(float u0, float u1) {
+  float z = 1.f - 2.f * u0;
+  float r = sqrtf(fmaxf(0.f, 1.f - z * z));
+  float phi = 2.f * kPi * u1;
+  return V3{r * cosf(phi), r * sinf(phi), z};
+}
+
+// src/sampler/sampling.cpp:20-27
+__device__ __forceinline__ V3 uniform_sample_cone(float u0, float u1, float cos_max) {
+  float cos_t = (1.f - u0) + u0 * cos_max;
+  float sin_t = sqrtf(1.f - cos_t * cos_t);
+  float phi = u1 * 2.f * kPi;
+  return V3{cosf(phi) * sin_t, sinf(phi) * sin_t, cos_t};
+}
+
+// coordinateSystem (src/core/geometry.h:902-909): x, y completing z.
+__device__ __forceinline__ void coordinate_system(V3 z, V3* x, V3* y) {
+  if (fabsf(z.x) > fabsf(z.y))
+    *y = vdiv(V3{-z.z, 0.f, z.x}, sqrtf(z.x * z.x + z.z * z.z));
+  else
+    *y = vdiv(V3{0.f, z.z, -z.y}, sqrtf(z.y * z.y + z.z * z.z));
+  *x = cross(*y, z);
+}
+
+// Spectrum::intensity (src/core/spectrum.h:88-91)
+__device__ __forceinline__ float spectrum_intensity(V3 c) { return 0.212671f * c.x + 0.715160f * c.y + 0.072169f * c.z; }
 
 // src/sampler/sampling.h:49-52
 __device__ __forceinline__ float power_heuristic(float fpdf, float gpdf) {

@@ -27,6 +27,7 @@ struct SceneView {
   int env_idx[8];
   int num_env;
   float world_radius;
+  float world_center[3];  // Bounds3::boundingSphere (distant and environment photons)
   unsigned class_mask;  // shading classes of the scene's triangles (bit ShadeClass), SC_MISS always
   DevCamera cam;
 };
@@ -225,6 +226,63 @@ void launch_batch_iteration(const WaveView& w, const BatchView& b, const uint32_
                             cudaStream_t stream, StageTimer* timer);
 // Resets the batch control block and the free-slot list for `capacity` slots.
 void launch_batch_init(const WaveView& w, const BatchView& b, int capacity, cudaStream_t stream);
+
+// ------------------------------------------------------------------ SPPM
+//
+// Stochastic progressive photon mapping (src/integrator/sppm.cpp:58-322):
+// per iteration a camera pass leaves one visible point per pixel, a hash
+// grid over the visible points is built, a photon pass adds photon
+// contributions to the visible points near each photon hit, and a per-pixel
+// update shrinks the radii and adds the iteration's estimate to the film.
+
+struct SppmGrid {
+  float lo[3], hi[3];  // bounds of the visible points' spheres
+  int res[3];
+  float max_radius;
+  int any;             // some pixel has a visible point
+};
+
+struct SppmView {
+  int width, height, npix;
+  int max_depth, iterations, photons;  // photons per iteration
+  const uint32_t* sobol;               // dimension-major Sobol matrices
+  // per pixel
+  float4* vp_pr;    // visible point p, search radius (kept across iterations)
+  float4* vp_wo;    // wo, material index (int bits; -1: no visible point)
+  float4* vp_beta;  // beta, texture u
+  float4* vp_ns;    // shading normal, texture v
+  float4* vp_ng;    // geometric normal
+  float4* vp_su;    // shading frame s
+  float4* vp_sv;    // shading frame t
+  float4* ld;       // direct light sum Ld, photon count N
+  float4* tau;      // tau
+  float* phi;       // 3 per pixel, photon flux of this iteration
+  int* m;           // photons gathered this iteration
+  // grid: hash cell -> visible points, cells [start[h], start[h + 1]) of `entries`
+  SppmGrid* grid;
+  float4* part_lo;  // per block of the bounds pass: lo, max radius
+  float4* part_hi;  // hi, any
+  int* cell_start;  // npix + 1 (counts, then their exclusive scan)
+  int* cell_fill;   // npix
+  int* scan_part;   // per scan block
+  int* entries;
+  int entries_cap;
+  float* film;      // W*H*3 sums of the iterations' estimates
+  unsigned* film_count;
+  unsigned long long* rays;
+};
+
+constexpr int kSppmBoundsBlocks = 1024;  // blocks of the bounds pass (part_lo / part_hi entries)
+constexpr int kScanBlock = 1024;         // elements per block of the cell-count scan
+
+// Resets per-pixel state (radius r0, no visible point) and the film.
+void launch_sppm_init(const SppmView& v, float radius0, cudaStream_t stream);
+// Camera pass, grid bounds and cell counts of iteration `iter`.
+void launch_sppm_visible_points(const SceneView& s, const SppmView& v, int iter, cudaStream_t stream);
+// Exclusive scan of the cell counts; cell_start[npix] is then the entry count.
+void launch_sppm_scan(const SppmView& v, cudaStream_t stream);
+// Fills the cell lists, traces the photons, updates the pixels and the film.
+void launch_sppm_photons(const SceneView& s, const SppmView& v, int iter, cudaStream_t stream);
 
 // Component hooks for the parity tests.
 void launch_sobol(const uint32_t* sobol, int64_t n, const uint64_t* index, const uint32_t* dim, float* out,

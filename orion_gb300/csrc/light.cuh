@@ -221,6 +221,119 @@ __device__ __forceinline__ float env_pdf_li(const DevLight& L, const DevEnvMap* 
   return dist2d_pdf(envmaps[L.image], phi * kInv2Pi, theta * kInv2Pi) / (2.f * kPi * kPi * st);
 }
 
+// Light::sample_Le for every light type (src/light/diffuse.cpp:32-44,
+// point.cpp:20-27, spot.cpp:30-38, distant.cpp:28-41, envmap.cpp:82-104):
+// an emitted ray (origin, direction), the emitter normal, and the position
+// and direction pdfs. r0 / r1 are the reference's two Point2f samples.
+struct EmittedRay {
+  V3 Le, o, d, n;
+  float pdf_pos, pdf_dir;
+};
+
+static __device__ __noinline__ EmittedRay sample_le(const DevLight& L, const PrimShade* __restrict__ prims,
+                                                    const DevEnvMap* envmaps, const float* world_center,
+                                                    float world_radius, float r0x, float r0y, float r1x, float r1y) {
+  EmittedRay e;
+  e.Le = V3{0, 0, 0};
+  e.o = e.d = e.n = V3{0, 0, 1};
+  e.pdf_pos = e.pdf_dir = 0.f;
+  const V3 wc = ld3(world_center);
+  switch (L.kind) {
+    case DL_AREA: {  // Triangle::sample (triangle.cpp:85-106), cosine-weighted direction about ng
+      const PrimShade& sh = prims[L.prim];
+      V3 p0 = ld3(sh.p), p1 = ld3(sh.p + 3), p2 = ld3(sh.p + 6);
+      V3 n0 = ld3(sh.n), n1 = ld3(sh.n + 3), n2 = ld3(sh.n + 6);
+      float b0, b1;
+      uniform_sample_triangle(r0x, r0y, &b0, &b1);
+      float b2 = 1.f - b0 - b1;
+      V3 p = b0 * p0 + b1 * p1 + b2 * p2;
+      V3 ng = normalize(cross(p1 - p0, p2 - p0));
+      V3 ns = n0 * b0 + n1 * b1 + n2 * b2;
+      ng = faceforward(ng, ns);
+      e.pdf_pos = 1.f / L.area;
+      e.n = ng;
+      V3 w = cosine_sample_hemisphere(r1x, r1y);
+      e.pdf_dir = w.z * kInvPi;
+      V3 x, y;
+      coordinate_system(ng, &x, &y);
+      w = w.x * x + w.y * y + w.z * ng;
+      e.o = offset_ray_origin(p, ng, w);
+      e.d = w;
+      e.Le = dot(ng, w) > 0.f ? ld3(L.L) : V3{0, 0, 0};
+      return e;
+    }
+    case DL_POINT:
+      e.o = ld3(L.p);
+      e.d = uniform_sample_sphere(r0x, r0y);
+      e.n = e.d;
+      e.pdf_pos = 1.f;
+      e.pdf_dir = kInv4Pi;
+      e.Le = ld3(L.L);
+      return e;
+    case DL_SPOT: {
+      e.o = ld3(L.p);
+      e.d = mat3_mul(L.minv, uniform_sample_cone(r0x, r0y, L.cos_total));
+      e.n = e.d;
+      e.pdf_pos = 1.f;
+      e.pdf_dir = 1.f / (2.f * kPi * (1.f - L.cos_total));
+      V3 wl = normalize(mat3_mul(L.m, e.d));
+      float c = wl.z, fall;
+      if (c < L.cos_total)
+        fall = 0.f;
+      else if (c > L.cos_falloff)
+        fall = 1.f;
+      else {
+        float delta = (c - L.cos_total) / (L.cos_falloff - L.cos_total);
+        fall = (delta * delta) * (delta * delta);
+      }
+      e.Le = ld3(L.L) * fall;
+      return e;
+    }
+    case DL_DISTANT: {
+      const V3 dir = ld3(L.p);
+      V3 v1, v2;
+      coordinate_system(dir, &v1, &v2);
+      float cx, cy;
+      concentric_sample_disk(r0x, r0y, &cx, &cy);
+      V3 pd = wc + world_radius * (cx * v1 + cy * v2);
+      e.o = pd + world_radius * dir;
+      e.d = -dir;
+      e.n = e.d;
+      e.pdf_pos = 1.f / (kPi * world_radius * world_radius);
+      e.pdf_dir = 1.f;
+      e.Le = ld3(L.L);
+      return e;
+    }
+    case DL_ENV: {
+      float su, sv, map_pdf;
+      if (L.image >= 0) {
+        dist2d_sample(envmaps[L.image], r0x, r0y, &su, &sv, &map_pdf);
+      } else {  // 1x1 distribution: uv = u, mapPdf = 1 (0 for a zero-intensity map)
+        su = r0x;
+        sv = r0y;
+        map_pdf = L.area == 0.f ? 0.f : 1.f;
+      }
+      if (map_pdf == 0.f) return e;
+      const float theta = sv * kPi, phi = su * 2.f * kPi;
+      const float ct = cosf(theta), st = sinf(theta), sp = sinf(phi), cp = cosf(phi);
+      const V3 d = -mat3_mul(L.m, V3{st * cp, st * sp, ct});
+      e.n = d;
+      V3 v1, v2;
+      coordinate_system(-d, &v1, &v2);
+      float cx, cy;
+      concentric_sample_disk(r1x, r1y, &cx, &cy);
+      V3 pd = wc + world_radius * (cx * v1 + cy * v2);
+      e.o = pd + world_radius * -d;
+      e.d = d;
+      e.pdf_dir = st == 0.f ? 0.f : map_pdf / (2.f * kPi * kPi * st);
+      e.pdf_pos = 1.f / (kPi * world_radius * world_radius);
+      e.Le = L.image >= 0 ? env_texel(envmaps[L.image], su, sv) : ld3(L.L);
+      return e;
+    }
+  }
+  return e;
+}
+
 __device__ __forceinline__ bool is_delta_light(int kind) { return kind == DL_POINT || kind == DL_SPOT || kind == DL_DISTANT; }
 
 }  // namespace orion_gb300

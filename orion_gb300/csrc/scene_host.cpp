@@ -17,7 +17,7 @@
 // the reference opens relative to the working directory
 // (src/util/parser.cpp:438-443), is looked up in the resource directory, then
 // the scene's directory, then the working directory; features outside the
-// path tracer (SPD files, named metals, sppm and pseudo samplers) are
+// path tracer (SPD files, named metals, the pseudo-random sampler) are
 // reported as ORION_ERR_UNSUPPORTED instead of being loaded.
 #include "scene_host.h"
 #include "image_io.h"
@@ -1101,10 +1101,23 @@ class Loader {
     const XmlNode* n = root_->child("Integrator");
     if (!n) raise(ORION_ERR_PARSE, "no <Integrator>");
     std::string type = trim(n->attr("type") ? n->attr("type") : "");
-    if (type != "path") raise(ORION_ERR_UNSUPPORTED, "integrator '" + type + "' (only path)");
     ParamMap ps = params_of(n);
+    if (type == "sppm") {  // createSPPMIntegrator (src/integrator/sppm.cpp:324-333)
+      for (const char* k : {"numIterations", "maxDepth", "photonsPerIteration", "initRadius"})
+        if (!ps.has(k)) raise(ORION_ERR_PARSE, std::string("sppm integrator needs ") + k);
+      out_->integrator = ORION_INTEGRATOR_SPPM;
+      out_->sppm.iterations = parse_int(ps.get("numIterations"));
+      out_->sppm.max_depth = parse_int(ps.get("maxDepth"));
+      out_->sppm.photons_per_iter = parse_int(ps.get("photonsPerIteration"));
+      out_->sppm.initial_radius = parse_float(ps.get("initRadius"));
+      out_->max_depth = out_->sppm.max_depth;
+      out_->spp = out_->sppm.iterations;
+      return;
+    }
+    if (type != "path") raise(ORION_ERR_UNSUPPORTED, "integrator '" + type + "' (path or sppm)");
     if (!ps.has("maxDepth") || !ps.has("nSamplesPerPixel"))
       raise(ORION_ERR_PARSE, "path integrator needs maxDepth and nSamplesPerPixel");
+    out_->integrator = ORION_INTEGRATOR_PATH;
     out_->max_depth = parse_int(ps.get("maxDepth"));
     out_->spp = parse_int(ps.get("nSamplesPerPixel"));
   }
@@ -1204,6 +1217,8 @@ void HostScene::desc(orion_scene_desc* d) const {
   d->max_depth = max_depth;
   d->num_images = (int32_t)image_desc.size();
   d->images = image_desc.empty() ? nullptr : image_desc.data();
+  d->integrator = integrator;
+  d->sppm = sppm;
 }
 
 void HostScene::index_images() {
@@ -1302,9 +1317,15 @@ int scene_from_desc(const orion_scene_desc& d, HostScene* out, std::string* err)
       *err = "scene description: bad material type at " + std::to_string(i);
       return ORION_ERR_INVALID;
     }
+  if (d.integrator != ORION_INTEGRATOR_PATH && d.integrator != ORION_INTEGRATOR_SPPM) {
+    *err = "scene description: unknown integrator";
+    return ORION_ERR_INVALID;
+  }
   out->camera = d.camera;
   out->spp = d.spp;
   out->max_depth = d.max_depth;
+  out->integrator = d.integrator;
+  out->sppm = d.sppm;
   out->source.clear();
   return ORION_OK;
 }

@@ -53,11 +53,13 @@ struct HostScene {
   std::vector<int32_t> light_of_prim;
   std::vector<orion_material> materials;
   std::vector<orion_light> lights;
-  std::vector<HostImage> images;   // environment map texels (orion_light.image = index + 1)
+  std::vector<HostImage> images;   // environment map and texture texels (orion_light.image, orion_material.tex = index + 1)
   std::vector<orion_image> image_desc;  // views of `images` for desc()
   orion_camera camera{};
   int32_t spp = 1;
   int32_t max_depth = 5;
+  int32_t integrator = ORION_INTEGRATOR_PATH;
+  orion_sppm_params sppm{0, 0, 0.f, 0};
   std::string source;             // file the scene was read from ("" if built from a desc)
 
   int64_t num_prims() const { return (int64_t)material_of_prim.size(); }

@@ -264,7 +264,10 @@ bool prepare_scene(const HostScene& s, PreparedScene* out, std::string* err) {
         d.kind = DL_SPOT;
         set3(d.p, l.p);
         for (int rr = 0; rr < 3; ++rr)
-          for (int c = 0; c < 3; ++c) d.m[3 * rr + c] = l.w2l[4 * rr + c];
+          for (int c = 0; c < 3; ++c) {
+            d.m[3 * rr + c] = l.w2l[4 * rr + c];
+            d.minv[3 * rr + c] = l.l2w[4 * rr + c];
+          }
         d.cos_total = l.cos_total;
         d.cos_falloff = l.cos_falloff;
         float f = 1 - .5f * (l.cos_falloff + l.cos_total);

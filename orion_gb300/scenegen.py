@@ -237,6 +237,7 @@ class Scene:
     envmaps: list = field(default_factory=list)   # dicts: constant radiance L, worldUp
     lens_radius: float = 0.0
     focal_distance: float = 0.0
+    sppm: dict | None = None  # <Integrator type="sppm">: iterations, photons, radius, max_depth
     meta: dict = field(default_factory=dict)
 
     @property
@@ -318,6 +319,28 @@ def cornell(res: int = 256, spp: int = 16, subdiv: int = 4, max_depth: int = 5) 
     p, f, nn = quad([(-0.25, 0.99, -0.25), (0.25, 0.99, -0.25), (0.25, 0.99, 0.25), (-0.25, 0.99, 0.25)],
                     (0, -1, 0))
     s.meshes.append(Mesh("light", p, f, nn, matte((0, 0, 0)), area_le=(17.0, 12.0, 4.0)))
+    return s
+
+
+def caustics(res: int = 64, iterations: int = 8, photons: int = 20000, radius: float = 0.05, max_depth: int = 5,
+             subdiv: int = 3) -> Scene:
+    """The Cornell box for SPPM: smooth and rough glass and a metal sphere under the area light, plus a
+    point light, a spotlight, a distant light and a constant environment (every Light::sample_Le)."""
+    s = cornell(res, 1, subdiv, max_depth)
+    s.name = "caustics"
+    s.meta = {"config": "sppm caustics box", "seed": 0}
+    s.meshes = [m for m in s.meshes if not m.name.startswith("sphere")]
+    for name, centre, mat in [("sphere_glass", (-0.35, -0.7, 0.1), glass(1.5, 0.0)),
+                              ("sphere_rough", (0.4, -0.7, -0.3), glass(1.4, 0.3)),
+                              ("sphere_metal", (0.05, -0.75, 0.55), metal((0.2, 0.42, 1.37), (3.9, 2.4, 2.1), 0.2))]:
+        v, f = icosphere(subdiv)
+        s.meshes.insert(len(s.meshes) - 1, Mesh(name, v * 0.25 + np.asarray(centre), f, v.copy(), mat))
+    s.lights.append({"type": "point", "I": (0.6, 0.6, 0.5), "from": (0.0, 0.5, 0.5)})
+    s.lights.append({"type": "spot", "intensity": (1.5, 1.5, 2.0), "angle": 25.0, "delta": 5.0,
+                     "from": (-0.6, 0.8, 0.8), "to": (0.0, -1.0, 0.0)})
+    s.lights.append({"type": "distant", "L": (0.3, 0.3, 0.3), "from": (0.0, -1.0, -1.0), "to": (0.0, 0.0, 0.0)})
+    s.envmaps.append({"L": (0.05, 0.05, 0.06), "worldUp": (0, 1, 0)})
+    s.sppm = {"iterations": iterations, "photons": photons, "radius": radius, "max_depth": max_depth}
     return s
 
 
@@ -530,8 +553,15 @@ def write_ori(scene: Scene, directory: str, mesh_prefix: str | None = None) -> s
             name = f'    <Param name="{fn}"/>\n'
         out.append(f'  <Envmap>\n    <Param L="{_fmt(e["L"])}"/>\n    <Param nLightSamples="1"/>\n{name}'
                    f'    <Param worldUp="{_fmt(e["worldUp"])}"/>\n  </Envmap>\n')
-    out.append(f'  <Integrator type="path">\n    <Param maxDepth="{scene.max_depth}"/>\n'
-               f'    <Param nSamplesPerPixel="{scene.spp}"/>\n  </Integrator>\n')
+    if scene.sppm is not None:
+        q = scene.sppm
+        out.append(f'  <Integrator type="sppm">\n    <Param numIterations="{q["iterations"]}"/>\n'
+                   f'    <Param maxDepth="{q["max_depth"]}"/>\n'
+                   f'    <Param photonsPerIteration="{q["photons"]}"/>\n'
+                   f'    <Param initRadius="{_fmt([q["radius"]])}"/>\n  </Integrator>\n')
+    else:
+        out.append(f'  <Integrator type="path">\n    <Param maxDepth="{scene.max_depth}"/>\n'
+                   f'    <Param nSamplesPerPixel="{scene.spp}"/>\n  </Integrator>\n')
     out.append('  <Sampler type="sobol"/>\n</Scene>\n')
     path = os.path.join(directory, f"{scene.name}.ori")
     with open(path, "w") as fh:
@@ -791,7 +821,7 @@ def to_host_scene(scene: Scene, text_rounding: bool = False):
     cam = og.look_at_camera(scene.eye, scene.look, scene.up, scene.fov, scene.width, scene.height,
                             scene.lens_radius, scene.focal_distance)
     return og.HostScene.from_arrays(P, N, mesh_of, mats, lights, cam, scene.spp, scene.max_depth,
-                                    light_of_prim=light_of, uvs=uvs, images=images)
+                                    light_of_prim=light_of, uvs=uvs, images=images, sppm=scene.sppm)
 
 
 def job_views(s: Scene, views: int = 16):

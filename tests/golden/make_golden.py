@@ -12,6 +12,7 @@ records its outputs on fixed inputs:
   image_*.npz  PathTracing::render film sums                (src/integrator/path.cpp:15-37);
                image_envlit lit by an image environment map (src/light/envmap.cpp),
                image_textured with image textures on every material input (src/core/texture.cpp)
+  image_caustics_sppm.npz  SPPM::render film sums (src/integrator/sppm.cpp:58-322), one thread
   stats_*.npz  FP64 per-pixel mean and variance at high spp (for 3-sigma checks)
   geometry.npz loader output digests
 
@@ -185,6 +186,21 @@ def main():
             ref.lib.ref_scene_free(h)
             print("image", name, time.time() - t0)
         np.savez_compressed(os.path.join(HERE, "geometry.npz"), **geo)
+
+        # SPPM through the reference's own SPPM::render, one OpenMP thread so that the photon
+        # sums and the grid's cell lists have one order.
+        sppm_kw = dict(res=48, iterations=8, photons=20000, radius=0.08, max_depth=5)
+        path = helpers.write_scene("caustics", os.path.join(tmp, "sppm"), **sppm_kw)
+        h, info = ref.load(path)
+        W, H = int(info[0]), int(info[1])
+        img = np.zeros((H, W, 3), np.float32)
+        ref.lib.ref_set_threads(1)
+        ref.lib.ref_scene_render(h, vp(img))
+        ref.lib.ref_set_threads(0)
+        np.savez_compressed(os.path.join(HERE, "image_caustics_sppm.npz"), film=img, width=W, height=H,
+                            hash=np.frombuffer(helpers.scene_hash(path).encode(), np.uint8), **sppm_kw)
+        ref.lib.ref_scene_free(h)
+        print("sppm", time.time() - t0)
 
         # FP64 statistics: Cornell at the full C1 resolution, a seeded pixel subset at high spp.
         spp_hi = 4096 if args.quick else 65536

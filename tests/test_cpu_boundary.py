@@ -98,7 +98,8 @@ GOOD = """<Scene>
     (lambda s: s.replace('type="meshHandy"', 'type="mesh" filename="missing.obj"'), -2),
     (lambda s: s.replace('<Param n="0,0,1"/>', ""), -3),                        # normals are required
     (lambda s: s.replace('type="sobol"', 'type="pseudo"'), -6),
-    (lambda s: s.replace('type="path"', 'type="sppm"'), -6),
+    (lambda s: s.replace('type="path"', 'type="sppm"'), -3),                    # sppm needs its parameters
+    (lambda s: s.replace('type="path"', 'type="bdpt"'), -6),
     (lambda s: s.replace('<Kd><Param type="constant"/><Param color="0.5,0.5,0.5"/></Kd>', ""), -3),
     (lambda s: s.replace('<Param fov="40"/>', ""), -3),
 ])
@@ -197,3 +198,20 @@ def test_large_obj_parsed_in_pieces_equals_sequential_reading(built, tmp_path):
     P, N = _reference_obj(text)
     assert a["positions"].shape == P.shape
     assert np.array_equal(a["positions"], P) and np.array_equal(a["normals"], N)
+
+
+def test_sppm_integrator_parameters_load_and_round_trip(tmp_path):
+    """<Integrator type="sppm"> (src/util/parser.cpp:132-133, src/integrator/sppm.cpp:324-333)."""
+    import orion_gb300 as og
+    from orion_gb300 import scenegen
+    sc = scenegen.caustics(res=16, iterations=3, photons=-1, radius=0.125, max_depth=4, subdiv=1)
+    host = og.HostScene.load(scenegen.write_ori(sc, str(tmp_path)))
+    d = host.desc()
+    assert d.integrator == og.INTEGRATOR_SPPM
+    assert (d.sppm.iterations, d.sppm.photons_per_iter, d.sppm.initial_radius, d.sppm.max_depth) == (3, -1, 0.125, 4)
+    mem = scenegen.to_host_scene(sc).desc()
+    assert mem.integrator == og.INTEGRATOR_SPPM and mem.sppm.photons_per_iter == -1
+    bad = tmp_path / "bad.ori"
+    bad.write_text(open(scenegen.write_ori(sc, str(tmp_path))).read().replace('<Param initRadius="0.125"/>', ""))
+    with pytest.raises(og.OrionError, match="initRadius"):
+        og.HostScene.load(str(bad))

@@ -107,3 +107,19 @@ def test_port_statistics_agree_with_high_spp_reference(port, tmp_path):
     sigma = np.sqrt(var / n + rvar / rn) + 1e-6
     z = np.abs(mean - rmean) / sigma
     assert (z <= 3).mean() >= 0.9, f"3-sigma agreement {(z <= 3).mean():.3f}"
+
+
+def test_port_sppm_matches_reference_render(port, tmp_path):
+    """SPPM::render (src/integrator/sppm.cpp:58-322): the oracle against the reference run on one thread."""
+    g = helpers.golden("image_caustics_sppm.npz")
+    kw = {k: (float(g[k]) if k == "radius" else int(g[k])) for k in ("res", "iterations", "photons", "radius",
+                                                                      "max_depth")}
+    path = helpers.write_scene("caustics", str(tmp_path / "c"), **kw)
+    assert helpers.scene_hash(path) == bytes(g["hash"]).decode()
+    film, rays = port.Scene.load(path).render_sppm()
+    if EXACT:
+        assert np.array_equal(film.view(np.uint32), g["film"].view(np.uint32)), "oracle SPPM differs from the reference"
+    else:
+        close = (np.abs(film - g["film"]) <= 1e-4 * np.abs(g["film"]) + 1e-5).all(2).mean()
+        assert close > 0.95
+    assert rays > 0

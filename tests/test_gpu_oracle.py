@@ -111,3 +111,45 @@ def test_render_statistics_within_3_sigma_of_reference(ctx, tmp_path):
     print(f"{len(pix)} pixels: {frac:.3f} within 3 sigma, relative RMSE {rmse:.4f} vs {ref_spp}-spp FP64 reference")
     assert frac >= 0.95
     assert rmse < 0.05
+
+
+def test_sppm_matches_oracle(ctx, port, tmp_path):
+    """SPPM on the GPU against the oracle (pinned bit-exact to the reference's single-thread SPPM).
+
+    The same sample indices drive both; photon flux adds up in another order on the GPU (atomics) and
+    device transcendental functions round differently, so a pixel agrees to FP32 rounding unless one of
+    its photons took another path: most pixels within 1e-3 relative, the image within 1% RMSE."""
+    import orion_gb300 as og
+    kw = dict(res=48, iterations=8, photons=20000, radius=0.08, max_depth=5)
+    path = helpers.write_scene("caustics", str(tmp_path / "c"), **kw)
+    host = og.HostScene.load(path)
+    ref, _ = port.Scene(host).render_sppm()
+    sid = ctx.upload(host)
+    gpu, cnt = ctx.render_sppm(sid, 48, 48)
+    st = ctx.last_stats()
+    ctx.release(sid)
+    assert (cnt == kw["iterations"]).all() and np.isfinite(gpu).all()
+    rel = np.abs(gpu.astype(np.float64) - ref) / np.maximum(np.abs(ref), 1e-3)
+    close = (rel <= 1e-3).all(2).mean()
+    rmse = float(np.sqrt(np.mean((gpu.astype(np.float64) - ref) ** 2)) / np.sqrt(np.mean(ref.astype(np.float64) ** 2)))
+    print(f"sppm: {close:.4f} of pixels within 1e-3, relative RMSE {rmse:.2e}, {st['rays']} rays, "
+          f"{st['device_ms']:.2f} ms")
+    assert close >= 0.9
+    assert rmse < 0.01
+
+
+def test_sppm_parameters_and_errors(ctx, tmp_path):
+    import orion_gb300 as og
+    path = helpers.write_scene("caustics", str(tmp_path / "c"), res=24, iterations=2, photons=-1, radius=0.1)
+    host = og.HostScene.load(path)
+    sid = ctx.upload(host)
+    try:
+        a, ca = ctx.render_sppm(sid, 24, 24)                       # the scene's parameters (photons = W*H)
+        b, cb = ctx.render_sppm(sid, 24, 24, photons=24 * 24)       # the same, explicitly
+        assert np.allclose(a, b, rtol=1e-4, atol=1e-6) and (ca == 2).all()  # photon sums: atomics, any order
+        c, cc = ctx.render_sppm(sid, 24, 24, iterations=3)
+        assert (cc == 3).all()
+        with pytest.raises(og.OrionError, match="radius"):
+            ctx.render_sppm(sid, 24, 24, radius=0.0)
+    finally:
+        ctx.release(sid)
