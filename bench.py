@@ -279,6 +279,9 @@ def run_ours(args) -> dict:
     if rank == 0 and args.serve_scenes > 0:
         out["served"] = run_served(ctx, args.serve_scenes, args.serve_views, args.serve_rates, args.serve_requests,
                                    budget_gb=150.0, spp_chunk=args.spp_chunk, plain_n=args.plain_requests)
+    if rank == 0 and args.sppm_res > 0:
+        out["sppm"] = run_sppm(ctx, args.sppm_res, args.sppm_iterations, steps=max(1, min(args.steps, 3)),
+                               cpu_iterations=1)
     if rank == 0 and not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(args.workload, threads=os.cpu_count() or 1, seconds=args.cpu_seconds)
     ctx.close()
@@ -465,6 +468,48 @@ def run_served(ctx, n_scenes: int, views: int, rates: list, per_rate: int, budge
     }
 
 
+def run_sppm(ctx, res: int, iterations: int, steps: int, cpu_iterations: int) -> dict:
+    """SPPM leg: the caustics box (every light type, smooth and rough glass) rendered by
+    orion_gpu_render_sppm, against the CPU oracle's restatement of SPPM::render on one thread
+    (the reference's photon pass sums with atomics; the oracle runs it in one order) over the
+    first `cpu_iterations` iterations of the same configuration."""
+    import orion_gb300 as og
+    from orion_gb300 import scenegen
+    kw = dict(res=res, iterations=iterations, photons=res * res, radius=0.05, max_depth=5, subdiv=5)
+    d = os.path.join(tempfile.gettempdir(), "orion_bench_sppm")
+    path = scenegen.write_ori(scenegen.caustics(**kw), d)
+    host = og.HostScene.load(path)
+    sid = ctx.upload(host)
+    ctx.render_sppm(sid, res, res, iterations=2)  # warm-up
+    ms, rays = [], 0
+    for _ in range(steps):
+        film, cnt = ctx.render_sppm(sid, res, res)
+        st = ctx.last_stats()
+        ms.append(st["device_ms"])
+        rays = st["rays"]
+    ctx.release(sid)
+    units = iterations * 2 * res * res  # camera paths + photons
+    gpu_ms = float(np.median(ms))
+    out = {"config": {"workload": f"caustics box SPPM {res}x{res}, {iterations} iterations x {res * res} photons, "
+                                  f"radius 0.05, depth 5", "triangles": int(host.desc().num_prims)},
+           "gpu": {"ms": round(gpu_ms, 2), "mpaths_s": round(units / (gpu_ms * 1e-3) / 1e6, 2),
+                   "mrays_s": round(rays / (gpu_ms * 1e-3) / 1e6, 2), "launches": st["kernel_launches"]},
+           "unit": "Mpaths/s (camera paths + photons)", "finite": bool(np.isfinite(film).all())}
+    try:
+        from oracle import port
+        sc = port.Scene(host)
+        t = time.time()
+        sc.render_sppm(iterations=cpu_iterations)
+        cpu_s = time.time() - t
+        cu = cpu_iterations * 2 * res * res
+        out["cpu_baseline"] = {"value": round(cu / cpu_s / 1e6, 4), "cores": 1, "kind": "port",
+                               "sample": f"first {cpu_iterations} of the {iterations} iterations, {cpu_s:.2f} s"}
+        out["gpu_vs_cpu"] = round(out["gpu"]["mpaths_s"] / out["cpu_baseline"]["value"], 1)
+    except Exception as e:  # the oracle is optional on a machine without its build
+        out["cpu_baseline"] = {"unavailable": str(e)[:200]}
+    return out
+
+
 def run_reference(args) -> dict | None:
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -513,9 +558,11 @@ def main():
     ap.add_argument("--spp-chunk", type=int, default=4, help="served leg: progressive spp per pass")
     ap.add_argument("--plain-requests", type=int, default=32, help="served leg: requests timed on the plain path")
     ap.add_argument("--batch-only", action="store_true", help="run the batched leg alone (profiling)")
+    ap.add_argument("--sppm-res", type=int, default=512, help="SPPM leg: image side (0 = skip)")
+    ap.add_argument("--sppm-iterations", type=int, default=16)
     args = ap.parse_args()
     if args.quick:
-        args.batch_jobs = args.serve_scenes = 0
+        args.batch_jobs = args.serve_scenes = args.sppm_res = 0
     from orion_gb300 import build
     build.build_product()
     build.build_port()
