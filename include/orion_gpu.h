@@ -355,6 +355,13 @@ int orion_server_status(orion_server* srv, int64_t ticket, orion_request_status*
 int orion_server_wait(orion_server* srv, int64_t ticket, double timeout_s);
 /* Copies the request's film so far (progressive results): W*H*3 sums and sums of squares, W*H counts. */
 int orion_server_result(orion_server* srv, int64_t ticket, double* sum, double* sumsq, uint32_t* count);
+/* The request's film so far as 8-bit pixels B, G, R, 255 (W*H*4 bytes):
+ * RenderTarget::getAveraged then saveAsBmp's clamp(c, 0, 1) * 255 truncated
+ * (src/core/texture.cpp:77-136), computed on the device. Rows top-down, or
+ * bottom-up as in a BMP file with ORION_PREVIEW_BOTTOM_UP. Unsampled pixels
+ * are black. */
+enum { ORION_PREVIEW_BOTTOM_UP = 1 };
+int orion_server_preview(orion_server* srv, int64_t ticket, uint8_t* bgra, int32_t flags);
 int orion_server_cancel(orion_server* srv, int64_t ticket);
 /* Frees a finished, failed or cancelled request's film. */
 int orion_server_release(orion_server* srv, int64_t ticket);

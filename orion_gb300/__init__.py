@@ -175,6 +175,7 @@ def library() -> C.CDLL:
             "orion_server_status": (i32, [vp, i64, C.POINTER(RequestStatus)]),
             "orion_server_wait": (i32, [vp, i64, C.c_double]),
             "orion_server_result": (i32, [vp, i64, vp, vp, vp]),
+            "orion_server_preview": (i32, [vp, i64, vp, i32]),
             "orion_server_cancel": (i32, [vp, i64]),
             "orion_server_release": (i32, [vp, i64]),
             "orion_server_stats_get": (i32, [vp, C.POINTER(ServerStats)]),
@@ -647,6 +648,13 @@ class Server:
         c = np.zeros((h, w), np.uint32)
         _check(library().orion_server_result(self._h, ticket, _ptr(s), _ptr(q), _ptr(c)))
         return s, q, c
+
+    def preview(self, ticket: int, bottom_up: bool = False) -> np.ndarray:
+        """The request's film so far as (H, W, 4) uint8 B, G, R, 255 (saveAsBmp's pixels), made on the device."""
+        st = self.status(ticket)
+        out = np.zeros((st["height"], st["width"], 4), np.uint8)
+        _check(library().orion_server_preview(self._h, ticket, _ptr(out), 1 if bottom_up else 0))
+        return out
 
     def cancel(self, ticket: int) -> None:
         _check(library().orion_server_cancel(self._h, ticket))

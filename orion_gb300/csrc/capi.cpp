@@ -156,6 +156,7 @@ struct orion_gpu_ctx {
   unsigned bgraph_mask = 0;  // shading classes the captured loop launches
   // SPPM: per-pixel state in one block, the grid's cell lists apart
   DevBuf sppm_block, sppm_entries;
+  DevBuf preview;  // 8-bit previews of server films
   int64_t sppm_pixels = 0;
   int sppm_entries_cap = 0;
   int smem_limit = 48 * 1024;  // opt-in dynamic shared memory per block
@@ -999,6 +1000,20 @@ int ctx_copy_to_host(orion_gpu_ctx* ctx, void* dst, const void* src, size_t byte
   std::lock_guard<std::mutex> g(ctx->mu);
   CUDA_TRY(cudaSetDevice(ctx->device));
   CUDA_TRY(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return ORION_OK;
+}
+
+int ctx_film_preview(orion_gpu_ctx* ctx, const void* film, int width, int height, int bottom_up, uint8_t* bgra) {
+  std::lock_guard<std::mutex> g(ctx->mu);
+  CUDA_TRY(cudaSetDevice(ctx->device));
+  const size_t wh = (size_t)width * height;
+  if (ctx->preview.bytes < wh * 4) RC(ctx->preview.alloc(wh * 4));
+  const char* base = static_cast<const char*>(film);
+  launch_film_preview(reinterpret_cast<const double*>(base), reinterpret_cast<const uint32_t*>(base + wh * 48), width,
+                      height, bottom_up, ctx->preview.as<uint8_t>(), ctx->stream);
+  CUDA_TRY(cudaGetLastError());
+  CUDA_TRY(cudaMemcpyAsync(bgra, ctx->preview.p, wh * 4, cudaMemcpyDeviceToHost, ctx->stream));
   CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   return ORION_OK;
 }

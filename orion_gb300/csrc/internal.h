@@ -30,6 +30,9 @@ int ctx_scene_info(orion_gpu_ctx* ctx, orion_scene_id id, int* width, int* heigh
 int64_t ctx_pool_bytes(orion_gpu_ctx* ctx);
 // Device -> host copy ordered after all work queued on the context's stream.
 int ctx_copy_to_host(orion_gpu_ctx* ctx, void* dst, const void* src, size_t bytes);
+// 8-bit preview (B, G, R, 255 per pixel) of a device film laid out as sums
+// (W*H*3 doubles), sums of squares, counts (W*H uint32), into host `bgra`.
+int ctx_film_preview(orion_gpu_ctx* ctx, const void* film, int width, int height, int bottom_up, uint8_t* bgra);
 // Records an error message for orion_last_error() and returns `code`.
 int ctx_fail(int code, const char* msg);
 

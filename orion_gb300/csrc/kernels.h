@@ -284,6 +284,11 @@ void launch_sppm_scan(const SppmView& v, cudaStream_t stream);
 // Fills the cell lists, traces the photons, updates the pixels and the film.
 void launch_sppm_photons(const SceneView& s, const SppmView& v, int iter, cudaStream_t stream);
 
+// Averaged FP64 film (W*H*3 sums, W*H counts) -> W*H pixels of bytes B, G,
+// R, 255 as saveAsBmp writes them; rows bottom-up when `bottom_up`.
+void launch_film_preview(const double* sum, const uint32_t* count, int width, int height, int bottom_up,
+                         uint8_t* bgra, cudaStream_t stream);
+
 // Component hooks for the parity tests.
 void launch_sobol(const uint32_t* sobol, int64_t n, const uint64_t* index, const uint32_t* dim, float* out,
                   cudaStream_t stream);

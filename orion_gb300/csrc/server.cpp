@@ -386,6 +386,22 @@ extern "C" int orion_server_result(orion_server* s, int64_t ticket, double* sum,
   return rc;
 }
 
+extern "C" int orion_server_preview(orion_server* s, int64_t ticket, uint8_t* bgra, int32_t flags) {
+  if (!s || !bgra) return ctx_fail(ORION_ERR_INVALID, "null argument");
+  void* film;
+  int w, h;
+  {
+    std::lock_guard<std::mutex> lk(s->mu);
+    Request* r = find(s, ticket);
+    if (!r) return ctx_fail(ORION_ERR_INVALID, "unknown ticket");
+    if (!r->film) return ctx_fail(ORION_ERR_NOT_READY, "request not admitted yet");
+    film = r->film;
+    w = r->width;
+    h = r->height;
+  }
+  return ctx_film_preview(s->ctx, film, w, h, (flags & ORION_PREVIEW_BOTTOM_UP) != 0, bgra);
+}
+
 extern "C" int orion_server_cancel(orion_server* s, int64_t ticket) {
   if (!s) return ctx_fail(ORION_ERR_INVALID, "null argument");
   std::lock_guard<std::mutex> lk(s->mu);

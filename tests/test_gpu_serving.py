@@ -145,3 +145,26 @@ def test_cancel(ctx, hosts):
         assert srv.stats()["submitted"] == 1
     finally:
         srv.close()
+
+
+def test_preview_is_the_bmp_of_the_averaged_film(ctx, hosts, tmp_path):
+    """orion_server_preview: the device-side 8-bit preview equals the pixels orion_film_write_bmp writes
+    for the averaged film (saveAsBmp, src/core/texture.cpp:77-136), top-down and bottom-up."""
+    import orion_gb300 as og
+    srv = og.Server(ctx, spp_chunk=2)
+    try:
+        t = srv.submit(hosts["cornell"])
+        assert srv.wait(t, 60)
+        s, _, c = srv.result(t)
+        top = srv.preview(t)
+        bottom = srv.preview(t, bottom_up=True)
+        srv.release(t)
+    finally:
+        srv.close()
+    avg = (s / c[..., None]).astype(np.float32)
+    bmp = tmp_path / "film.bmp"
+    og.saveAsBmp(avg, str(bmp))
+    data = np.frombuffer(open(bmp, "rb").read()[54:], np.uint8).reshape(avg.shape[0], avg.shape[1], 4)
+    assert np.array_equal(bottom, data)
+    assert np.array_equal(top, data[::-1])
+    assert (top[..., 3] == 255).all() and top[..., :3].any()
