@@ -33,7 +33,7 @@ def lib() -> C.CDLL:
             ("port_render", i64, [vp, i32, i64, i32, i32, i32, i32, vp, i32]),
             ("port_render_pixels", i32, [vp, i64, vp, i64, i32, i32, i32, vp, vp, i32]),
             ("port_scene_info", i32, [vp, vp]),
-            ("port_render_sppm", i64, [vp, i32, i32, C.c_float, i32, vp]),
+            ("port_render_sppm", i64, [vp, i32, i32, C.c_float, i32, vp, i32]),
         ]:
             f = getattr(l, name)
             f.restype, f.argtypes = res, args
@@ -109,9 +109,10 @@ class Scene:
                                  threads)
         return film, int(rays)
 
-    def render_sppm(self, iterations=None, photons=None, radius=None, max_depth=None):
+    def render_sppm(self, iterations=None, photons=None, radius=None, max_depth=None, threads=1):
         """FP32 film sums (H, W, 3) of SPPM::render: one estimate per iteration added to the film.
-        Defaults: the scene's sppm parameters (photons < 0: W x H)."""
+        Defaults: the scene's sppm parameters (photons < 0: W x H). threads=1: the reference's
+        single-thread order (parity); 0: all cores with atomic photon sums (timing)."""
         it0, ph0, r0, md0 = self.sppm
         it = it0 if iterations is None else iterations
         ph = ph0 if photons is None else photons
@@ -119,7 +120,7 @@ class Scene:
             ph = self.width * self.height
         film = np.zeros((self.height, self.width, 3), np.float32)
         rays = lib().port_render_sppm(self._h, it, ph, r0 if radius is None else radius,
-                                      md0 if max_depth is None else max_depth, _p(film))
+                                      md0 if max_depth is None else max_depth, _p(film), threads)
         return film, int(rays)
 
     def render_pixels(self, pix, spp, first_pass=0, max_depth=None, rr_depth=3, threads=0):

@@ -1304,15 +1304,24 @@ inline unsigned sppmHash(const int* c, int size) {
 }
 
 // film: W*H*3 sums of each iteration's estimate (RenderTarget::acumulate).
-void renderSppm(const Scene& s, int nIter, int photons, float radius0, int maxDepth, float* film, int64_t* rays) {
+// threads == 1: the reference's single-thread order (the parity oracle);
+// otherwise the camera and photon passes run on OpenMP threads with atomic
+// photon sums, as the reference runs them (a timing baseline).
+void renderSppm(const Scene& s, int nIter, int photons, float radius0, int maxDepth, float* film, int64_t* rays,
+                int threads) {
   const int W = s.cam.width, H = s.cam.height, nPix = W * H;
   std::vector<SppmPixel> px(nPix);
   for (SppmPixel& p : px) p.radius = radius0;
   const int nL = (int)s.lights.size();
+  const bool par = threads != 1;
+  if (threads > 1) omp_set_num_threads(threads);
+  int64_t nrays = 0;
   for (int iter = 0; iter < nIter; ++iter) {
     // Visible points (sppm.cpp:78-140).
+#pragma omp parallel for schedule(dynamic, 1) reduction(+ : nrays) if (par)
     for (int j = 0; j < H; ++j)
       for (int i = 0; i < W; ++i) {
+        int64_t* rays = &nrays;
         Sampler smp{(uint64_t)iter * nPix + (uint64_t)W * j + i};
         V ro, rd;
         cameraRay(s, smp, i, j, &ro, &rd);
@@ -1408,7 +1417,10 @@ void renderSppm(const Scene& s, int nIter, int photons, float radius0, int maxDe
       }
     }
     // Photons (sppm.cpp:197-270).
-    for (int k = 0; any && k < photons; ++k) {
+#pragma omp parallel for schedule(dynamic, 64) reduction(+ : nrays) if (par)
+    for (int k = 0; k < photons; ++k) {
+      if (!any) continue;
+      int64_t* rays = &nrays;
       Sampler smp{(uint64_t)nIter * nPix + (uint64_t)iter * photons + k};
       float lightPdf;
       int ln = sampleDiscrete(s, smp.next(), &lightPdf);
@@ -1433,8 +1445,19 @@ void renderSppm(const Scene& s, int nIter, int photons, float radius0, int maxDe
               if (len_sq(p.vpP - it.p) > p.radius * p.radius) continue;
               V wi = -rd;
               V Phi = mul(beta, bsdfF(p.vpMat, p.vpFr, wi, p.vpWo, ALL));
-              p.phi = p.phi + Phi;
-              ++p.M;
+              if (par) {
+#pragma omp atomic
+                p.phi.x += Phi.x;
+#pragma omp atomic
+                p.phi.y += Phi.y;
+#pragma omp atomic
+                p.phi.z += Phi.z;
+#pragma omp atomic
+                ++p.M;
+              } else {
+                p.phi = p.phi + Phi;
+                ++p.M;
+              }
             }
           }
         }
@@ -1480,6 +1503,7 @@ void renderSppm(const Scene& s, int nIter, int photons, float radius0, int maxDe
       film[3 * pi + 2] += L.z;
     }
   }
+  *rays += nrays;
 }
 
 // Scene setup: Scene::Scene + light preprocess + PathTracing::preprocess.
@@ -1737,10 +1761,12 @@ int port_render_pixels(void* h, int64_t npix, const int32_t* pix, int64_t k0, in
   return 0;
 }
 
-// SPPM::render with the given parameters; film: W*H*3 floats, zeroed by the caller.
-int64_t port_render_sppm(void* h, int32_t iterations, int32_t photons, float radius, int32_t max_depth, float* film) {
+// SPPM::render with the given parameters; film: W*H*3 floats, zeroed by the caller;
+// threads 1 = the deterministic single-thread order, 0 = all cores.
+int64_t port_render_sppm(void* h, int32_t iterations, int32_t photons, float radius, int32_t max_depth, float* film,
+                         int32_t threads) {
   int64_t rays = 0;
-  renderSppm(*static_cast<Scene*>(h), iterations, photons, radius, max_depth, film, &rays);
+  renderSppm(*static_cast<Scene*>(h), iterations, photons, radius, max_depth, film, &rays, threads);
   return rays;
 }
 
