@@ -495,6 +495,8 @@ def run_sppm(ctx, res: int, iterations: int, steps: int, cpu_iterations: int) ->
            "gpu": {"ms": round(gpu_ms, 2), "mpaths_s": round(units / (gpu_ms * 1e-3) / 1e6, 2),
                    "mrays_s": round(rays / (gpu_ms * 1e-3) / 1e6, 2), "launches": st["kernel_launches"]},
            "unit": "Mpaths/s (camera paths + photons)", "finite": bool(np.isfinite(film).all())}
+    if cpu_iterations <= 0:
+        return out
     try:
         from oracle import port
         sc = port.Scene(host)
@@ -562,12 +564,20 @@ def main():
     ap.add_argument("--batch-only", action="store_true", help="run the batched leg alone (profiling)")
     ap.add_argument("--sppm-res", type=int, default=512, help="SPPM leg: image side (0 = skip)")
     ap.add_argument("--sppm-iterations", type=int, default=16)
+    ap.add_argument("--sppm-only", action="store_true", help="run the SPPM leg alone (profiling)")
     args = ap.parse_args()
     if args.quick:
         args.batch_jobs = args.serve_scenes = args.sppm_res = 0
     from orion_gb300 import build
     build.build_product()
     build.build_port()
+    if args.sppm_only:  # profiling runs of the SPPM leg alone
+        import orion_gb300 as og
+        ctx = og.Context(0)
+        print(json.dumps(run_sppm(ctx, args.sppm_res or 512, args.sppm_iterations, steps=max(1, args.steps),
+                                  cpu_iterations=0)))
+        ctx.close()
+        return
     if args.batch_only:  # profiling runs of the batched engine alone
         import orion_gb300 as og
         ctx = og.Context(0)
