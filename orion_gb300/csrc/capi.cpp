@@ -155,10 +155,8 @@ struct orion_gpu_ctx {
   int bgraph_slots = 0;
   unsigned bgraph_mask = 0;  // shading classes the captured loop launches
   // SPPM: per-pixel state in one block, the grid's cell lists apart
-  DevBuf sppm_block, sppm_entries;
+  DevBuf sppm_block, sppm_hits;
   DevBuf preview;  // 8-bit previews of server films
-  int64_t sppm_pixels = 0;
-  int sppm_entries_cap = 0;
   int smem_limit = 48 * 1024;  // opt-in dynamic shared memory per block
   KernelLimits limits{1024, 1024};
   std::mutex mu;
@@ -626,8 +624,8 @@ extern "C" int orion_gpu_render_sppm(orion_gpu_ctx* ctx, orion_scene_id id, cons
   const int W = d.view.cam.width, H = d.view.cam.height;
   const int64_t npix = (int64_t)W * H;
   const int64_t photons = p.photons_per_iter < 0 ? npix : p.photons_per_iter;
-  // A visible point lists itself in at most 27 cells: entry counts stay below 2^31.
-  if (npix <= 0 || npix > (1 << 26) || photons > (1LL << 30)) return fail(ORION_ERR_INVALID, "sppm: size out of range");
+  const int64_t hits_cap = photons * std::max(1, p.max_depth - 1);  // hits after each photon's first
+  if (npix <= 0 || npix > (1 << 28) || hits_cap > INT32_MAX) return fail(ORION_ERR_INVALID, "sppm: size out of range");
   if ((int64_t)p.iterations * (npix + photons) >= (1LL << 52))
     return fail(ORION_ERR_INVALID, "sppm: sample indices exceed the Sobol matrices");
   cudaStream_t st = ctx->stream;
@@ -654,6 +652,7 @@ extern "C" int orion_gpu_render_sppm(orion_gpu_ctx* ctx, orion_scene_id id, cons
   pieces.push_back({(void**)&v.film, sizeof(float) * 3 * (size_t)npix});
   pieces.push_back({(void**)&v.film_count, sizeof(unsigned) * (size_t)npix});
   pieces.push_back({(void**)&v.rays, sizeof(unsigned long long)});
+  pieces.push_back({(void**)&v.hit_count, sizeof(int)});
   size_t total = 0;
   for (const Piece& pc : pieces) total += (pc.bytes + 255) & ~(size_t)255;
   if (ctx->sppm_block.bytes < total) RC(ctx->sppm_block.alloc(total));
@@ -673,12 +672,13 @@ extern "C" int orion_gpu_render_sppm(orion_gpu_ctx* ctx, orion_scene_id id, cons
   v.iterations = p.iterations;
   v.photons = (int)photons;
   v.sobol = ctx->sobol.as<uint32_t>();
-  if (ctx->sppm_entries_cap < 8 * npix) {
-    RC(ctx->sppm_entries.alloc(sizeof(int) * 8 * (size_t)npix));
-    ctx->sppm_entries_cap = (int)std::min<int64_t>(8 * npix, INT32_MAX);
-  }
-  v.entries = ctx->sppm_entries.as<int>();
-  v.entries_cap = ctx->sppm_entries_cap;
+  // Photon hits (3 float4) and their cell-list entries (int), one block.
+  const size_t hit_bytes = ((size_t)hits_cap * 3 * sizeof(float4) + 255) & ~(size_t)255;
+  if (ctx->sppm_hits.bytes < hit_bytes + sizeof(int) * (size_t)hits_cap)
+    RC(ctx->sppm_hits.alloc(hit_bytes + sizeof(int) * (size_t)hits_cap));
+  v.hits = ctx->sppm_hits.as<float4>();
+  v.entries = reinterpret_cast<int*>(static_cast<char*>(ctx->sppm_hits.p) + hit_bytes);
+  v.hits_cap = (int)hits_cap;
 
   launch_sppm_init(v, p.initial_radius, st);
   CUDA_TRY(cudaMemsetAsync(v.rays, 0, sizeof(unsigned long long), st));
@@ -687,21 +687,9 @@ extern "C" int orion_gpu_render_sppm(orion_gpu_ctx* ctx, orion_scene_id id, cons
   int64_t launches = 1;
   for (int iter = 0; iter < p.iterations; ++iter) {
     launch_sppm_visible_points(d.view, v, iter, st);
-    launch_sppm_scan(v, st);
-    int entries = 0;
-    CUDA_TRY(cudaMemcpyAsync(&entries, v.cell_start + npix, sizeof(int), cudaMemcpyDeviceToHost, st));
-    CUDA_TRY(cudaStreamSynchronize(st));
-    if (entries < 0) return fail(ORION_ERR_DEVICE, "sppm: grid entry count overflow");
-    if (entries > v.entries_cap) {  // grow the cell lists (the stream is idle here)
-      const int64_t cap = std::min<int64_t>((int64_t)entries + entries / 4 + 1024, INT32_MAX);
-      RC(ctx->sppm_entries.alloc(sizeof(int) * (size_t)cap));
-      ctx->sppm_entries_cap = (int)cap;
-      v.entries = ctx->sppm_entries.as<int>();
-      v.entries_cap = (int)cap;
-    }
     launch_sppm_photons(d.view, v, iter, st);
     CUDA_TRY(cudaGetLastError());
-    launches += 12;
+    launches += 10;
   }
   CUDA_TRY(cudaEventRecord(ctx->ev1, st));
   unsigned long long rays = 0;

@@ -258,15 +258,18 @@ struct SppmView {
   float4* tau;      // tau
   float* phi;       // 3 per pixel, photon flux of this iteration
   int* m;           // photons gathered this iteration
-  // grid: hash cell -> visible points, cells [start[h], start[h + 1]) of `entries`
   SppmGrid* grid;
   float4* part_lo;  // per block of the bounds pass: lo, max radius
   float4* part_hi;  // hi, any
+  // photon hits of this iteration: 3 float4 each (point + hash cell, wi, beta)
+  float4* hits;
+  int hits_cap;     // photons x (max depth - 1): every hit after a photon's first
+  int* hit_count;
+  // hash cell -> photon hits: cell h lists entries [cell_start[h], cell_start[h + 1])
   int* cell_start;  // npix + 1 (counts, then their exclusive scan)
   int* cell_fill;   // npix
   int* scan_part;   // per scan block
-  int* entries;
-  int entries_cap;
+  int* entries;     // hits_cap
   float* film;      // W*H*3 sums of the iterations' estimates
   unsigned* film_count;
   unsigned long long* rays;
@@ -277,11 +280,12 @@ constexpr int kScanBlock = 1024;         // elements per block of the cell-count
 
 // Resets per-pixel state (radius r0, no visible point) and the film.
 void launch_sppm_init(const SppmView& v, float radius0, cudaStream_t stream);
-// Camera pass, grid bounds and cell counts of iteration `iter`.
+// Camera pass and the grid over the visible points of iteration `iter`.
 void launch_sppm_visible_points(const SceneView& s, const SppmView& v, int iter, cudaStream_t stream);
-// Exclusive scan of the cell counts; cell_start[npix] is then the entry count.
+// Exclusive scan of the cell counts (cell_start).
 void launch_sppm_scan(const SppmView& v, cudaStream_t stream);
-// Fills the cell lists, traces the photons, updates the pixels and the film.
+// Photon pass, photon lists by cell, gather at the visible points, pixel
+// update and film. No host synchronisation between iterations.
 void launch_sppm_photons(const SceneView& s, const SppmView& v, int iter, cudaStream_t stream);
 
 // Averaged FP64 film (W*H*3 sums, W*H counts) -> W*H pixels of bytes B, G,

@@ -8,14 +8,23 @@
 //                    src/core/integrator.cpp:8-27), the visible point kept
 //   k_sppm_bounds    bounds of the visible points' spheres, block partials
 //   k_sppm_grid      the grid resolution (sppm.cpp:145-160)
-//   k_sppm_count     visible points per hash cell
-//   k_scan_*         exclusive scan: each cell's first list entry
-//   k_sppm_fill      the cell lists
 //   k_sppm_photons   one thread per photon: Light::sample_Le, then a photon
-//                    path whose hits after the first add beta * f to every
-//                    visible point within its radius (atomics), with
-//                    TransportMode::Photon BSDFs and throughput roulette
+//                    path with TransportMode::Photon BSDFs and throughput
+//                    roulette; every hit after the first that falls inside
+//                    the grid is recorded (point, wi, beta) and counted in
+//                    its hash cell
+//   k_scan_*         exclusive scan: each hash cell's first list entry
+//   k_sppm_fill      the photon hits listed by hash cell
+//   k_sppm_gather    one thread per visible point: for each hash cell its
+//                    sphere overlaps, the recorded photons in that cell
+//                    within its radius add beta * f(wi, wo) (sppm.cpp:226-247)
 //   k_sppm_update    radius / N / tau update and the film (sppm.cpp:272-320)
+// The reference walks, per photon hit, the visible points listed in the hit's
+// hash cell; here each visible point walks the photon hits listed in the hash
+// cells of its own sphere. Both consider a (visible point, photon) pair once
+// per cell of the sphere whose hash equals the hash of the photon's cell, so
+// the sums have the same terms; only their order differs. A visible point's
+// material and frame are loaded once, and no flux atomics are needed.
 // Paths and photons trace with the per-thread 8-wide traversal
 // (traverse.cuh); the per-pixel and per-photon loops are short and their
 // bounce counts vary, so a thread follows its own path to the end.
@@ -302,30 +311,53 @@ __device__ __forceinline__ unsigned cell_hash(int x, int y, int z, int size) {
   return (((unsigned)x * 73856093u) ^ ((unsigned)y * 19349663u) ^ ((unsigned)z * 83492791u)) % (unsigned)size;
 }
 
-// Visits the cells a visible point's sphere overlaps (sppm.cpp:167-190).
-template <bool FILL>
-__global__ void __launch_bounds__(256) k_sppm_cells(SppmView v) {
-  const SppmGrid g = *v.grid;
-  if (!g.any) return;
-  for (int pix = blockIdx.x * blockDim.x + threadIdx.x; pix < v.npix; pix += gridDim.x * blockDim.x) {
-    if (!has_vp(v, pix)) continue;
-    const float4 pr = v.vp_pr[pix];
-    const V3 p = xyz(pr), r = V3{pr.w, pr.w, pr.w};
-    int lo[3], hi[3];
-    to_grid(g, p - r, lo);
-    to_grid(g, p + r, hi);
-    for (int z = lo[2]; z <= hi[2]; ++z)
-      for (int y = lo[1]; y <= hi[1]; ++y)
-        for (int x = lo[0]; x <= hi[0]; ++x) {
-          const unsigned h = cell_hash(x, y, z, v.npix);
-          if (FILL) {
-            const int e = v.cell_start[h] + atomicAdd(v.cell_fill + h, 1);
-            if (e < v.entries_cap) v.entries[e] = pix;
-          } else {
-            atomicAdd(v.cell_start + h, 1);
-          }
-        }
+// Lists the recorded photon hits by hash cell (cell_start holds each
+// cell's first entry after the scan).
+__global__ void __launch_bounds__(256) k_sppm_fill(SppmView v) {
+  const int n = min(*v.hit_count, v.hits_cap);
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const unsigned h = (unsigned)__float_as_int(v.hits[3 * (size_t)i].w);
+    v.entries[v.cell_start[h] + atomicAdd(v.cell_fill + h, 1)] = i;
   }
+}
+
+// Photon flux at each visible point (sppm.cpp:226-247, seen from the visible
+// point): the cells its sphere overlaps (sppm.cpp:167-190), the photon hits
+// listed under each cell's hash, those within the radius.
+__global__ void __launch_bounds__(128) k_sppm_gather(SceneView s, SppmView v) {
+  const int pix = blockIdx.x * blockDim.x + threadIdx.x;
+  if (pix >= v.npix || !has_vp(v, pix)) return;
+  const SppmGrid g = *v.grid;
+  const float4 pr = v.vp_pr[pix], wo4 = v.vp_wo[pix], b4 = v.vp_beta[pix], ns4 = v.vp_ns[pix];
+  const V3 p = xyz(pr), wo = xyz(wo4), r = V3{pr.w, pr.w, pr.w};
+  const float rr = pr.w * pr.w;
+  DevMaterial vm;
+  const DevMaterial& m = *material_at(s, __float_as_int(wo4.w), b4.w, ns4.w, &vm);
+  const Frame fr{xyz(v.vp_ng[pix]), xyz(ns4), xyz(v.vp_su[pix]), xyz(v.vp_sv[pix])};
+  int lo[3], hi[3];
+  to_grid(g, p - r, lo);
+  to_grid(g, p + r, hi);
+  V3 phi = V3{0, 0, 0};
+  int count = 0;
+  for (int z = lo[2]; z <= hi[2]; ++z)
+    for (int y = lo[1]; y <= hi[1]; ++y)
+      for (int x = lo[0]; x <= hi[0]; ++x) {
+        const unsigned h = cell_hash(x, y, z, v.npix);
+        const int e1 = v.cell_start[h + 1];
+        for (int e = v.cell_start[h]; e < e1; ++e) {
+          const float4* rec = v.hits + 3 * (size_t)v.entries[e];
+          const float4 hp = rec[0];
+          if (length_sq(p - xyz(hp)) > rr) continue;
+          const float4 wi4 = rec[1], hb = rec[2];
+          phi = phi + mul(xyz(hb), bsdf_f<kLobeAll>(m, fr, xyz(wi4), wo, BXDF_ALL));
+          ++count;
+        }
+      }
+  float* ph = v.phi + 3 * (size_t)pix;
+  ph[0] = phi.x;
+  ph[1] = phi.y;
+  ph[2] = phi.z;
+  v.m[pix] = count;
 }
 
 // Exclusive scan of n ints in place: per-block scans, a scan of the block
@@ -405,25 +437,24 @@ __global__ void __launch_bounds__(kSppmBlock) k_sppm_photons(SceneView s, SppmVi
     const int prim = __ldg(ts.tri_prim + rh.tri);
     const PrimShade& sh = s.prims[prim];
     const Hit h = reconstruct(sh, rh.u, rh.v);
-    if (depth > 0) {
+    if (depth > 0) {  // recorded for the gather when inside the grid (sppm.cpp:226-229)
       int cell[3];
-      if (to_grid(g, h.p, cell)) {
-        const unsigned hc = cell_hash(cell[0], cell[1], cell[2], v.npix);
-        const int e0 = v.cell_start[hc], e1 = min(v.cell_start[hc + 1], v.entries_cap);
-        const V3 wi = -dir;
-        for (int q = e0; q < e1; ++q) {
-          const int pix = v.entries[q];
-          const float4 pr = v.vp_pr[pix];
-          if (length_sq(xyz(pr) - h.p) > pr.w * pr.w) continue;
-          const float4 wo4 = v.vp_wo[pix], b4 = v.vp_beta[pix], ns4 = v.vp_ns[pix];
-          DevMaterial vm;
-          const DevMaterial& m = *material_at(s, __float_as_int(wo4.w), b4.w, ns4.w, &vm);
-          const Frame fr{xyz(v.vp_ng[pix]), xyz(ns4), xyz(v.vp_su[pix]), xyz(v.vp_sv[pix])};
-          const V3 phi = mul(beta, bsdf_f<kLobeAll>(m, fr, wi, xyz(wo4), BXDF_ALL));
-          atomicAdd(v.phi + 3 * (size_t)pix, phi.x);
-          atomicAdd(v.phi + 3 * (size_t)pix + 1, phi.y);
-          atomicAdd(v.phi + 3 * (size_t)pix + 2, phi.z);
-          atomicAdd(v.m + pix, 1);
+      const bool in = to_grid(g, h.p, cell);
+      const unsigned hc = in ? cell_hash(cell[0], cell[1], cell[2], v.npix) : 0u;
+      const unsigned act = __activemask();
+      const unsigned want = __ballot_sync(act, in);
+      if (in) {
+        const int lane = threadIdx.x & 31, leader = __ffs(want) - 1;
+        int base = 0;
+        if (lane == leader) base = atomicAdd(v.hit_count, __popc(want));
+        base = __shfl_sync(want, base, leader);
+        const int slot = base + __popc(want & ((1u << lane) - 1u));
+        if (slot < v.hits_cap) {
+          float4* rec = v.hits + 3 * (size_t)slot;
+          rec[0] = f4(h.p, __int_as_float((int)hc));
+          rec[1] = f4(-dir, 0.f);
+          rec[2] = f4(beta, 0.f);
+          atomicAdd(v.cell_start + hc, 1);
         }
       }
     }
@@ -519,8 +550,6 @@ void launch_sppm_visible_points(const SceneView& s, const SppmView& v, int iter,
   k_sppm_camera<kSppmStack><<<blocks_for(v.npix, kSppmBlock), kSppmBlock, smem, stream>>>(s, v, iter);
   k_sppm_bounds<<<kSppmBoundsBlocks, 256, 0, stream>>>(v);
   k_sppm_grid<<<1, 256, 0, stream>>>(v, kSppmBoundsBlocks);
-  cudaMemsetAsync(v.cell_start, 0, sizeof(int) * ((size_t)v.npix + 1), stream);
-  k_sppm_cells<false><<<std::min(blocks_for(v.npix, 256), 8192), 256, 0, stream>>>(v);
 }
 
 void launch_sppm_scan(const SppmView& v, cudaStream_t stream) {
@@ -532,11 +561,15 @@ void launch_sppm_scan(const SppmView& v, cudaStream_t stream) {
 }
 
 void launch_sppm_photons(const SceneView& s, const SppmView& v, int iter, cudaStream_t stream) {
+  cudaMemsetAsync(v.cell_start, 0, sizeof(int) * ((size_t)v.npix + 1), stream);
   cudaMemsetAsync(v.cell_fill, 0, sizeof(int) * (size_t)v.npix, stream);
-  k_sppm_cells<true><<<std::min(blocks_for(v.npix, 256), 8192), 256, 0, stream>>>(v);
+  cudaMemsetAsync(v.hit_count, 0, sizeof(int), stream);
   const size_t smem = (size_t)kSppmStack * kSppmBlock * sizeof(int2);
   if (v.photons > 0)
     k_sppm_photons<kSppmStack><<<blocks_for(v.photons, kSppmBlock), kSppmBlock, smem, stream>>>(s, v, iter);
+  launch_sppm_scan(v, stream);
+  k_sppm_fill<<<std::min(blocks_for(v.hits_cap, 256), 8192), 256, 0, stream>>>(v);
+  k_sppm_gather<<<blocks_for(v.npix, 128), 128, 0, stream>>>(s, v);
   k_sppm_update<<<blocks_for(v.npix, 256), 256, 0, stream>>>(v);
 }
 
