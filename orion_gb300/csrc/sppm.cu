@@ -15,7 +15,7 @@
 //                    its hash cell
 //   k_scan_*         exclusive scan: each hash cell's first list entry
 //   k_sppm_fill      the photon hits listed by hash cell
-//   k_sppm_gather    one thread per visible point: for each hash cell its
+//   k_sppm_gather    one warp per visible point: for each hash cell its
 //                    sphere overlaps, the recorded photons in that cell
 //                    within its radius add beta * f(wi, wo) (sppm.cpp:226-247)
 //   k_sppm_update    radius / N / tau update and the film (sppm.cpp:272-320)
@@ -323,10 +323,13 @@ __global__ void __launch_bounds__(256) k_sppm_fill(SppmView v) {
 
 // Photon flux at each visible point (sppm.cpp:226-247, seen from the visible
 // point): the cells its sphere overlaps (sppm.cpp:167-190), the photon hits
-// listed under each cell's hash, those within the radius.
+// listed under each cell's hash, those within the radius. One warp per
+// visible point: the lanes take a cell's hits in turn, so every lane runs the
+// same material's BSDF, and the lanes' sums are added at the end.
 __global__ void __launch_bounds__(128) k_sppm_gather(SceneView s, SppmView v) {
-  const int pix = blockIdx.x * blockDim.x + threadIdx.x;
-  if (pix >= v.npix || !has_vp(v, pix)) return;
+  const int pix = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (pix >= v.npix || !has_vp(v, pix)) return;  // uniform across the warp
   const SppmGrid g = *v.grid;
   const float4 pr = v.vp_pr[pix], wo4 = v.vp_wo[pix], b4 = v.vp_beta[pix], ns4 = v.vp_ns[pix];
   const V3 p = xyz(pr), wo = xyz(wo4), r = V3{pr.w, pr.w, pr.w};
@@ -344,7 +347,7 @@ __global__ void __launch_bounds__(128) k_sppm_gather(SceneView s, SppmView v) {
       for (int x = lo[0]; x <= hi[0]; ++x) {
         const unsigned h = cell_hash(x, y, z, v.npix);
         const int e1 = v.cell_start[h + 1];
-        for (int e = v.cell_start[h]; e < e1; ++e) {
+        for (int e = v.cell_start[h] + lane; e < e1; e += 32) {
           const float4* rec = v.hits + 3 * (size_t)v.entries[e];
           const float4 hp = rec[0];
           if (length_sq(p - xyz(hp)) > rr) continue;
@@ -353,11 +356,19 @@ __global__ void __launch_bounds__(128) k_sppm_gather(SceneView s, SppmView v) {
           ++count;
         }
       }
-  float* ph = v.phi + 3 * (size_t)pix;
-  ph[0] = phi.x;
-  ph[1] = phi.y;
-  ph[2] = phi.z;
-  v.m[pix] = count;
+  for (int off = 16; off > 0; off >>= 1) {
+    phi.x += __shfl_xor_sync(0xffffffffu, phi.x, off);
+    phi.y += __shfl_xor_sync(0xffffffffu, phi.y, off);
+    phi.z += __shfl_xor_sync(0xffffffffu, phi.z, off);
+    count += __shfl_xor_sync(0xffffffffu, count, off);
+  }
+  if (lane == 0) {
+    float* ph = v.phi + 3 * (size_t)pix;
+    ph[0] = phi.x;
+    ph[1] = phi.y;
+    ph[2] = phi.z;
+    v.m[pix] = count;
+  }
 }
 
 // Exclusive scan of n ints in place: per-block scans, a scan of the block
@@ -569,7 +580,7 @@ void launch_sppm_photons(const SceneView& s, const SppmView& v, int iter, cudaSt
     k_sppm_photons<kSppmStack><<<blocks_for(v.photons, kSppmBlock), kSppmBlock, smem, stream>>>(s, v, iter);
   launch_sppm_scan(v, stream);
   k_sppm_fill<<<std::min(blocks_for(v.hits_cap, 256), 8192), 256, 0, stream>>>(v);
-  k_sppm_gather<<<blocks_for(v.npix, 128), 128, 0, stream>>>(s, v);
+  k_sppm_gather<<<blocks_for((int64_t)v.npix * 32, 128), 128, 0, stream>>>(s, v);
   k_sppm_update<<<blocks_for(v.npix, 256), 256, 0, stream>>>(v);
 }
 
