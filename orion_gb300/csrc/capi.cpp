@@ -458,6 +458,8 @@ extern "C" int orion_gpu_scene_upload(orion_gpu_ctx* ctx, const orion_host_scene
   v.light_func_int = ps.light_func_int;
   v.num_lights = (int)ps.lights.size();
   v.num_env = (int)ps.env_idx.size();
+  v.num_area_lights = 0;
+  for (const DevLight& l : ps.lights) v.num_area_lights += l.kind == DL_AREA ? 1 : 0;
   for (int i = 0; i < v.num_env; ++i) v.env_idx[i] = ps.env_idx[i];
   v.world_radius = ps.world_radius;
   for (int k = 0; k < 3; ++k) v.world_center[k] = ps.world_center[k];

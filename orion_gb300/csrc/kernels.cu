@@ -323,12 +323,19 @@ void launch_wave(const SceneView& s, const WaveView& w, const WaveArgs& a, const
       begin(ST_TRACE_SHADOW);
       trace_dispatch(TK_SHADOW, s, w, cur, cfg, tgrid, stream);
       end();
+      // MIS rays exist only towards area lights (closest hit) and environment
+      // lights (occlusion); a scene without one kind skips its launch.
       begin(ST_TRACE_MIS);
-      trace_dispatch(TK_MIS, s, w, cur, cfg, tgrid, stream);
+      int mis = 0;
+      if (s.num_area_lights > 0) {
+        trace_dispatch(TK_MIS, s, w, cur, cfg, tgrid, stream);
+        ++mis;
+      }
       if (s.num_env > 0) {
         trace_dispatch(TK_MIS_ENV, s, w, cur, cfg, tgrid, stream);
-        ++nl;
+        ++mis;
       }
+      nl += mis - 1;  // end() counts one
       end();
       begin(ST_RESOLVE);
       k_resolve<<<sgrid, cfg.shade_block, 0, stream>>>(s, w);

@@ -26,6 +26,7 @@ struct SceneView {
   int num_lights;
   int env_idx[8];
   int num_env;
+  int num_area_lights;
   float world_radius;
   float world_center[3];  // Bounds3::boundingSphere (distant and environment photons)
   unsigned class_mask;  // shading classes of the scene's triangles (bit ShadeClass), SC_MISS always
