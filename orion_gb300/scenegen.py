@@ -344,6 +344,26 @@ def caustics(res: int = 64, iterations: int = 8, photons: int = 20000, radius: f
     return s
 
 
+def with_sppm(scene: Scene, iterations: int = 4, photons: int = 10000, radius: float = 0.08,
+              max_depth: int = 5) -> Scene:
+    """The scene rendered by <Integrator type="sppm"> instead of the path tracer."""
+    scene.sppm = {"iterations": iterations, "photons": photons, "radius": radius, "max_depth": max_depth}
+    scene.name = scene.name + "_sppm"
+    return scene
+
+
+def envlit_sppm(res: int = 32, iterations: int = 4, photons: int = 10000, radius: float = 0.08,
+                subdiv: int = 2) -> Scene:
+    """`envlit` (image environment map: photons emitted by its Distribution2D) under SPPM."""
+    return with_sppm(envlit(res, 1, 5, subdiv), iterations, photons, radius)
+
+
+def textured_sppm(res: int = 32, iterations: int = 4, photons: int = 10000, radius: float = 0.08,
+                  subdiv: int = 2) -> Scene:
+    """`textured` (image textures on every material input) under SPPM."""
+    return with_sppm(textured(res, 1, 5, subdiv), iterations, photons, radius)
+
+
 def displaced(res: int = 1024, spp: int = 64, subdiv: int = 8, max_depth: int = 8, seed: int = 1) -> Scene:
     rng = Rng(seed)
     roughness = float(rng.uniform(0.05, 0.5))

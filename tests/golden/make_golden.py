@@ -12,7 +12,8 @@ records its outputs on fixed inputs:
   image_*.npz  PathTracing::render film sums                (src/integrator/path.cpp:15-37);
                image_envlit lit by an image environment map (src/light/envmap.cpp),
                image_textured with image textures on every material input (src/core/texture.cpp)
-  image_caustics_sppm.npz  SPPM::render film sums (src/integrator/sppm.cpp:58-322), one thread
+  image_*_sppm.npz  SPPM::render film sums (src/integrator/sppm.cpp:58-322), one thread:
+               caustics (every light type), envlit (image environment map), textured
   stats_*.npz  FP64 per-pixel mean and variance at high spp (for 3-sigma checks)
   geometry.npz loader output digests
 
@@ -200,6 +201,19 @@ def main():
         np.savez_compressed(os.path.join(HERE, "image_caustics_sppm.npz"), film=img, width=W, height=H,
                             hash=np.frombuffer(helpers.scene_hash(path).encode(), np.uint8), **sppm_kw)
         ref.lib.ref_scene_free(h)
+        # SPPM with photons from an image environment map, and with image textures
+        for name in ("envlit_sppm", "textured_sppm"):
+            kw = dict(res=32, iterations=4, photons=10000, radius=0.08)
+            path = helpers.write_scene(name, os.path.join(tmp, name), **kw)
+            h, info = ref.load_in_scene_dir(path)
+            W, H = int(info[0]), int(info[1])
+            img = np.zeros((H, W, 3), np.float32)
+            ref.lib.ref_set_threads(1)
+            ref.lib.ref_scene_render(h, vp(img))
+            ref.lib.ref_set_threads(0)
+            np.savez_compressed(os.path.join(HERE, f"image_{name}.npz"), film=img, width=W, height=H,
+                                hash=np.frombuffer(helpers.scene_hash(path).encode(), np.uint8), **kw)
+            ref.lib.ref_scene_free(h)
         print("sppm", time.time() - t0)
 
         # FP64 statistics: Cornell at the full C1 resolution, a seeded pixel subset at high spp.

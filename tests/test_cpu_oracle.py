@@ -109,12 +109,13 @@ def test_port_statistics_agree_with_high_spp_reference(port, tmp_path):
     assert (z <= 3).mean() >= 0.9, f"3-sigma agreement {(z <= 3).mean():.3f}"
 
 
-def test_port_sppm_matches_reference_render(port, tmp_path):
+@pytest.mark.parametrize("name", ["caustics", "envlit_sppm", "textured_sppm"])
+def test_port_sppm_matches_reference_render(port, tmp_path, name):
     """SPPM::render (src/integrator/sppm.cpp:58-322): the oracle against the reference run on one thread."""
-    g = helpers.golden("image_caustics_sppm.npz")
+    g = helpers.golden(f"image_{name}.npz" if name.endswith("_sppm") else f"image_{name}_sppm.npz")
     kw = {k: (float(g[k]) if k == "radius" else int(g[k])) for k in ("res", "iterations", "photons", "radius",
-                                                                      "max_depth")}
-    path = helpers.write_scene("caustics", str(tmp_path / "c"), **kw)
+                                                                      "max_depth") if k in g}
+    path = helpers.write_scene(name, str(tmp_path / "c"), **kw)
     assert helpers.scene_hash(path) == bytes(g["hash"]).decode()
     film, rays = port.Scene.load(path).render_sppm()
     if EXACT:

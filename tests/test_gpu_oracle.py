@@ -113,26 +113,30 @@ def test_render_statistics_within_3_sigma_of_reference(ctx, tmp_path):
     assert rmse < 0.05
 
 
-def test_sppm_matches_oracle(ctx, port, tmp_path):
+@pytest.mark.parametrize("name,kw", [
+    ("caustics", dict(res=48, iterations=8, photons=20000, radius=0.08, max_depth=5)),
+    ("envlit_sppm", dict(res=32, iterations=4, photons=10000, radius=0.08)),
+    ("textured_sppm", dict(res=32, iterations=4, photons=10000, radius=0.08)),
+])
+def test_sppm_matches_oracle(ctx, port, tmp_path, name, kw):
     """SPPM on the GPU against the oracle (pinned bit-exact to the reference's single-thread SPPM).
 
     The same sample indices drive both; photon flux adds up in another order on the GPU (atomics) and
     device transcendental functions round differently, so a pixel agrees to FP32 rounding unless one of
     its photons took another path: most pixels within 1e-3 relative, the image within 1% RMSE."""
     import orion_gb300 as og
-    kw = dict(res=48, iterations=8, photons=20000, radius=0.08, max_depth=5)
-    path = helpers.write_scene("caustics", str(tmp_path / "c"), **kw)
+    path = helpers.write_scene(name, str(tmp_path / "c"), **kw)
     host = og.HostScene.load(path)
     ref, _ = port.Scene(host).render_sppm()
     sid = ctx.upload(host)
-    gpu, cnt = ctx.render_sppm(sid, 48, 48)
+    gpu, cnt = ctx.render_sppm(sid, kw["res"], kw["res"])
     st = ctx.last_stats()
     ctx.release(sid)
     assert (cnt == kw["iterations"]).all() and np.isfinite(gpu).all()
     rel = np.abs(gpu.astype(np.float64) - ref) / np.maximum(np.abs(ref), 1e-3)
     close = (rel <= 1e-3).all(2).mean()
     rmse = float(np.sqrt(np.mean((gpu.astype(np.float64) - ref) ** 2)) / np.sqrt(np.mean(ref.astype(np.float64) ** 2)))
-    print(f"sppm: {close:.4f} of pixels within 1e-3, relative RMSE {rmse:.2e}, {st['rays']} rays, "
+    print(f"{name}: {close:.4f} of pixels within 1e-3, relative RMSE {rmse:.2e}, {st['rays']} rays, "
           f"{st['device_ms']:.2f} ms")
     assert close >= 0.9
     assert rmse < 0.01
