@@ -132,6 +132,11 @@ struct orion_gpu_ctx {
   std::map<int, std::unique_ptr<DeviceScene>> scenes;
   int next_id = 1;
   Wave wave;
+  // Plain renders overlap consecutive waves on two streams: the second
+  // wave's state, stream and the events that order the film writes.
+  Wave wave2;
+  cudaStream_t stream2 = nullptr;
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_film[2] = {nullptr, nullptr};
   DevBuf film_sum, film_count, film64, filmsq64;
   int64_t film_pixels = 0;
   int64_t budget = 0;
@@ -240,20 +245,20 @@ static int ensure_film(orion_gpu_ctx* c, int64_t pixels, bool fp64) {
   return ORION_OK;
 }
 
-static int ensure_wave(orion_gpu_ctx* c, int capacity) {
-  if (c->wave.capacity >= capacity) return ORION_OK;
+static int alloc_wave(Wave& wave, int capacity) {
+  if (wave.capacity >= capacity) return ORION_OK;
   const size_t n = (size_t)capacity;
   auto round256 = [](size_t b) { return (b + 255) & ~(size_t)255; };
   const size_t recb = round256(n * sizeof(PathRec)), neeb = round256(n * sizeof(NeeRec));
   const size_t f4 = round256(n * sizeof(float4)), i4 = round256(n * sizeof(int));
   const size_t bytes = recb + neeb + f4 + (8 + kShadeClasses) * i4 + 256 + 4096;
-  int rc = c->wave.block.alloc(bytes);
+  int rc = wave.block.alloc(bytes);
   if (rc != ORION_OK) {
-    c->wave.capacity = 0;
+    wave.capacity = 0;
     return rc;
   }
-  char* p = c->wave.block.as<char>();
-  WaveView& w = c->wave.view;
+  char* p = wave.block.as<char>();
+  WaveView& w = wave.view;
   w.rec = reinterpret_cast<PathRec*>(p);
   p += recb;
   w.nee = reinterpret_cast<NeeRec*>(p);
@@ -296,9 +301,11 @@ static int ensure_wave(orion_gpu_ctx* c, int capacity) {
   p += 64;
   w.error_word = reinterpret_cast<int*>(p);
   w.capacity = capacity;
-  c->wave.capacity = capacity;
+  wave.capacity = capacity;
   return ORION_OK;
 }
+
+static int ensure_wave(orion_gpu_ctx* c, int capacity) { return alloc_wave(c->wave, capacity); }
 
 extern "C" int orion_gpu_create(const orion_gpu_opts* opts, orion_gpu_ctx** out) {
   if (!out) return fail(ORION_ERR_INVALID, "null argument");
@@ -312,8 +319,12 @@ extern "C" int orion_gpu_create(const orion_gpu_opts* opts, orion_gpu_ctx** out)
   CUDA_TRY(cudaGetDeviceProperties(&prop, c->device));
   c->num_sms = prop.multiProcessorCount;
   CUDA_TRY(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  CUDA_TRY(cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking));
   CUDA_TRY(cudaEventCreate(&c->ev0));
   CUDA_TRY(cudaEventCreate(&c->ev1));
+  CUDA_TRY(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
+  CUDA_TRY(cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming));
+  for (cudaEvent_t& e : c->ev_film) CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   size_t free_b = 0, total_b = 0;
   CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
   c->budget = (opts && opts->memory_budget > 0) ? opts->memory_budget : (int64_t)(free_b * 0.9);
@@ -350,13 +361,18 @@ extern "C" int orion_gpu_destroy(orion_gpu_ctx* ctx) {
   if (!ctx) return ORION_OK;
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
+  if (ctx->stream2) cudaStreamSynchronize(ctx->stream2);
   ctx->scenes.clear();
   ctx->wave.block.alloc(0);
+  ctx->wave2.block.alloc(0);
   if (ctx->bexec) cudaGraphExecDestroy(ctx->bexec);
   if (ctx->bgraph) cudaGraphDestroy(ctx->bgraph);
   for (cudaEvent_t e : ctx->prof_events) cudaEventDestroy(e);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+  for (cudaEvent_t e : {ctx->ev_fork, ctx->ev_join, ctx->ev_film[0], ctx->ev_film[1]})
+    if (e) cudaEventDestroy(e);
+  if (ctx->stream2) cudaStreamDestroy(ctx->stream2);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return ORION_OK;
@@ -521,6 +537,13 @@ static int render_impl(orion_gpu_ctx* ctx, orion_scene_id id, const orion_render
   wave = std::min<int64_t>(wave, std::max<int64_t>(total, 1));
   int rc = ensure_wave(ctx, (int)wave);
   if (rc != ORION_OK) return rc;
+  // Consecutive waves alternate between two streams and two path-state
+  // blocks, so one wave's kernels fill the SMs another's kernel tails leave
+  // idle; the film is written wave after wave (events), in sample order.
+  // Profiled renders stay on one stream so that stage times add up.
+  const int64_t nwaves = (total + wave - 1) / wave;
+  const bool two = !ctx->profiling && nwaves > 1;
+  if (two && (rc = alloc_wave(ctx->wave2, (int)wave)) != ORION_OK) return rc;
   const bool fp64 = sum64 != nullptr;
   if ((rc = ensure_film(ctx, wh, fp64)) != ORION_OK) return rc;
   cudaStream_t s = ctx->stream;
@@ -532,6 +555,10 @@ static int render_impl(orion_gpu_ctx* ctx, orion_scene_id id, const orion_render
   }
   CUDA_TRY(cudaMemsetAsync(ctx->wave.view.ray_stats, 0, 3 * sizeof(unsigned long long), s));
   CUDA_TRY(cudaMemsetAsync(ctx->wave.view.error_word, 0, sizeof(int), s));
+  if (two) {
+    CUDA_TRY(cudaMemsetAsync(ctx->wave2.view.ray_stats, 0, 3 * sizeof(unsigned long long), s));
+    CUDA_TRY(cudaMemsetAsync(ctx->wave2.view.error_word, 0, sizeof(int), s));
+  }
   FilmView film{ctx->film_sum.as<float>(), ctx->film_count.as<uint32_t>(), fp64 ? ctx->film64.as<double>() : nullptr,
                 fp64 ? ctx->filmsq64.as<double>() : nullptr};
   int launches = 0;
@@ -548,7 +575,13 @@ static int render_impl(orion_gpu_ctx* ctx, orion_scene_id id, const orion_render
     timer = StageTimer{ctx->prof_events.data(), ctx->prof_stage.data(), need, 0};
   }
   CUDA_TRY(cudaEventRecord(ctx->ev0, s));
-  for (int64_t off = 0; off < total; off += wave) {
+  if (two) {
+    CUDA_TRY(cudaEventRecord(ctx->ev_fork, s));
+    CUDA_TRY(cudaStreamWaitEvent(ctx->stream2, ctx->ev_fork, 0));
+  }
+  int64_t k = 0;
+  for (int64_t off = 0; off < total; off += wave, ++k) {
+    const bool second = two && (k & 1);
     WaveArgs a;
     a.sobol = ctx->sobol.as<uint32_t>();
     a.sobol_bitmajor = ctx->sobol_bitmajor.as<uint32_t>();
@@ -559,9 +592,16 @@ static int render_impl(orion_gpu_ctx* ctx, orion_scene_id id, const orion_render
     a.max_depth = max_depth;
     a.rr_depth = rr_depth;
     a.class_mask = d.class_mask;
-    launch_wave(d.view, ctx->wave.view, a, film, ctx->cfg, s, &launches, ctx->profiling ? &timer : nullptr);
+    const cudaEvent_t film_wait = two && k > 0 ? ctx->ev_film[(k - 1) & 1] : nullptr;
+    const cudaEvent_t film_done = two ? ctx->ev_film[k & 1] : nullptr;
+    launch_wave(d.view, second ? ctx->wave2.view : ctx->wave.view, a, film, ctx->cfg, second ? ctx->stream2 : s,
+                &launches, ctx->profiling ? &timer : nullptr, film_wait, film_done);
   }
   CUDA_TRY(cudaGetLastError());
+  if (two) {
+    CUDA_TRY(cudaEventRecord(ctx->ev_join, ctx->stream2));
+    CUDA_TRY(cudaStreamWaitEvent(s, ctx->ev_join, 0));
+  }
   CUDA_TRY(cudaEventRecord(ctx->ev1, s));
   if (film_rgb)
     CUDA_TRY(cudaMemcpyAsync(film_rgb, ctx->film_sum.p, wh * 3 * sizeof(float), cudaMemcpyDeviceToHost, s));
@@ -571,11 +611,17 @@ static int render_impl(orion_gpu_ctx* ctx, orion_scene_id id, const orion_render
     CUDA_TRY(cudaMemcpyAsync(sum64, ctx->film64.p, wh * 3 * sizeof(double), cudaMemcpyDeviceToHost, s));
     CUDA_TRY(cudaMemcpyAsync(sumsq64, ctx->filmsq64.p, wh * 3 * sizeof(double), cudaMemcpyDeviceToHost, s));
   }
-  unsigned long long stats[3] = {0, 0, 0};
-  int err_word = 0;
+  unsigned long long stats[3] = {0, 0, 0}, stats2[3] = {0, 0, 0};
+  int err_word = 0, err_word2 = 0;
   CUDA_TRY(cudaMemcpyAsync(stats, ctx->wave.view.ray_stats, sizeof(stats), cudaMemcpyDeviceToHost, s));
   CUDA_TRY(cudaMemcpyAsync(&err_word, ctx->wave.view.error_word, sizeof(int), cudaMemcpyDeviceToHost, s));
+  if (two) {
+    CUDA_TRY(cudaMemcpyAsync(stats2, ctx->wave2.view.ray_stats, sizeof(stats2), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaMemcpyAsync(&err_word2, ctx->wave2.view.error_word, sizeof(int), cudaMemcpyDeviceToHost, s));
+  }
   CUDA_TRY(cudaStreamSynchronize(s));
+  for (int i = 0; i < 3; ++i) stats[i] += stats2[i];
+  err_word = err_word ? err_word : err_word2;
   float ms = 0.f;
   CUDA_TRY(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
   ctx->last.paths = total;

@@ -275,7 +275,8 @@ void trace_dispatch(int kind, const SceneView& s, const WaveView& w, int cur, co
 }  // namespace
 
 void launch_wave(const SceneView& s, const WaveView& w, const WaveArgs& a, const FilmView& film,
-                 const LaunchConfig& cfg, cudaStream_t stream, int* launches, StageTimer* timer) {
+                 const LaunchConfig& cfg, cudaStream_t stream, int* launches, StageTimer* timer,
+                 cudaEvent_t film_wait, cudaEvent_t film_done) {
   const int persistent = cfg.num_sms * cfg.blocks_per_sm;
   int nl = 0;
   auto begin = [&](int st) {
@@ -343,9 +344,11 @@ void launch_wave(const SceneView& s, const WaveView& w, const WaveArgs& a, const
     }
     cur ^= 1;
   }
+  if (film_wait) cudaStreamWaitEvent(stream, film_wait, 0);
   begin(ST_FILM);
   k_film<<<grid_for(a.n_paths, 256, persistent * 4), 256, 0, stream>>>(w, a, film);
   end();
+  if (film_done) cudaEventRecord(film_done, stream);
   if (launches) *launches += nl;
 }
 

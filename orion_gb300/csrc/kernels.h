@@ -200,8 +200,11 @@ struct StageTimer {
 
 // One full wave: camera rays, then (trace, shade, shadow/MIS trace,
 // resolve) per bounce, then film accumulation. All on `stream`, no host sync.
+// The film kernel first waits for `film_wait` (the previous wave's film
+// write, when waves run on two streams) and then records `film_done`.
 void launch_wave(const SceneView& s, const WaveView& w, const WaveArgs& a, const FilmView& film,
-                 const LaunchConfig& cfg, cudaStream_t stream, int* launches, StageTimer* timer = nullptr);
+                 const LaunchConfig& cfg, cudaStream_t stream, int* launches, StageTimer* timer = nullptr,
+                 cudaEvent_t film_wait = nullptr, cudaEvent_t film_done = nullptr);
 
 // Launch limits of the kernel families, and the dynamic shared-memory
 // allowance of the traversal kernels (raised to `smem_bytes`, the device's

@@ -1,0 +1,46 @@
+"""Wave scheduling: a render is split into waves of path slots, and consecutive
+waves run on two streams. Every pixel's film sum is taken in sample order
+(RenderTarget::acumulate, src/texture/rendertarget.cpp:22-27), so the film
+must be bit-identical whatever the wave size, whether waves overlap on two
+streams or run on one (profiled renders), and from run to run."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import helpers
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def scene(ctx, tmp_path_factory):
+    import orion_gb300 as og
+    path = helpers.write_scene("zoo", str(tmp_path_factory.mktemp("waves") / "zoo"), res=48, spp=12)
+    host = og.HostScene.load(path)
+    sid = ctx.upload(host)
+    yield sid
+    ctx.release(sid)
+
+
+def test_film_independent_of_waves_and_streams(ctx, scene):
+    total = 48 * 48 * 12
+    ref, cnt = ctx.render(scene, 48, 48, wave_paths=total)  # one wave, one stream
+    assert (cnt == 12).all()
+    for wave in (4096, 3001, 48 * 48):
+        img, c = ctx.render(scene, 48, 48, wave_paths=wave)  # several waves on two streams
+        assert np.array_equal(c, cnt)
+        assert np.array_equal(img.view(np.uint32), ref.view(np.uint32)), f"wave {wave}"
+    s1, q1 = ctx.render(scene, 48, 48, wave_paths=total, fp64=True)
+    s2, q2 = ctx.render(scene, 48, 48, wave_paths=5000, fp64=True)
+    assert np.array_equal(s1, s2) and np.array_equal(q1, q2)
+    ctx.set_profiling(True)
+    try:
+        img, _ = ctx.render(scene, 48, 48, wave_paths=4096)  # profiled: one stream
+    finally:
+        ctx.set_profiling(False)
+    assert np.array_equal(img.view(np.uint32), ref.view(np.uint32))
+    st = ctx.last_stats()
+    again, _ = ctx.render(scene, 48, 48, wave_paths=4096)
+    assert np.array_equal(again.view(np.uint32), ref.view(np.uint32))
+    assert ctx.last_stats()["rays"] == st["rays"]
