@@ -116,7 +116,7 @@ class BatchStats(C.Structure):
 class LaunchConfig(C.Structure):
     _fields_ = [("trace_block", C.c_int32), ("shade_block", C.c_int32), ("smem_stack", C.c_int32),
                 ("blocks_per_sm", C.c_int32), ("wave_paths", C.c_int32), ("batch_slots", C.c_int32),
-                ("refill_below", C.c_int32), ("reserved", C.c_int32)]
+                ("refill_below", C.c_int32), ("streams", C.c_int32)]
 
 class ServerOpts(C.Structure):
     _fields_ = [("memory_budget", C.c_int64), ("spp_chunk", C.c_int32), ("max_jobs", C.c_int32)]

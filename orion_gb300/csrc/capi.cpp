@@ -116,6 +116,8 @@ struct DeviceScene {
   orion_sppm_params sppm{0, 0, 0.f, 0};  // the scene's <Integrator type="sppm"> parameters
 };
 
+constexpr int kMaxWaveStreams = 4;  // plain-render waves in flight at once
+
 struct Wave {
   int capacity = 0;
   DevBuf block;  // all per-path arrays in one allocation
@@ -132,11 +134,14 @@ struct orion_gpu_ctx {
   std::map<int, std::unique_ptr<DeviceScene>> scenes;
   int next_id = 1;
   Wave wave;
-  // Plain renders overlap consecutive waves on two streams: the second
-  // wave's state, stream and the events that order the film writes.
-  Wave wave2;
-  cudaStream_t stream2 = nullptr;
-  cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_film[2] = {nullptr, nullptr};
+  // Plain renders overlap consecutive waves on up to kWaveStreams streams:
+  // per extra stream its wave state, the stream, its join event; the events
+  // that order the film writes wave after wave.
+  static constexpr int kWaveStreams = kMaxWaveStreams;
+  int wave_streams = 2;
+  Wave xwave[kWaveStreams - 1];
+  cudaStream_t xstream[kWaveStreams - 1] = {};
+  cudaEvent_t ev_fork = nullptr, ev_join[kWaveStreams - 1] = {}, ev_film[kWaveStreams] = {};
   DevBuf film_sum, film_count, film64, filmsq64;
   int64_t film_pixels = 0;
   int64_t budget = 0;
@@ -319,11 +324,11 @@ extern "C" int orion_gpu_create(const orion_gpu_opts* opts, orion_gpu_ctx** out)
   CUDA_TRY(cudaGetDeviceProperties(&prop, c->device));
   c->num_sms = prop.multiProcessorCount;
   CUDA_TRY(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
-  CUDA_TRY(cudaStreamCreateWithFlags(&c->stream2, cudaStreamNonBlocking));
+  for (cudaStream_t& x : c->xstream) CUDA_TRY(cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking));
   CUDA_TRY(cudaEventCreate(&c->ev0));
   CUDA_TRY(cudaEventCreate(&c->ev1));
   CUDA_TRY(cudaEventCreateWithFlags(&c->ev_fork, cudaEventDisableTiming));
-  CUDA_TRY(cudaEventCreateWithFlags(&c->ev_join, cudaEventDisableTiming));
+  for (cudaEvent_t& e : c->ev_join) CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   for (cudaEvent_t& e : c->ev_film) CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   size_t free_b = 0, total_b = 0;
   CUDA_TRY(cudaMemGetInfo(&free_b, &total_b));
@@ -361,18 +366,23 @@ extern "C" int orion_gpu_destroy(orion_gpu_ctx* ctx) {
   if (!ctx) return ORION_OK;
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
-  if (ctx->stream2) cudaStreamSynchronize(ctx->stream2);
+  for (cudaStream_t x : ctx->xstream)
+    if (x) cudaStreamSynchronize(x);
   ctx->scenes.clear();
   ctx->wave.block.alloc(0);
-  ctx->wave2.block.alloc(0);
+  for (Wave& w : ctx->xwave) w.block.alloc(0);
   if (ctx->bexec) cudaGraphExecDestroy(ctx->bexec);
   if (ctx->bgraph) cudaGraphDestroy(ctx->bgraph);
   for (cudaEvent_t e : ctx->prof_events) cudaEventDestroy(e);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
-  for (cudaEvent_t e : {ctx->ev_fork, ctx->ev_join, ctx->ev_film[0], ctx->ev_film[1]})
+  if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+  for (cudaEvent_t e : ctx->ev_join)
     if (e) cudaEventDestroy(e);
-  if (ctx->stream2) cudaStreamDestroy(ctx->stream2);
+  for (cudaEvent_t e : ctx->ev_film)
+    if (e) cudaEventDestroy(e);
+  for (cudaStream_t x : ctx->xstream)
+    if (x) cudaStreamDestroy(x);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return ORION_OK;
@@ -537,13 +547,17 @@ static int render_impl(orion_gpu_ctx* ctx, orion_scene_id id, const orion_render
   wave = std::min<int64_t>(wave, std::max<int64_t>(total, 1));
   int rc = ensure_wave(ctx, (int)wave);
   if (rc != ORION_OK) return rc;
-  // Consecutive waves alternate between two streams and two path-state
-  // blocks, so one wave's kernels fill the SMs another's kernel tails leave
-  // idle; the film is written wave after wave (events), in sample order.
-  // Profiled renders stay on one stream so that stage times add up.
+  // Consecutive waves take turns on `ns` streams, each with its own
+  // path-state block, so one wave's kernels fill the SMs that another's
+  // kernel tails leave idle; the film is written wave after wave (events),
+  // so every pixel still sums its samples in sample order. Profiled renders
+  // stay on one stream so that stage times add up.
   const int64_t nwaves = (total + wave - 1) / wave;
-  const bool two = !ctx->profiling && nwaves > 1;
-  if (two && (rc = alloc_wave(ctx->wave2, (int)wave)) != ORION_OK) return rc;
+  const int ns = ctx->profiling ? 1 : (int)std::min<int64_t>(ctx->wave_streams, nwaves);
+  for (int i = 1; i < ns; ++i)
+    if ((rc = alloc_wave(ctx->xwave[i - 1], (int)wave)) != ORION_OK) return rc;
+  auto wave_view = [&](int i) -> const WaveView& { return i == 0 ? ctx->wave.view : ctx->xwave[i - 1].view; };
+  auto wave_stream = [&](int i) { return i == 0 ? ctx->stream : ctx->xstream[i - 1]; };
   const bool fp64 = sum64 != nullptr;
   if ((rc = ensure_film(ctx, wh, fp64)) != ORION_OK) return rc;
   cudaStream_t s = ctx->stream;
@@ -553,11 +567,9 @@ static int render_impl(orion_gpu_ctx* ctx, orion_scene_id id, const orion_render
     CUDA_TRY(cudaMemsetAsync(ctx->film64.p, 0, wh * 3 * sizeof(double), s));
     CUDA_TRY(cudaMemsetAsync(ctx->filmsq64.p, 0, wh * 3 * sizeof(double), s));
   }
-  CUDA_TRY(cudaMemsetAsync(ctx->wave.view.ray_stats, 0, 3 * sizeof(unsigned long long), s));
-  CUDA_TRY(cudaMemsetAsync(ctx->wave.view.error_word, 0, sizeof(int), s));
-  if (two) {
-    CUDA_TRY(cudaMemsetAsync(ctx->wave2.view.ray_stats, 0, 3 * sizeof(unsigned long long), s));
-    CUDA_TRY(cudaMemsetAsync(ctx->wave2.view.error_word, 0, sizeof(int), s));
+  for (int i = 0; i < ns; ++i) {
+    CUDA_TRY(cudaMemsetAsync(wave_view(i).ray_stats, 0, 3 * sizeof(unsigned long long), s));
+    CUDA_TRY(cudaMemsetAsync(wave_view(i).error_word, 0, sizeof(int), s));
   }
   FilmView film{ctx->film_sum.as<float>(), ctx->film_count.as<uint32_t>(), fp64 ? ctx->film64.as<double>() : nullptr,
                 fp64 ? ctx->filmsq64.as<double>() : nullptr};
@@ -575,13 +587,13 @@ static int render_impl(orion_gpu_ctx* ctx, orion_scene_id id, const orion_render
     timer = StageTimer{ctx->prof_events.data(), ctx->prof_stage.data(), need, 0};
   }
   CUDA_TRY(cudaEventRecord(ctx->ev0, s));
-  if (two) {
+  if (ns > 1) {
     CUDA_TRY(cudaEventRecord(ctx->ev_fork, s));
-    CUDA_TRY(cudaStreamWaitEvent(ctx->stream2, ctx->ev_fork, 0));
+    for (int i = 1; i < ns; ++i) CUDA_TRY(cudaStreamWaitEvent(wave_stream(i), ctx->ev_fork, 0));
   }
   int64_t k = 0;
   for (int64_t off = 0; off < total; off += wave, ++k) {
-    const bool second = two && (k & 1);
+    const int slot = (int)(k % ns);
     WaveArgs a;
     a.sobol = ctx->sobol.as<uint32_t>();
     a.sobol_bitmajor = ctx->sobol_bitmajor.as<uint32_t>();
@@ -592,15 +604,15 @@ static int render_impl(orion_gpu_ctx* ctx, orion_scene_id id, const orion_render
     a.max_depth = max_depth;
     a.rr_depth = rr_depth;
     a.class_mask = d.class_mask;
-    const cudaEvent_t film_wait = two && k > 0 ? ctx->ev_film[(k - 1) & 1] : nullptr;
-    const cudaEvent_t film_done = two ? ctx->ev_film[k & 1] : nullptr;
-    launch_wave(d.view, second ? ctx->wave2.view : ctx->wave.view, a, film, ctx->cfg, second ? ctx->stream2 : s,
-                &launches, ctx->profiling ? &timer : nullptr, film_wait, film_done);
+    const cudaEvent_t film_wait = ns > 1 && k > 0 ? ctx->ev_film[(k - 1) % ns] : nullptr;
+    const cudaEvent_t film_done = ns > 1 ? ctx->ev_film[k % ns] : nullptr;
+    launch_wave(d.view, wave_view(slot), a, film, ctx->cfg, wave_stream(slot), &launches,
+                ctx->profiling ? &timer : nullptr, film_wait, film_done);
   }
   CUDA_TRY(cudaGetLastError());
-  if (two) {
-    CUDA_TRY(cudaEventRecord(ctx->ev_join, ctx->stream2));
-    CUDA_TRY(cudaStreamWaitEvent(s, ctx->ev_join, 0));
+  for (int i = 1; i < ns; ++i) {
+    CUDA_TRY(cudaEventRecord(ctx->ev_join[i - 1], wave_stream(i)));
+    CUDA_TRY(cudaStreamWaitEvent(s, ctx->ev_join[i - 1], 0));
   }
   CUDA_TRY(cudaEventRecord(ctx->ev1, s));
   if (film_rgb)
@@ -611,17 +623,19 @@ static int render_impl(orion_gpu_ctx* ctx, orion_scene_id id, const orion_render
     CUDA_TRY(cudaMemcpyAsync(sum64, ctx->film64.p, wh * 3 * sizeof(double), cudaMemcpyDeviceToHost, s));
     CUDA_TRY(cudaMemcpyAsync(sumsq64, ctx->filmsq64.p, wh * 3 * sizeof(double), cudaMemcpyDeviceToHost, s));
   }
-  unsigned long long stats[3] = {0, 0, 0}, stats2[3] = {0, 0, 0};
-  int err_word = 0, err_word2 = 0;
-  CUDA_TRY(cudaMemcpyAsync(stats, ctx->wave.view.ray_stats, sizeof(stats), cudaMemcpyDeviceToHost, s));
-  CUDA_TRY(cudaMemcpyAsync(&err_word, ctx->wave.view.error_word, sizeof(int), cudaMemcpyDeviceToHost, s));
-  if (two) {
-    CUDA_TRY(cudaMemcpyAsync(stats2, ctx->wave2.view.ray_stats, sizeof(stats2), cudaMemcpyDeviceToHost, s));
-    CUDA_TRY(cudaMemcpyAsync(&err_word2, ctx->wave2.view.error_word, sizeof(int), cudaMemcpyDeviceToHost, s));
+  unsigned long long wstats[kMaxWaveStreams][3] = {};
+  int werr[kMaxWaveStreams] = {};
+  for (int i = 0; i < ns; ++i) {
+    CUDA_TRY(cudaMemcpyAsync(wstats[i], wave_view(i).ray_stats, sizeof(wstats[i]), cudaMemcpyDeviceToHost, s));
+    CUDA_TRY(cudaMemcpyAsync(&werr[i], wave_view(i).error_word, sizeof(int), cudaMemcpyDeviceToHost, s));
   }
   CUDA_TRY(cudaStreamSynchronize(s));
-  for (int i = 0; i < 3; ++i) stats[i] += stats2[i];
-  err_word = err_word ? err_word : err_word2;
+  unsigned long long stats[3] = {0, 0, 0};
+  int err_word = 0;
+  for (int i = 0; i < ns; ++i) {
+    for (int j = 0; j < 3; ++j) stats[j] += wstats[i][j];
+    err_word = err_word ? err_word : werr[i];
+  }
   float ms = 0.f;
   CUDA_TRY(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
   ctx->last.paths = total;
@@ -1118,7 +1132,7 @@ extern "C" int orion_gpu_get_config(orion_gpu_ctx* ctx, orion_launch_config* out
   out->wave_paths = ctx->default_wave;
   out->batch_slots = ctx->default_batch_slots;
   out->refill_below = ctx->cfg.refill_below;
-  out->reserved = 0;
+  out->streams = ctx->wave_streams;
   return ORION_OK;
 }
 
@@ -1134,7 +1148,10 @@ extern "C" int orion_gpu_set_config(orion_gpu_ctx* ctx, const orion_launch_confi
   if (!why.empty()) return fail(ORION_ERR_INVALID, "launch configuration: " + why);
   if (cfg->wave_paths < 1024 || cfg->batch_slots < 1024)
     return fail(ORION_ERR_INVALID, "launch configuration: wave_paths and batch_slots must be >= 1024");
+  if (cfg->streams < 0 || cfg->streams > kMaxWaveStreams)
+    return fail(ORION_ERR_INVALID, "launch configuration: streams must be 0.." + std::to_string(kMaxWaveStreams));
   std::lock_guard<std::mutex> g(ctx->mu);
+  if (cfg->streams > 0) ctx->wave_streams = cfg->streams;
   ctx->cfg = c;
   ctx->default_wave = cfg->wave_paths;
   ctx->default_batch_slots = cfg->batch_slots;
@@ -1217,7 +1234,7 @@ extern "C" int orion_gpu_autotune(orion_gpu_ctx* ctx, orion_scene_id id, int32_t
     best_out->wave_paths = best_wave;
     best_out->batch_slots = best_wave;
     best_out->refill_below = best.refill_below;
-    best_out->reserved = 0;
+    best_out->streams = ctx->wave_streams;
   }
   if (best_mpaths) *best_mpaths = paths / (best_ms * 1e-3) / 1e6;
   return ORION_OK;
@@ -1303,7 +1320,7 @@ extern "C" int orion_gpu_autotune_batch(orion_gpu_ctx* ctx, int32_t njobs, const
     best_out->wave_paths = ctx->default_wave;
     best_out->batch_slots = best_slots;
     best_out->refill_below = best.refill_below;
-    best_out->reserved = 0;
+    best_out->streams = ctx->wave_streams;
   }
   if (best_mpaths) *best_mpaths = (double)total / (best_ms * 1e-3) / 1e6;
   return ORION_OK;

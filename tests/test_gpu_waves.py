@@ -27,10 +27,16 @@ def test_film_independent_of_waves_and_streams(ctx, scene):
     total = 48 * 48 * 12
     ref, cnt = ctx.render(scene, 48, 48, wave_paths=total)  # one wave, one stream
     assert (cnt == 12).all()
-    for wave in (4096, 3001, 48 * 48):
-        img, c = ctx.render(scene, 48, 48, wave_paths=wave)  # several waves on two streams
-        assert np.array_equal(c, cnt)
-        assert np.array_equal(img.view(np.uint32), ref.view(np.uint32)), f"wave {wave}"
+    cfg = ctx.get_config()
+    try:
+        for streams in (1, 2, 3, 4):
+            ctx.set_config(streams=streams)
+            for wave in (4096, 3001, 48 * 48):
+                img, c = ctx.render(scene, 48, 48, wave_paths=wave)  # several waves on `streams` streams
+                assert np.array_equal(c, cnt)
+                assert np.array_equal(img.view(np.uint32), ref.view(np.uint32)), f"wave {wave}, {streams} streams"
+    finally:
+        ctx.set_config(**cfg)
     # FP64 sums of squares are grouped by wave (rounding depends on the wave size), so the FP64
     # film is compared at one wave size: two streams against one.
     s1, q1 = ctx.render(scene, 48, 48, wave_paths=5000, fp64=True)
