@@ -296,7 +296,8 @@ typedef struct orion_launch_config {
   int32_t wave_paths;     /* paths per plain-render wave */
   int32_t batch_slots;    /* path slots of the batched pool */
   int32_t refill_below;   /* a traversal warp takes new rays once fewer lanes than this hold one (1..32) */
-  int32_t streams;        /* plain renders: waves in flight at once, each on its own stream (1..4); 0 = keep */
+  int32_t streams;        /* plain renders: waves in flight at once, each on its own stream (1..4);
+                             batches: concurrent pooled engines, min(streams, 2); 0 = keep */
 } orion_launch_config;
 
 int orion_gpu_get_config(orion_gpu_ctx* ctx, orion_launch_config* out);

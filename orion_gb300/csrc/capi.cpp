@@ -118,6 +118,25 @@ struct DeviceScene {
 
 constexpr int kMaxWaveStreams = 4;  // plain-render waves in flight at once
 
+// One pooled batch engine: its free and retire lists, control block, job
+// table and captured device-side loop (the path slots are a Wave).
+struct BatchEngine {
+  DevBuf retire, free_list, ctl, jobs;
+  int slots_alloc = 0, jobs_alloc = 0;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  const void* key[4] = {nullptr, nullptr, nullptr, nullptr};  // buffers the graph was captured with
+  LaunchConfig cfg{};
+  int slots = 0;
+  unsigned mask = 0;  // shading classes the captured loop launches
+  void drop_graph() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    exec = nullptr;
+    graph = nullptr;
+  }
+};
+
 struct Wave {
   int capacity = 0;
   DevBuf block;  // all per-path arrays in one allocation
@@ -157,16 +176,13 @@ struct orion_gpu_ctx {
   std::vector<int> prof_stage;
   orion_stage_times stage_times{};
   // batched mode
-  DevBuf b_retire, b_free, b_ctl, b_jobs, b_films;
-  int batch_slots_alloc = 0;
-  int jobs_alloc = 0;
   int default_batch_slots = 1 << 23;
-  cudaGraph_t bgraph = nullptr;
-  cudaGraphExec_t bexec = nullptr;
-  const void* bgraph_key[4] = {nullptr, nullptr, nullptr, nullptr};
-  LaunchConfig bgraph_cfg{};
-  int bgraph_slots = 0;
-  unsigned bgraph_mask = 0;  // shading classes the captured loop launches
+  DevBuf b_films;
+  // Pooled batch engines: a batch's jobs are split between as many as the
+  // `streams` knob allows (at most kBatchEngines) and they run concurrently,
+  // engine e on the wave state and stream of wave slot e.
+  static constexpr int kBatchEngines = 2;
+  BatchEngine beng[kBatchEngines];
   // SPPM: per-pixel state in one block, the grid's cell lists apart
   DevBuf sppm_block, sppm_hits;
   DevBuf preview;  // 8-bit previews of server films
@@ -374,8 +390,7 @@ extern "C" int orion_gpu_destroy(orion_gpu_ctx* ctx) {
   ctx->scenes.clear();
   ctx->wave.block.alloc(0);
   for (Wave& w : ctx->xwave) w.block.alloc(0);
-  if (ctx->bexec) cudaGraphExecDestroy(ctx->bexec);
-  if (ctx->bgraph) cudaGraphDestroy(ctx->bgraph);
+  for (BatchEngine& e : ctx->beng) e.drop_graph();
   for (cudaEvent_t e : ctx->prof_events) cudaEventDestroy(e);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
@@ -795,23 +810,25 @@ extern "C" int orion_gpu_stage_times(orion_gpu_ctx* ctx, orion_stage_times* out)
 
 // ------------------------------------------------------------ batches
 
+// Wave state and stream of batch engine e (shared with plain-render wave slot e).
+static Wave& engine_wave(orion_gpu_ctx* ctx, int e) { return e == 0 ? ctx->wave : ctx->xwave[e - 1]; }
+static cudaStream_t engine_stream(orion_gpu_ctx* ctx, int e) { return e == 0 ? ctx->stream : ctx->xstream[e - 1]; }
+
 // The captured loop launches the shading kernels of the classes in `mask`;
 // a graph that launches a superset is reused (an absent class's kernel
 // finds an empty queue), so the mask of a long-lived context only grows.
-static int build_batch_graph(orion_gpu_ctx* ctx, const BatchView& bv, int slots, unsigned mask) {
-  const void* key[4] = {ctx->wave.block.p, ctx->b_jobs.p, ctx->b_retire.p, ctx->b_ctl.p};
-  bool same = ctx->bexec && ctx->bgraph_slots == slots && std::memcmp(key, ctx->bgraph_key, sizeof(key)) == 0 &&
-              std::memcmp(&ctx->bgraph_cfg, &ctx->cfg, sizeof(LaunchConfig)) == 0 &&
-              (mask & ~ctx->bgraph_mask) == 0;
+static int build_batch_graph(orion_gpu_ctx* ctx, int e, const BatchView& bv, int slots, unsigned mask) {
+  BatchEngine& be = ctx->beng[e];
+  Wave& wave = engine_wave(ctx, e);
+  const void* key[4] = {wave.block.p, be.jobs.p, be.retire.p, be.ctl.p};
+  bool same = be.exec && be.slots == slots && std::memcmp(key, be.key, sizeof(key)) == 0 &&
+              std::memcmp(&be.cfg, &ctx->cfg, sizeof(LaunchConfig)) == 0 && (mask & ~be.mask) == 0;
   if (same) return ORION_OK;
-  if (ctx->bexec) mask |= ctx->bgraph_mask;
-  if (ctx->bexec) cudaGraphExecDestroy(ctx->bexec);
-  if (ctx->bgraph) cudaGraphDestroy(ctx->bgraph);
-  ctx->bexec = nullptr;
-  ctx->bgraph = nullptr;
-  CUDA_TRY(cudaGraphCreate(&ctx->bgraph, 0));
+  if (be.exec) mask |= be.mask;
+  be.drop_graph();
+  CUDA_TRY(cudaGraphCreate(&be.graph, 0));
   cudaGraphConditionalHandle cond;
-  CUDA_TRY(cudaGraphConditionalHandleCreate(&cond, ctx->bgraph, 1, cudaGraphCondAssignDefault));
+  CUDA_TRY(cudaGraphConditionalHandleCreate(&cond, be.graph, 1, cudaGraphCondAssignDefault));
   // cudaGraphNodeParams has no usable default constructor in host C++;
   // zeroed storage is its documented initial state.
   alignas(cudaGraphNodeParams) unsigned char np_storage[sizeof(cudaGraphNodeParams)] = {};
@@ -821,56 +838,52 @@ static int build_batch_graph(orion_gpu_ctx* ctx, const BatchView& bv, int slots,
   np.conditional.type = cudaGraphCondTypeWhile;
   np.conditional.size = 1;
   cudaGraphNode_t node;
-  CUDA_TRY(cudaGraphAddNode(&node, ctx->bgraph, nullptr, nullptr, 0, &np));
+  CUDA_TRY(cudaGraphAddNode(&node, be.graph, nullptr, nullptr, 0, &np));
   cudaGraph_t body = np.conditional.phGraph_out[0];
-  cudaError_t ce = capture_batch_iteration(ctx->wave.view, bv, ctx->sobol.as<uint32_t>(),
-                                           ctx->sobol_bitmajor.as<uint32_t>(), ctx->cfg, mask, cond, ctx->stream, body);
+  cudaError_t ce = capture_batch_iteration(wave.view, bv, ctx->sobol.as<uint32_t>(), ctx->sobol_bitmajor.as<uint32_t>(),
+                                           ctx->cfg, mask, cond, engine_stream(ctx, e), body);
   if (ce != cudaSuccess) {
     // A graph whose loop-body capture was invalidated is dropped, not
     // destroyed: nothing is assumed about its state after the failure.
-    ctx->bgraph = nullptr;
+    be.graph = nullptr;
     cudaGetLastError();
     return fail(ORION_ERR_CUDA, std::string("batch loop capture: ") + cudaGetErrorString(ce));
   }
-  CUDA_TRY(cudaGraphInstantiate(&ctx->bexec, ctx->bgraph, 0));
-  std::memcpy(ctx->bgraph_key, key, sizeof(key));
-  ctx->bgraph_cfg = ctx->cfg;
-  ctx->bgraph_slots = slots;
-  ctx->bgraph_mask = mask;
+  CUDA_TRY(cudaGraphInstantiate(&be.exec, be.graph, 0));
+  std::memcpy(be.key, key, sizeof(key));
+  be.cfg = ctx->cfg;
+  be.slots = slots;
+  be.mask = mask;
   return ORION_OK;
 }
 
-// One batch launch over `dj` (film pointers set; films zeroed or holding
-// earlier passes to add to, in stream order before this call). Caller holds
-// ctx->mu. On return `out` is the final control block, `ms` the device time.
-static int run_batch_locked(orion_gpu_ctx* ctx, std::vector<DevJob>& dj, unsigned long long total, int max_depth_all,
-                            BatchCtl* out_ctl, float* ms_out) {
-  const int njobs = (int)dj.size();
+// Buffers of engine e for `njobs` jobs and up to `slots` path slots.
+static int prepare_engine(orion_gpu_ctx* ctx, int e, int njobs, int slots, BatchView* bv, int* cap) {
+  BatchEngine& be = ctx->beng[e];
+  Wave& wave = engine_wave(ctx, e);
   int rc;
-  const int slots = (int)std::min<unsigned long long>((unsigned long long)ctx->default_batch_slots,
-                                                       std::max<unsigned long long>(total, 1024ULL));
-  if ((rc = ensure_wave(ctx, slots)) != ORION_OK) return rc;
-  const int cap = ctx->wave.capacity;
-  if (ctx->batch_slots_alloc < cap) {
-    if ((rc = ctx->b_retire.alloc((size_t)cap * 4)) != ORION_OK) return rc;
-    if ((rc = ctx->b_free.alloc((size_t)cap * 4)) != ORION_OK) return rc;
-    ctx->batch_slots_alloc = cap;
+  if ((rc = alloc_wave(wave, slots)) != ORION_OK) return rc;
+  *cap = wave.capacity;
+  if (be.slots_alloc < *cap) {
+    if ((rc = be.retire.alloc((size_t)*cap * 4)) != ORION_OK) return rc;
+    if ((rc = be.free_list.alloc((size_t)*cap * 4)) != ORION_OK) return rc;
+    be.slots_alloc = *cap;
   }
-  if (!ctx->b_ctl.p && (rc = ctx->b_ctl.alloc(sizeof(BatchCtl))) != ORION_OK) return rc;
-  if (ctx->jobs_alloc < njobs) {
-    int n = std::max(njobs, 64);
-    if ((rc = ctx->b_jobs.alloc((size_t)n * sizeof(DevJob))) != ORION_OK) return rc;
-    ctx->jobs_alloc = n;
+  if (!be.ctl.p && (rc = be.ctl.alloc(sizeof(BatchCtl))) != ORION_OK) return rc;
+  if (be.jobs_alloc < njobs) {
+    const int n = std::max(njobs, 64);
+    if ((rc = be.jobs.alloc((size_t)n * sizeof(DevJob))) != ORION_OK) return rc;
+    be.jobs_alloc = n;
   }
-  BatchView bv;
-  bv.jobs = ctx->b_jobs.as<DevJob>();
-  bv.ctl = ctx->b_ctl.as<BatchCtl>();
-  bv.q_retire = ctx->b_retire.as<int>();
-  bv.q_free = ctx->b_free.as<int>();
-  unsigned mask = 1u << SC_MISS;
-  for (const DevJob& J : dj) mask |= J.scene.class_mask;
-  if (!ctx->profiling && (rc = build_batch_graph(ctx, bv, cap, mask)) != ORION_OK) return rc;
+  bv->jobs = be.jobs.as<DevJob>();
+  bv->ctl = be.ctl.as<BatchCtl>();
+  bv->q_retire = be.retire.as<int>();
+  bv->q_free = be.free_list.as<int>();
+  return ORION_OK;
+}
 
+// Control block of a fresh batch of `total` work items on `cap` slots.
+static BatchCtl initial_ctl(unsigned long long total, int njobs, int cap, int max_depth_all) {
   BatchCtl c;
   std::memset(&c, 0, sizeof(c));
   c.total = total;
@@ -879,17 +892,74 @@ static int run_batch_locked(orion_gpu_ctx* ctx, std::vector<DevJob>& dj, unsigne
   // Every live path advances one bounce per iteration: a bound on the loop.
   const unsigned long long refills = (total + cap - 1) / cap + 1;
   c.max_iterations = (int)std::min<unsigned long long>(2ULL * refills * (max_depth_all + 2) + 64, 1u << 30);
+  return c;
+}
+
+// One batch over `dj` (film pointers set; films zeroed or holding earlier
+// passes to add to, in stream order on ctx->stream before this call).
+// Caller holds ctx->mu. With more than one job, the jobs are split into
+// groups of about equal path counts, one per engine, and the engines run
+// concurrently on their own streams (each group's paths fill the SMs the
+// other group's kernel tails leave idle). Profiled batches run on one
+// engine, driven from the host. On return `out` holds the engines' summed
+// counts (iterations: the most any engine ran), `ms` the device time.
+static int run_batch_locked(orion_gpu_ctx* ctx, std::vector<DevJob>& dj, unsigned long long total, int max_depth_all,
+                            BatchCtl* out_ctl, float* ms_out) {
+  const int njobs = (int)dj.size();
+  int rc;
+  const int ne = ctx->profiling ? 1 : std::min(std::min(ctx->wave_streams, (int)orion_gpu_ctx::kBatchEngines), njobs);
+  // Split by path count: largest jobs first, each to the lighter group.
+  std::vector<std::vector<DevJob>> group(ne);
+  std::vector<unsigned long long> gtotal(ne, 0);
+  std::vector<int> order(njobs);
+  for (int i = 0; i < njobs; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int a, int b) { return dj[a].num_paths > dj[b].num_paths; });
+  for (int i : order) {
+    int g = 0;
+    for (int k = 1; k < ne; ++k)
+      if (gtotal[k] < gtotal[g]) g = k;
+    DevJob J = dj[i];
+    J.work_begin = (long long)gtotal[g];
+    group[g].push_back(J);
+    gtotal[g] += (unsigned long long)J.num_paths;
+  }
+  int ng = 0;  // engines with work
+  for (int g = 0; g < ne; ++g) ng += gtotal[g] > 0 ? 1 : 0;
+  if (ng == 0) ng = 1;
+  std::vector<BatchView> bvs(ng);
+  std::vector<int> caps(ng);
+  std::vector<unsigned> masks(ng, 1u << SC_MISS);
+  for (int e = 0; e < ng; ++e) {
+    const int slots = (int)std::min<unsigned long long>((unsigned long long)ctx->default_batch_slots,
+                                                         std::max<unsigned long long>(gtotal[e], 1024ULL));
+    if ((rc = prepare_engine(ctx, e, (int)group[e].size(), slots, &bvs[e], &caps[e])) != ORION_OK) return rc;
+    for (const DevJob& J : group[e]) masks[e] |= J.scene.class_mask;
+    if (!ctx->profiling && (rc = build_batch_graph(ctx, e, bvs[e], caps[e], masks[e])) != ORION_OK) return rc;
+  }
   cudaStream_t s = ctx->stream;
-  CUDA_TRY(cudaMemcpyAsync(bv.jobs, dj.data(), njobs * sizeof(DevJob), cudaMemcpyHostToDevice, s));
-  CUDA_TRY(cudaMemcpyAsync(bv.ctl, &c, sizeof(c), cudaMemcpyHostToDevice, s));
-  launch_batch_init(ctx->wave.view, bv, cap, s);
-  CUDA_TRY(cudaGetLastError());
   std::memset(&ctx->stage_times, 0, sizeof(ctx->stage_times));
+  CUDA_TRY(cudaEventRecord(ctx->ev0, s));
+  if (ng > 1) {
+    CUDA_TRY(cudaEventRecord(ctx->ev_fork, s));
+    for (int e = 1; e < ng; ++e) CUDA_TRY(cudaStreamWaitEvent(engine_stream(ctx, e), ctx->ev_fork, 0));
+  }
+  std::vector<BatchCtl> init(ng);
+  for (int e = 0; e < ng; ++e) {
+    cudaStream_t es = engine_stream(ctx, e);
+    init[e] = initial_ctl(gtotal[e], (int)group[e].size(), caps[e], max_depth_all);
+    if (!group[e].empty())
+      CUDA_TRY(cudaMemcpyAsync(bvs[e].jobs, group[e].data(), group[e].size() * sizeof(DevJob),
+                               cudaMemcpyHostToDevice, es));
+    CUDA_TRY(cudaMemcpyAsync(bvs[e].ctl, &init[e], sizeof(BatchCtl), cudaMemcpyHostToDevice, es));
+    launch_batch_init(engine_wave(ctx, e).view, bvs[e], caps[e], es);
+    CUDA_TRY(cudaGetLastError());
+  }
   if (ctx->profiling) {
     // Profiling: the same iterations driven from the host, every stage timed
     // (one host round trip per iteration, so device_ms includes those gaps).
     const int per_iter = 8;
-    const int need = (int)std::min<int64_t>((int64_t)c.max_iterations * per_iter, 200000);
+    const int need = (int)std::min<int64_t>((int64_t)init[0].max_iterations * per_iter, 200000);
     while ((int)ctx->prof_events.size() < 2 * need) {
       cudaEvent_t e;
       CUDA_TRY(cudaEventCreate(&e));
@@ -897,13 +967,12 @@ static int run_batch_locked(orion_gpu_ctx* ctx, std::vector<DevJob>& dj, unsigne
     }
     ctx->prof_stage.resize(need);
     StageTimer timer{ctx->prof_events.data(), ctx->prof_stage.data(), need, 0};
-    CUDA_TRY(cudaEventRecord(ctx->ev0, s));
     int more = 1;
-    for (int it = 0; more && it < c.max_iterations; ++it) {
-      launch_batch_iteration(ctx->wave.view, bv, ctx->sobol.as<uint32_t>(), ctx->sobol_bitmajor.as<uint32_t>(),
-                             ctx->cfg, mask, s, &timer);
+    for (int it = 0; more && it < init[0].max_iterations; ++it) {
+      launch_batch_iteration(ctx->wave.view, bvs[0], ctx->sobol.as<uint32_t>(), ctx->sobol_bitmajor.as<uint32_t>(),
+                             ctx->cfg, masks[0], s, &timer);
       CUDA_TRY(cudaGetLastError());
-      CUDA_TRY(cudaMemcpyAsync(&more, &bv.ctl->more, sizeof(int), cudaMemcpyDeviceToHost, s));
+      CUDA_TRY(cudaMemcpyAsync(&more, &bvs[0].ctl->more, sizeof(int), cudaMemcpyDeviceToHost, s));
       CUDA_TRY(cudaStreamSynchronize(s));
     }
     CUDA_TRY(cudaEventRecord(ctx->ev1, s));
@@ -915,24 +984,43 @@ static int run_batch_locked(orion_gpu_ctx* ctx, std::vector<DevJob>& dj, unsigne
       ctx->stage_times.launches[timer.stage[i]] += 1;
     }
   } else {
-    CUDA_TRY(cudaEventRecord(ctx->ev0, s));
-    CUDA_TRY(cudaGraphLaunch(ctx->bexec, s));
+    for (int e = 0; e < ng; ++e) CUDA_TRY(cudaGraphLaunch(ctx->beng[e].exec, engine_stream(ctx, e)));
+    for (int e = 1; e < ng; ++e) {
+      CUDA_TRY(cudaEventRecord(ctx->ev_join[e - 1], engine_stream(ctx, e)));
+      CUDA_TRY(cudaStreamWaitEvent(s, ctx->ev_join[e - 1], 0));
+    }
     CUDA_TRY(cudaEventRecord(ctx->ev1, s));
   }
-  CUDA_TRY(cudaMemcpyAsync(out_ctl, bv.ctl, sizeof(BatchCtl), cudaMemcpyDeviceToHost, s));
+  std::vector<BatchCtl> outs(ng);
+  for (int e = 0; e < ng; ++e)
+    CUDA_TRY(cudaMemcpyAsync(&outs[e], bvs[e].ctl, sizeof(BatchCtl), cudaMemcpyDeviceToHost, s));
   CUDA_TRY(cudaStreamSynchronize(s));
   float ms = 0.f;
   CUDA_TRY(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
   *ms_out = ms;
-  const BatchCtl& out = *out_ctl;
+  BatchCtl& out = *out_ctl;
+  out = outs[0];
+  int64_t launches = 0;
+  bool error = false;
+  for (int e = 0; e < ng; ++e) {
+    const BatchCtl& o = outs[e];
+    if (e > 0) {
+      out.paths_done += o.paths_done;
+      for (int k = 0; k < 3; ++k) out.rays[k] += o.rays[k];
+      out.iterations = std::max(out.iterations, o.iterations);
+    }
+    error = error || o.error;
+    // Per iteration: plan, regen, 4 traces, one shade per class, resolve, retire, control; plus the init.
+    const unsigned launched = ctx->profiling ? masks[e] : ctx->beng[e].mask;
+    launches += (9LL + __builtin_popcount(launched)) * o.iterations + 1;
+  }
+  out.error = error ? 1 : 0;
   ctx->last.paths = (int64_t)out.paths_done;
   ctx->last.ext_rays = (int64_t)out.rays[0];
   ctx->last.shadow_rays = (int64_t)out.rays[1];
   ctx->last.mis_rays = (int64_t)out.rays[2];
   ctx->last.rays = (int64_t)(out.rays[0] + out.rays[1] + out.rays[2]);
-  // Per iteration: plan, regen, 4 traces, one shade per class, resolve, retire, control; plus the init.
-  const unsigned launched = ctx->profiling ? mask : ctx->bgraph_mask;
-  ctx->last.kernel_launches = (9LL + __builtin_popcount(launched)) * out.iterations + 1;
+  ctx->last.kernel_launches = launches;
   ctx->last.device_ms = ms;
   if (out.error) return fail(ORION_ERR_DEVICE, "batch loop reached its iteration cap");
   if (out.paths_done != total)
@@ -1271,56 +1359,62 @@ extern "C" int orion_gpu_autotune_batch(orion_gpu_ctx* ctx, int32_t njobs, const
   }
   CUDA_TRY(cudaMemsetAsync(films.p, 0, film_bytes, ctx->stream));
   LaunchConfig best = ctx->cfg;
-  int best_slots = ctx->default_batch_slots;
+  int best_slots = ctx->default_batch_slots, best_streams = ctx->wave_streams;
   double best_ms = 1e30, used = 0;
-  auto trial = [&](const LaunchConfig& c, int slots, double* ms) -> int {
+  auto trial = [&](const LaunchConfig& c, int slots, int streams, double* ms) -> int {
     LaunchConfig saved = ctx->cfg;
-    int saved_slots = ctx->default_batch_slots;
+    int saved_slots = ctx->default_batch_slots, saved_streams = ctx->wave_streams;
     ctx->cfg = c;
     ctx->default_batch_slots = slots;
+    ctx->wave_streams = streams;
     BatchCtl out;
     float fms = 0.f;
     int rc = run_batch_locked(ctx, dj, total, max_depth_all, &out, &fms);
     ctx->cfg = saved;
     ctx->default_batch_slots = saved_slots;
+    ctx->wave_streams = saved_streams;
     *ms = fms;
     used += fms;
     return rc;
   };
   double ms;
-  RC(trial(best, best_slots, &ms));  // warm-up (graph instantiation)
-  RC(trial(best, best_slots, &best_ms));
+  RC(trial(best, best_slots, best_streams, &ms));  // warm-up (graph instantiation)
+  RC(trial(best, best_slots, best_streams, &best_ms));
   const int trace_blocks[] = {64, 128, 256};
   const int stacks[] = {8, 16, 32};
   const int shade_blocks[] = {64, 128, 256};
   const int bpsm[] = {4, 8, 16};
   const int slot_counts[] = {1 << 22, 1 << 23, 1 << 24, 1 << 25};
   const int refills[] = {8, 16, 24, 32};
-  for (int knob = 0; knob < 6 && used < budget_ms; ++knob) {
-    const int n = knob >= 4 ? 4 : 3;
+  const int engine_counts[] = {1, 2};
+  for (int knob = 0; knob < 7 && used < budget_ms; ++knob) {
+    const int n = knob == 6 ? 2 : (knob >= 4 ? 4 : 3);
     for (int v = 0; v < n && used < budget_ms; ++v) {
       LaunchConfig c = best;
-      int slots = best_slots;
+      int slots = best_slots, streams = best_streams;
       if (knob == 0) c.trace_block = trace_blocks[v];
       if (knob == 1) c.smem_stack = stacks[v];
       if (knob == 2) c.shade_block = shade_blocks[v];
       if (knob == 3) c.blocks_per_sm = bpsm[v];
       if (knob == 4) slots = slot_counts[v];
       if (knob == 5) c.refill_below = refills[v];
-      if (std::memcmp(&c, &best, sizeof(c)) == 0 && slots == best_slots) continue;
+      if (knob == 6) streams = engine_counts[v];
+      if (std::memcmp(&c, &best, sizeof(c)) == 0 && slots == best_slots && streams == best_streams) continue;
       if (!config_problem(ctx, c).empty()) continue;
-      int rc = trial(c, slots, &ms);
+      int rc = trial(c, slots, streams, &ms);
       if (rc == ORION_ERR_NOMEM) continue;
       if (rc != ORION_OK) return rc;
       if (ms < best_ms) {
         best_ms = ms;
         best = c;
         best_slots = slots;
+        best_streams = streams;
       }
     }
   }
   ctx->cfg = best;
   ctx->default_batch_slots = best_slots;
+  ctx->wave_streams = best_streams;
   if (best_out) {
     best_out->trace_block = best.trace_block;
     best_out->shade_block = best.shade_block;
