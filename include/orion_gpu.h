@@ -294,11 +294,19 @@ typedef struct orion_launch_config {
   int32_t smem_stack;     /* traversal stack entries kept in shared memory: 0, 8, 16, 24 or 32 */
   int32_t blocks_per_sm;  /* grid size factor of the grid-stride kernels */
   int32_t wave_paths;     /* paths per plain-render wave */
-  int32_t batch_slots;    /* path slots of the batched pool */
+  int32_t batch_slots;    /* batches: path slots of the pool (pooled mode) or paths per wave (wave mode) */
   int32_t refill_below;   /* a traversal warp takes new rays once fewer lanes than this hold one (1..32) */
   int32_t streams;        /* plain renders: waves in flight at once, each on its own stream (1..4);
                              batches: concurrent pooled engines, min(streams, 2); 0 = keep */
 } orion_launch_config;
+
+/* How orion_gpu_render_batch (and the server) run a batch:
+ * ORION_BATCH_WAVES (default): the jobs' concatenated work list in waves of
+ *   batch_slots paths, each wave's paths bouncing until none is alive;
+ * ORION_BATCH_POOLED: a pool of batch_slots path slots refilled from the
+ *   work list every bounce. */
+enum { ORION_BATCH_POOLED = 0, ORION_BATCH_WAVES = 1 };
+int orion_gpu_set_batch_mode(orion_gpu_ctx* ctx, int32_t mode);
 
 int orion_gpu_get_config(orion_gpu_ctx* ctx, orion_launch_config* out);
 int orion_gpu_set_config(orion_gpu_ctx* ctx, const orion_launch_config* cfg);

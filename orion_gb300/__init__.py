@@ -31,6 +31,7 @@ ERRORS = {-1: "invalid", -2: "io", -3: "parse", -4: "cuda", -5: "nomem", -6: "un
 
 MAT_MATTE, MAT_METAL, MAT_MIRROR, MAT_GLASS, MAT_PLASTIC, MAT_UBER = range(6)
 INTEGRATOR_PATH, INTEGRATOR_SPPM = 0, 1
+BATCH_POOLED, BATCH_WAVES = 0, 1
 DIST_GGX, DIST_BECKMANN = 0, 1
 LIGHT_AREA, LIGHT_POINT, LIGHT_SPOT, LIGHT_DISTANT, LIGHT_ENV = range(5)
 NOALLOC_MAX_RAYS = 65536  # ORION_NOALLOC_MAX_RAYS
@@ -160,6 +161,7 @@ def library() -> C.CDLL:
             "orion_gpu_render": (i32, [vp, i32, C.POINTER(RenderParams), vp, vp]),
             "orion_gpu_render_fp64": (i32, [vp, i32, C.POINTER(RenderParams), vp, vp]),
             "orion_gpu_render_sppm": (i32, [vp, i32, C.POINTER(SppmParams), vp, vp]),
+            "orion_gpu_set_batch_mode": (i32, [vp, i32]),
             "orion_gpu_last_stats": (i32, [vp, C.POINTER(RenderStats)]),
             "orion_gpu_set_profiling": (i32, [vp, i32]),
             "orion_gpu_stage_times": (i32, [vp, C.POINTER(StageTimes)]),
@@ -411,6 +413,10 @@ class Context:
         _check(library().orion_gpu_autotune_batch(self._h, len(jobs), C.cast(arr, C.c_void_p), spp_cap, budget_ms,
                                                   C.byref(c), C.byref(mp)))
         return {k: getattr(c, k) for k, _ in LaunchConfig._fields_}, mp.value
+
+    def set_batch_mode(self, mode: int) -> None:
+        """BATCH_WAVES (default): batches run as waves over the jobs' work list; BATCH_POOLED: a refilled pool."""
+        _check(library().orion_gpu_set_batch_mode(self._h, mode))
 
     def get_config(self) -> dict:
         c = LaunchConfig()

@@ -181,6 +181,73 @@ __global__ void k_b_retire(WaveView w, BatchView b) {
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&c.paths_done, (unsigned long long)n);
 }
 
+// ------------------------------------------------------------ wave mode
+//
+// A batch can also run as waves over its concatenated work list: wave k
+// takes work items [base, base + n) onto slots 0..n-1 in order, its paths
+// bounce until none is alive (no refills), and the radiance of all n paths
+// goes to the jobs' films at the end, slot after slot, so neighbouring slots
+// add to neighbouring pixels of one job.
+
+// Resets the per-wave control fields (rays, paths and iterations stay
+// cumulative over the batch's waves).
+__global__ void k_b_wave_begin(BatchView b, int n, int iteration_cap) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  BatchCtl& c = *b.ctl;
+  c.cursor = c.total = c.take_base = 0ULL;
+  c.take = 0;
+  c.cur = 0;
+  for (int k = 0; k < kCounterSlots; ++k) c.counters[k] = 0;
+  c.counters[CNT_EXT0] = n;
+  c.max_iterations = c.iterations + iteration_cap;
+  c.more = 1;
+}
+
+__global__ void k_b_wave_camera(WaveView w, BatchView b, const uint32_t* sobol, unsigned long long base, int n) {
+  const int njobs = b.ctl->njobs;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const unsigned long long work = base + (unsigned long long)i;
+    const int job = job_of_work(b.jobs, njobs, work);
+    const DevJob& J = b.jobs[job];
+    const long long index = J.first_index + (long long)(work - (unsigned long long)J.work_begin);
+    const long long wh = (long long)J.width * J.height;
+    const long long pix = index % wh;
+    PathSampler smp{sobol, (uint64_t)index, 5u};
+    V3 o, d;
+    camera_ray(J.scene.cam, smp, (int)(pix % J.width), (int)(pix / J.width), &o, &d);
+    PathRec r;
+    r.o = f4(o, 0.f);
+    r.d = f4(d, 0.f);
+    r.beta = make_float4(1.f, 1.f, 1.f, 0.f);
+    r.L = make_float4(0.f, 0.f, 0.f, __uint_as_float((uint32_t)(unsigned long long)index));
+    r.hit = make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
+    r.meta = make_int4((int)smp.dim, job, 0, (int)((unsigned long long)index >> 32));
+    w.rec[i] = r;
+    w.q_ext[0][i] = i;
+  }
+}
+
+__global__ void k_b_wave_film(WaveView w, BatchView b, int n) {
+  for (int pid = blockIdx.x * blockDim.x + threadIdx.x; pid < n; pid += gridDim.x * blockDim.x) {
+    const float4 l = w.L[pid];
+    const int4 meta = w.rec[pid].meta;
+    const DevJob& J = b.jobs[meta.y];
+    const long long index =
+        (long long)(((unsigned long long)(unsigned)meta.w << 32) | (unsigned long long)__float_as_uint(l.w));
+    const long long pix = index % ((long long)J.width * J.height);
+    atomicAdd(&J.sum[3 * pix], (double)l.x);
+    atomicAdd(&J.sum[3 * pix + 1], (double)l.y);
+    atomicAdd(&J.sum[3 * pix + 2], (double)l.z);
+    if (J.sumsq) {
+      atomicAdd(&J.sumsq[3 * pix], (double)l.x * l.x);
+      atomicAdd(&J.sumsq[3 * pix + 1], (double)l.y * l.y);
+      atomicAdd(&J.sumsq[3 * pix + 2], (double)l.z * l.z);
+    }
+    if (J.count) atomicAdd(&J.count[pix], 1u);
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&b.ctl->paths_done, (unsigned long long)n);
+}
+
 // in_graph: sets the while-node's condition; otherwise leaves the decision in
 // ctl->more for a host-driven loop (profiling runs).
 __global__ void k_b_control(BatchView b, cudaGraphConditionalHandle cond, int in_graph) {
@@ -263,8 +330,8 @@ namespace {
 
 // One loop iteration's kernels on `stream`, optionally timed per stage.
 void enqueue_iteration(const WaveView& w, const BatchView& b, const uint32_t* sobol, const uint32_t* sobol_bitmajor,
-                       const LaunchConfig& cfg, unsigned class_mask, cudaGraphConditionalHandle cond, int in_graph,
-                       cudaStream_t stream, StageTimer* timer) {
+                       const LaunchConfig& cfg, unsigned class_mask, bool waves, cudaGraphConditionalHandle cond,
+                       int in_graph, cudaStream_t stream, StageTimer* timer) {
   const int cap = w.capacity;
   const int persistent = cfg.num_sms * cfg.blocks_per_sm;
   const int tgrid = grid_cap(cap, cfg.trace_block, persistent * 2);
@@ -276,8 +343,8 @@ void enqueue_iteration(const WaveView& w, const BatchView& b, const uint32_t* so
     if (timer) timer->end(stream);
   };
   begin(ST_CAMERA);
-  k_b_plan<<<1, 32, 0, stream>>>(b);
-  k_b_regen<<<grid_cap(cap, 256, persistent * 4), 256, 0, stream>>>(w, b, sobol);
+  k_b_plan<<<1, 32, 0, stream>>>(b);  // wave mode: counters reset, nothing to take
+  if (!waves) k_b_regen<<<grid_cap(cap, 256, persistent * 4), 256, 0, stream>>>(w, b, sobol);
   end();
   begin(ST_TRACE_EXT);
   b_trace(cfg, w, b, 0, tgrid, stream);
@@ -307,9 +374,11 @@ void enqueue_iteration(const WaveView& w, const BatchView& b, const uint32_t* so
   begin(ST_RESOLVE);
   k_b_resolve<<<sgrid, cfg.shade_block, 0, stream>>>(w, b);
   end();
-  begin(ST_FILM);
-  k_b_retire<<<sgrid, cfg.shade_block, 0, stream>>>(w, b);
-  end();
+  if (!waves) {  // wave mode: the film is written once the wave is done
+    begin(ST_FILM);
+    k_b_retire<<<sgrid, cfg.shade_block, 0, stream>>>(w, b);
+    end();
+  }
   begin(ST_OTHER);
   k_b_control<<<1, 32, 0, stream>>>(b, cond, in_graph);
   end();
@@ -319,10 +388,11 @@ void enqueue_iteration(const WaveView& w, const BatchView& b, const uint32_t* so
 
 cudaError_t capture_batch_iteration(const WaveView& w, const BatchView& b, const uint32_t* sobol,
                                     const uint32_t* sobol_bitmajor, const LaunchConfig& cfg, unsigned class_mask,
-                                    cudaGraphConditionalHandle cond, cudaStream_t stream, cudaGraph_t body) {
+                                    bool waves, cudaGraphConditionalHandle cond, cudaStream_t stream,
+                                    cudaGraph_t body) {
   cudaError_t e = cudaStreamBeginCaptureToGraph(stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
   if (e != cudaSuccess) return e;
-  enqueue_iteration(w, b, sobol, sobol_bitmajor, cfg, class_mask, cond, 1, stream, nullptr);
+  enqueue_iteration(w, b, sobol, sobol_bitmajor, cfg, class_mask, waves, cond, 1, stream, nullptr);
   cudaGraph_t out = body;
   cudaError_t e2 = cudaStreamEndCapture(stream, &out);
   cudaError_t e3 = cudaGetLastError();
@@ -330,9 +400,20 @@ cudaError_t capture_batch_iteration(const WaveView& w, const BatchView& b, const
 }
 
 void launch_batch_iteration(const WaveView& w, const BatchView& b, const uint32_t* sobol,
-                            const uint32_t* sobol_bitmajor, const LaunchConfig& cfg, unsigned class_mask,
+                            const uint32_t* sobol_bitmajor, const LaunchConfig& cfg, unsigned class_mask, bool waves,
                             cudaStream_t stream, StageTimer* timer) {
-  enqueue_iteration(w, b, sobol, sobol_bitmajor, cfg, class_mask, cudaGraphConditionalHandle{}, 0, stream, timer);
+  enqueue_iteration(w, b, sobol, sobol_bitmajor, cfg, class_mask, waves, cudaGraphConditionalHandle{}, 0, stream,
+                    timer);
+}
+
+void launch_batch_wave_begin(const WaveView& w, const BatchView& b, const uint32_t* sobol, unsigned long long base,
+                             int n, int iteration_cap, int num_sms, cudaStream_t stream) {
+  k_b_wave_begin<<<1, 32, 0, stream>>>(b, n, iteration_cap);
+  k_b_wave_camera<<<grid_cap(n, 256, num_sms * 32), 256, 0, stream>>>(w, b, sobol, base, n);
+}
+
+void launch_batch_wave_film(const WaveView& w, const BatchView& b, int n, int num_sms, cudaStream_t stream) {
+  k_b_wave_film<<<grid_cap(n, 256, num_sms * 32), 256, 0, stream>>>(w, b, n);
 }
 
 }  // namespace orion_gb300

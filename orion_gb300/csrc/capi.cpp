@@ -120,20 +120,28 @@ constexpr int kMaxWaveStreams = 4;  // plain-render waves in flight at once
 
 // One pooled batch engine: its free and retire lists, control block, job
 // table and captured device-side loop (the path slots are a Wave).
-struct BatchEngine {
-  DevBuf retire, free_list, ctl, jobs;
-  int slots_alloc = 0, jobs_alloc = 0;
+// A captured device-side loop of one batch mode (pooled or waves).
+struct BatchGraph {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   const void* key[4] = {nullptr, nullptr, nullptr, nullptr};  // buffers the graph was captured with
   LaunchConfig cfg{};
   int slots = 0;
   unsigned mask = 0;  // shading classes the captured loop launches
-  void drop_graph() {
+  void drop() {
     if (exec) cudaGraphExecDestroy(exec);
     if (graph) cudaGraphDestroy(graph);
     exec = nullptr;
     graph = nullptr;
+  }
+};
+
+struct BatchEngine {
+  DevBuf retire, free_list, ctl, jobs;
+  int slots_alloc = 0, jobs_alloc = 0;
+  BatchGraph loop[2];  // [ORION_BATCH_POOLED], [ORION_BATCH_WAVES]
+  void drop_graph() {
+    for (BatchGraph& g : loop) g.drop();
   }
 };
 
@@ -176,13 +184,14 @@ struct orion_gpu_ctx {
   std::vector<int> prof_stage;
   orion_stage_times stage_times{};
   // batched mode
-  int default_batch_slots = 1 << 23;
+  int default_batch_slots = 1 << 24;  // pooled: path slots; waves: paths per wave
   DevBuf b_films;
   // Pooled batch engines: a batch's jobs are split between as many as the
   // `streams` knob allows (at most kBatchEngines) and they run concurrently,
   // engine e on the wave state and stream of wave slot e.
   static constexpr int kBatchEngines = 2;
   BatchEngine beng[kBatchEngines];
+  int batch_mode = ORION_BATCH_WAVES;
   // SPPM: per-pixel state in one block, the grid's cell lists apart
   DevBuf sppm_block, sppm_hits;
   DevBuf preview;  // 8-bit previews of server films
@@ -817,15 +826,16 @@ static cudaStream_t engine_stream(orion_gpu_ctx* ctx, int e) { return e == 0 ? c
 // The captured loop launches the shading kernels of the classes in `mask`;
 // a graph that launches a superset is reused (an absent class's kernel
 // finds an empty queue), so the mask of a long-lived context only grows.
-static int build_batch_graph(orion_gpu_ctx* ctx, int e, const BatchView& bv, int slots, unsigned mask) {
-  BatchEngine& be = ctx->beng[e];
+static int build_batch_graph(orion_gpu_ctx* ctx, int e, int mode, const BatchView& bv, int slots, unsigned mask) {
+  BatchEngine& eng = ctx->beng[e];
+  BatchGraph& be = eng.loop[mode];
   Wave& wave = engine_wave(ctx, e);
-  const void* key[4] = {wave.block.p, be.jobs.p, be.retire.p, be.ctl.p};
+  const void* key[4] = {wave.block.p, eng.jobs.p, eng.retire.p, eng.ctl.p};
   bool same = be.exec && be.slots == slots && std::memcmp(key, be.key, sizeof(key)) == 0 &&
               std::memcmp(&be.cfg, &ctx->cfg, sizeof(LaunchConfig)) == 0 && (mask & ~be.mask) == 0;
   if (same) return ORION_OK;
   if (be.exec) mask |= be.mask;
-  be.drop_graph();
+  be.drop();
   CUDA_TRY(cudaGraphCreate(&be.graph, 0));
   cudaGraphConditionalHandle cond;
   CUDA_TRY(cudaGraphConditionalHandleCreate(&cond, be.graph, 1, cudaGraphCondAssignDefault));
@@ -841,7 +851,7 @@ static int build_batch_graph(orion_gpu_ctx* ctx, int e, const BatchView& bv, int
   CUDA_TRY(cudaGraphAddNode(&node, be.graph, nullptr, nullptr, 0, &np));
   cudaGraph_t body = np.conditional.phGraph_out[0];
   cudaError_t ce = capture_batch_iteration(wave.view, bv, ctx->sobol.as<uint32_t>(), ctx->sobol_bitmajor.as<uint32_t>(),
-                                           ctx->cfg, mask, cond, engine_stream(ctx, e), body);
+                                           ctx->cfg, mask, mode == ORION_BATCH_WAVES, cond, engine_stream(ctx, e), body);
   if (ce != cudaSuccess) {
     // A graph whose loop-body capture was invalidated is dropped, not
     // destroyed: nothing is assumed about its state after the failure.
@@ -903,8 +913,8 @@ static BatchCtl initial_ctl(unsigned long long total, int njobs, int cap, int ma
 // other group's kernel tails leave idle). Profiled batches run on one
 // engine, driven from the host. On return `out` holds the engines' summed
 // counts (iterations: the most any engine ran), `ms` the device time.
-static int run_batch_locked(orion_gpu_ctx* ctx, std::vector<DevJob>& dj, unsigned long long total, int max_depth_all,
-                            BatchCtl* out_ctl, float* ms_out) {
+static int run_batch_pooled_locked(orion_gpu_ctx* ctx, std::vector<DevJob>& dj, unsigned long long total,
+                                   int max_depth_all, BatchCtl* out_ctl, float* ms_out) {
   const int njobs = (int)dj.size();
   int rc;
   const int ne = ctx->profiling ? 1 : std::min(std::min(ctx->wave_streams, (int)orion_gpu_ctx::kBatchEngines), njobs);
@@ -935,7 +945,8 @@ static int run_batch_locked(orion_gpu_ctx* ctx, std::vector<DevJob>& dj, unsigne
                                                          std::max<unsigned long long>(gtotal[e], 1024ULL));
     if ((rc = prepare_engine(ctx, e, (int)group[e].size(), slots, &bvs[e], &caps[e])) != ORION_OK) return rc;
     for (const DevJob& J : group[e]) masks[e] |= J.scene.class_mask;
-    if (!ctx->profiling && (rc = build_batch_graph(ctx, e, bvs[e], caps[e], masks[e])) != ORION_OK) return rc;
+    if (!ctx->profiling && (rc = build_batch_graph(ctx, e, ORION_BATCH_POOLED, bvs[e], caps[e], masks[e])) != ORION_OK)
+      return rc;
   }
   cudaStream_t s = ctx->stream;
   std::memset(&ctx->stage_times, 0, sizeof(ctx->stage_times));
@@ -970,7 +981,7 @@ static int run_batch_locked(orion_gpu_ctx* ctx, std::vector<DevJob>& dj, unsigne
     int more = 1;
     for (int it = 0; more && it < init[0].max_iterations; ++it) {
       launch_batch_iteration(ctx->wave.view, bvs[0], ctx->sobol.as<uint32_t>(), ctx->sobol_bitmajor.as<uint32_t>(),
-                             ctx->cfg, masks[0], s, &timer);
+                             ctx->cfg, masks[0], false, s, &timer);
       CUDA_TRY(cudaGetLastError());
       CUDA_TRY(cudaMemcpyAsync(&more, &bvs[0].ctl->more, sizeof(int), cudaMemcpyDeviceToHost, s));
       CUDA_TRY(cudaStreamSynchronize(s));
@@ -984,7 +995,8 @@ static int run_batch_locked(orion_gpu_ctx* ctx, std::vector<DevJob>& dj, unsigne
       ctx->stage_times.launches[timer.stage[i]] += 1;
     }
   } else {
-    for (int e = 0; e < ng; ++e) CUDA_TRY(cudaGraphLaunch(ctx->beng[e].exec, engine_stream(ctx, e)));
+    for (int e = 0; e < ng; ++e)
+      CUDA_TRY(cudaGraphLaunch(ctx->beng[e].loop[ORION_BATCH_POOLED].exec, engine_stream(ctx, e)));
     for (int e = 1; e < ng; ++e) {
       CUDA_TRY(cudaEventRecord(ctx->ev_join[e - 1], engine_stream(ctx, e)));
       CUDA_TRY(cudaStreamWaitEvent(s, ctx->ev_join[e - 1], 0));
@@ -1011,7 +1023,7 @@ static int run_batch_locked(orion_gpu_ctx* ctx, std::vector<DevJob>& dj, unsigne
     }
     error = error || o.error;
     // Per iteration: plan, regen, 4 traces, one shade per class, resolve, retire, control; plus the init.
-    const unsigned launched = ctx->profiling ? masks[e] : ctx->beng[e].mask;
+    const unsigned launched = ctx->profiling ? masks[e] : ctx->beng[e].loop[ORION_BATCH_POOLED].mask;
     launches += (9LL + __builtin_popcount(launched)) * o.iterations + 1;
   }
   out.error = error ? 1 : 0;
@@ -1027,6 +1039,135 @@ static int run_batch_locked(orion_gpu_ctx* ctx, std::vector<DevJob>& dj, unsigne
     return fail(ORION_ERR_DEVICE, "batch finished " + std::to_string(out.paths_done) + " of " + std::to_string(total) +
                                       " paths");
   return ORION_OK;
+}
+
+// Wave mode: the concatenated work list in waves of up to `wave_paths`
+// paths, consecutive waves on the engines in turn (concurrently, one stream
+// each). Films take FP64 atomics, so waves may finish in any order.
+static int run_batch_waves_locked(orion_gpu_ctx* ctx, std::vector<DevJob>& dj, unsigned long long total,
+                                  int max_depth_all, BatchCtl* out_ctl, float* ms_out) {
+  const int njobs = (int)dj.size();
+  int rc;
+  const int64_t wave = std::max<int64_t>(1024, std::min<int64_t>(ctx->default_batch_slots, (int64_t)total));
+  const int64_t nwaves = std::max<int64_t>(1, ((int64_t)total + wave - 1) / wave);
+  const int ne = ctx->profiling ? 1 : (int)std::min<int64_t>(std::min(ctx->wave_streams, (int)orion_gpu_ctx::kBatchEngines),
+                                                            nwaves);
+  std::vector<BatchView> bvs(ne);
+  std::vector<int> caps(ne);
+  unsigned mask = 1u << SC_MISS;
+  for (const DevJob& J : dj) mask |= J.scene.class_mask;
+  for (int e = 0; e < ne; ++e) {
+    if ((rc = prepare_engine(ctx, e, njobs, (int)wave, &bvs[e], &caps[e])) != ORION_OK) return rc;
+    if (!ctx->profiling && (rc = build_batch_graph(ctx, e, ORION_BATCH_WAVES, bvs[e], caps[e], mask)) != ORION_OK)
+      return rc;
+  }
+  cudaStream_t s = ctx->stream;
+  std::memset(&ctx->stage_times, 0, sizeof(ctx->stage_times));
+  CUDA_TRY(cudaEventRecord(ctx->ev0, s));
+  if (ne > 1) {
+    CUDA_TRY(cudaEventRecord(ctx->ev_fork, s));
+    for (int e = 1; e < ne; ++e) CUDA_TRY(cudaStreamWaitEvent(engine_stream(ctx, e), ctx->ev_fork, 0));
+  }
+  BatchCtl zero;
+  std::memset(&zero, 0, sizeof(zero));
+  zero.njobs = njobs;
+  for (int e = 0; e < ne; ++e) {
+    cudaStream_t es = engine_stream(ctx, e);
+    CUDA_TRY(cudaMemcpyAsync(bvs[e].jobs, dj.data(), (size_t)njobs * sizeof(DevJob), cudaMemcpyHostToDevice, es));
+    CUDA_TRY(cudaMemcpyAsync(bvs[e].ctl, &zero, sizeof(BatchCtl), cudaMemcpyHostToDevice, es));
+  }
+  const int iteration_cap = 2 * (max_depth_all + 2) + 8;  // every live path advances one bounce per iteration
+  StageTimer timer{nullptr, nullptr, 0, 0};
+  if (ctx->profiling) {
+    const int need = (int)std::min<int64_t>(nwaves * iteration_cap * 8, 200000);
+    while ((int)ctx->prof_events.size() < 2 * need) {
+      cudaEvent_t e;
+      CUDA_TRY(cudaEventCreate(&e));
+      ctx->prof_events.push_back(e);
+    }
+    ctx->prof_stage.resize(need);
+    timer = StageTimer{ctx->prof_events.data(), ctx->prof_stage.data(), need, 0};
+  }
+  for (int64_t k = 0; k < nwaves; ++k) {
+    const int e = (int)(k % ne);
+    cudaStream_t es = engine_stream(ctx, e);
+    const WaveView& wv = engine_wave(ctx, e).view;
+    const unsigned long long base = (unsigned long long)(k * wave);
+    const int n = (int)std::min<unsigned long long>((unsigned long long)wave, total - base);
+    if (ctx->profiling) timer.begin(ST_CAMERA, es);
+    launch_batch_wave_begin(wv, bvs[e], ctx->sobol.as<uint32_t>(), base, n, iteration_cap, ctx->num_sms, es);
+    if (ctx->profiling) timer.end(es);
+    if (ctx->profiling) {
+      int more = 1;
+      for (int it = 0; more && it < iteration_cap; ++it) {
+        launch_batch_iteration(wv, bvs[e], ctx->sobol.as<uint32_t>(), ctx->sobol_bitmajor.as<uint32_t>(), ctx->cfg,
+                               mask, true, es, &timer);
+        CUDA_TRY(cudaGetLastError());
+        CUDA_TRY(cudaMemcpyAsync(&more, &bvs[e].ctl->more, sizeof(int), cudaMemcpyDeviceToHost, es));
+        CUDA_TRY(cudaStreamSynchronize(es));
+      }
+    } else {
+      CUDA_TRY(cudaGraphLaunch(ctx->beng[e].loop[ORION_BATCH_WAVES].exec, es));
+    }
+    if (ctx->profiling) timer.begin(ST_FILM, es);
+    launch_batch_wave_film(wv, bvs[e], n, ctx->num_sms, es);
+    if (ctx->profiling) timer.end(es);
+    CUDA_TRY(cudaGetLastError());
+  }
+  for (int e = 1; e < ne; ++e) {
+    CUDA_TRY(cudaEventRecord(ctx->ev_join[e - 1], engine_stream(ctx, e)));
+    CUDA_TRY(cudaStreamWaitEvent(s, ctx->ev_join[e - 1], 0));
+  }
+  CUDA_TRY(cudaEventRecord(ctx->ev1, s));
+  std::vector<BatchCtl> outs(ne);
+  for (int e = 0; e < ne; ++e)
+    CUDA_TRY(cudaMemcpyAsync(&outs[e], bvs[e].ctl, sizeof(BatchCtl), cudaMemcpyDeviceToHost, s));
+  CUDA_TRY(cudaStreamSynchronize(s));
+  float ms = 0.f;
+  CUDA_TRY(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+  *ms_out = ms;
+  for (int i = 0; i < std::min(timer.used, timer.capacity); ++i) {
+    float e = 0.f;
+    CUDA_TRY(cudaEventElapsedTime(&e, timer.events[2 * i], timer.events[2 * i + 1]));
+    ctx->stage_times.ms[timer.stage[i]] += e;
+    ctx->stage_times.launches[timer.stage[i]] += 1;
+  }
+  BatchCtl& out = *out_ctl;
+  out = outs[0];
+  int64_t launches = 0;
+  bool error = false;
+  for (int e = 0; e < ne; ++e) {
+    const BatchCtl& o = outs[e];
+    if (e > 0) {
+      out.paths_done += o.paths_done;
+      for (int j = 0; j < 3; ++j) out.rays[j] += o.rays[j];
+      out.iterations += o.iterations;
+    }
+    error = error || o.error;
+    // Per iteration: plan, 4 traces, one shade per class, resolve, control.
+    const unsigned launched = ctx->profiling ? mask : ctx->beng[e].loop[ORION_BATCH_WAVES].mask;
+    launches += (7LL + __builtin_popcount(launched)) * o.iterations;
+  }
+  launches += 3 * nwaves;  // begin, camera, film per wave
+  out.error = error ? 1 : 0;
+  ctx->last.paths = (int64_t)out.paths_done;
+  ctx->last.ext_rays = (int64_t)out.rays[0];
+  ctx->last.shadow_rays = (int64_t)out.rays[1];
+  ctx->last.mis_rays = (int64_t)out.rays[2];
+  ctx->last.rays = (int64_t)(out.rays[0] + out.rays[1] + out.rays[2]);
+  ctx->last.kernel_launches = launches;
+  ctx->last.device_ms = ms;
+  if (out.error) return fail(ORION_ERR_DEVICE, "batch loop reached its iteration cap");
+  if (out.paths_done != total)
+    return fail(ORION_ERR_DEVICE, "batch finished " + std::to_string(out.paths_done) + " of " + std::to_string(total) +
+                                      " paths");
+  return ORION_OK;
+}
+
+static int run_batch_locked(orion_gpu_ctx* ctx, std::vector<DevJob>& dj, unsigned long long total, int max_depth_all,
+                            BatchCtl* out_ctl, float* ms_out) {
+  return ctx->batch_mode == ORION_BATCH_WAVES ? run_batch_waves_locked(ctx, dj, total, max_depth_all, out_ctl, ms_out)
+                                              : run_batch_pooled_locked(ctx, dj, total, max_depth_all, out_ctl, ms_out);
 }
 
 // Job table and film layout of a batch (films packed into one device block).
@@ -1214,6 +1355,14 @@ int ctx_run_device_jobs(orion_gpu_ctx* ctx, const DeviceFilmJob* jobs, int njobs
 
 // ---------------------------------------------------- launch config, tuning
 
+extern "C" int orion_gpu_set_batch_mode(orion_gpu_ctx* ctx, int32_t mode) {
+  if (!ctx) return fail(ORION_ERR_INVALID, "null context");
+  if (mode != ORION_BATCH_POOLED && mode != ORION_BATCH_WAVES) return fail(ORION_ERR_INVALID, "unknown batch mode");
+  std::lock_guard<std::mutex> g(ctx->mu);
+  ctx->batch_mode = mode;
+  return ORION_OK;
+}
+
 extern "C" int orion_gpu_get_config(orion_gpu_ctx* ctx, orion_launch_config* out) {
   if (!ctx || !out) return fail(ORION_ERR_INVALID, "null argument");
   out->trace_block = ctx->cfg.trace_block;
@@ -1358,28 +1507,33 @@ extern "C" int orion_gpu_autotune_batch(orion_gpu_ctx* ctx, int32_t njobs, const
     dj[i].count = reinterpret_cast<unsigned int*>(dj[i].sumsq + 3 * wh);
   }
   CUDA_TRY(cudaMemsetAsync(films.p, 0, film_bytes, ctx->stream));
+  // batch_slots is the pool size (pooled mode) or the wave size (wave mode).
   LaunchConfig best = ctx->cfg;
-  int best_slots = ctx->default_batch_slots, best_streams = ctx->wave_streams;
+  int best_slots = ctx->default_batch_slots;
+  int best_streams = ctx->wave_streams, best_mode = ctx->batch_mode;
   double best_ms = 1e30, used = 0;
-  auto trial = [&](const LaunchConfig& c, int slots, int streams, double* ms) -> int {
+  auto trial = [&](const LaunchConfig& c, int slots, int streams, int mode, double* ms) -> int {
     LaunchConfig saved = ctx->cfg;
     int saved_slots = ctx->default_batch_slots, saved_streams = ctx->wave_streams;
+    int saved_mode = ctx->batch_mode;
     ctx->cfg = c;
     ctx->default_batch_slots = slots;
     ctx->wave_streams = streams;
+    ctx->batch_mode = mode;
     BatchCtl out;
     float fms = 0.f;
     int rc = run_batch_locked(ctx, dj, total, max_depth_all, &out, &fms);
     ctx->cfg = saved;
     ctx->default_batch_slots = saved_slots;
     ctx->wave_streams = saved_streams;
+    ctx->batch_mode = saved_mode;
     *ms = fms;
     used += fms;
     return rc;
   };
   double ms;
-  RC(trial(best, best_slots, best_streams, &ms));  // warm-up (graph instantiation)
-  RC(trial(best, best_slots, best_streams, &best_ms));
+  RC(trial(best, best_slots, best_streams, best_mode, &ms));  // warm-up (graph instantiation)
+  RC(trial(best, best_slots, best_streams, best_mode, &best_ms));
   const int trace_blocks[] = {64, 128, 256};
   const int stacks[] = {8, 16, 32};
   const int shade_blocks[] = {64, 128, 256};
@@ -1387,11 +1541,12 @@ extern "C" int orion_gpu_autotune_batch(orion_gpu_ctx* ctx, int32_t njobs, const
   const int slot_counts[] = {1 << 22, 1 << 23, 1 << 24, 1 << 25};
   const int refills[] = {8, 16, 24, 32};
   const int engine_counts[] = {1, 2};
-  for (int knob = 0; knob < 7 && used < budget_ms; ++knob) {
-    const int n = knob == 6 ? 2 : (knob >= 4 ? 4 : 3);
+  const int modes[] = {ORION_BATCH_POOLED, ORION_BATCH_WAVES};
+  for (int knob = 0; knob < 8 && used < budget_ms; ++knob) {
+    const int n = knob >= 6 ? 2 : (knob >= 4 ? 4 : 3);
     for (int v = 0; v < n && used < budget_ms; ++v) {
       LaunchConfig c = best;
-      int slots = best_slots, streams = best_streams;
+      int slots = best_slots, streams = best_streams, mode = best_mode;
       if (knob == 0) c.trace_block = trace_blocks[v];
       if (knob == 1) c.smem_stack = stacks[v];
       if (knob == 2) c.shade_block = shade_blocks[v];
@@ -1399,9 +1554,12 @@ extern "C" int orion_gpu_autotune_batch(orion_gpu_ctx* ctx, int32_t njobs, const
       if (knob == 4) slots = slot_counts[v];
       if (knob == 5) c.refill_below = refills[v];
       if (knob == 6) streams = engine_counts[v];
-      if (std::memcmp(&c, &best, sizeof(c)) == 0 && slots == best_slots && streams == best_streams) continue;
+      if (knob == 7) mode = modes[v];
+      if (std::memcmp(&c, &best, sizeof(c)) == 0 && slots == best_slots && streams == best_streams &&
+          mode == best_mode)
+        continue;
       if (!config_problem(ctx, c).empty()) continue;
-      int rc = trial(c, slots, streams, &ms);
+      int rc = trial(c, slots, streams, mode, &ms);
       if (rc == ORION_ERR_NOMEM) continue;
       if (rc != ORION_OK) return rc;
       if (ms < best_ms) {
@@ -1409,12 +1567,14 @@ extern "C" int orion_gpu_autotune_batch(orion_gpu_ctx* ctx, int32_t njobs, const
         best = c;
         best_slots = slots;
         best_streams = streams;
+        best_mode = mode;
       }
     }
   }
   ctx->cfg = best;
   ctx->default_batch_slots = best_slots;
   ctx->wave_streams = best_streams;
+  ctx->batch_mode = best_mode;
   if (best_out) {
     best_out->trace_block = best.trace_block;
     best_out->shade_block = best.shade_block;

@@ -220,14 +220,22 @@ cudaError_t configure_batch_kernels(int smem_bytes, KernelLimits* lim);
 // into `body` by stream capture on `stream`. The loop keeps running while
 // work or live paths remain; `cond` is the graph's while-condition handle.
 // Shading kernels are launched for the classes in `class_mask` only.
+// waves: the iteration of wave mode (no refills, no per-iteration film).
 cudaError_t capture_batch_iteration(const WaveView& w, const BatchView& b, const uint32_t* sobol,
                                     const uint32_t* sobol_bitmajor, const LaunchConfig& cfg, unsigned class_mask,
-                                    cudaGraphConditionalHandle cond, cudaStream_t stream, cudaGraph_t body);
+                                    bool waves, cudaGraphConditionalHandle cond, cudaStream_t stream,
+                                    cudaGraph_t body);
 // The same iteration launched directly (a host-driven loop reading ctl->more),
 // each stage timed by `timer`: the profiling path of the batched engine.
 void launch_batch_iteration(const WaveView& w, const BatchView& b, const uint32_t* sobol,
-                            const uint32_t* sobol_bitmajor, const LaunchConfig& cfg, unsigned class_mask,
+                            const uint32_t* sobol_bitmajor, const LaunchConfig& cfg, unsigned class_mask, bool waves,
                             cudaStream_t stream, StageTimer* timer);
+// Wave mode: starts a wave of work items [base, base + n) on slots 0..n-1
+// (at most `iteration_cap` more loop iterations), and after its loop adds
+// the n paths' radiance to their jobs' films.
+void launch_batch_wave_begin(const WaveView& w, const BatchView& b, const uint32_t* sobol, unsigned long long base,
+                             int n, int iteration_cap, int num_sms, cudaStream_t stream);
+void launch_batch_wave_film(const WaveView& w, const BatchView& b, int n, int num_sms, cudaStream_t stream);
 // Resets the batch control block and the free-slot list for `capacity` slots.
 void launch_batch_init(const WaveView& w, const BatchView& b, int capacity, cudaStream_t stream);
 
