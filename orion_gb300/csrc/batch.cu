@@ -1,23 +1,25 @@
-// Batched wavefront path tracing: many render jobs in one graph launch.
+// Batched wavefront path tracing: many render jobs per device-side loop.
 //
-// The jobs' sample ranges are concatenated into one work list. A pool of
-// path slots is shared by all jobs; one iteration of the device-side loop
+// The jobs' sample ranges are concatenated into one work list. One
+// iteration of the device-side loop
 //
 //   k_b_plan     take = min(free slots, work left); reset this iteration's queues
-//   k_b_regen    start `take` new camera paths in free slots (Pinhole::generateRay)
+//   k_b_regen    pooled mode: start `take` new camera paths in free slots
 //   k_b_trace    closest hit for every live path (each against its job's scene)
 //   k_b_shade    one bounce of PathTracing::Li per path (shared shade_one)
 //   k_b_trace    shadow rays (any hit) and MIS rays (closest hit)
 //   k_b_resolve  direct-light estimate into the path radiance
-//   k_b_retire   finished paths: radiance into the job's FP64 film, slot freed
+//   k_b_retire   pooled mode: finished paths' radiance into the job's FP64
+//                film, slot freed
 //   k_b_control  flip queues; keep looping while work or live paths remain
 //
-// runs inside a CUDA graph while-node, so the whole batch is a single
-// cudaGraphLaunch. Paths of different jobs, depths and bounces share every
-// launch; finished slots are refilled each iteration, so the trace kernels
-// see a full pool until the work list runs dry. Each path's arithmetic is
-// exactly the plain path's; only the film's order of accumulation differs
-// (FP64 atomics, so the per-pixel sums agree to FP64 rounding).
+// runs inside a CUDA graph while-node. Pooled mode shares one pool of path
+// slots among all jobs and refills finished slots every iteration. Wave mode
+// starts a wave of contiguous work items on slots 0..n-1
+// (k_b_wave_begin / k_b_wave_camera), loops until none is alive and writes
+// the film once (k_b_wave_film). Paths of different jobs, depths and bounces
+// share every launch. Each path runs the plain path's device functions on
+// the same samples; the film's order of accumulation differs (FP64 atomics).
 #include <cuda_runtime.h>
 
 #include "kernels.h"
