@@ -384,7 +384,7 @@ extern "C" int orion_gpu_create(const orion_gpu_opts* opts, orion_gpu_ctx** out)
   c->cfg.smem_stack = 16;
   c->cfg.refill_below = 20;
   c->smem_limit = (int)prop.sharedMemPerBlockOptin;
-  c->limits = KernelLimits{1024, 1024, 1 << 30};
+  c->limits = KernelLimits{1024, 1024};
   CUDA_TRY(configure_kernels(c->smem_limit, &c->limits));
   CUDA_TRY(configure_batch_kernels(c->smem_limit, &c->limits));
   *out = c.release();
