@@ -196,7 +196,7 @@ struct orion_gpu_ctx {
   DevBuf sppm_block, sppm_hits;
   DevBuf preview;  // 8-bit previews of server films
   int smem_limit = 48 * 1024;  // opt-in dynamic shared memory per block
-  KernelLimits limits{1024, 1024, 1 << 30};
+  KernelLimits limits{1024, 1024};
   std::mutex mu;
 };
 
@@ -208,9 +208,8 @@ static std::string config_problem(const orion_gpu_ctx* ctx, const LaunchConfig& 
   if (c.shade_block < 32 || c.shade_block % 32 || c.shade_block > ctx->limits.max_shade_block)
     return "shade_block must be a multiple of 32 up to " + std::to_string(ctx->limits.max_shade_block);
   if (!(st == 0 || st == 8 || st == 16 || st == 24 || st == 32)) return "smem_stack must be 0, 8, 16, 24 or 32";
-  if ((int64_t)st * c.trace_block * 8 > std::min(ctx->smem_limit, ctx->limits.max_trace_smem))
-    return "traversal stack (smem_stack x trace_block x 8 bytes) exceeds " +
-           std::to_string(std::min(ctx->smem_limit, ctx->limits.max_trace_smem)) +
+  if ((int64_t)st * c.trace_block * 8 > ctx->smem_limit)
+    return "traversal stack (smem_stack x trace_block x 8 bytes) exceeds " + std::to_string(ctx->smem_limit) +
            " bytes of shared memory";
   if (c.blocks_per_sm < 1 || c.blocks_per_sm > 64) return "blocks_per_sm out of range (1..64)";
   if (c.refill_below < 1 || c.refill_below > 32) return "refill_below out of range (1..32)";
@@ -516,7 +515,6 @@ extern "C" int orion_gpu_scene_upload(orion_gpu_ctx* ctx, const orion_host_scene
   for (const DevLight& l : ps.lights) v.num_area_lights += l.kind == DL_AREA ? 1 : 0;
   for (int i = 0; i < v.num_env; ++i) v.env_idx[i] = ps.env_idx[i];
   v.world_radius = ps.world_radius;
-  v.num_nodes = (int)bvh.wide.size();
   for (int k = 0; k < 3; ++k) v.world_center[k] = ps.world_center[k];
   v.cam = ps.cam;
   d->bytes = bytes;

@@ -50,39 +50,25 @@ __global__ void k_camera(SceneView s, WaveView w, WaveArgs a) {
 
 // Closest hit: extension rays (RayView = RecF4, hits into the path records,
 // slots sorted by shading class) or MIS rays (NeeF4, hits into mis_hit).
-// Both trace one scene: each block first stages its top-level nodes in
-// shared memory (stage_top_levels); `err` is set if a copy did not complete.
 template <int SMEM, class RayView, class HitView>
 __global__ void __launch_bounds__(512, 2)
     k_trace(SceneView s, const int* queue, const int* count, int* fetch, RayView ray_o, RayView ray_d, HitView hit,
-            unsigned long long* stat, int refill_below, int* cls_counters, int* q_cls, int cls_stride, int* err) {
+            unsigned long long* stat, int refill_below, int* cls_counters, int* q_cls, int cls_stride) {
   extern __shared__ int2 stack_smem[];
-  __shared__ __align__(128) float4 top[5 * kTopNodes];
-  __shared__ __align__(8) uint64_t bar;
   const int n = *count;
-  if (n == 0) return;
-  const int count_top = min(kTopNodes, s.num_nodes);
-  const int ntop = stage_top_levels(top, &bar, s.nodes, count_top, err);
   trace_persistent<false, SMEM>(SingleScene{&s}, queue, n, fetch, ray_o, ray_d, hit, nullptr, stack_smem,
-                                refill_below, cls_counters, q_cls, cls_stride, top, ntop);
-  drain_top_levels(&bar, ntop, count_top);
+                                refill_below, cls_counters, q_cls, cls_stride);
   if (stat && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(stat, (unsigned long long)n);
 }
 
 template <int SMEM>
 __global__ void __launch_bounds__(512, 2)
     k_trace_sh(SceneView s, const int* queue, const int* count, int* fetch, NeeF4 ray_o, NeeF4 ray_d, int* occluded,
-               unsigned long long* stat, int refill_below, int* err) {
+               unsigned long long* stat, int refill_below) {
   extern __shared__ int2 stack_smem[];
-  __shared__ __align__(128) float4 top[5 * kTopNodes];
-  __shared__ __align__(8) uint64_t bar;
   const int n = *count;
-  if (n == 0) return;
-  const int count_top = min(kTopNodes, s.num_nodes);
-  const int ntop = stage_top_levels(top, &bar, s.nodes, count_top, err);
   trace_persistent<true, SMEM>(SingleScene{&s}, queue, n, fetch, ray_o, ray_d, F4{nullptr}, occluded, stack_smem,
-                               refill_below, nullptr, nullptr, 0, top, ntop);
-  drain_top_levels(&bar, ntop, count_top);
+                               refill_below);
   if (stat && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(stat, (unsigned long long)n);
 }
 
@@ -260,19 +246,19 @@ void launch_trace_kernels(int kind, const SceneView& s, const WaveView& w, int c
   if (kind == TK_EXT)
     k_trace<SMEM, RecF4, RecF4><<<grid, block, smem, stream>>>(
         s, w.q_ext[cur], w.counters + cur, w.counters + CNT_FETCH_EXT, w.ray_o, w.ray_d, w.hit, w.ray_stats, refill,
-        w.counters + CNT_CLS0, w.q_cls, w.capacity, w.error_word);
+        w.counters + CNT_CLS0, w.q_cls, w.capacity);
   else if (kind == TK_SHADOW)
     k_trace_sh<SMEM><<<grid, block, smem, stream>>>(s, w.q_sh, w.counters + CNT_SH, w.counters + CNT_FETCH_SH, w.sh_o,
-                                                    w.sh_d, w.occluded, w.ray_stats + 1, refill, w.error_word);
+                                                    w.sh_d, w.occluded, w.ray_stats + 1, refill);
   else if (kind == TK_MIS_ENV)
     k_trace_sh<SMEM><<<grid, block, smem, stream>>>(s, w.q_mis_env, w.counters + CNT_MIS_ENV,
                                                     w.counters + CNT_FETCH_MIS_ENV, w.mis_o, w.mis_d,
-                                                    w.mis_occluded, w.ray_stats + 2, refill, w.error_word);
+                                                    w.mis_occluded, w.ray_stats + 2, refill);
   else
     k_trace<SMEM, NeeF4, F4><<<grid, block, smem, stream>>>(s, w.q_mis, w.counters + CNT_MIS,
                                                             w.counters + CNT_FETCH_MIS, w.mis_o, w.mis_d,
                                                             F4{w.mis_hit}, w.ray_stats + 2, refill, nullptr,
-                                                            nullptr, 0, w.error_word);
+                                                            nullptr, 0);
 }
 
 void trace_dispatch(int kind, const SceneView& s, const WaveView& w, int cur, const LaunchConfig& cfg, int grid,
@@ -380,18 +366,14 @@ void launch_trace(const SceneView& s, int64_t n, const float* rays, int any_hit,
 
 namespace {
 
-// Raises a kernel's dynamic shared memory to what the opt-in maximum leaves
-// beside its static shared memory; records the launch limits.
-cudaError_t limit_of(const void* f, int smem_bytes, int* max_block, int* max_dyn_smem = nullptr) {
+cudaError_t limit_of(const void* f, int smem_bytes, int* max_block) {
+  if (smem_bytes > 0) {
+    cudaError_t e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, smem_bytes);
+    if (e != cudaSuccess) return e;
+  }
   cudaFuncAttributes a;
   cudaError_t e = cudaFuncGetAttributes(&a, f);
   if (e != cudaSuccess) return e;
-  if (smem_bytes > 0) {
-    const int dyn = smem_bytes - (int)a.sharedSizeBytes;
-    e = cudaFuncSetAttribute(f, cudaFuncAttributeMaxDynamicSharedMemorySize, dyn);
-    if (e != cudaSuccess) return e;
-    if (max_dyn_smem) *max_dyn_smem = std::min(*max_dyn_smem, dyn);
-  }
   *max_block = std::min(*max_block, a.maxThreadsPerBlock);
   return cudaSuccess;
 }
@@ -413,7 +395,7 @@ cudaError_t configure_kernels(int smem_bytes, KernelLimits* lim) {
                          (const void*)k_shade<SC_PLASTIC>, (const void*)k_shade<SC_GENERAL>, (const void*)k_shade<SC_TEXTURED>,
                          (const void*)k_shade<SC_MISS>, (const void*)k_resolve};
   for (const void* f : trace) {
-    cudaError_t e = limit_of(f, smem_bytes, &lim->max_trace_block, &lim->max_trace_smem);
+    cudaError_t e = limit_of(f, smem_bytes, &lim->max_trace_block);
     if (e != cudaSuccess) return e;
   }
   for (const void* f : shade) {

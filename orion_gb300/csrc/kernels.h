@@ -29,7 +29,6 @@ struct SceneView {
   int num_area_lights;
   float world_radius;
   float world_center[3];  // Bounds3::boundingSphere (distant and environment photons)
-  int num_nodes;          // 8-wide BVH nodes
   unsigned class_mask;  // shading classes of the scene's triangles (bit ShadeClass), SC_MISS always
   DevCamera cam;
 };
@@ -213,7 +212,6 @@ void launch_wave(const SceneView& s, const WaveView& w, const WaveArgs& a, const
 struct KernelLimits {
   int max_trace_block;  // threads per block the traversal kernels can launch with
   int max_shade_block;  // same for the shade / resolve / retire kernels
-  int max_trace_smem;   // dynamic shared memory (traversal stacks) the traversal kernels can take
 };
 cudaError_t configure_kernels(int smem_bytes, KernelLimits* lim);
 cudaError_t configure_batch_kernels(int smem_bytes, KernelLimits* lim);

@@ -118,9 +118,7 @@ static __device__ __noinline__ void textured_material(const SceneView& s, int mi
   build_material(in, m);
 }
 
-__device__ __forceinline__ TraceScene trace_scene(const SceneView& s) {
-  return TraceScene{s.nodes, s.woop, s.tri_prim, s.tri_class, nullptr, 0};
-}
+__device__ __forceinline__ TraceScene trace_scene(const SceneView& s) { return TraceScene{s.nodes, s.woop, s.tri_prim, s.tri_class}; }
 
 // Pinhole::generateRay (src/camera/pinhole.cpp:8-33).
 // Sampler::next2() builds Point2f(next(), next()) (src/core/sampler.h:29); the
@@ -351,21 +349,19 @@ struct JobScene {
 // counter that must be zero at launch. Block size must be a multiple of 32.
 // With `q_cls` (closest hit only), each finished ray's slot is also appended
 // to the queue of the shading class of what it hit (SC_MISS for a miss).
-// `top`/`ntop`: the block's shared-memory copy of the scene's top-level
-// nodes (single-scene traces only; null/0 otherwise).
 template <bool ANY, int SMEM, class SceneOf, class RayView, class HitView>
 __device__ __forceinline__ void trace_persistent(const SceneOf& scene_of, const int* queue, int n, int* fetch,
                                                  RayView ray_o, RayView ray_d, HitView hit, int* occluded,
                                                  int2* stack_smem, int refill_below,
                                                  int* cls_counters = nullptr, int* q_cls = nullptr,
-                                                 int cls_stride = 0, const float4* top = nullptr, int ntop = 0) {
+                                                 int cls_stride = 0) {
   constexpr unsigned kFull = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   TraversalStack<SMEM> st;
   st.smem = stack_smem + threadIdx.x;
   st.stride = blockDim.x;
   LaneRay r;
-  TraceScene ts{nullptr, nullptr, nullptr, nullptr, nullptr, 0};
+  TraceScene ts{nullptr, nullptr, nullptr, nullptr};
   int pid = -1;
   bool active = false, exhausted = false;
   while (true) {
@@ -382,7 +378,7 @@ __device__ __forceinline__ void trace_persistent(const SceneOf& scene_of, const 
         if (my < n) {
           pid = queue[my];
           const SceneView& s = scene_of(pid);
-          ts = TraceScene{s.nodes, s.woop, s.tri_prim, s.tri_class, top, ntop};
+          ts = TraceScene{s.nodes, s.woop, s.tri_prim, s.tri_class};
           const float4 o4 = ray_o[pid], d4 = ray_d[pid];
           st.sp = 0;
           lane_start(r, o4, d4, ANY ? o4.w : kFloatMax);

@@ -22,69 +22,7 @@ struct TraceScene {
   const float4* __restrict__ woop;   // 3 float4 per triangle, leaf order
   const int* __restrict__ tri_prim;  // leaf order -> primID
   const uint8_t* __restrict__ tri_class;  // leaf order -> ShadeClass
-  const float4* top;  // shared-memory copy of nodes [0, ntop) (the top levels), or null
-  int ntop;
 };
-
-// ------------------------------------------ top levels in shared memory
-//
-// The host builder lays the top levels of the 8-wide tree out breadth first
-// at the start of the node array (bvh_build.cpp), so nodes [0, 73) are
-// levels 0-2 of a full tree. A block that traces against one scene copies
-// them into shared memory with one bulk asynchronous copy (TMA,
-// cp.async.bulk completing on an mbarrier), and node visits below 73 read the
-// copy; every other visit reads global memory.
-
-constexpr int kTopNodes = 73;  // 1 + 8 + 64: levels 0-2
-constexpr int kTopBytes = kTopNodes * 80;
-
-__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, uint32_t phase) {
-  uint32_t done;
-  asm volatile(
-      "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
-      : "=r"(done)
-      : "r"(smem_u32(bar)), "r"(phase)
-      : "memory");
-  return done != 0;
-}
-
-// Stages nodes [0, count) (count <= kTopNodes) into `dst`; every thread of
-// the block calls it. Returns the number of nodes staged: `count`, or 0 if
-// the copy did not complete within the wait bound (visits then read global
-// memory; *err is set). The wait is bounded: no thread spins forever.
-__device__ __forceinline__ int stage_top_levels(float4* dst, uint64_t* bar, const float4* nodes, int count, int* err) {
-  if (count <= 0) return 0;
-  const uint32_t bytes = (uint32_t)count * 80u;  // a multiple of 16; both addresses 16-byte aligned
-  if (threadIdx.x == 0) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(bar)) : "memory");
-    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
-                 : "memory");
-    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
-                     smem_u32(dst)),
-                 "l"(nodes), "r"(bytes), "r"(smem_u32(bar))
-                 : "memory");
-  }
-  __syncthreads();
-  bool done = false;
-  for (int i = 0; i < (1 << 16) && !done; ++i) done = mbar_try_wait(bar, 0u);
-  if (!done) {
-    if (err) atomicExch(err, 1);
-    return 0;
-  }
-  return count;
-}
-
-// Before a block that staged the top levels exits without having seen its
-// copy complete, it waits once more (bounded) so the copy does not land in
-// shared memory the block no longer owns.
-__device__ __forceinline__ void drain_top_levels(uint64_t* bar, int staged, int count) {
-  if (count > 0 && staged == 0)
-    for (int i = 0; i < (1 << 16) && !mbar_try_wait(bar, 0u); ++i) {
-    }
-}
 
 struct RayHit {
   float t, u, v;
@@ -198,23 +136,10 @@ __device__ __forceinline__ uint32_t octant_permute(uint32_t x, uint32_t oct) {
   return x;
 }
 
-__device__ __forceinline__ float4 ld_shared4(uint32_t a) {
-  float4 v;
-  asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "r"(a));
-  return v;
-}
-
-__device__ __forceinline__ void wide_node(const float4* __restrict__ nodes, const float4* top, int ntop, int idx, V3 o,
-                                          V3 idir, uint32_t oct, float tnear, float tmax, uint2& ng, uint2& tg) {
-  float4 n0, n1, n2, n3, n4;
-  if (idx < ntop) {  // a top-level node: the shared-memory copy
-    const uint32_t a = smem_u32(top + 5 * idx);
-    n0 = ld_shared4(a), n1 = ld_shared4(a + 16), n2 = ld_shared4(a + 32), n3 = ld_shared4(a + 48);
-    n4 = ld_shared4(a + 64);
-  } else {
-    const float4* n = nodes + 5 * (size_t)idx;
-    n0 = __ldg(n), n1 = __ldg(n + 1), n2 = __ldg(n + 2), n3 = __ldg(n + 3), n4 = __ldg(n + 4);
-  }
+__device__ __forceinline__ void wide_node(const float4* __restrict__ nodes, int idx, V3 o, V3 idir, uint32_t oct,
+                                          float tnear, float tmax, uint2& ng, uint2& tg) {
+  const float4* n = nodes + 5 * (size_t)idx;
+  const float4 n0 = __ldg(n), n1 = __ldg(n + 1), n2 = __ldg(n + 2), n3 = __ldg(n + 3), n4 = __ldg(n + 4);
   const uint32_t ew = __float_as_uint(n0.w);
   const float sx = __uint_as_float((ew & 0xffu) << 23) * idir.x;
   const float sy = __uint_as_float(((ew >> 8) & 0xffu) << 23) * idir.y;
@@ -283,7 +208,7 @@ __device__ __forceinline__ RayHit traverse(const TraceScene& s, V3 o, V3 d, floa
     if (ng.y > 0x00ffffffu) {
       const int child = take_child(ng, oct);
       if (ng.y) st.push(make_int2((int)ng.x, (int)ng.y));
-      wide_node(s.nodes, s.top, s.ntop, child, o, idir, oct, tnear, h.t, ng, tg);
+      wide_node(s.nodes, child, o, idir, oct, tnear, h.t, ng, tg);
     } else {
       tg = ng;
       ng = make_uint2(0u, 0u);
@@ -360,7 +285,7 @@ __device__ __forceinline__ bool lane_step(LaneRay& r, const TraceScene& s, Trave
   if (r.ng.y > 0x00ffffffu) {
     const int child = take_child(r.ng, r.oct);
     if (r.ng.y) st.push(make_int2((int)r.ng.x, (int)r.ng.y));
-    wide_node(s.nodes, s.top, s.ntop, child, r.o, r.idir, r.oct, r.tnear, r.tmax, r.ng, r.tg);
+    wide_node(s.nodes, child, r.o, r.idir, r.oct, r.tnear, r.tmax, r.ng, r.tg);
   } else {
     r.tg = r.ng;
     r.ng = make_uint2(0u, 0u);
