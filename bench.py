@@ -279,6 +279,8 @@ def run_ours(args) -> dict:
     if rank == 0 and args.serve_scenes > 0:
         out["served"] = run_served(ctx, args.serve_scenes, args.serve_views, args.serve_rates, args.serve_requests,
                                    budget_gb=150.0, spp_chunk=args.spp_chunk, plain_n=args.plain_requests)
+    if rank == 0 and not args.quick:
+        out["other_configs"] = run_other_configs(ctx)
     if rank == 0 and args.sppm_res > 0:
         out["sppm"] = run_sppm(ctx, args.sppm_res, args.sppm_iterations, steps=max(1, min(args.steps, 3)),
                                cpu_iterations=4)
@@ -466,6 +468,32 @@ def run_served(ctx, n_scenes: int, views: int, rates: list, per_rate: int, budge
         "server": {"launches": int(stats["launches"]), "paths": int(stats["paths"]),
                    "device_ms": round(stats["device_ms"], 1), "resident_scenes": int(stats["resident_scenes"])},
     }
+
+
+def run_other_configs(ctx, names=("cornell", "mixed"), steps: int = 3) -> dict:
+    """The other single-image configurations at their full sizes (C1: Cornell box 256x256, 16 spp, depth 5;
+    C3: eight displaced icospheres, 5 materials, thin lens, 1920x1080, 128 spp, depth 16): device time of
+    a plain render, median of `steps` after one warm-up."""
+    import orion_gb300 as og
+    out = {}
+    for name in names:
+        host = og.HostScene.load(scene_path(name))
+        d = host.desc()
+        W, H, spp = d.camera.width, d.camera.height, d.spp
+        sid = ctx.upload(host)
+        ctx.render(sid, W, H)
+        ms, rays = [], 0
+        for _ in range(steps):
+            ctx.render(sid, W, H)
+            st = ctx.last_stats()
+            ms.append(st["device_ms"])
+            rays = st["rays"]
+        ctx.release(sid)
+        t = float(np.median(ms))
+        out[name] = {"workload": WORKLOADS[name][2], "paths": W * H * spp, "ms": round(t, 2),
+                     "mpaths_s": round(W * H * spp / (t * 1e-3) / 1e6, 2), "mrays_s": round(rays / (t * 1e-3) / 1e6, 2),
+                     "triangles": int(d.num_prims)}
+    return out
 
 
 def run_sppm(ctx, res: int, iterations: int, steps: int, cpu_iterations: int) -> dict:
