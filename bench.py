@@ -280,7 +280,7 @@ def run_ours(args) -> dict:
         out["served"] = run_served(ctx, args.serve_scenes, args.serve_views, args.serve_rates, args.serve_requests,
                                    budget_gb=150.0, spp_chunk=args.spp_chunk, plain_n=args.plain_requests)
     if rank == 0 and not args.quick:
-        out["other_configs"] = run_other_configs(ctx)
+        out["other_configs"] = run_other_configs(ctx, cpu_seconds=0.0 if args.no_cpu_baseline else 6.0)
     if rank == 0 and args.sppm_res > 0:
         out["sppm"] = run_sppm(ctx, args.sppm_res, args.sppm_iterations, steps=max(1, min(args.steps, 3)),
                                cpu_iterations=4)
@@ -470,7 +470,7 @@ def run_served(ctx, n_scenes: int, views: int, rates: list, per_rate: int, budge
     }
 
 
-def run_other_configs(ctx, names=("cornell", "mixed"), steps: int = 3) -> dict:
+def run_other_configs(ctx, names=("cornell", "mixed"), steps: int = 3, cpu_seconds: float = 0.0) -> dict:
     """The other single-image configurations at their full sizes (C1: Cornell box 256x256, 16 spp, depth 5;
     C3: eight displaced icospheres, 5 materials, thin lens, 1920x1080, 128 spp, depth 16): device time of
     a plain render, median of `steps` after one warm-up."""
@@ -493,6 +493,8 @@ def run_other_configs(ctx, names=("cornell", "mixed"), steps: int = 3) -> dict:
         out[name] = {"workload": WORKLOADS[name][2], "paths": W * H * spp, "ms": round(t, 2),
                      "mpaths_s": round(W * H * spp / (t * 1e-3) / 1e6, 2), "mrays_s": round(rays / (t * 1e-3) / 1e6, 2),
                      "triangles": int(d.num_prims)}
+        if cpu_seconds > 0:
+            out[name]["cpu_baseline"] = cpu_baseline(name, threads=os.cpu_count() or 1, seconds=cpu_seconds)
     return out
 
 
