@@ -770,12 +770,11 @@ extern "C" int orion_gpu_render_sppm(orion_gpu_ctx* ctx, orion_scene_id id, cons
   v.iterations = p.iterations;
   v.photons = (int)photons;
   v.sobol = ctx->sobol.as<uint32_t>();
-  // Photon hits (3 float4) and their cell-list entries (int), one block.
+  // Photon hits (3 float4) as recorded and in hash-cell order, one block.
   const size_t hit_bytes = ((size_t)hits_cap * 3 * sizeof(float4) + 255) & ~(size_t)255;
-  if (ctx->sppm_hits.bytes < hit_bytes + sizeof(int) * (size_t)hits_cap)
-    RC(ctx->sppm_hits.alloc(hit_bytes + sizeof(int) * (size_t)hits_cap));
+  if (ctx->sppm_hits.bytes < 2 * hit_bytes) RC(ctx->sppm_hits.alloc(2 * hit_bytes));
   v.hits = ctx->sppm_hits.as<float4>();
-  v.entries = reinterpret_cast<int*>(static_cast<char*>(ctx->sppm_hits.p) + hit_bytes);
+  v.by_cell = reinterpret_cast<float4*>(static_cast<char*>(ctx->sppm_hits.p) + hit_bytes);
   v.hits_cap = (int)hits_cap;
 
   launch_sppm_init(v, p.initial_radius, st);

@@ -277,11 +277,11 @@ struct SppmView {
   float4* hits;
   int hits_cap;     // photons x (max depth - 1): every hit after a photon's first
   int* hit_count;
-  // hash cell -> photon hits: cell h lists entries [cell_start[h], cell_start[h + 1])
+  // hash cell -> photon hits: cell h holds records [cell_start[h], cell_start[h + 1]) of by_cell
   int* cell_start;  // npix + 1 (counts, then their exclusive scan)
   int* cell_fill;   // npix
   int* scan_part;   // per scan block
-  int* entries;     // hits_cap
+  float4* by_cell;  // the hits in hash-cell order, 3 float4 each (hits_cap)
   float* film;      // W*H*3 sums of the iterations' estimates
   unsigned* film_count;
   unsigned long long* rays;

@@ -14,7 +14,7 @@
 //                    the grid is recorded (point, wi, beta) and counted in
 //                    its hash cell
 //   k_scan_*         exclusive scan: each hash cell's first list entry
-//   k_sppm_fill      the photon hits listed by hash cell
+//   k_sppm_fill      the photon hits copied into hash-cell order
 //   k_sppm_gather    one warp per visible point: for each hash cell its
 //                    sphere overlaps, the recorded photons in that cell
 //                    within its radius add beta * f(wi, wo) (sppm.cpp:226-247)
@@ -311,13 +311,19 @@ __device__ __forceinline__ unsigned cell_hash(int x, int y, int z, int size) {
   return (((unsigned)x * 73856093u) ^ ((unsigned)y * 19349663u) ^ ((unsigned)z * 83492791u)) % (unsigned)size;
 }
 
-// Lists the recorded photon hits by hash cell (cell_start holds each
-// cell's first entry after the scan).
+// Copies the recorded photon hits into hash-cell order (cell_start holds
+// each cell's first entry after the scan), so a gather reads a cell's hits
+// from consecutive records.
 __global__ void __launch_bounds__(256) k_sppm_fill(SppmView v) {
   const int n = min(*v.hit_count, v.hits_cap);
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-    const unsigned h = (unsigned)__float_as_int(v.hits[3 * (size_t)i].w);
-    v.entries[v.cell_start[h] + atomicAdd(v.cell_fill + h, 1)] = i;
+    const float4* src = v.hits + 3 * (size_t)i;
+    const float4 a = src[0], b = src[1], c = src[2];
+    const unsigned h = (unsigned)__float_as_int(a.w);
+    float4* dst = v.by_cell + 3 * (size_t)(v.cell_start[h] + atomicAdd(v.cell_fill + h, 1));
+    dst[0] = a;
+    dst[1] = b;
+    dst[2] = c;
   }
 }
 
@@ -348,7 +354,7 @@ __global__ void __launch_bounds__(128) k_sppm_gather(SceneView s, SppmView v) {
         const unsigned h = cell_hash(x, y, z, v.npix);
         const int e1 = v.cell_start[h + 1];
         for (int e = v.cell_start[h] + lane; e < e1; e += 32) {
-          const float4* rec = v.hits + 3 * (size_t)v.entries[e];
+          const float4* rec = v.by_cell + 3 * (size_t)e;
           const float4 hp = rec[0];
           if (length_sq(p - xyz(hp)) > rr) continue;
           const float4 wi4 = rec[1], hb = rec[2];
