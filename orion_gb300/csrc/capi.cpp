@@ -13,37 +13,12 @@
 #include <cstddef>
 #include <cstdio>
 #include <cstring>
-#include <map>
-#include <memory>
-#include <mutex>
 #include <string>
 #include <vector>
 
-#include "../../include/orion_gpu.h"
-#include "bvh_build.h"
-#include "internal.h"
-#include "kernels.h"
-#include "scene_host.h"
-#include "scene_prep.h"
+#include "context.h"
 
 using namespace orion_gb300;
-
-struct orion_host_scene {
-  HostScene s;
-  // Host BVH and device records, built on the first upload and reused by
-  // later uploads of the same scene (resident-scene serving, re-uploads).
-  std::unique_ptr<BvhBuild> bvh;
-  std::unique_ptr<PreparedScene> prep;
-  std::vector<uint8_t> tri_class;  // leaf order -> shading class
-  unsigned class_mask = 0;
-  // The upload arrays above are page-locked once (portable across contexts)
-  // so every upload copies at DMA speed; unlocked when the scene is freed.
-  std::vector<void*> pinned;
-  std::mutex mu;
-  ~orion_host_scene() {
-    for (void* p : pinned) cudaHostUnregister(p);
-  }
-};
 
 namespace {
 template <class T>
@@ -57,151 +32,21 @@ void pin(orion_host_scene* h, const std::vector<T>& v) {
 }
 }  // namespace
 
-namespace {
+namespace orion_gb300 {
 
+namespace {
 thread_local std::string g_error;
+}  // namespace
 
 int fail(int code, const std::string& msg) {
   g_error = msg;
   return code;
 }
 
-#define CUDA_TRY(call)                                                                             \
-  do {                                                                                             \
-    cudaError_t e_ = (call);                                                                       \
-    if (e_ != cudaSuccess) return fail(ORION_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
-  } while (0)
-
-#define RC(x)                      \
-  do {                             \
-    int rc_ = (x);                 \
-    if (rc_ != ORION_OK) return rc_; \
-  } while (0)
-
-struct DevBuf {
-  void* p = nullptr;
-  size_t bytes = 0;
-  ~DevBuf() {
-    if (p) cudaFree(p);
-  }
-  int alloc(size_t n) {
-    if (p) cudaFree(p);
-    p = nullptr;
-    bytes = 0;
-    if (n == 0) n = 16;
-    cudaError_t e = cudaMalloc(&p, n);
-    if (e != cudaSuccess) {
-      p = nullptr;
-      return fail(e == cudaErrorMemoryAllocation ? ORION_ERR_NOMEM : ORION_ERR_CUDA,
-                  std::string("cudaMalloc(") + std::to_string(n) + "): " + cudaGetErrorString(e));
-    }
-    bytes = n;
-    return ORION_OK;
-  }
-  template <class T>
-  T* as() const {
-    return static_cast<T*>(p);
-  }
-};
-
-struct DeviceScene {
-  DevBuf nodes, woop, tri_prim, tri_class, prims, mats, lights, lfunc, lcdf, env_data, envmaps;
-  DevBuf mat_src, textures, prim_uv;  // image textures (empty when no material is textured)
-  SceneView view{};
-  int64_t bytes = 0;
-  int64_t num_prims = 0;
-  int width = 0, height = 0, spp = 1, max_depth = 5;
-  int bvh_depth = 0;
-  unsigned class_mask = 1u << SC_MISS;  // shading classes of the scene's triangles, and misses
-  orion_sppm_params sppm{0, 0, 0.f, 0};  // the scene's <Integrator type="sppm"> parameters
-};
-
-constexpr int kMaxWaveStreams = 4;  // plain-render waves in flight at once
-
-// One pooled batch engine: its free and retire lists, control block, job
-// table and captured device-side loop (the path slots are a Wave).
-// A captured device-side loop of one batch mode (pooled or waves).
-struct BatchGraph {
-  cudaGraph_t graph = nullptr;
-  cudaGraphExec_t exec = nullptr;
-  const void* key[4] = {nullptr, nullptr, nullptr, nullptr};  // buffers the graph was captured with
-  LaunchConfig cfg{};
-  int slots = 0;
-  unsigned mask = 0;  // shading classes the captured loop launches
-  void drop() {
-    if (exec) cudaGraphExecDestroy(exec);
-    if (graph) cudaGraphDestroy(graph);
-    exec = nullptr;
-    graph = nullptr;
-  }
-};
-
-struct BatchEngine {
-  DevBuf retire, free_list, ctl, jobs;
-  int slots_alloc = 0, jobs_alloc = 0;
-  BatchGraph loop[2];  // [ORION_BATCH_POOLED], [ORION_BATCH_WAVES]
-  void drop_graph() {
-    for (BatchGraph& g : loop) g.drop();
-  }
-};
-
-struct Wave {
-  int capacity = 0;
-  DevBuf block;  // all per-path arrays in one allocation
-  WaveView view{};
-};
-
-}  // namespace
-
-struct orion_gpu_ctx {
-  int device = 0;
-  cudaStream_t stream = nullptr;
-  int num_sms = 0;
-  DevBuf sobol, sobol_bitmajor;
-  std::map<int, std::unique_ptr<DeviceScene>> scenes;
-  int next_id = 1;
-  Wave wave;
-  // Plain renders overlap consecutive waves on up to kWaveStreams streams:
-  // per extra stream its wave state, the stream, its join event; the events
-  // that order the film writes wave after wave.
-  static constexpr int kWaveStreams = kMaxWaveStreams;
-  int wave_streams = 2;
-  Wave xwave[kWaveStreams - 1];
-  cudaStream_t xstream[kWaveStreams - 1] = {};
-  cudaEvent_t ev_fork = nullptr, ev_join[kWaveStreams - 1] = {}, ev_film[kWaveStreams] = {};
-  DevBuf film_sum, film_count, film64, filmsq64;
-  int64_t film_pixels = 0;
-  int64_t budget = 0;
-  orion_render_stats last{};
-  LaunchConfig cfg{};
-  // Large waves amortise each bounce's kernel tails over more paths, and two
-  // waves in flight fill the tails that remain (C2: 449 Mpaths/s with one
-  // stream of 4M-path waves, 708 with two streams of 32M).
-  int default_wave = 1 << 25;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  bool profiling = false;
-  std::vector<cudaEvent_t> prof_events;
-  std::vector<int> prof_stage;
-  orion_stage_times stage_times{};
-  // batched mode
-  int default_batch_slots = 1 << 24;  // pooled: path slots; waves: paths per wave
-  DevBuf b_films;
-  // Pooled batch engines: a batch's jobs are split between as many as the
-  // `streams` knob allows (at most kBatchEngines) and they run concurrently,
-  // engine e on the wave state and stream of wave slot e.
-  static constexpr int kBatchEngines = 2;
-  BatchEngine beng[kBatchEngines];
-  int batch_mode = ORION_BATCH_WAVES;
-  // SPPM: per-pixel state in one block, the grid's cell lists apart
-  DevBuf sppm_block, sppm_hits;
-  DevBuf preview;  // 8-bit previews of server films
-  int smem_limit = 48 * 1024;  // opt-in dynamic shared memory per block
-  KernelLimits limits{1024, 1024};
-  std::mutex mu;
-};
+}  // namespace orion_gb300
 
 // Why a launch configuration cannot run on this context ("" if it can).
-static std::string config_problem(const orion_gpu_ctx* ctx, const LaunchConfig& c) {
+std::string orion_gb300::config_problem(const orion_gpu_ctx* ctx, const LaunchConfig& c) {
   const int st = c.smem_stack;
   if (c.trace_block < 32 || c.trace_block % 32 || c.trace_block > ctx->limits.max_trace_block)
     return "trace_block must be a multiple of 32 up to " + std::to_string(ctx->limits.max_trace_block);
@@ -216,7 +61,7 @@ static std::string config_problem(const orion_gpu_ctx* ctx, const LaunchConfig& 
   return std::string();
 }
 
-extern "C" const char* orion_last_error(void) { return g_error.c_str(); }
+extern "C" const char* orion_last_error(void) { return orion_gb300::g_error.c_str(); }
 
 // ------------------------------------------------------------- scenes
 
@@ -278,7 +123,7 @@ static int ensure_film(orion_gpu_ctx* c, int64_t pixels, bool fp64) {
   return ORION_OK;
 }
 
-static int alloc_wave(Wave& wave, int capacity) {
+int orion_gb300::alloc_wave(Wave& wave, int capacity) {
   if (wave.capacity >= capacity) return ORION_OK;
   const size_t n = (size_t)capacity;
   auto round256 = [](size_t b) { return (b + 255) & ~(size_t)255; };
@@ -703,109 +548,6 @@ extern "C" int orion_gpu_render_fp64(orion_gpu_ctx* ctx, orion_scene_id id, cons
   return render_impl(ctx, id, params, nullptr, nullptr, sum, sumsq);
 }
 
-// ------------------------------------------------------------ SPPM
-
-extern "C" int orion_gpu_render_sppm(orion_gpu_ctx* ctx, orion_scene_id id, const orion_sppm_params* params,
-                                     float* film_rgb_sum, uint32_t* film_count) {
-  if (!ctx || !film_rgb_sum) return fail(ORION_ERR_INVALID, "null argument");
-  std::lock_guard<std::mutex> g(ctx->mu);
-  CUDA_TRY(cudaSetDevice(ctx->device));
-  auto it = ctx->scenes.find(id);
-  if (it == ctx->scenes.end()) return fail(ORION_ERR_INVALID, "unknown scene id");
-  const DeviceScene& d = *it->second;
-  const orion_sppm_params p = params ? *params : d.sppm;
-  if (p.iterations <= 0) return fail(ORION_ERR_INVALID, "sppm: iterations must be positive");
-  if (p.max_depth < 0 || p.max_depth > 1024) return fail(ORION_ERR_INVALID, "sppm: max_depth out of range");
-  if (!(p.initial_radius > 0.f)) return fail(ORION_ERR_INVALID, "sppm: initial radius must be positive");
-  // SPPM::render requires a light (CHECK_INFO, src/integrator/sppm.cpp:72-73).
-  if (d.view.num_lights == 0) return fail(ORION_ERR_INVALID, "sppm: the scene has no light");
-  const int W = d.view.cam.width, H = d.view.cam.height;
-  const int64_t npix = (int64_t)W * H;
-  const int64_t photons = p.photons_per_iter < 0 ? npix : p.photons_per_iter;
-  const int64_t hits_cap = photons * std::max(1, p.max_depth - 1);  // hits after each photon's first
-  if (npix <= 0 || npix > (1 << 28) || hits_cap > INT32_MAX) return fail(ORION_ERR_INVALID, "sppm: size out of range");
-  if ((int64_t)p.iterations * (npix + photons) >= (1LL << 52))
-    return fail(ORION_ERR_INVALID, "sppm: sample indices exceed the Sobol matrices");
-  cudaStream_t st = ctx->stream;
-
-  // Per-pixel state, 16-byte aligned pieces of one allocation.
-  const int nparts = kSppmBoundsBlocks;
-  const int nscan = (int)((npix + 1 + kScanBlock - 1) / kScanBlock);
-  struct Piece {
-    void** dst;
-    size_t bytes;
-  };
-  SppmView v{};
-  float4* f4s[9];
-  std::vector<Piece> pieces;
-  for (int k = 0; k < 9; ++k) pieces.push_back({(void**)&f4s[k], sizeof(float4) * (size_t)npix});
-  pieces.push_back({(void**)&v.phi, sizeof(float) * 3 * (size_t)npix});
-  pieces.push_back({(void**)&v.m, sizeof(int) * (size_t)npix});
-  pieces.push_back({(void**)&v.cell_start, sizeof(int) * ((size_t)npix + 1)});
-  pieces.push_back({(void**)&v.cell_fill, sizeof(int) * (size_t)npix});
-  pieces.push_back({(void**)&v.scan_part, sizeof(int) * (size_t)nscan});
-  pieces.push_back({(void**)&v.part_lo, sizeof(float4) * (size_t)nparts});
-  pieces.push_back({(void**)&v.part_hi, sizeof(float4) * (size_t)nparts});
-  pieces.push_back({(void**)&v.grid, sizeof(SppmGrid)});
-  pieces.push_back({(void**)&v.film, sizeof(float) * 3 * (size_t)npix});
-  pieces.push_back({(void**)&v.film_count, sizeof(unsigned) * (size_t)npix});
-  pieces.push_back({(void**)&v.rays, sizeof(unsigned long long)});
-  pieces.push_back({(void**)&v.hit_count, sizeof(int)});
-  size_t total = 0;
-  for (const Piece& pc : pieces) total += (pc.bytes + 255) & ~(size_t)255;
-  if (ctx->sppm_block.bytes < total) RC(ctx->sppm_block.alloc(total));
-  {
-    char* base = static_cast<char*>(ctx->sppm_block.p);
-    for (const Piece& pc : pieces) {
-      *pc.dst = base;
-      base += (pc.bytes + 255) & ~(size_t)255;
-    }
-  }
-  v.vp_pr = f4s[0], v.vp_wo = f4s[1], v.vp_beta = f4s[2], v.vp_ns = f4s[3], v.vp_ng = f4s[4];
-  v.vp_su = f4s[5], v.vp_sv = f4s[6], v.ld = f4s[7], v.tau = f4s[8];
-  v.width = W;
-  v.height = H;
-  v.npix = (int)npix;
-  v.max_depth = p.max_depth;
-  v.iterations = p.iterations;
-  v.photons = (int)photons;
-  v.sobol = ctx->sobol.as<uint32_t>();
-  // Photon hits (3 float4) as recorded and in hash-cell order, one block.
-  const size_t hit_bytes = ((size_t)hits_cap * 3 * sizeof(float4) + 255) & ~(size_t)255;
-  if (ctx->sppm_hits.bytes < 2 * hit_bytes) RC(ctx->sppm_hits.alloc(2 * hit_bytes));
-  v.hits = ctx->sppm_hits.as<float4>();
-  v.by_cell = reinterpret_cast<float4*>(static_cast<char*>(ctx->sppm_hits.p) + hit_bytes);
-  v.hits_cap = (int)hits_cap;
-
-  launch_sppm_init(v, p.initial_radius, st);
-  CUDA_TRY(cudaMemsetAsync(v.rays, 0, sizeof(unsigned long long), st));
-  CUDA_TRY(cudaGetLastError());
-  CUDA_TRY(cudaEventRecord(ctx->ev0, st));
-  int64_t launches = 1;
-  for (int iter = 0; iter < p.iterations; ++iter) {
-    launch_sppm_visible_points(d.view, v, iter, st);
-    launch_sppm_photons(d.view, v, iter, st);
-    CUDA_TRY(cudaGetLastError());
-    launches += 10;
-  }
-  CUDA_TRY(cudaEventRecord(ctx->ev1, st));
-  unsigned long long rays = 0;
-  CUDA_TRY(cudaMemcpyAsync(film_rgb_sum, v.film, sizeof(float) * 3 * (size_t)npix, cudaMemcpyDeviceToHost, st));
-  if (film_count)
-    CUDA_TRY(cudaMemcpyAsync(film_count, v.film_count, sizeof(uint32_t) * (size_t)npix, cudaMemcpyDeviceToHost, st));
-  CUDA_TRY(cudaMemcpyAsync(&rays, v.rays, sizeof(rays), cudaMemcpyDeviceToHost, st));
-  CUDA_TRY(cudaStreamSynchronize(st));
-  float ms = 0.f;
-  CUDA_TRY(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
-  ctx->last = orion_render_stats{};
-  ctx->last.paths = npix * p.iterations + photons * p.iterations;
-  ctx->last.rays = (int64_t)rays;
-  ctx->last.ext_rays = (int64_t)rays;
-  ctx->last.kernel_launches = launches;
-  ctx->last.device_ms = ms;
-  return ORION_OK;
-}
-
 extern "C" int orion_gpu_last_stats(orion_gpu_ctx* ctx, orion_render_stats* out) {
   if (!ctx || !out) return fail(ORION_ERR_INVALID, "null argument");
   *out = ctx->last;
@@ -822,458 +564,6 @@ extern "C" int orion_gpu_set_profiling(orion_gpu_ctx* ctx, int32_t enable) {
 extern "C" int orion_gpu_stage_times(orion_gpu_ctx* ctx, orion_stage_times* out) {
   if (!ctx || !out) return fail(ORION_ERR_INVALID, "null argument");
   *out = ctx->stage_times;
-  return ORION_OK;
-}
-
-// ------------------------------------------------------------ batches
-
-// Wave state and stream of batch engine e (shared with plain-render wave slot e).
-static Wave& engine_wave(orion_gpu_ctx* ctx, int e) { return e == 0 ? ctx->wave : ctx->xwave[e - 1]; }
-static cudaStream_t engine_stream(orion_gpu_ctx* ctx, int e) { return e == 0 ? ctx->stream : ctx->xstream[e - 1]; }
-
-// The captured loop launches the shading kernels of the classes in `mask`;
-// a graph that launches a superset is reused (an absent class's kernel
-// finds an empty queue), so the mask of a long-lived context only grows.
-static int build_batch_graph(orion_gpu_ctx* ctx, int e, int mode, const BatchView& bv, int slots, unsigned mask) {
-  BatchEngine& eng = ctx->beng[e];
-  BatchGraph& be = eng.loop[mode];
-  Wave& wave = engine_wave(ctx, e);
-  const void* key[4] = {wave.block.p, eng.jobs.p, eng.retire.p, eng.ctl.p};
-  bool same = be.exec && be.slots == slots && std::memcmp(key, be.key, sizeof(key)) == 0 &&
-              std::memcmp(&be.cfg, &ctx->cfg, sizeof(LaunchConfig)) == 0 && (mask & ~be.mask) == 0;
-  if (same) return ORION_OK;
-  if (be.exec) mask |= be.mask;
-  be.drop();
-  CUDA_TRY(cudaGraphCreate(&be.graph, 0));
-  cudaGraphConditionalHandle cond;
-  CUDA_TRY(cudaGraphConditionalHandleCreate(&cond, be.graph, 1, cudaGraphCondAssignDefault));
-  // cudaGraphNodeParams has no usable default constructor in host C++;
-  // zeroed storage is its documented initial state.
-  alignas(cudaGraphNodeParams) unsigned char np_storage[sizeof(cudaGraphNodeParams)] = {};
-  cudaGraphNodeParams& np = *reinterpret_cast<cudaGraphNodeParams*>(np_storage);
-  np.type = cudaGraphNodeTypeConditional;
-  np.conditional.handle = cond;
-  np.conditional.type = cudaGraphCondTypeWhile;
-  np.conditional.size = 1;
-  cudaGraphNode_t node;
-  CUDA_TRY(cudaGraphAddNode(&node, be.graph, nullptr, nullptr, 0, &np));
-  cudaGraph_t body = np.conditional.phGraph_out[0];
-  cudaError_t ce = capture_batch_iteration(wave.view, bv, ctx->sobol.as<uint32_t>(), ctx->sobol_bitmajor.as<uint32_t>(),
-                                           ctx->cfg, mask, mode == ORION_BATCH_WAVES, cond, engine_stream(ctx, e), body);
-  if (ce != cudaSuccess) {
-    // A graph whose loop-body capture was invalidated is dropped, not
-    // destroyed: nothing is assumed about its state after the failure.
-    be.graph = nullptr;
-    cudaGetLastError();
-    return fail(ORION_ERR_CUDA, std::string("batch loop capture: ") + cudaGetErrorString(ce));
-  }
-  CUDA_TRY(cudaGraphInstantiate(&be.exec, be.graph, 0));
-  std::memcpy(be.key, key, sizeof(key));
-  be.cfg = ctx->cfg;
-  be.slots = slots;
-  be.mask = mask;
-  return ORION_OK;
-}
-
-// Buffers of engine e for `njobs` jobs and up to `slots` path slots.
-static int prepare_engine(orion_gpu_ctx* ctx, int e, int njobs, int slots, BatchView* bv, int* cap) {
-  BatchEngine& be = ctx->beng[e];
-  Wave& wave = engine_wave(ctx, e);
-  int rc;
-  if ((rc = alloc_wave(wave, slots)) != ORION_OK) return rc;
-  *cap = wave.capacity;
-  if (be.slots_alloc < *cap) {
-    if ((rc = be.retire.alloc((size_t)*cap * 4)) != ORION_OK) return rc;
-    if ((rc = be.free_list.alloc((size_t)*cap * 4)) != ORION_OK) return rc;
-    be.slots_alloc = *cap;
-  }
-  if (!be.ctl.p && (rc = be.ctl.alloc(sizeof(BatchCtl))) != ORION_OK) return rc;
-  if (be.jobs_alloc < njobs) {
-    const int n = std::max(njobs, 64);
-    if ((rc = be.jobs.alloc((size_t)n * sizeof(DevJob))) != ORION_OK) return rc;
-    be.jobs_alloc = n;
-  }
-  bv->jobs = be.jobs.as<DevJob>();
-  bv->ctl = be.ctl.as<BatchCtl>();
-  bv->q_retire = be.retire.as<int>();
-  bv->q_free = be.free_list.as<int>();
-  return ORION_OK;
-}
-
-// Control block of a fresh batch of `total` work items on `cap` slots.
-static BatchCtl initial_ctl(unsigned long long total, int njobs, int cap, int max_depth_all) {
-  BatchCtl c;
-  std::memset(&c, 0, sizeof(c));
-  c.total = total;
-  c.njobs = njobs;
-  c.counters[CNT_FREE] = cap;
-  // Every live path advances one bounce per iteration: a bound on the loop.
-  const unsigned long long refills = (total + cap - 1) / cap + 1;
-  c.max_iterations = (int)std::min<unsigned long long>(2ULL * refills * (max_depth_all + 2) + 64, 1u << 30);
-  return c;
-}
-
-// One batch over `dj` (film pointers set; films zeroed or holding earlier
-// passes to add to, in stream order on ctx->stream before this call).
-// Caller holds ctx->mu. With more than one job, the jobs are split into
-// groups of about equal path counts, one per engine, and the engines run
-// concurrently on their own streams (each group's paths fill the SMs the
-// other group's kernel tails leave idle). Profiled batches run on one
-// engine, driven from the host. On return `out` holds the engines' summed
-// counts (iterations: the most any engine ran), `ms` the device time.
-static int run_batch_pooled_locked(orion_gpu_ctx* ctx, std::vector<DevJob>& dj, unsigned long long total,
-                                   int max_depth_all, BatchCtl* out_ctl, float* ms_out) {
-  const int njobs = (int)dj.size();
-  int rc;
-  const int ne = ctx->profiling ? 1 : std::min(std::min(ctx->wave_streams, (int)orion_gpu_ctx::kBatchEngines), njobs);
-  // Split by path count: largest jobs first, each to the lighter group.
-  std::vector<std::vector<DevJob>> group(ne);
-  std::vector<unsigned long long> gtotal(ne, 0);
-  std::vector<int> order(njobs);
-  for (int i = 0; i < njobs; ++i) order[i] = i;
-  std::stable_sort(order.begin(), order.end(),
-                   [&](int a, int b) { return dj[a].num_paths > dj[b].num_paths; });
-  for (int i : order) {
-    int g = 0;
-    for (int k = 1; k < ne; ++k)
-      if (gtotal[k] < gtotal[g]) g = k;
-    DevJob J = dj[i];
-    J.work_begin = (long long)gtotal[g];
-    group[g].push_back(J);
-    gtotal[g] += (unsigned long long)J.num_paths;
-  }
-  int ng = 0;  // engines with work
-  for (int g = 0; g < ne; ++g) ng += gtotal[g] > 0 ? 1 : 0;
-  if (ng == 0) ng = 1;
-  std::vector<BatchView> bvs(ng);
-  std::vector<int> caps(ng);
-  std::vector<unsigned> masks(ng, 1u << SC_MISS);
-  for (int e = 0; e < ng; ++e) {
-    const int slots = (int)std::min<unsigned long long>((unsigned long long)ctx->default_batch_slots,
-                                                         std::max<unsigned long long>(gtotal[e], 1024ULL));
-    if ((rc = prepare_engine(ctx, e, (int)group[e].size(), slots, &bvs[e], &caps[e])) != ORION_OK) return rc;
-    for (const DevJob& J : group[e]) masks[e] |= J.scene.class_mask;
-    if (!ctx->profiling && (rc = build_batch_graph(ctx, e, ORION_BATCH_POOLED, bvs[e], caps[e], masks[e])) != ORION_OK)
-      return rc;
-  }
-  cudaStream_t s = ctx->stream;
-  std::memset(&ctx->stage_times, 0, sizeof(ctx->stage_times));
-  CUDA_TRY(cudaEventRecord(ctx->ev0, s));
-  if (ng > 1) {
-    CUDA_TRY(cudaEventRecord(ctx->ev_fork, s));
-    for (int e = 1; e < ng; ++e) CUDA_TRY(cudaStreamWaitEvent(engine_stream(ctx, e), ctx->ev_fork, 0));
-  }
-  std::vector<BatchCtl> init(ng);
-  for (int e = 0; e < ng; ++e) {
-    cudaStream_t es = engine_stream(ctx, e);
-    init[e] = initial_ctl(gtotal[e], (int)group[e].size(), caps[e], max_depth_all);
-    if (!group[e].empty())
-      CUDA_TRY(cudaMemcpyAsync(bvs[e].jobs, group[e].data(), group[e].size() * sizeof(DevJob),
-                               cudaMemcpyHostToDevice, es));
-    CUDA_TRY(cudaMemcpyAsync(bvs[e].ctl, &init[e], sizeof(BatchCtl), cudaMemcpyHostToDevice, es));
-    launch_batch_init(engine_wave(ctx, e).view, bvs[e], caps[e], es);
-    CUDA_TRY(cudaGetLastError());
-  }
-  if (ctx->profiling) {
-    // Profiling: the same iterations driven from the host, every stage timed
-    // (one host round trip per iteration, so device_ms includes those gaps).
-    const int per_iter = 8;
-    const int need = (int)std::min<int64_t>((int64_t)init[0].max_iterations * per_iter, 200000);
-    while ((int)ctx->prof_events.size() < 2 * need) {
-      cudaEvent_t e;
-      CUDA_TRY(cudaEventCreate(&e));
-      ctx->prof_events.push_back(e);
-    }
-    ctx->prof_stage.resize(need);
-    StageTimer timer{ctx->prof_events.data(), ctx->prof_stage.data(), need, 0};
-    int more = 1;
-    for (int it = 0; more && it < init[0].max_iterations; ++it) {
-      launch_batch_iteration(ctx->wave.view, bvs[0], ctx->sobol.as<uint32_t>(), ctx->sobol_bitmajor.as<uint32_t>(),
-                             ctx->cfg, masks[0], false, s, &timer);
-      CUDA_TRY(cudaGetLastError());
-      CUDA_TRY(cudaMemcpyAsync(&more, &bvs[0].ctl->more, sizeof(int), cudaMemcpyDeviceToHost, s));
-      CUDA_TRY(cudaStreamSynchronize(s));
-    }
-    CUDA_TRY(cudaEventRecord(ctx->ev1, s));
-    CUDA_TRY(cudaStreamSynchronize(s));
-    for (int i = 0; i < std::min(timer.used, timer.capacity); ++i) {
-      float e = 0.f;
-      CUDA_TRY(cudaEventElapsedTime(&e, timer.events[2 * i], timer.events[2 * i + 1]));
-      ctx->stage_times.ms[timer.stage[i]] += e;
-      ctx->stage_times.launches[timer.stage[i]] += 1;
-    }
-  } else {
-    for (int e = 0; e < ng; ++e)
-      CUDA_TRY(cudaGraphLaunch(ctx->beng[e].loop[ORION_BATCH_POOLED].exec, engine_stream(ctx, e)));
-    for (int e = 1; e < ng; ++e) {
-      CUDA_TRY(cudaEventRecord(ctx->ev_join[e - 1], engine_stream(ctx, e)));
-      CUDA_TRY(cudaStreamWaitEvent(s, ctx->ev_join[e - 1], 0));
-    }
-    CUDA_TRY(cudaEventRecord(ctx->ev1, s));
-  }
-  std::vector<BatchCtl> outs(ng);
-  for (int e = 0; e < ng; ++e)
-    CUDA_TRY(cudaMemcpyAsync(&outs[e], bvs[e].ctl, sizeof(BatchCtl), cudaMemcpyDeviceToHost, s));
-  CUDA_TRY(cudaStreamSynchronize(s));
-  float ms = 0.f;
-  CUDA_TRY(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
-  *ms_out = ms;
-  BatchCtl& out = *out_ctl;
-  out = outs[0];
-  int64_t launches = 0;
-  bool error = false;
-  for (int e = 0; e < ng; ++e) {
-    const BatchCtl& o = outs[e];
-    if (e > 0) {
-      out.paths_done += o.paths_done;
-      for (int k = 0; k < 3; ++k) out.rays[k] += o.rays[k];
-      out.iterations = std::max(out.iterations, o.iterations);
-    }
-    error = error || o.error;
-    // Per iteration: plan, regen, 4 traces, one shade per class, resolve, retire, control; plus the init.
-    const unsigned launched = ctx->profiling ? masks[e] : ctx->beng[e].loop[ORION_BATCH_POOLED].mask;
-    launches += (9LL + __builtin_popcount(launched)) * o.iterations + 1;
-  }
-  out.error = error ? 1 : 0;
-  ctx->last.paths = (int64_t)out.paths_done;
-  ctx->last.ext_rays = (int64_t)out.rays[0];
-  ctx->last.shadow_rays = (int64_t)out.rays[1];
-  ctx->last.mis_rays = (int64_t)out.rays[2];
-  ctx->last.rays = (int64_t)(out.rays[0] + out.rays[1] + out.rays[2]);
-  ctx->last.kernel_launches = launches;
-  ctx->last.device_ms = ms;
-  if (out.error) return fail(ORION_ERR_DEVICE, "batch loop reached its iteration cap");
-  if (out.paths_done != total)
-    return fail(ORION_ERR_DEVICE, "batch finished " + std::to_string(out.paths_done) + " of " + std::to_string(total) +
-                                      " paths");
-  return ORION_OK;
-}
-
-// Wave mode: the concatenated work list in waves of up to `wave_paths`
-// paths, consecutive waves on the engines in turn (concurrently, one stream
-// each). Films take FP64 atomics, so waves may finish in any order.
-static int run_batch_waves_locked(orion_gpu_ctx* ctx, std::vector<DevJob>& dj, unsigned long long total,
-                                  int max_depth_all, BatchCtl* out_ctl, float* ms_out) {
-  const int njobs = (int)dj.size();
-  int rc;
-  const int64_t wave = std::max<int64_t>(1024, std::min<int64_t>(ctx->default_batch_slots, (int64_t)total));
-  const int64_t nwaves = std::max<int64_t>(1, ((int64_t)total + wave - 1) / wave);
-  const int ne = ctx->profiling ? 1 : (int)std::min<int64_t>(std::min(ctx->wave_streams, (int)orion_gpu_ctx::kBatchEngines),
-                                                            nwaves);
-  std::vector<BatchView> bvs(ne);
-  std::vector<int> caps(ne);
-  unsigned mask = 1u << SC_MISS;
-  for (const DevJob& J : dj) mask |= J.scene.class_mask;
-  for (int e = 0; e < ne; ++e) {
-    if ((rc = prepare_engine(ctx, e, njobs, (int)wave, &bvs[e], &caps[e])) != ORION_OK) return rc;
-    if (!ctx->profiling && (rc = build_batch_graph(ctx, e, ORION_BATCH_WAVES, bvs[e], caps[e], mask)) != ORION_OK)
-      return rc;
-  }
-  cudaStream_t s = ctx->stream;
-  std::memset(&ctx->stage_times, 0, sizeof(ctx->stage_times));
-  CUDA_TRY(cudaEventRecord(ctx->ev0, s));
-  if (ne > 1) {
-    CUDA_TRY(cudaEventRecord(ctx->ev_fork, s));
-    for (int e = 1; e < ne; ++e) CUDA_TRY(cudaStreamWaitEvent(engine_stream(ctx, e), ctx->ev_fork, 0));
-  }
-  BatchCtl zero;
-  std::memset(&zero, 0, sizeof(zero));
-  zero.njobs = njobs;
-  for (int e = 0; e < ne; ++e) {
-    cudaStream_t es = engine_stream(ctx, e);
-    CUDA_TRY(cudaMemcpyAsync(bvs[e].jobs, dj.data(), (size_t)njobs * sizeof(DevJob), cudaMemcpyHostToDevice, es));
-    CUDA_TRY(cudaMemcpyAsync(bvs[e].ctl, &zero, sizeof(BatchCtl), cudaMemcpyHostToDevice, es));
-  }
-  const int iteration_cap = 2 * (max_depth_all + 2) + 8;  // every live path advances one bounce per iteration
-  StageTimer timer{nullptr, nullptr, 0, 0};
-  if (ctx->profiling) {
-    const int need = (int)std::min<int64_t>(nwaves * iteration_cap * 8, 200000);
-    while ((int)ctx->prof_events.size() < 2 * need) {
-      cudaEvent_t e;
-      CUDA_TRY(cudaEventCreate(&e));
-      ctx->prof_events.push_back(e);
-    }
-    ctx->prof_stage.resize(need);
-    timer = StageTimer{ctx->prof_events.data(), ctx->prof_stage.data(), need, 0};
-  }
-  for (int64_t k = 0; k < nwaves; ++k) {
-    const int e = (int)(k % ne);
-    cudaStream_t es = engine_stream(ctx, e);
-    const WaveView& wv = engine_wave(ctx, e).view;
-    const unsigned long long base = (unsigned long long)(k * wave);
-    const int n = (int)std::min<unsigned long long>((unsigned long long)wave, total - base);
-    if (ctx->profiling) timer.begin(ST_CAMERA, es);
-    launch_batch_wave_begin(wv, bvs[e], ctx->sobol.as<uint32_t>(), base, n, iteration_cap, ctx->num_sms, es);
-    if (ctx->profiling) timer.end(es);
-    if (ctx->profiling) {
-      int more = 1;
-      for (int it = 0; more && it < iteration_cap; ++it) {
-        launch_batch_iteration(wv, bvs[e], ctx->sobol.as<uint32_t>(), ctx->sobol_bitmajor.as<uint32_t>(), ctx->cfg,
-                               mask, true, es, &timer);
-        CUDA_TRY(cudaGetLastError());
-        CUDA_TRY(cudaMemcpyAsync(&more, &bvs[e].ctl->more, sizeof(int), cudaMemcpyDeviceToHost, es));
-        CUDA_TRY(cudaStreamSynchronize(es));
-      }
-    } else {
-      CUDA_TRY(cudaGraphLaunch(ctx->beng[e].loop[ORION_BATCH_WAVES].exec, es));
-    }
-    if (ctx->profiling) timer.begin(ST_FILM, es);
-    launch_batch_wave_film(wv, bvs[e], n, ctx->num_sms, es);
-    if (ctx->profiling) timer.end(es);
-    CUDA_TRY(cudaGetLastError());
-  }
-  for (int e = 1; e < ne; ++e) {
-    CUDA_TRY(cudaEventRecord(ctx->ev_join[e - 1], engine_stream(ctx, e)));
-    CUDA_TRY(cudaStreamWaitEvent(s, ctx->ev_join[e - 1], 0));
-  }
-  CUDA_TRY(cudaEventRecord(ctx->ev1, s));
-  std::vector<BatchCtl> outs(ne);
-  for (int e = 0; e < ne; ++e)
-    CUDA_TRY(cudaMemcpyAsync(&outs[e], bvs[e].ctl, sizeof(BatchCtl), cudaMemcpyDeviceToHost, s));
-  CUDA_TRY(cudaStreamSynchronize(s));
-  float ms = 0.f;
-  CUDA_TRY(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
-  *ms_out = ms;
-  for (int i = 0; i < std::min(timer.used, timer.capacity); ++i) {
-    float e = 0.f;
-    CUDA_TRY(cudaEventElapsedTime(&e, timer.events[2 * i], timer.events[2 * i + 1]));
-    ctx->stage_times.ms[timer.stage[i]] += e;
-    ctx->stage_times.launches[timer.stage[i]] += 1;
-  }
-  BatchCtl& out = *out_ctl;
-  out = outs[0];
-  int64_t launches = 0;
-  bool error = false;
-  for (int e = 0; e < ne; ++e) {
-    const BatchCtl& o = outs[e];
-    if (e > 0) {
-      out.paths_done += o.paths_done;
-      for (int j = 0; j < 3; ++j) out.rays[j] += o.rays[j];
-      out.iterations += o.iterations;
-    }
-    error = error || o.error;
-    // Per iteration: plan, 4 traces, one shade per class, resolve, control.
-    const unsigned launched = ctx->profiling ? mask : ctx->beng[e].loop[ORION_BATCH_WAVES].mask;
-    launches += (7LL + __builtin_popcount(launched)) * o.iterations;
-  }
-  launches += 3 * nwaves;  // begin, camera, film per wave
-  out.error = error ? 1 : 0;
-  ctx->last.paths = (int64_t)out.paths_done;
-  ctx->last.ext_rays = (int64_t)out.rays[0];
-  ctx->last.shadow_rays = (int64_t)out.rays[1];
-  ctx->last.mis_rays = (int64_t)out.rays[2];
-  ctx->last.rays = (int64_t)(out.rays[0] + out.rays[1] + out.rays[2]);
-  ctx->last.kernel_launches = launches;
-  ctx->last.device_ms = ms;
-  if (out.error) return fail(ORION_ERR_DEVICE, "batch loop reached its iteration cap");
-  if (out.paths_done != total)
-    return fail(ORION_ERR_DEVICE, "batch finished " + std::to_string(out.paths_done) + " of " + std::to_string(total) +
-                                      " paths");
-  return ORION_OK;
-}
-
-static int run_batch_locked(orion_gpu_ctx* ctx, std::vector<DevJob>& dj, unsigned long long total, int max_depth_all,
-                            BatchCtl* out_ctl, float* ms_out) {
-  return ctx->batch_mode == ORION_BATCH_WAVES ? run_batch_waves_locked(ctx, dj, total, max_depth_all, out_ctl, ms_out)
-                                              : run_batch_pooled_locked(ctx, dj, total, max_depth_all, out_ctl, ms_out);
-}
-
-// Job table and film layout of a batch (films packed into one device block).
-static int plan_batch(orion_gpu_ctx* ctx, int32_t njobs, const orion_job* jobs, int spp_cap, std::vector<DevJob>& dj,
-                      std::vector<size_t>& film_off, size_t* film_bytes_out, unsigned long long* total_out,
-                      int* max_depth_out) {
-  dj.assign(njobs, DevJob{});
-  film_off.assign(njobs, 0);
-  size_t film_bytes = 0;
-  unsigned long long total = 0;
-  int max_depth_all = 0;
-  for (int i = 0; i < njobs; ++i) {
-    auto it = ctx->scenes.find(jobs[i].scene);
-    if (it == ctx->scenes.end()) return fail(ORION_ERR_INVALID, "job " + std::to_string(i) + ": unknown scene id");
-    const DeviceScene& d = *it->second;
-    const orion_render_params& p = jobs[i].params;
-    DevJob& J = dj[i];
-    std::memset(&J, 0, sizeof(J));
-    J.scene = d.view;
-    if (jobs[i].camera) {
-      if (jobs[i].camera->width <= 0 || jobs[i].camera->height <= 0)
-        return fail(ORION_ERR_INVALID, "job " + std::to_string(i) + ": film size must be positive");
-      J.scene.cam = prepare_camera(*jobs[i].camera);
-    }
-    J.width = J.scene.cam.width;
-    J.height = J.scene.cam.height;
-    int spp = p.spp > 0 ? p.spp : d.spp;
-    if (spp_cap > 0) spp = std::min(spp, spp_cap);
-    J.max_depth = p.max_depth >= 0 ? p.max_depth : d.max_depth;
-    J.rr_depth = p.rr_depth;
-    if (J.max_depth > 120 || 17 + 8 * (int64_t)J.max_depth > 1024)
-      return fail(ORION_ERR_INVALID, "job " + std::to_string(i) + ": max_depth out of range");
-    const long long wh = (long long)J.width * J.height;
-    J.first_index = p.first_pass * wh;
-    J.num_paths = wh * spp;
-    J.work_begin = (long long)total;
-    total += (unsigned long long)J.num_paths;
-    max_depth_all = std::max(max_depth_all, J.max_depth);
-    film_off[i] = film_bytes;
-    film_bytes += (size_t)((wh * (3 * 8 * 2 + 4) + 255) & ~255LL);
-  }
-  *film_bytes_out = film_bytes;
-  *total_out = total;
-  *max_depth_out = max_depth_all;
-  return ORION_OK;
-}
-
-extern "C" int orion_gpu_render_batch(orion_gpu_ctx* ctx, int32_t njobs, const orion_job* jobs,
-                                      orion_batch_stats* stats) {
-  if (!ctx || njobs < 0 || (njobs > 0 && !jobs)) return fail(ORION_ERR_INVALID, "bad argument");
-  std::lock_guard<std::mutex> g(ctx->mu);
-  CUDA_TRY(cudaSetDevice(ctx->device));
-  if (njobs == 0) {
-    if (stats) std::memset(stats, 0, sizeof(*stats));
-    return ORION_OK;
-  }
-  std::vector<DevJob> dj;
-  std::vector<size_t> film_off;
-  size_t film_bytes = 0;
-  unsigned long long total = 0;
-  int max_depth_all = 0;
-  RC(plan_batch(ctx, njobs, jobs, 0, dj, film_off, &film_bytes, &total, &max_depth_all));
-  int rc;
-  if (ctx->b_films.bytes < film_bytes && (rc = ctx->b_films.alloc(film_bytes)) != ORION_OK) return rc;
-  char* fb = ctx->b_films.as<char>();
-  for (int i = 0; i < njobs; ++i) {
-    const long long wh = (long long)dj[i].width * dj[i].height;
-    dj[i].sum = reinterpret_cast<double*>(fb + film_off[i]);
-    // Every pixel of a finished job has exactly its spp samples, so counts are
-    // written on the host, not counted on the device (one atomic per path less).
-    dj[i].count = nullptr;
-    // Sums of squares only for callers that want them (they cost 3 FP64 atomics per path).
-    dj[i].sumsq = jobs[i].sumsq ? dj[i].sum + 3 * wh : nullptr;
-  }
-  cudaStream_t s = ctx->stream;
-  CUDA_TRY(cudaMemsetAsync(ctx->b_films.p, 0, film_bytes, s));
-  BatchCtl out;
-  float ms = 0.f;
-  rc = run_batch_locked(ctx, dj, total, max_depth_all, &out, &ms);
-  if (rc != ORION_OK) return rc;
-  for (int i = 0; i < njobs; ++i) {
-    const size_t wh = (size_t)dj[i].width * dj[i].height;
-    if (jobs[i].sum) CUDA_TRY(cudaMemcpyAsync(jobs[i].sum, dj[i].sum, wh * 24, cudaMemcpyDeviceToHost, s));
-    if (jobs[i].sumsq) CUDA_TRY(cudaMemcpyAsync(jobs[i].sumsq, dj[i].sumsq, wh * 24, cudaMemcpyDeviceToHost, s));
-  }
-  for (int i = 0; i < njobs; ++i)
-    if (jobs[i].count) {
-      const size_t wh = (size_t)dj[i].width * dj[i].height;
-      std::fill(jobs[i].count, jobs[i].count + wh, (uint32_t)(dj[i].num_paths / (long long)wh));
-    }
-  CUDA_TRY(cudaStreamSynchronize(s));
-  if (stats) {
-    stats->paths = (int64_t)out.paths_done;
-    stats->rays = (int64_t)(out.rays[0] + out.rays[1] + out.rays[2]);
-    stats->iterations = out.iterations;
-    stats->capacity = ctx->wave.capacity;
-    stats->device_ms = ms;
-  }
   return ORION_OK;
 }
 
@@ -1319,57 +609,9 @@ int ctx_scene_info(orion_gpu_ctx* ctx, orion_scene_id id, int* width, int* heigh
   return ORION_OK;
 }
 
-int ctx_run_device_jobs(orion_gpu_ctx* ctx, const DeviceFilmJob* jobs, int njobs, double* device_ms,
-                        int64_t* paths) {
-  std::lock_guard<std::mutex> g(ctx->mu);
-  CUDA_TRY(cudaSetDevice(ctx->device));
-  std::vector<DevJob> dj(njobs);
-  unsigned long long total = 0;
-  int max_depth_all = 0;
-  for (int i = 0; i < njobs; ++i) {
-    auto it = ctx->scenes.find(jobs[i].scene);
-    if (it == ctx->scenes.end()) return fail(ORION_ERR_INVALID, "unknown scene id");
-    const DeviceScene& d = *it->second;
-    const orion_render_params& p = jobs[i].params;
-    DevJob& J = dj[i];
-    std::memset(&J, 0, sizeof(J));
-    J.scene = d.view;
-    if (jobs[i].camera) J.scene.cam = prepare_camera(*jobs[i].camera);
-    J.width = J.scene.cam.width;
-    J.height = J.scene.cam.height;
-    const int spp = p.spp > 0 ? p.spp : d.spp;
-    J.max_depth = p.max_depth >= 0 ? p.max_depth : d.max_depth;
-    J.rr_depth = p.rr_depth;
-    if (J.max_depth > 120) return fail(ORION_ERR_INVALID, "max_depth out of range");
-    const long long wh = (long long)J.width * J.height;
-    J.first_index = p.first_pass * wh;
-    J.num_paths = wh * spp;
-    J.work_begin = (long long)total;
-    total += (unsigned long long)J.num_paths;
-    max_depth_all = std::max(max_depth_all, J.max_depth);
-    J.sum = jobs[i].sum;
-    J.sumsq = jobs[i].sumsq;
-    J.count = jobs[i].count;
-  }
-  BatchCtl out;
-  float ms = 0.f;
-  int rc = run_batch_locked(ctx, dj, total, max_depth_all, &out, &ms);
-  if (device_ms) *device_ms = ms;
-  if (paths) *paths = (int64_t)out.paths_done;
-  return rc;
-}
-
 }  // namespace orion_gb300
 
 // ---------------------------------------------------- launch config, tuning
-
-extern "C" int orion_gpu_set_batch_mode(orion_gpu_ctx* ctx, int32_t mode) {
-  if (!ctx) return fail(ORION_ERR_INVALID, "null context");
-  if (mode != ORION_BATCH_POOLED && mode != ORION_BATCH_WAVES) return fail(ORION_ERR_INVALID, "unknown batch mode");
-  std::lock_guard<std::mutex> g(ctx->mu);
-  ctx->batch_mode = mode;
-  return ORION_OK;
-}
 
 extern "C" int orion_gpu_get_config(orion_gpu_ctx* ctx, orion_launch_config* out) {
   if (!ctx || !out) return fail(ORION_ERR_INVALID, "null argument");
@@ -1491,109 +733,6 @@ extern "C" int orion_gpu_autotune(orion_gpu_ctx* ctx, orion_scene_id id, int32_t
     best_out->streams = ctx->wave_streams;
   }
   if (best_mpaths) *best_mpaths = paths / (best_ms * 1e-3) / 1e6;
-  return ORION_OK;
-}
-
-extern "C" int orion_gpu_autotune_batch(orion_gpu_ctx* ctx, int32_t njobs, const orion_job* jobs, int32_t spp_cap,
-                                        double budget_ms, orion_launch_config* best_out, double* best_mpaths) {
-  if (!ctx || njobs <= 0 || !jobs) return fail(ORION_ERR_INVALID, "bad argument");
-  std::lock_guard<std::mutex> g(ctx->mu);
-  CUDA_TRY(cudaSetDevice(ctx->device));
-  std::vector<DevJob> dj;
-  std::vector<size_t> film_off;
-  size_t film_bytes = 0;
-  unsigned long long total = 0;
-  int max_depth_all = 0;
-  RC(plan_batch(ctx, njobs, jobs, spp_cap, dj, film_off, &film_bytes, &total, &max_depth_all));
-  DevBuf films;  // trial films: accumulated into and discarded
-  RC(films.alloc(film_bytes));
-  char* fb = films.as<char>();
-  for (int i = 0; i < njobs; ++i) {
-    const long long wh = (long long)dj[i].width * dj[i].height;
-    dj[i].sum = reinterpret_cast<double*>(fb + film_off[i]);
-    dj[i].sumsq = dj[i].sum + 3 * wh;
-    dj[i].count = reinterpret_cast<unsigned int*>(dj[i].sumsq + 3 * wh);
-  }
-  CUDA_TRY(cudaMemsetAsync(films.p, 0, film_bytes, ctx->stream));
-  // batch_slots is the pool size (pooled mode) or the wave size (wave mode).
-  LaunchConfig best = ctx->cfg;
-  int best_slots = ctx->default_batch_slots;
-  int best_streams = ctx->wave_streams, best_mode = ctx->batch_mode;
-  double best_ms = 1e30, used = 0;
-  auto trial = [&](const LaunchConfig& c, int slots, int streams, int mode, double* ms) -> int {
-    LaunchConfig saved = ctx->cfg;
-    int saved_slots = ctx->default_batch_slots, saved_streams = ctx->wave_streams;
-    int saved_mode = ctx->batch_mode;
-    ctx->cfg = c;
-    ctx->default_batch_slots = slots;
-    ctx->wave_streams = streams;
-    ctx->batch_mode = mode;
-    BatchCtl out;
-    float fms = 0.f;
-    int rc = run_batch_locked(ctx, dj, total, max_depth_all, &out, &fms);
-    ctx->cfg = saved;
-    ctx->default_batch_slots = saved_slots;
-    ctx->wave_streams = saved_streams;
-    ctx->batch_mode = saved_mode;
-    *ms = fms;
-    used += fms;
-    return rc;
-  };
-  double ms;
-  RC(trial(best, best_slots, best_streams, best_mode, &ms));  // warm-up (graph instantiation)
-  RC(trial(best, best_slots, best_streams, best_mode, &best_ms));
-  const int trace_blocks[] = {64, 128, 256};
-  const int stacks[] = {8, 16, 32};
-  const int shade_blocks[] = {64, 128, 256};
-  const int bpsm[] = {4, 8, 16};
-  const int slot_counts[] = {1 << 22, 1 << 23, 1 << 24, 1 << 25};
-  const int refills[] = {8, 16, 24, 32};
-  const int engine_counts[] = {1, 2};
-  const int modes[] = {ORION_BATCH_POOLED, ORION_BATCH_WAVES};
-  for (int knob = 0; knob < 8 && used < budget_ms; ++knob) {
-    const int n = knob >= 6 ? 2 : (knob >= 4 ? 4 : 3);
-    for (int v = 0; v < n && used < budget_ms; ++v) {
-      LaunchConfig c = best;
-      int slots = best_slots, streams = best_streams, mode = best_mode;
-      if (knob == 0) c.trace_block = trace_blocks[v];
-      if (knob == 1) c.smem_stack = stacks[v];
-      if (knob == 2) c.shade_block = shade_blocks[v];
-      if (knob == 3) c.blocks_per_sm = bpsm[v];
-      if (knob == 4) slots = slot_counts[v];
-      if (knob == 5) c.refill_below = refills[v];
-      if (knob == 6) streams = engine_counts[v];
-      if (knob == 7) mode = modes[v];
-      if (std::memcmp(&c, &best, sizeof(c)) == 0 && slots == best_slots && streams == best_streams &&
-          mode == best_mode)
-        continue;
-      if (!config_problem(ctx, c).empty()) continue;
-      int rc = trial(c, slots, streams, mode, &ms);
-      if (rc == ORION_ERR_NOMEM) continue;
-      if (rc != ORION_OK) return rc;
-      if (ms < best_ms) {
-        best_ms = ms;
-        best = c;
-        best_slots = slots;
-        best_streams = streams;
-        best_mode = mode;
-      }
-    }
-  }
-  ctx->cfg = best;
-  ctx->default_batch_slots = best_slots;
-  ctx->wave_streams = best_streams;
-  ctx->batch_mode = best_mode;
-  if (best_out) {
-    best_out->trace_block = best.trace_block;
-    best_out->shade_block = best.shade_block;
-    best_out->smem_stack = best.smem_stack;
-    best_out->blocks_per_sm = best.blocks_per_sm;
-    best_out->wave_paths = ctx->default_wave;
-    best_out->batch_slots = best_slots;
-    best_out->refill_below = best.refill_below;
-    best_out->streams = ctx->wave_streams;
-  }
-  if (best_mpaths) *best_mpaths = (double)total / (best_ms * 1e-3) / 1e6;
   return ORION_OK;
 }
 
