@@ -135,6 +135,7 @@ def measured_peaks() -> dict:
 
 # Algorithmic bytes per unit of work (one ray or one path), independent of
 # BVH quality: what the stage must read and write at minimum.
+NODE_BYTES, TRI_BYTES = 80, 48  # one 8-wide BVH node; one Woop triangle
 ALG_BYTES = {
     "trace_ext": 32 + 16,      # ray in (o, d), hit out (t, u, v, prim)
     "trace_shadow": 32 + 4,    # ray in, occlusion flag out
@@ -254,6 +255,24 @@ def run_ours(args) -> dict:
                 "peak_source": peaks["source"],
                 "alg_bytes_per_unit": ALG_BYTES[top], "units": int(units[top]),
                 "launches": stages[top]["launches"], "stage_ms": round(stages[top]["ms"], 3)}
+    # Model bytes: BVH nodes (80 B) and triangles (48 B) the trace kernels
+    # fetch, counted on the device over the workload's first sample pass
+    # (1/spp of its paths, every bounce); per ray, then scaled to the timed
+    # render's rays of the top kernel's kind.
+    kind = {"trace_ext": "ext", "trace_shadow": "shadow", "trace_mis": "mis"}.get(top)
+    ctx.set_profiling(og.PROFILE_TRAVERSAL)
+    ctx.render(sid, W, H, spp=1, first_pass=first)
+    work = ctx.traversal_work()
+    ctx.set_profiling(False)
+    per_ray = {k: {"nodes": round(w["nodes"] / w["rays"], 2), "triangles": round(w["triangles"] / w["rays"], 2)}
+               for k, w in work.items() if w["rays"]}
+    model = {"sample": f"1 of {spp} sample passes ({work['ext']['rays']} extension rays), counted on the device",
+             "per_ray": per_ray, "node_bytes": NODE_BYTES, "triangle_bytes": TRI_BYTES}
+    if kind in per_ray:
+        mb = (NODE_BYTES * per_ray[kind]["nodes"] + TRI_BYTES * per_ray[kind]["triangles"]) * units[top]
+        model.update({"kernel": top, "bytes_per_launch": int(mb / max(stages[top]["launches"], 1)),
+                      "achieved_gbs": round(mb / (stages[top]["ms"] * 1e-3) / 1e9, 1)})
+    roofline["model"] = model
 
     out = {
         "metric": METRIC, "value": round(value, 3), "unit": "Mpaths/s", "n_gpus": world, "steps": args.steps,

@@ -250,8 +250,27 @@ typedef struct orion_stage_times {
   double ms[ORION_NUM_STAGES];
   int64_t launches[ORION_NUM_STAGES];
 } orion_stage_times;
+/* `enable` is a bit set: ORION_PROFILE_STAGES times every stage as above;
+ * ORION_PROFILE_TRAVERSAL makes plain renders count the BVH work of their
+ * trace kernels (same traversal and film, slower kernels), read back with
+ * orion_gpu_traversal_work. 0 turns both off. */
+#define ORION_PROFILE_STAGES 1
+#define ORION_PROFILE_TRAVERSAL 2
 int orion_gpu_set_profiling(orion_gpu_ctx* ctx, int32_t enable);
 int orion_gpu_stage_times(orion_gpu_ctx* ctx, orion_stage_times* out);
+
+/* BVH work of the last plain render made with ORION_PROFILE_TRAVERSAL (all
+ * zero otherwise), per ray kind [extension, shadow, MIS]: rays traced,
+ * 8-wide nodes visited (80 bytes each) and triangles tested (48 bytes each).
+ * Embree's traversal inside EmbreeKernel::intersect (src/core/kernel.cpp:111)
+ * has no counterpart; these figures explain the trace kernels' memory
+ * traffic. */
+typedef struct orion_traversal_work {
+  int64_t rays[3];
+  int64_t nodes[3];
+  int64_t triangles[3];
+} orion_traversal_work;
+int orion_gpu_traversal_work(orion_gpu_ctx* ctx, orion_traversal_work* out);
 
 /* ----------------------------------------------------------- film output */
 /* saveAsBmp (src/core/texture.cpp:77-136): the averaged film `rgb`

@@ -32,6 +32,7 @@ ERRORS = {-1: "invalid", -2: "io", -3: "parse", -4: "cuda", -5: "nomem", -6: "un
 MAT_MATTE, MAT_METAL, MAT_MIRROR, MAT_GLASS, MAT_PLASTIC, MAT_UBER = range(6)
 INTEGRATOR_PATH, INTEGRATOR_SPPM = 0, 1
 BATCH_POOLED, BATCH_WAVES = 0, 1
+PROFILE_STAGES, PROFILE_TRAVERSAL = 1, 2
 DIST_GGX, DIST_BECKMANN = 0, 1
 LIGHT_AREA, LIGHT_POINT, LIGHT_SPOT, LIGHT_DISTANT, LIGHT_ENV = range(5)
 NOALLOC_MAX_RAYS = 65536  # ORION_NOALLOC_MAX_RAYS
@@ -101,6 +102,10 @@ class StageTimes(C.Structure):
     _fields_ = [("ms", C.c_double * 8), ("launches", C.c_int64 * 8)]
 
 
+class TraversalWork(C.Structure):
+    _fields_ = [("rays", C.c_int64 * 3), ("nodes", C.c_int64 * 3), ("triangles", C.c_int64 * 3)]
+
+
 STAGES = ("camera", "trace_ext", "shade", "trace_shadow", "trace_mis", "resolve", "film", "other")
 
 
@@ -165,6 +170,7 @@ def library() -> C.CDLL:
             "orion_gpu_last_stats": (i32, [vp, C.POINTER(RenderStats)]),
             "orion_gpu_set_profiling": (i32, [vp, i32]),
             "orion_gpu_stage_times": (i32, [vp, C.POINTER(StageTimes)]),
+            "orion_gpu_traversal_work": (i32, [vp, C.POINTER(TraversalWork)]),
             "orion_film_write_bmp": (i32, [C.c_char_p, i32, i32, vp]),
             "orion_gpu_render_batch": (i32, [vp, i32, vp, C.POINTER(BatchStats)]),
             "orion_gpu_get_config": (i32, [vp, C.POINTER(LaunchConfig)]),
@@ -366,8 +372,16 @@ class Context:
         _check(library().orion_gpu_last_stats(self._h, C.byref(s)))
         return {k: getattr(s, k) for k, _ in RenderStats._fields_}
 
-    def set_profiling(self, on: bool) -> None:
+    def set_profiling(self, on: bool | int) -> None:
+        """True or PROFILE_STAGES: per-stage times; PROFILE_TRAVERSAL: count BVH work; False: off."""
         _check(library().orion_gpu_set_profiling(self._h, int(on)))
+
+    def traversal_work(self) -> dict:
+        """BVH work of the last plain render made under PROFILE_TRAVERSAL, per ray kind."""
+        t = TraversalWork()
+        _check(library().orion_gpu_traversal_work(self._h, C.byref(t)))
+        return {kind: {"rays": t.rays[i], "nodes": t.nodes[i], "triangles": t.triangles[i]}
+                for i, kind in enumerate(("ext", "shadow", "mis"))}
 
     def stage_times(self) -> dict:
         t = StageTimes()

@@ -175,8 +175,9 @@ int orion_gb300::alloc_wave(Wave& wave, int capacity) {
   p += kShadeClasses * i4;
   w.counters = reinterpret_cast<int*>(p);
   p += 128;
-  w.ray_stats = reinterpret_cast<unsigned long long*>(p);
-  p += 64;
+  w.ray_stats = reinterpret_cast<unsigned long long*>(p);  // [0, 3) rays, [4, 10) traversal work
+  w.trace_work = nullptr;
+  p += 128;
   w.error_word = reinterpret_cast<int*>(p);
   w.capacity = capacity;
   wave.capacity = capacity;
@@ -448,8 +449,9 @@ static int render_impl(orion_gpu_ctx* ctx, orion_scene_id id, const orion_render
     CUDA_TRY(cudaMemsetAsync(ctx->film64.p, 0, wh * 3 * sizeof(double), s));
     CUDA_TRY(cudaMemsetAsync(ctx->filmsq64.p, 0, wh * 3 * sizeof(double), s));
   }
+  const bool count_work = ctx->count_work;
   for (int i = 0; i < ns; ++i) {
-    CUDA_TRY(cudaMemsetAsync(wave_view(i).ray_stats, 0, 3 * sizeof(unsigned long long), s));
+    CUDA_TRY(cudaMemsetAsync(wave_view(i).ray_stats, 0, 10 * sizeof(unsigned long long), s));
     CUDA_TRY(cudaMemsetAsync(wave_view(i).error_word, 0, sizeof(int), s));
   }
   FilmView film{ctx->film_sum.as<float>(), ctx->film_count.as<uint32_t>(), fp64 ? ctx->film64.as<double>() : nullptr,
@@ -487,8 +489,10 @@ static int render_impl(orion_gpu_ctx* ctx, orion_scene_id id, const orion_render
     a.class_mask = d.class_mask;
     const cudaEvent_t film_wait = ns > 1 && k > 0 ? ctx->ev_film[(k - 1) % ns] : nullptr;
     const cudaEvent_t film_done = ns > 1 ? ctx->ev_film[k % ns] : nullptr;
-    launch_wave(d.view, wave_view(slot), a, film, ctx->cfg, wave_stream(slot), &launches,
-                ctx->profiling ? &timer : nullptr, film_wait, film_done);
+    WaveView wv = wave_view(slot);
+    if (count_work) wv.trace_work = wv.ray_stats + 4;
+    launch_wave(d.view, wv, a, film, ctx->cfg, wave_stream(slot), &launches, ctx->profiling ? &timer : nullptr,
+                film_wait, film_done);
   }
   CUDA_TRY(cudaGetLastError());
   for (int i = 1; i < ns; ++i) {
@@ -504,17 +508,17 @@ static int render_impl(orion_gpu_ctx* ctx, orion_scene_id id, const orion_render
     CUDA_TRY(cudaMemcpyAsync(sum64, ctx->film64.p, wh * 3 * sizeof(double), cudaMemcpyDeviceToHost, s));
     CUDA_TRY(cudaMemcpyAsync(sumsq64, ctx->filmsq64.p, wh * 3 * sizeof(double), cudaMemcpyDeviceToHost, s));
   }
-  unsigned long long wstats[kMaxWaveStreams][3] = {};
+  unsigned long long wstats[kMaxWaveStreams][10] = {};
   int werr[kMaxWaveStreams] = {};
   for (int i = 0; i < ns; ++i) {
     CUDA_TRY(cudaMemcpyAsync(wstats[i], wave_view(i).ray_stats, sizeof(wstats[i]), cudaMemcpyDeviceToHost, s));
     CUDA_TRY(cudaMemcpyAsync(&werr[i], wave_view(i).error_word, sizeof(int), cudaMemcpyDeviceToHost, s));
   }
   CUDA_TRY(cudaStreamSynchronize(s));
-  unsigned long long stats[3] = {0, 0, 0};
+  unsigned long long stats[10] = {};
   int err_word = 0;
   for (int i = 0; i < ns; ++i) {
-    for (int j = 0; j < 3; ++j) stats[j] += wstats[i][j];
+    for (int j = 0; j < 10; ++j) stats[j] += wstats[i][j];
     err_word = err_word ? err_word : werr[i];
   }
   float ms = 0.f;
@@ -526,6 +530,13 @@ static int render_impl(orion_gpu_ctx* ctx, orion_scene_id id, const orion_render
   ctx->last.rays = (int64_t)(stats[0] + stats[1] + stats[2]);
   ctx->last.kernel_launches = launches;
   ctx->last.device_ms = ms;
+  std::memset(&ctx->last_work, 0, sizeof(ctx->last_work));
+  if (count_work)
+    for (int j = 0; j < 3; ++j) {
+      ctx->last_work.rays[j] = (int64_t)stats[j];
+      ctx->last_work.nodes[j] = (int64_t)stats[4 + j];
+      ctx->last_work.triangles[j] = (int64_t)stats[7 + j];
+    }
   std::memset(&ctx->stage_times, 0, sizeof(ctx->stage_times));
   for (int i = 0; i < std::min(timer.used, timer.capacity); ++i) {
     float e = 0.f;
@@ -557,7 +568,15 @@ extern "C" int orion_gpu_last_stats(orion_gpu_ctx* ctx, orion_render_stats* out)
 extern "C" int orion_gpu_set_profiling(orion_gpu_ctx* ctx, int32_t enable) {
   if (!ctx) return fail(ORION_ERR_INVALID, "null context");
   std::lock_guard<std::mutex> g(ctx->mu);
-  ctx->profiling = enable != 0;
+  ctx->profiling = (enable & ORION_PROFILE_STAGES) != 0;
+  ctx->count_work = (enable & ORION_PROFILE_TRAVERSAL) != 0;
+  return ORION_OK;
+}
+
+extern "C" int orion_gpu_traversal_work(orion_gpu_ctx* ctx, orion_traversal_work* out) {
+  if (!ctx || !out) return fail(ORION_ERR_INVALID, "null argument");
+  std::lock_guard<std::mutex> g(ctx->mu);
+  *out = ctx->last_work;
   return ORION_OK;
 }
 

@@ -156,6 +156,8 @@ struct orion_gpu_ctx {
   int default_wave = 1 << 25;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
   bool profiling = false;
+  bool count_work = false;  // plain renders count BVH node visits and triangle tests
+  orion_traversal_work last_work{};
   std::vector<cudaEvent_t> prof_events;
   std::vector<int> prof_stage;
   orion_stage_times stage_times{};

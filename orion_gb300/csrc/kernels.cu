@@ -50,25 +50,28 @@ __global__ void k_camera(SceneView s, WaveView w, WaveArgs a) {
 
 // Closest hit: extension rays (RayView = RecF4, hits into the path records,
 // slots sorted by shading class) or MIS rays (NeeF4, hits into mis_hit).
-template <int SMEM, class RayView, class HitView>
+// COUNT: the same traversal, adding its node visits and triangle tests to
+// work[0] and work[3] (a diagnostic render; see WaveView::trace_work).
+template <int SMEM, class RayView, class HitView, bool COUNT = false>
 __global__ void __launch_bounds__(512, 2)
     k_trace(SceneView s, const int* queue, const int* count, int* fetch, RayView ray_o, RayView ray_d, HitView hit,
-            unsigned long long* stat, int refill_below, int* cls_counters, int* q_cls, int cls_stride) {
+            unsigned long long* stat, int refill_below, int* cls_counters, int* q_cls, int cls_stride,
+            unsigned long long* work) {
   extern __shared__ int2 stack_smem[];
   const int n = *count;
-  trace_persistent<false, SMEM>(SingleScene{&s}, queue, n, fetch, ray_o, ray_d, hit, nullptr, stack_smem,
-                                refill_below, cls_counters, q_cls, cls_stride);
+  trace_persistent<false, SMEM, COUNT>(SingleScene{&s}, queue, n, fetch, ray_o, ray_d, hit, nullptr, stack_smem,
+                                       refill_below, cls_counters, q_cls, cls_stride, work);
   if (stat && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(stat, (unsigned long long)n);
 }
 
-template <int SMEM>
+template <int SMEM, bool COUNT = false>
 __global__ void __launch_bounds__(512, 2)
     k_trace_sh(SceneView s, const int* queue, const int* count, int* fetch, NeeF4 ray_o, NeeF4 ray_d, int* occluded,
-               unsigned long long* stat, int refill_below) {
+               unsigned long long* stat, int refill_below, unsigned long long* work) {
   extern __shared__ int2 stack_smem[];
   const int n = *count;
-  trace_persistent<true, SMEM>(SingleScene{&s}, queue, n, fetch, ray_o, ray_d, F4{nullptr}, occluded, stack_smem,
-                               refill_below);
+  trace_persistent<true, SMEM, COUNT>(SingleScene{&s}, queue, n, fetch, ray_o, ray_d, F4{nullptr}, occluded,
+                                      stack_smem, refill_below, nullptr, nullptr, 0, work);
   if (stat && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(stat, (unsigned long long)n);
 }
 
@@ -237,32 +240,39 @@ int grid_for(int64_t n, int block, int max_blocks) {
 
 enum TraceKind { TK_EXT = 0, TK_SHADOW = 1, TK_MIS = 2, TK_MIS_ENV = 3 };
 
-template <int SMEM>
+template <int SMEM, bool COUNT = false>
 void launch_trace_kernels(int kind, const SceneView& s, const WaveView& w, int cur, const LaunchConfig& cfg,
                           int grid, cudaStream_t stream) {
   const int block = cfg.trace_block;
   const int refill = cfg.refill_below < 1 ? 1 : (cfg.refill_below > 32 ? 32 : cfg.refill_below);
   size_t smem = (size_t)SMEM * block * sizeof(int2);
+  unsigned long long* work = w.trace_work;  // nodes[ext, shadow, mis], then tris[ext, shadow, mis]
   if (kind == TK_EXT)
-    k_trace<SMEM, RecF4, RecF4><<<grid, block, smem, stream>>>(
+    k_trace<SMEM, RecF4, RecF4, COUNT><<<grid, block, smem, stream>>>(
         s, w.q_ext[cur], w.counters + cur, w.counters + CNT_FETCH_EXT, w.ray_o, w.ray_d, w.hit, w.ray_stats, refill,
-        w.counters + CNT_CLS0, w.q_cls, w.capacity);
+        w.counters + CNT_CLS0, w.q_cls, w.capacity, work);
   else if (kind == TK_SHADOW)
-    k_trace_sh<SMEM><<<grid, block, smem, stream>>>(s, w.q_sh, w.counters + CNT_SH, w.counters + CNT_FETCH_SH, w.sh_o,
-                                                    w.sh_d, w.occluded, w.ray_stats + 1, refill);
+    k_trace_sh<SMEM, COUNT><<<grid, block, smem, stream>>>(s, w.q_sh, w.counters + CNT_SH,
+                                                           w.counters + CNT_FETCH_SH, w.sh_o, w.sh_d, w.occluded,
+                                                           w.ray_stats + 1, refill, COUNT ? work + 1 : nullptr);
   else if (kind == TK_MIS_ENV)
-    k_trace_sh<SMEM><<<grid, block, smem, stream>>>(s, w.q_mis_env, w.counters + CNT_MIS_ENV,
-                                                    w.counters + CNT_FETCH_MIS_ENV, w.mis_o, w.mis_d,
-                                                    w.mis_occluded, w.ray_stats + 2, refill);
+    k_trace_sh<SMEM, COUNT><<<grid, block, smem, stream>>>(s, w.q_mis_env, w.counters + CNT_MIS_ENV,
+                                                           w.counters + CNT_FETCH_MIS_ENV, w.mis_o, w.mis_d,
+                                                           w.mis_occluded, w.ray_stats + 2, refill,
+                                                           COUNT ? work + 2 : nullptr);
   else
-    k_trace<SMEM, NeeF4, F4><<<grid, block, smem, stream>>>(s, w.q_mis, w.counters + CNT_MIS,
-                                                            w.counters + CNT_FETCH_MIS, w.mis_o, w.mis_d,
-                                                            F4{w.mis_hit}, w.ray_stats + 2, refill, nullptr,
-                                                            nullptr, 0);
+    k_trace<SMEM, NeeF4, F4, COUNT><<<grid, block, smem, stream>>>(s, w.q_mis, w.counters + CNT_MIS,
+                                                                   w.counters + CNT_FETCH_MIS, w.mis_o, w.mis_d,
+                                                                   F4{w.mis_hit}, w.ray_stats + 2, refill, nullptr,
+                                                                   nullptr, 0, COUNT ? work + 2 : nullptr);
 }
 
 void trace_dispatch(int kind, const SceneView& s, const WaveView& w, int cur, const LaunchConfig& cfg, int grid,
                     cudaStream_t stream) {
+  if (w.trace_work) {  // counting render: the stack's split between shared and local memory is irrelevant
+    launch_trace_kernels<0, true>(kind, s, w, cur, cfg, grid, stream);
+    return;
+  }
   switch (cfg.smem_stack) {
     case 0: launch_trace_kernels<0>(kind, s, w, cur, cfg, grid, stream); break;
     case 8: launch_trace_kernels<8>(kind, s, w, cur, cfg, grid, stream); break;
@@ -389,7 +399,9 @@ cudaError_t configure_kernels(int smem_bytes, KernelLimits* lim) {
       (const void*)k_trace<24, NeeF4, F4>,    (const void*)k_trace<32, NeeF4, F4>,
       (const void*)k_trace_sh<0>,             (const void*)k_trace_sh<8>,
       (const void*)k_trace_sh<16>,            (const void*)k_trace_sh<24>,
-      (const void*)k_trace_sh<32>,            (const void*)k_trace_rays<16>};
+      (const void*)k_trace_sh<32>,            (const void*)k_trace_rays<16>,
+      (const void*)k_trace<0, RecF4, RecF4, true>, (const void*)k_trace<0, NeeF4, F4, true>,
+      (const void*)k_trace_sh<0, true>};
   const void* shade[] = {(const void*)k_shade<SC_DIFFUSE>, (const void*)k_shade<SC_CONDUCTOR>,
                          (const void*)k_shade<SC_SPECULAR>, (const void*)k_shade<SC_DIELECTRIC>,
                          (const void*)k_shade<SC_PLASTIC>, (const void*)k_shade<SC_GENERAL>, (const void*)k_shade<SC_TEXTURED>,

@@ -92,6 +92,9 @@ struct WaveView {
   int* q_cls;        // extension hits by shading class: kShadeClasses queues of `capacity`
   int* counters;     // kCounterSlots ints
   unsigned long long* ray_stats;  // ext, shadow, mis
+  // Null, or (a counting render) 6 counters the trace kernels add to: node
+  // visits of the extension, shadow and MIS rays, then their triangle tests.
+  unsigned long long* trace_work;
   int* error_word;
   int capacity;
 };

@@ -349,12 +349,14 @@ struct JobScene {
 // counter that must be zero at launch. Block size must be a multiple of 32.
 // With `q_cls` (closest hit only), each finished ray's slot is also appended
 // to the queue of the shading class of what it hit (SC_MISS for a miss).
-template <bool ANY, int SMEM, class SceneOf, class RayView, class HitView>
+// COUNT adds the kernel's node visits to work[0] and its triangle tests to
+// work[3].
+template <bool ANY, int SMEM, bool COUNT = false, class SceneOf, class RayView, class HitView>
 __device__ __forceinline__ void trace_persistent(const SceneOf& scene_of, const int* queue, int n, int* fetch,
                                                  RayView ray_o, RayView ray_d, HitView hit, int* occluded,
                                                  int2* stack_smem, int refill_below,
                                                  int* cls_counters = nullptr, int* q_cls = nullptr,
-                                                 int cls_stride = 0) {
+                                                 int cls_stride = 0, unsigned long long* work = nullptr) {
   constexpr unsigned kFull = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   TraversalStack<SMEM> st;
@@ -364,6 +366,7 @@ __device__ __forceinline__ void trace_persistent(const SceneOf& scene_of, const 
   TraceScene ts{nullptr, nullptr, nullptr, nullptr};
   int pid = -1;
   bool active = false, exhausted = false;
+  TraceWork wk;
   while (true) {
     unsigned act = __ballot_sync(kFull, active);
     if (!exhausted && __popc(act) < refill_below) {
@@ -392,7 +395,7 @@ __device__ __forceinline__ void trace_persistent(const SceneOf& scene_of, const 
       continue;
     }
     if (active) {
-      if (lane_step<ANY, SMEM>(r, ts, st)) {
+      if (lane_step<ANY, SMEM, COUNT>(r, ts, st, &wk)) {
         if (ANY) {
           occluded[pid] = r.tri >= 0;
         } else {
@@ -404,6 +407,16 @@ __device__ __forceinline__ void trace_persistent(const SceneOf& scene_of, const 
         }
         active = false;
       }
+    }
+  }
+  if (COUNT) {  // the loop ends for the whole warp at once (act and exhausted are warp-uniform)
+    for (int o = 16; o > 0; o >>= 1) {
+      wk.nodes += __shfl_down_sync(kFull, wk.nodes, o);
+      wk.tris += __shfl_down_sync(kFull, wk.tris, o);
+    }
+    if (lane == 0) {
+      atomicAdd(work, wk.nodes);
+      atomicAdd(work + 3, wk.tris);
     }
   }
 }

@@ -278,14 +278,22 @@ __device__ __forceinline__ void lane_start(LaneRay& r, float4 o4, float4 d4, flo
   r.tg = make_uint2(0u, 0u);
 }
 
+// Node visits and triangle tests of one lane (COUNT instantiations only).
+struct TraceWork {
+  unsigned long long nodes = 0, tris = 0;
+};
+
 // One node visit and its triangles. Returns true when the lane's ray is done:
-// its stack ran empty, or (ANY) a hit was found.
-template <bool ANY, int SMEM>
-__device__ __forceinline__ bool lane_step(LaneRay& r, const TraceScene& s, TraversalStack<SMEM>& st) {
+// its stack ran empty, or (ANY) a hit was found. COUNT adds the node visit
+// and the triangle tests to `wk`; the traversal itself is the same.
+template <bool ANY, int SMEM, bool COUNT = false>
+__device__ __forceinline__ bool lane_step(LaneRay& r, const TraceScene& s, TraversalStack<SMEM>& st,
+                                          TraceWork* wk = nullptr) {
   if (r.ng.y > 0x00ffffffu) {
     const int child = take_child(r.ng, r.oct);
     if (r.ng.y) st.push(make_int2((int)r.ng.x, (int)r.ng.y));
     wide_node(s.nodes, child, r.o, r.idir, r.oct, r.tnear, r.tmax, r.ng, r.tg);
+    if (COUNT) ++wk->nodes;
   } else {
     r.tg = r.ng;
     r.ng = make_uint2(0u, 0u);
@@ -299,6 +307,7 @@ __device__ __forceinline__ bool lane_step(LaneRay& r, const TraceScene& s, Trave
     const int k = (int)r.tg.x + __ffs(r.tg.y) - 1;
     r.tg.y &= r.tg.y - 1u;
     float t, u, v;
+    if (COUNT) ++wk->tris;
     if (woop_hit(s.woop, k, r.o, r.d, r.tnear, r.tmax, &t, &u, &v)) {
       if (ANY) {
         r.tmax = t;

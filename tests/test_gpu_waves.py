@@ -53,3 +53,34 @@ def test_film_independent_of_waves_and_streams(ctx, scene):
     again, _ = ctx.render(scene, 48, 48, wave_paths=4096)
     assert np.array_equal(again.view(np.uint32), ref.view(np.uint32))
     assert ctx.last_stats()["rays"] == st["rays"]
+
+
+def test_traversal_work_counts(ctx, scene):
+    """A counting render traces the same rays into the same film and reports
+    per-kind BVH work: every ray visits the root node at least."""
+    import orion_gb300 as og
+    ref, _ = ctx.render(scene, 48, 48, wave_paths=4096)
+    assert all(v == 0 for k in ctx.traversal_work().values() for v in k.values())
+    ctx.set_profiling(og.PROFILE_TRAVERSAL)
+    try:
+        img, _ = ctx.render(scene, 48, 48, wave_paths=4096)
+        st = ctx.last_stats()
+        work = ctx.traversal_work()
+        ctx.set_profiling(og.PROFILE_STAGES | og.PROFILE_TRAVERSAL)
+        both, _ = ctx.render(scene, 48, 48, wave_paths=4096)
+        assert ctx.stage_times()["trace_ext"]["launches"] > 0
+        assert ctx.traversal_work()["ext"]["rays"] == work["ext"]["rays"]
+    finally:
+        ctx.set_profiling(False)
+    assert np.array_equal(img.view(np.uint32), ref.view(np.uint32))
+    assert np.array_equal(both.view(np.uint32), ref.view(np.uint32))
+    assert work["ext"]["rays"] == st["ext_rays"]
+    assert work["shadow"]["rays"] == st["shadow_rays"]
+    assert work["mis"]["rays"] == st["mis_rays"]
+    for kind, w in work.items():
+        if w["rays"]:
+            assert w["nodes"] >= w["rays"], kind
+            assert w["triangles"] > 0, kind
+            assert w["nodes"] < 10_000 * w["rays"], kind
+    ctx.render(scene, 48, 48, wave_paths=4096)
+    assert ctx.traversal_work()["ext"]["nodes"] == 0
