@@ -15,7 +15,7 @@
 
 namespace orion_gb300 {
 
-constexpr int kMaxStack = 96;  // >= wide-tree depth (< 48) + postponed triangle groups (< 40) + 1
+constexpr int kMaxStack = 96;  // >= wide-tree depth (< 48) + 1
 
 struct TraceScene {
   const float4* __restrict__ nodes;  // 5 float4 per WideNode
@@ -94,12 +94,10 @@ __device__ __forceinline__ bool woop_hit(const float4* __restrict__ woop, int k,
 //                  so taking the lowest bit first visits them roughly near
 //                  to far;
 //   triangle group (tri_base, mask): the triangles of the hit leaf children.
-// A stack entry is a node group (top byte non-zero) or a postponed triangle
-// group (top byte zero). The root is the single internal child of a virtual
-// group.
+// A stack entry is a node group (top byte non-zero); an entry with a zero
+// top byte would be taken as a triangle group. The root is the single
+// internal child of a virtual group.
 
-constexpr int kPostponeLanes = 6;   // fewer lanes than this testing triangles: postpone them
-constexpr int kPostponeDepth = 40;  // postpone only while the stack is shallower than this
 
 // Octant of a ray from the signs of its reciprocal direction (never zero,
 // see safe_inv), so the near-plane choice agrees with the slab arithmetic
@@ -248,9 +246,10 @@ __device__ __forceinline__ RayHit traverse(const TraceScene& s, V3 o, V3 d, floa
 //
 // The kernels below trace a queue of rays with warps that stay resident.
 // Each loop iteration visits one node per lane and then tests the triangles
-// it yielded; when fewer than kPostponeLanes lanes of the warp have triangles
-// to test, they push the triangle group and keep descending instead, so the
-// warp's lanes stay busy with node visits together. When fewer than
+// it yielded. (Postponing the triangles of lanes that are few in their warp,
+// to keep descending with the rest, was measured 11% slower on the 8-wide
+// tree: a leaf visit costs about as much as the node visits it waits for.)
+// When fewer than
 // `refill_below` lanes still hold a ray, the warp takes new rays for its idle
 // lanes from the queue with one atomicAdd. Warp votes only steer scheduling;
 // each ray's result does not depend on them.
@@ -299,11 +298,6 @@ __device__ __forceinline__ bool lane_step(LaneRay& r, const TraceScene& s, Trave
     r.ng = make_uint2(0u, 0u);
   }
   while (r.tg.y != 0u) {
-    if (r.ng.y != 0u && st.sp < kPostponeDepth && __popc(__activemask()) < kPostponeLanes) {
-      st.push(make_int2((int)r.tg.x, (int)r.tg.y));
-      r.tg.y = 0u;
-      break;
-    }
     const int k = (int)r.tg.x + __ffs(r.tg.y) - 1;
     r.tg.y &= r.tg.y - 1u;
     float t, u, v;
