@@ -132,25 +132,35 @@ class Scene:
         return s, q
 
 
-def time_sample(path: str, threads: int, seconds: float = 15.0) -> dict:
+def time_sample(path: str, threads: int, seconds: float = 15.0, runs: int = 3) -> dict:
     """Mpaths/s of the CPU oracle on a band of image rows at the scene's spp.
 
-    The band grows until one render takes about `seconds` / 4, then the
-    measured band is rendered once more and timed.
+    The band grows until one render takes about `seconds` / (runs + 2); the
+    measured band is then rendered `runs` more times and the median time is
+    reported.
     """
     sc = Scene.load(path)
     rows = 1
+    target = seconds / (runs + 2)
+
+    def band(n):  # n rows from the middle of the image, moved up to stay inside it
+        r0 = max(0, min(sc.height // 2, sc.height - n))
+        return (r0, r0 + n)
+
     while True:
         t = time.time()
-        sc.render(rows=(sc.height // 2, sc.height // 2 + rows), threads=threads)
+        sc.render(rows=band(rows), threads=threads)
         dt = time.time() - t
-        if dt > seconds / 4 or rows >= sc.height:
+        if dt > target or rows >= sc.height:
             break
-        rows = min(sc.height, max(rows * 2, int(rows * (seconds / 4) / max(dt, 1e-3))))
-    t = time.time()
-    _, rays = sc.render(rows=(sc.height // 2, sc.height // 2 + rows), threads=threads)
-    dt = time.time() - t
+        rows = min(sc.height, max(rows * 2, int(rows * target / max(dt, 1e-3))))
+    times = []
+    for _ in range(max(1, runs)):
+        t = time.time()
+        _, rays = sc.render(rows=band(rows), threads=threads)
+        times.append(time.time() - t)
+    dt = sorted(times)[len(times) // 2]
     paths = rows * sc.width * sc.spp
     return {"value": round(paths / dt / 1e6, 4), "unit": "Mpaths/s", "cores": threads, "kind": "port",
-            "sample": f"{rows} image rows x {sc.width} px x {sc.spp} spp = {paths} paths in {dt:.2f} s, "
-                      f"{rays} rays", "mrays_per_s": round(rays / dt / 1e6, 3)}
+            "sample": f"{rows} image rows x {sc.width} px x {sc.spp} spp = {paths} paths, median of "
+                      f"{len(times)} runs {dt:.2f} s, {rays} rays", "mrays_per_s": round(rays / dt / 1e6, 3)}
