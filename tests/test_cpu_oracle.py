@@ -124,3 +124,14 @@ def test_port_sppm_matches_reference_render(port, tmp_path, name):
         close = (np.abs(film - g["film"]) <= 1e-4 * np.abs(g["film"]) + 1e-5).all(2).mean()
         assert close > 0.95
     assert rays > 0
+
+
+def test_time_sample_counts_only_rendered_rows(port, tmp_path):
+    """The timed band of rows stays inside the image, so the paths it counts
+    are the paths it rendered: a whole-image sample traces as many rays as a
+    whole-image render."""
+    path = helpers.write_scene("cornell", str(tmp_path / "c"), res=24, spp=2)
+    r = port.time_sample(path, threads=2, seconds=1e6, runs=1)  # grows to the whole image
+    assert r["sample"].startswith("24 image rows x 24 px x 2 spp = 1152 paths")
+    _, rays = port.Scene.load(path).render(threads=2)
+    assert r["sample"].endswith(f", {rays} rays")
