@@ -314,7 +314,8 @@ typedef struct orion_launch_config {
   int32_t blocks_per_sm;  /* grid size factor of the grid-stride kernels */
   int32_t wave_paths;     /* paths per plain-render wave */
   int32_t batch_slots;    /* batches: path slots of the pool (pooled mode) or paths per wave (wave mode) */
-  int32_t refill_below;   /* a traversal warp takes new rays once fewer lanes than this hold one (1..32) */
+  int32_t refill_below;   /* a traversal warp takes new rays once fewer lanes than this hold one (1..32);
+                             plain renders' any-hit launches use this + 4 (at most 32) */
   int32_t streams;        /* plain renders: waves in flight at once, each on its own stream (1..4);
                              batches: concurrent pooled engines, min(streams, 2); 0 = keep */
 } orion_launch_config;
