@@ -294,6 +294,8 @@ typedef struct orion_job {
   double* sum;                 /* host W*H*3 FP64 radiance sums, or NULL */
   double* sumsq;               /* host W*H*3 FP64 sums of squares, or NULL */
   uint32_t* count;             /* host W*H samples per pixel, or NULL */
+  float* sum32;                /* host W*H*3 radiance sums rounded to FP32 on the device (half the
+                                  read-back of `sum`, the film type of orion_gpu_render), or NULL */
 } orion_job;
 
 typedef struct orion_batch_stats {
@@ -404,6 +406,26 @@ int orion_gpu_sobol(orion_gpu_ctx* ctx, int64_t n, const uint64_t* index, const 
  * n x 8 floats (o, d, tnear, tfar). prim = -1 for a miss. */
 int orion_gpu_trace(orion_gpu_ctx* ctx, orion_scene_id id, int64_t n, const float* rays, int32_t any_hit,
                     float* t, float* u, float* v, int32_t* prim);
+/* The same queries traced by the renderer's own persistent kernels: closest-hit
+ * rays become a wave's extension rays (k_trace), any-hit rays its shadow rays
+ * (k_trace_sh, occlusion within (0, tfar]). Every ray's tnear must be 0, as
+ * for the renderer's rays; closest-hit rays ignore tfar (extension rays are
+ * unbounded). prim = -1 for a miss; for any_hit = 1, prim = 1 when occluded
+ * and t, u, v are 0. Replaces rtcIntersect / rtcOccluded as the renderer calls
+ * them (src/core/kernel.cpp:111-174, src/core/light.h:17-30). Returns
+ * ORION_ERR_DEVICE if a traversal overflowed its stack. */
+int orion_gpu_trace_wave(orion_gpu_ctx* ctx, orion_scene_id id, int64_t n, const float* rays, int32_t any_hit,
+                         float* t, float* u, float* v, int32_t* prim);
+/* Free and total bytes of the context's device (cudaMemGetInfo): lets a caller
+ * check that a call allocated nothing. No counterpart in the reference. */
+int orion_gpu_mem_info(orion_gpu_ctx* ctx, int64_t* free_bytes, int64_t* total_bytes);
+/* Failure-path test knobs (0, 0 = normal operation). stack_entries = 2 makes
+ * plain renders and orion_gpu_trace_wave trace with kernels whose traversal
+ * stack holds 2 entries, so deep traversals overflow and the call returns
+ * ORION_ERR_DEVICE; batch_iterations > 0 stops every batch loop after that
+ * many iterations, so unfinished batches return ORION_ERR_DEVICE. No
+ * counterpart in the reference, which prints and continues (src/orion.h:33-37). */
+int orion_gpu_set_test_limits(orion_gpu_ctx* ctx, int32_t stack_entries, int32_t batch_iterations);
 /* orion_gpu_trace without any device allocation. No counterpart in the
  * reference: it exists for callers that must not allocate, such as a ray query
  * (picking) from a second context while a long render runs on the same device

@@ -1702,20 +1702,22 @@ int port_camera_rays(void* h, int64_t n, const int64_t* index, float* rays) {
 }
 
 // PathTracing::render (path.cpp:15-37): passes k in [k0, k0 + spp), OpenMP over
-// rows, FP32 film sums in sample order. Rows [row0, row1) only (the CPU
-// baseline renders a bounded band of the image). Returns traced rays.
-int64_t port_render(void* h, int32_t spp, int64_t k0, int32_t max_depth, int32_t rr_depth, int32_t row0,
-                    int32_t row1, float* film, int32_t threads) {
+// rows, FP32 film sums in sample order. Only the `nrows` rows listed in `rows`
+// (the CPU baseline renders a bounded sample of the image's rows); the film is
+// the whole W x H x 3 image. Returns traced rays.
+int64_t port_render_rows(void* h, int32_t spp, int64_t k0, int32_t max_depth, int32_t rr_depth, int32_t nrows,
+                         const int32_t* rows, float* film, int32_t threads) {
   const Scene& s = *static_cast<Scene*>(h);
   const int W = s.cam.width, H = s.cam.height;
-  if (row1 > H) row1 = H;
+  for (int q = 0; q < nrows; ++q)
+    if (rows[q] < 0 || rows[q] >= H) return -1;
   const int64_t wh = (int64_t)W * H;
   if (threads > 0) omp_set_num_threads(threads);
   int64_t rays = 0;
   for (int64_t k = k0; k < k0 + spp; ++k) {
 #pragma omp parallel for schedule(dynamic, 1) reduction(+ : rays)
-    for (int j = row0; j < row1; ++j)
-      for (int i = 0; i < W; ++i) {
+    for (int q = 0; q < nrows; ++q)
+      for (int i = 0, j = rows[q]; i < W; ++i) {
         Sampler smp{(uint64_t)(k * wh + (int64_t)j * W + i)};
         V o, d;
         cameraRay(s, smp, i, j, &o, &d);
@@ -1729,6 +1731,16 @@ int64_t port_render(void* h, int32_t spp, int64_t k0, int32_t max_depth, int32_t
       }
   }
   return rays;
+}
+
+// Rows [row0, row1) of port_render_rows.
+int64_t port_render(void* h, int32_t spp, int64_t k0, int32_t max_depth, int32_t rr_depth, int32_t row0,
+                    int32_t row1, float* film, int32_t threads) {
+  const int H = static_cast<Scene*>(h)->cam.height;
+  if (row1 > H) row1 = H;
+  std::vector<int32_t> rows;
+  for (int j = row0; j < row1; ++j) rows.push_back(j);
+  return port_render_rows(h, spp, k0, max_depth, rr_depth, (int32_t)rows.size(), rows.data(), film, threads);
 }
 
 // FP64 per-pixel sums and sums of squares over passes [k0, k0 + spp).

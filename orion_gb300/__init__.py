@@ -111,7 +111,7 @@ STAGES = ("camera", "trace_ext", "shade", "trace_shadow", "trace_mis", "resolve"
 
 class Job(C.Structure):
     _fields_ = [("scene", C.c_int32), ("reserved", C.c_int32), ("params", RenderParams), ("camera", C.c_void_p),
-                ("sum", C.c_void_p), ("sumsq", C.c_void_p), ("count", C.c_void_p)]
+                ("sum", C.c_void_p), ("sumsq", C.c_void_p), ("count", C.c_void_p), ("sum32", C.c_void_p)]
 
 
 class BatchStats(C.Structure):
@@ -191,6 +191,9 @@ def library() -> C.CDLL:
             "orion_gpu_sobol": (i32, [vp, i64, vp, vp, vp]),
             "orion_gpu_trace": (i32, [vp, i32, i64, vp, i32, vp, vp, vp, vp]),
             "orion_gpu_trace_noalloc": (i32, [vp, i32, i64, vp, i32, vp, vp, vp, vp]),
+            "orion_gpu_trace_wave": (i32, [vp, i32, i64, vp, i32, vp, vp, vp, vp]),
+            "orion_gpu_set_test_limits": (i32, [vp, i32, i32]),
+            "orion_gpu_mem_info": (i32, [vp, vp, vp]),
             "orion_gpu_camera_rays": (i32, [vp, i32, i64, vp, vp]),
             "orion_gpu_bsdf_eval": (i32, [vp, C.POINTER(Material), i64, vp, vp, vp, vp, i32, vp, vp, vp, vp, vp,
                                           vp, vp]),
@@ -215,6 +218,38 @@ def _ptr(a: np.ndarray) -> C.c_void_p:
 # ------------------------------------------------------------------ scenes
 
 
+def desc_from_arrays(positions, normals, material_of_prim, materials, lights, camera: Camera, spp: int,
+                     max_depth: int, light_of_prim=None, uvs=None, images=None, sppm=None):
+    """An orion_scene_desc over the given arrays, built without the library: (desc, keep), where
+    `keep` holds the arrays the desc points into and must outlive every use of the desc.
+    Arguments as HostScene.from_arrays."""
+    pos = np.ascontiguousarray(positions, dtype=np.float32).reshape(-1, 9)
+    nrm = np.ascontiguousarray(normals, dtype=np.float32).reshape(-1, 9)
+    mop = np.ascontiguousarray(material_of_prim, dtype=np.int32)
+    lop = np.ascontiguousarray(light_of_prim if light_of_prim is not None else np.full(len(pos), -1), np.int32)
+    mats = (Material * len(materials))(*materials)
+    lts = (Light * max(1, len(lights)))(*lights)
+    d = SceneDesc()
+    d.num_prims = len(pos)
+    d.positions, d.normals = pos.ctypes.data, nrm.ctypes.data
+    uva = np.ascontiguousarray(uvs, np.float32).reshape(-1, 6) if uvs is not None else None
+    if uva is not None and len(uva) != len(pos):
+        raise ValueError("uvs must hold 6 floats per primitive")
+    d.uvs = uva.ctypes.data if uva is not None else None
+    d.material_of_prim, d.light_of_prim = mop.ctypes.data, lop.ctypes.data
+    d.num_materials, d.num_lights = len(materials), len(lights)
+    d.materials, d.lights = C.addressof(mats), C.addressof(lts)
+    d.camera, d.spp, d.max_depth = camera, spp, max_depth
+    imgs = [np.ascontiguousarray(im, np.float32) for im in (images or [])]
+    recs = (Image * max(1, len(imgs)))(*[Image(im.shape[1], im.shape[0], im.ctypes.data) for im in imgs])
+    d.num_images, d.images = len(imgs), C.addressof(recs)
+    if sppm is not None:
+        d.integrator = INTEGRATOR_SPPM
+        d.sppm = SppmParams(sppm["iterations"], sppm["photons"], sppm["radius"], sppm["max_depth"])
+        d.spp, d.max_depth = sppm["iterations"], sppm["max_depth"]
+    return d, (pos, nrm, mop, lop, mats, lts, uva, imgs, recs)
+
+
 class HostScene:
     """A parsed scene on the host (flat primitive arrays, materials, lights, camera)."""
 
@@ -234,32 +269,11 @@ class HostScene:
         """images: list of (H, W, 3) float arrays, referenced 1-based by Light.image and Material.tex;
         uvs: texture coordinates per primitive corner (T x 6) or None; sppm: dict (iterations, photons,
         radius, max_depth) for an <Integrator type="sppm"> scene."""
-        pos = np.ascontiguousarray(positions, dtype=np.float32).reshape(-1, 9)
-        nrm = np.ascontiguousarray(normals, dtype=np.float32).reshape(-1, 9)
-        mop = np.ascontiguousarray(material_of_prim, dtype=np.int32)
-        lop = np.ascontiguousarray(light_of_prim if light_of_prim is not None else np.full(len(pos), -1), np.int32)
-        mats = (Material * len(materials))(*materials)
-        lts = (Light * max(1, len(lights)))(*lights)
-        d = SceneDesc()
-        d.num_prims = len(pos)
-        d.positions, d.normals = pos.ctypes.data, nrm.ctypes.data
-        uva = np.ascontiguousarray(uvs, np.float32).reshape(-1, 6) if uvs is not None else None  # kept alive below
-        if uva is not None and len(uva) != len(pos):
-            raise ValueError("uvs must hold 6 floats per primitive")
-        d.uvs = uva.ctypes.data if uva is not None else None
-        d.material_of_prim, d.light_of_prim = mop.ctypes.data, lop.ctypes.data
-        d.num_materials, d.num_lights = len(materials), len(lights)
-        d.materials, d.lights = C.addressof(mats), C.addressof(lts)
-        d.camera, d.spp, d.max_depth = camera, spp, max_depth
-        imgs = [np.ascontiguousarray(im, np.float32) for im in (images or [])]
-        recs = (Image * max(1, len(imgs)))(*[Image(im.shape[1], im.shape[0], im.ctypes.data) for im in imgs])
-        d.num_images, d.images = len(imgs), C.addressof(recs)
-        if sppm is not None:
-            d.integrator = INTEGRATOR_SPPM
-            d.sppm = SppmParams(sppm["iterations"], sppm["photons"], sppm["radius"], sppm["max_depth"])
-            d.spp, d.max_depth = sppm["iterations"], sppm["max_depth"]
+        d, keep = desc_from_arrays(positions, normals, material_of_prim, materials, lights, camera, spp, max_depth,
+                                   light_of_prim=light_of_prim, uvs=uvs, images=images, sppm=sppm)
         h = C.c_void_p()
         _check(library().orion_scene_from_desc(C.byref(d), C.byref(h)))
+        del keep  # orion_scene_from_desc copied every array
         return cls(h.value)
 
     def desc(self) -> SceneDesc:
@@ -336,17 +350,23 @@ class Context:
         return b.value
 
     def render(self, sid: int, width: int, height: int, spp: int = 0, max_depth: int = -1, rr_depth: int = 3,
-               first_pass: int = 0, wave_paths: int = 0, fp64: bool = False):
-        """Film sums: FP32 (H, W, 3) sums and (H, W) counts; or FP64 (sum, sumsq) if fp64."""
+               first_pass: int = 0, wave_paths: int = 0, fp64: bool = False, out: tuple | None = None):
+        """Film sums: FP32 (H, W, 3) sums and (H, W) counts; or FP64 (sum, sumsq) if fp64.
+        out: arrays of those shapes and types to write into (reused host buffers), returned."""
         p = RenderParams(spp=spp, max_depth=max_depth, rr_depth=rr_depth, flags=1 if fp64 else 0,
                          first_pass=first_pass, wave_paths=wave_paths)
+        if out is not None:
+            a, b = out
+            want = (np.float64, np.float64) if fp64 else (np.float32, np.uint32)
+            if a.shape != (height, width, 3) or b.shape[:2] != (height, width) or (a.dtype, b.dtype) != want \
+                    or not (a.flags.c_contiguous and b.flags.c_contiguous):
+                raise ValueError("out arrays do not match the film")
         if fp64:
-            s = np.zeros((height, width, 3), np.float64)
-            q = np.zeros((height, width, 3), np.float64)
+            s, q = out if out is not None else (np.zeros((height, width, 3)), np.zeros((height, width, 3)))
             _check(library().orion_gpu_render_fp64(self._h, sid, C.byref(p), _ptr(s), _ptr(q)))
             return s, q
-        img = np.zeros((height, width, 3), np.float32)
-        cnt = np.zeros((height, width), np.uint32)
+        img, cnt = out if out is not None else (np.zeros((height, width, 3), np.float32),
+                                                np.zeros((height, width), np.uint32))
         _check(library().orion_gpu_render(self._h, sid, C.byref(p), _ptr(img), _ptr(cnt)))
         return img, cnt
 
@@ -388,21 +408,25 @@ class Context:
         _check(library().orion_gpu_stage_times(self._h, C.byref(t)))
         return {name: {"ms": t.ms[i], "launches": t.launches[i]} for i, name in enumerate(STAGES)}
 
-    def render_batch(self, jobs: list, sumsq: bool = True) -> tuple:
+    def render_batch(self, jobs: list, sumsq: bool = True, fp32: bool = False, outs: list | None = None) -> tuple:
         """jobs: dicts with sid, width, height and optional spp, max_depth, rr_depth, first_pass, camera.
 
         Returns ([(sum, sumsq, count) per job], stats): FP64 (H, W, 3) sums and
-        sums of squares (None when sumsq=False), (H, W) sample counts.
+        sums of squares (None when sumsq=False), (H, W) sample counts. fp32: the
+        sums come back rounded to FP32 on the device (float32 arrays, sumsq None).
+        outs: the list an earlier call returned, to write into again (reused host buffers).
         """
-        arr, outs = self._job_array(jobs, films=True, sumsq=sumsq)
+        arr, outs = self._job_array(jobs, films=True, sumsq=sumsq and not fp32, fp32=fp32, reuse=outs)
         st = BatchStats()
         _check(library().orion_gpu_render_batch(self._h, len(jobs), C.cast(arr, C.c_void_p), C.byref(st)))
         return outs, {k: getattr(st, k) for k, _ in BatchStats._fields_}
 
     @staticmethod
-    def _job_array(jobs: list, films: bool, sumsq: bool = True):
+    def _job_array(jobs: list, films: bool, sumsq: bool = True, fp32: bool = False, reuse: list | None = None):
         arr = (Job * max(1, len(jobs)))()
         outs = []
+        if reuse is not None and len(reuse) != len(jobs):
+            raise ValueError("outs must hold one entry per job")
         for i, j in enumerate(jobs):
             arr[i].scene = j["sid"]
             arr[i].params = RenderParams(spp=j.get("spp", 0), max_depth=j.get("max_depth", -1),
@@ -411,11 +435,21 @@ class Context:
                 arr[i].camera = C.addressof(j["camera"])
             if films:
                 h, w = j["height"], j["width"]
-                s = np.zeros((h, w, 3), np.float64)
-                q = np.zeros((h, w, 3), np.float64) if sumsq else None
-                c = np.zeros((h, w), np.uint32)
+                if reuse is not None:
+                    s, q, c = reuse[i]
+                    if s.shape != (h, w, 3) or s.dtype != (np.float32 if fp32 else np.float64) or \
+                            (q is None) == sumsq or c.shape != (h, w):
+                        raise ValueError(f"outs[{i}] does not match job {i}")
+                else:
+                    s = np.empty((h, w, 3), np.float32 if fp32 else np.float64)
+                    q = np.empty((h, w, 3), np.float64) if sumsq else None
+                    c = np.empty((h, w), np.uint32)
                 outs.append((s, q, c))
-                arr[i].sum, arr[i].count = s.ctypes.data, c.ctypes.data
+                if fp32:
+                    arr[i].sum32 = s.ctypes.data
+                else:
+                    arr[i].sum = s.ctypes.data
+                arr[i].count = c.ctypes.data
                 arr[i].sumsq = q.ctypes.data if sumsq else None
         return arr, outs
 
@@ -464,6 +498,27 @@ class Context:
         _check(library().orion_gpu_trace(self._h, sid, n, _ptr(rays), int(any_hit), _ptr(t), _ptr(u), _ptr(v),
                                          _ptr(prim)))
         return t, u, v, prim
+
+    def trace_wave(self, sid: int, rays, any_hit: bool = False):
+        """trace() through the renderer's persistent trace kernels (rays as a wave's extension or
+        shadow rays): tnear must be 0; closest-hit rays are unbounded; occluded rays get prim 1."""
+        rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
+        n = len(rays)
+        t, u, v = (np.zeros(n, np.float32) for _ in range(3))
+        prim = np.zeros(n, np.int32)
+        _check(library().orion_gpu_trace_wave(self._h, sid, n, _ptr(rays), int(any_hit), _ptr(t), _ptr(u), _ptr(v),
+                                              _ptr(prim)))
+        return t, u, v, prim
+
+    def mem_info(self) -> tuple:
+        """(free, total) bytes of the context's device."""
+        f, t = C.c_int64(), C.c_int64()
+        _check(library().orion_gpu_mem_info(self._h, C.byref(f), C.byref(t)))
+        return f.value, t.value
+
+    def set_test_limits(self, stack_entries: int = 0, batch_iterations: int = 0) -> None:
+        """Failure-path test knobs: a 2-entry traversal stack for plain renders, a batch-loop iteration cap."""
+        _check(library().orion_gpu_set_test_limits(self._h, stack_entries, batch_iterations))
 
     def trace_noalloc(self, sid: int, rays, any_hit: bool = False):
         """trace() through a fixed device scratch of NOALLOC_MAX_RAYS rays: no device allocation."""

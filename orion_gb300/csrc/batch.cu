@@ -108,19 +108,20 @@ __global__ void __launch_bounds__(512, 2) k_b_trace(WaveView w, BatchView b, int
   if (kind == 0) {
     n = c.counters[CNT_EXT0 + c.cur];
     trace_persistent<false, SMEM>(js, w.q_ext[c.cur], n, &c.counters[CNT_FETCH_EXT], w.ray_o, w.ray_d, w.hit,
-                                  nullptr, stack_smem, refill_below, &c.counters[CNT_CLS0], w.q_cls, w.capacity);
+                                  nullptr, stack_smem, refill_below, &c.error, &c.counters[CNT_CLS0], w.q_cls,
+                                  w.capacity);
   } else if (kind == 1) {
     n = c.counters[CNT_SH];
     trace_persistent<true, SMEM>(js, w.q_sh, n, &c.counters[CNT_FETCH_SH], w.sh_o, w.sh_d,
-                                 F4{nullptr}, w.occluded, stack_smem, refill_below);
+                                 F4{nullptr}, w.occluded, stack_smem, refill_below, &c.error);
   } else if (kind == 2) {
     n = c.counters[CNT_MIS];
     trace_persistent<false, SMEM>(js, w.q_mis, n, &c.counters[CNT_FETCH_MIS], w.mis_o, w.mis_d,
-                                  F4{w.mis_hit}, nullptr, stack_smem, refill_below);
+                                  F4{w.mis_hit}, nullptr, stack_smem, refill_below, &c.error);
   } else {  // 3: MIS rays towards environment lights, occlusion only
     n = c.counters[CNT_MIS_ENV];
     trace_persistent<true, SMEM>(js, w.q_mis_env, n, &c.counters[CNT_FETCH_MIS_ENV], w.mis_o, w.mis_d,
-                                 F4{nullptr}, w.mis_occluded, stack_smem, refill_below);
+                                 F4{nullptr}, w.mis_occluded, stack_smem, refill_below, &c.error);
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(&c.rays[kind < 3 ? kind : 2], (unsigned long long)n);
 }
@@ -259,7 +260,7 @@ __global__ void k_b_control(BatchView b, cudaGraphConditionalHandle cond, int in
   c.iterations += 1;
   bool more = c.cursor < c.total || c.counters[CNT_EXT0 + c.cur] > 0;
   if (more && c.iterations >= c.max_iterations) {
-    c.error = 1;  // bounded loop: report instead of spinning on
+    c.error |= kErrIterationCap;  // bounded loop: report instead of spinning on
     more = false;
   }
   if (in_graph)
@@ -412,6 +413,17 @@ void launch_batch_wave_begin(const WaveView& w, const BatchView& b, const uint32
                              int n, int iteration_cap, int num_sms, cudaStream_t stream) {
   k_b_wave_begin<<<1, 32, 0, stream>>>(b, n, iteration_cap);
   k_b_wave_camera<<<grid_cap(n, 256, num_sms * 32), 256, 0, stream>>>(w, b, sobol, base, n);
+}
+
+// FP64 film sums rounded to FP32 (orion_job.sum32).
+__global__ void k_film_to_f32(const double* __restrict__ src, float* __restrict__ dst, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n; i += (long long)gridDim.x * blockDim.x)
+    dst[i] = (float)src[i];
+}
+
+void launch_film_to_f32(const double* src, float* dst, long long n, int num_sms, cudaStream_t stream) {
+  const long long blocks = std::min<long long>((n + 255) / 256, (long long)num_sms * 8);
+  k_film_to_f32<<<(int)std::max<long long>(blocks, 1), 256, 0, stream>>>(src, dst, n);
 }
 
 void launch_batch_wave_film(const WaveView& w, const BatchView& b, int n, int num_sms, cudaStream_t stream) {

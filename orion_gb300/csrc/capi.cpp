@@ -106,6 +106,14 @@ static std::string default_sobol_path() {
   return "data/sobol_matrices.bin";
 }
 
+// The message for a launch's error word (kErr* bits).
+static std::string kernel_error(int bits) {
+  std::string m = "kernel error word " + std::to_string(bits) + ":";
+  if (bits & kErrIterationCap) m += " iteration cap reached;";
+  if (bits & kErrTraversalStack) m += " a BVH traversal overflowed its stack (its rays were counted as misses);";
+  return m;
+}
+
 static int ensure_film(orion_gpu_ctx* c, int64_t pixels, bool fp64) {
   if (pixels > c->film_pixels) {
     int rc;
@@ -544,7 +552,7 @@ static int render_impl(orion_gpu_ctx* ctx, orion_scene_id id, const orion_render
     ctx->stage_times.ms[timer.stage[i]] += e;
     ctx->stage_times.launches[timer.stage[i]] += 1;
   }
-  if (err_word) return fail(ORION_ERR_DEVICE, "kernel error word " + std::to_string(err_word));
+  if (err_word) return fail(ORION_ERR_DEVICE, kernel_error(err_word));
   return ORION_OK;
 }
 
@@ -811,6 +819,64 @@ extern "C" int orion_gpu_trace(orion_gpu_ctx* ctx, orion_scene_id id, int64_t n,
   RC(to_host(v, dv, n, ctx->stream));
   RC(to_host(prim, dp, n, ctx->stream));
   CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  return ORION_OK;
+}
+
+extern "C" int orion_gpu_trace_wave(orion_gpu_ctx* ctx, orion_scene_id id, int64_t n, const float* rays,
+                                    int32_t any_hit, float* t, float* u, float* v, int32_t* prim) {
+  if (!ctx || n < 0 || (n > 0 && (!rays || !t || !u || !v || !prim))) return fail(ORION_ERR_INVALID, "bad argument");
+  if (n > (int64_t)1 << 30) return fail(ORION_ERR_INVALID, "orion_gpu_trace_wave: more than 2^30 rays");
+  for (int64_t i = 0; i < n; ++i)
+    if (rays[8 * i + 6] != 0.f)
+      return fail(ORION_ERR_INVALID, "orion_gpu_trace_wave: tnear must be 0 (ray " + std::to_string(i) + ")");
+  std::lock_guard<std::mutex> g(ctx->mu);
+  CUDA_TRY(cudaSetDevice(ctx->device));
+  auto it = ctx->scenes.find(id);
+  if (it == ctx->scenes.end()) return fail(ORION_ERR_INVALID, "unknown scene id");
+  if (n == 0) return ORION_OK;
+  RC(ensure_wave(ctx, (int)n));
+  const WaveView& w = ctx->wave.view;
+  DevBuf dr, dt, du, dv, dp;
+  RC(to_device(dr, rays, 8 * (size_t)n, ctx->stream));
+  RC(dt.alloc(n * 4));
+  RC(du.alloc(n * 4));
+  RC(dv.alloc(n * 4));
+  RC(dp.alloc(n * 4));
+  CUDA_TRY(cudaMemsetAsync(w.error_word, 0, sizeof(int), ctx->stream));
+  launch_trace_wave(it->second->view, w, (int)n, dr.as<float>(), any_hit, dt.as<float>(), du.as<float>(),
+                    dv.as<float>(), dp.as<int>(), ctx->cfg, ctx->stream);
+  CUDA_TRY(cudaGetLastError());
+  int err_word = 0;
+  RC(to_host(t, dt, n, ctx->stream));
+  RC(to_host(u, du, n, ctx->stream));
+  RC(to_host(v, dv, n, ctx->stream));
+  RC(to_host(prim, dp, n, ctx->stream));
+  CUDA_TRY(cudaMemcpyAsync(&err_word, w.error_word, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  CUDA_TRY(cudaStreamSynchronize(ctx->stream));
+  if (err_word) return fail(ORION_ERR_DEVICE, kernel_error(err_word));
+  return ORION_OK;
+}
+
+extern "C" int orion_gpu_mem_info(orion_gpu_ctx* ctx, int64_t* free_bytes, int64_t* total_bytes) {
+  if (!ctx || !free_bytes || !total_bytes) return fail(ORION_ERR_INVALID, "null argument");
+  std::lock_guard<std::mutex> g(ctx->mu);
+  CUDA_TRY(cudaSetDevice(ctx->device));
+  size_t f = 0, t = 0;
+  CUDA_TRY(cudaMemGetInfo(&f, &t));
+  *free_bytes = (int64_t)f;
+  *total_bytes = (int64_t)t;
+  return ORION_OK;
+}
+
+extern "C" int orion_gpu_set_test_limits(orion_gpu_ctx* ctx, int32_t stack_entries, int32_t batch_iterations) {
+  if (!ctx) return fail(ORION_ERR_INVALID, "null context");
+  if (!(stack_entries == 0 || stack_entries == kTestStackEntries))
+    return fail(ORION_ERR_INVALID, "stack_entries must be 0 or " + std::to_string(kTestStackEntries));
+  if (batch_iterations < 0) return fail(ORION_ERR_INVALID, "batch_iterations must be >= 0");
+  std::lock_guard<std::mutex> g(ctx->mu);
+  ctx->cfg.test_stack_entries = stack_entries;
+  ctx->cfg.test_batch_iterations = batch_iterations;
+  for (orion_gb300::BatchEngine& e : ctx->beng) e.drop_graph();  // captured loops hold the old kernels
   return ORION_OK;
 }
 

@@ -96,7 +96,8 @@ static int prepare_engine(orion_gpu_ctx* ctx, int e, int njobs, int slots, Batch
 }
 
 // Control block of a fresh batch of `total` work items on `cap` slots.
-static BatchCtl initial_ctl(unsigned long long total, int njobs, int cap, int max_depth_all) {
+// `test_iterations` > 0 (orion_gpu_set_test_limits) replaces the loop bound.
+static BatchCtl initial_ctl(unsigned long long total, int njobs, int cap, int max_depth_all, int test_iterations) {
   BatchCtl c;
   std::memset(&c, 0, sizeof(c));
   c.total = total;
@@ -105,7 +106,16 @@ static BatchCtl initial_ctl(unsigned long long total, int njobs, int cap, int ma
   // Every live path advances one bounce per iteration: a bound on the loop.
   const unsigned long long refills = (total + cap - 1) / cap + 1;
   c.max_iterations = (int)std::min<unsigned long long>(2ULL * refills * (max_depth_all + 2) + 64, 1u << 30);
+  if (test_iterations > 0) c.max_iterations = test_iterations;
   return c;
+}
+
+// The error a batch's control block reports (its error bits), or "" for none.
+static std::string batch_error(int bits) {
+  std::string m;
+  if (bits & kErrIterationCap) m += "batch loop reached its iteration cap";
+  if (bits & kErrTraversalStack) m += std::string(m.empty() ? "" : "; ") + "a traversal overflowed its stack";
+  return m;
 }
 
 // One batch over `dj` (film pointers set; films zeroed or holding earlier
@@ -161,7 +171,7 @@ static int run_batch_pooled_locked(orion_gpu_ctx* ctx, std::vector<DevJob>& dj, 
   std::vector<BatchCtl> init(ng);
   for (int e = 0; e < ng; ++e) {
     cudaStream_t es = engine_stream(ctx, e);
-    init[e] = initial_ctl(gtotal[e], (int)group[e].size(), caps[e], max_depth_all);
+    init[e] = initial_ctl(gtotal[e], (int)group[e].size(), caps[e], max_depth_all, ctx->cfg.test_batch_iterations);
     if (!group[e].empty())
       CUDA_TRY(cudaMemcpyAsync(bvs[e].jobs, group[e].data(), group[e].size() * sizeof(DevJob),
                                cudaMemcpyHostToDevice, es));
@@ -216,7 +226,7 @@ static int run_batch_pooled_locked(orion_gpu_ctx* ctx, std::vector<DevJob>& dj, 
   BatchCtl& out = *out_ctl;
   out = outs[0];
   int64_t launches = 0;
-  bool error = false;
+  int error_bits = 0;
   for (int e = 0; e < ng; ++e) {
     const BatchCtl& o = outs[e];
     if (e > 0) {
@@ -224,12 +234,12 @@ static int run_batch_pooled_locked(orion_gpu_ctx* ctx, std::vector<DevJob>& dj, 
       for (int k = 0; k < 3; ++k) out.rays[k] += o.rays[k];
       out.iterations = std::max(out.iterations, o.iterations);
     }
-    error = error || o.error;
+    error_bits |= o.error;
     // Per iteration: plan, regen, 4 traces, one shade per class, resolve, retire, control; plus the init.
     const unsigned launched = ctx->profiling ? masks[e] : ctx->beng[e].loop[ORION_BATCH_POOLED].mask;
     launches += (9LL + __builtin_popcount(launched)) * o.iterations + 1;
   }
-  out.error = error ? 1 : 0;
+  out.error = error_bits;
   ctx->last.paths = (int64_t)out.paths_done;
   ctx->last.ext_rays = (int64_t)out.rays[0];
   ctx->last.shadow_rays = (int64_t)out.rays[1];
@@ -237,7 +247,7 @@ static int run_batch_pooled_locked(orion_gpu_ctx* ctx, std::vector<DevJob>& dj, 
   ctx->last.rays = (int64_t)(out.rays[0] + out.rays[1] + out.rays[2]);
   ctx->last.kernel_launches = launches;
   ctx->last.device_ms = ms;
-  if (out.error) return fail(ORION_ERR_DEVICE, "batch loop reached its iteration cap");
+  if (out.error) return fail(ORION_ERR_DEVICE, batch_error(out.error));
   if (out.paths_done != total)
     return fail(ORION_ERR_DEVICE, "batch finished " + std::to_string(out.paths_done) + " of " + std::to_string(total) +
                                       " paths");
@@ -279,7 +289,9 @@ static int run_batch_waves_locked(orion_gpu_ctx* ctx, std::vector<DevJob>& dj, u
     CUDA_TRY(cudaMemcpyAsync(bvs[e].jobs, dj.data(), (size_t)njobs * sizeof(DevJob), cudaMemcpyHostToDevice, es));
     CUDA_TRY(cudaMemcpyAsync(bvs[e].ctl, &zero, sizeof(BatchCtl), cudaMemcpyHostToDevice, es));
   }
-  const int iteration_cap = 2 * (max_depth_all + 2) + 8;  // every live path advances one bounce per iteration
+  // Every live path advances one bounce per iteration: a bound on each wave's loop.
+  const int iteration_cap =
+      ctx->cfg.test_batch_iterations > 0 ? ctx->cfg.test_batch_iterations : 2 * (max_depth_all + 2) + 8;
   StageTimer timer{nullptr, nullptr, 0, 0};
   if (ctx->profiling) {
     const int need = (int)std::min<int64_t>(nwaves * iteration_cap * 8, 200000);
@@ -338,7 +350,7 @@ static int run_batch_waves_locked(orion_gpu_ctx* ctx, std::vector<DevJob>& dj, u
   BatchCtl& out = *out_ctl;
   out = outs[0];
   int64_t launches = 0;
-  bool error = false;
+  int error_bits = 0;
   for (int e = 0; e < ne; ++e) {
     const BatchCtl& o = outs[e];
     if (e > 0) {
@@ -346,13 +358,13 @@ static int run_batch_waves_locked(orion_gpu_ctx* ctx, std::vector<DevJob>& dj, u
       for (int j = 0; j < 3; ++j) out.rays[j] += o.rays[j];
       out.iterations += o.iterations;
     }
-    error = error || o.error;
+    error_bits |= o.error;
     // Per iteration: plan, 4 traces, one shade per class, resolve, control.
     const unsigned launched = ctx->profiling ? mask : ctx->beng[e].loop[ORION_BATCH_WAVES].mask;
     launches += (7LL + __builtin_popcount(launched)) * o.iterations;
   }
   launches += 3 * nwaves;  // begin, camera, film per wave
-  out.error = error ? 1 : 0;
+  out.error = error_bits;
   ctx->last.paths = (int64_t)out.paths_done;
   ctx->last.ext_rays = (int64_t)out.rays[0];
   ctx->last.shadow_rays = (int64_t)out.rays[1];
@@ -360,7 +372,7 @@ static int run_batch_waves_locked(orion_gpu_ctx* ctx, std::vector<DevJob>& dj, u
   ctx->last.rays = (int64_t)(out.rays[0] + out.rays[1] + out.rays[2]);
   ctx->last.kernel_launches = launches;
   ctx->last.device_ms = ms;
-  if (out.error) return fail(ORION_ERR_DEVICE, "batch loop reached its iteration cap");
+  if (out.error) return fail(ORION_ERR_DEVICE, batch_error(out.error));
   if (out.paths_done != total)
     return fail(ORION_ERR_DEVICE, "batch finished " + std::to_string(out.paths_done) + " of " + std::to_string(total) +
                                       " paths");
@@ -451,10 +463,24 @@ extern "C" int orion_gpu_render_batch(orion_gpu_ctx* ctx, int32_t njobs, const o
   float ms = 0.f;
   rc = run_batch_locked(ctx, dj, total, max_depth_all, &out, &ms);
   if (rc != ORION_OK) return rc;
+  // FP32 read-back: every requested film rounded on the device into one
+  // staging block, then one copy per film.
+  size_t f32_bytes = 0;
+  for (int i = 0; i < njobs; ++i)
+    if (jobs[i].sum32) f32_bytes += (size_t)dj[i].width * dj[i].height * 12;
+  if (f32_bytes && ctx->b_films32.bytes < f32_bytes && (rc = ctx->b_films32.alloc(f32_bytes)) != ORION_OK) return rc;
+  size_t f32_off = 0;
   for (int i = 0; i < njobs; ++i) {
     const size_t wh = (size_t)dj[i].width * dj[i].height;
     if (jobs[i].sum) CUDA_TRY(cudaMemcpyAsync(jobs[i].sum, dj[i].sum, wh * 24, cudaMemcpyDeviceToHost, s));
     if (jobs[i].sumsq) CUDA_TRY(cudaMemcpyAsync(jobs[i].sumsq, dj[i].sumsq, wh * 24, cudaMemcpyDeviceToHost, s));
+    if (jobs[i].sum32) {
+      float* dst = reinterpret_cast<float*>(ctx->b_films32.as<char>() + f32_off);
+      launch_film_to_f32(dj[i].sum, dst, (long long)wh * 3, ctx->num_sms, s);
+      CUDA_TRY(cudaGetLastError());
+      CUDA_TRY(cudaMemcpyAsync(jobs[i].sum32, dst, wh * 12, cudaMemcpyDeviceToHost, s));
+      f32_off += wh * 12;
+    }
   }
   for (int i = 0; i < njobs; ++i)
     if (jobs[i].count) {

@@ -165,6 +165,7 @@ struct orion_gpu_ctx {
   // batched mode
   int default_batch_slots = 1 << 24;  // pooled: path slots; waves: paths per wave
   DevBuf b_films;
+  DevBuf b_films32;  // FP32 copies of batch films for read-back (orion_job.sum32)
   // Pooled batch engines: a batch's jobs are split between as many as the
   // `streams` knob allows (at most kBatchEngines) and they run concurrently,
   // engine e on the wave state and stream of wave slot e.

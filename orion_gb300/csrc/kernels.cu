@@ -52,26 +52,28 @@ __global__ void k_camera(SceneView s, WaveView w, WaveArgs a) {
 // slots sorted by shading class) or MIS rays (NeeF4, hits into mis_hit).
 // COUNT: the same traversal, adding its node visits and triangle tests to
 // work[0] and work[3] (a diagnostic render; see WaveView::trace_work).
-template <int SMEM, class RayView, class HitView, bool COUNT = false>
+// CAP: traversal stack capacity (kTestStackEntries only in the kernels that
+// exercise the overflow report); overflows set bits of *err.
+template <int SMEM, class RayView, class HitView, bool COUNT = false, int CAP = kMaxStack>
 __global__ void __launch_bounds__(512, 2)
     k_trace(SceneView s, const int* queue, const int* count, int* fetch, RayView ray_o, RayView ray_d, HitView hit,
             unsigned long long* stat, int refill_below, int* cls_counters, int* q_cls, int cls_stride,
-            unsigned long long* work) {
+            unsigned long long* work, int* err) {
   extern __shared__ int2 stack_smem[];
   const int n = *count;
-  trace_persistent<false, SMEM, COUNT>(SingleScene{&s}, queue, n, fetch, ray_o, ray_d, hit, nullptr, stack_smem,
-                                       refill_below, cls_counters, q_cls, cls_stride, work);
+  trace_persistent<false, SMEM, COUNT, CAP>(SingleScene{&s}, queue, n, fetch, ray_o, ray_d, hit, nullptr, stack_smem,
+                                            refill_below, err, cls_counters, q_cls, cls_stride, work);
   if (stat && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(stat, (unsigned long long)n);
 }
 
-template <int SMEM, bool COUNT = false>
+template <int SMEM, bool COUNT = false, int CAP = kMaxStack>
 __global__ void __launch_bounds__(512, 2)
     k_trace_sh(SceneView s, const int* queue, const int* count, int* fetch, NeeF4 ray_o, NeeF4 ray_d, int* occluded,
-               unsigned long long* stat, int refill_below, unsigned long long* work) {
+               unsigned long long* stat, int refill_below, unsigned long long* work, int* err) {
   extern __shared__ int2 stack_smem[];
   const int n = *count;
-  trace_persistent<true, SMEM, COUNT>(SingleScene{&s}, queue, n, fetch, ray_o, ray_d, F4{nullptr}, occluded,
-                                      stack_smem, refill_below, nullptr, nullptr, 0, work);
+  trace_persistent<true, SMEM, COUNT, CAP>(SingleScene{&s}, queue, n, fetch, ray_o, ray_d, F4{nullptr}, occluded,
+                                           stack_smem, refill_below, err, nullptr, nullptr, 0, work);
   if (stat && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(stat, (unsigned long long)n);
 }
 
@@ -186,6 +188,40 @@ __global__ void k_trace_rays(SceneView s, int64_t n, const float* rays, int any_
   }
 }
 
+// Production-traversal hook: n rays (o, d, tnear = 0, tfar) placed in a
+// wave's records as extension rays (closest hit) or shadow rays (occlusion,
+// tmax = tfar), so that the renderer's own persistent trace kernels trace them.
+__global__ void k_load_rays(WaveView w, int n, const float* rays, int any_hit) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const float* r = rays + 8 * (size_t)i;
+    if (any_hit) {
+      w.sh_o[i] = make_float4(r[0], r[1], r[2], r[7]);
+      w.sh_d[i] = make_float4(r[3], r[4], r[5], 0.f);
+      w.q_sh[i] = i;
+    } else {
+      w.ray_o[i] = make_float4(r[0], r[1], r[2], 0.f);
+      w.ray_d[i] = make_float4(r[3], r[4], r[5], 0.f);
+      w.q_ext[0][i] = i;
+    }
+  }
+}
+
+__global__ void k_store_hits(WaveView w, int n, int any_hit, float* t, float* u, float* v, int* prim) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    if (any_hit) {
+      t[i] = u[i] = v[i] = 0.f;
+      prim[i] = w.occluded[i] ? 1 : -1;
+    } else {
+      const float4 h = w.hit[i];
+      const int p = __float_as_int(h.w);
+      t[i] = p >= 0 ? h.x : 0.f;
+      u[i] = h.y;
+      v[i] = h.z;
+      prim[i] = p;
+    }
+  }
+}
+
 __global__ void k_camera_rays(SceneView s, const uint32_t* sobol, int64_t n, const int64_t* index, float* rays) {
   const int64_t wh = (int64_t)s.cam.width * s.cam.height;
   for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
@@ -240,7 +276,7 @@ int grid_for(int64_t n, int block, int max_blocks) {
 
 enum TraceKind { TK_EXT = 0, TK_SHADOW = 1, TK_MIS = 2, TK_MIS_ENV = 3 };
 
-template <int SMEM, bool COUNT = false>
+template <int SMEM, bool COUNT = false, int CAP = kMaxStack>
 void launch_trace_kernels(int kind, const SceneView& s, const WaveView& w, int cur, const LaunchConfig& cfg,
                           int grid, cudaStream_t stream) {
   const int block = cfg.trace_block;
@@ -251,30 +287,37 @@ void launch_trace_kernels(int kind, const SceneView& s, const WaveView& w, int c
   const int refill_any = refill + 4 > 32 ? 32 : refill + 4;
   size_t smem = (size_t)SMEM * block * sizeof(int2);
   unsigned long long* work = w.trace_work;  // nodes[ext, shadow, mis], then tris[ext, shadow, mis]
+  int* err = w.error_word;
   if (kind == TK_EXT)
-    k_trace<SMEM, RecF4, RecF4, COUNT><<<grid, block, smem, stream>>>(
+    k_trace<SMEM, RecF4, RecF4, COUNT, CAP><<<grid, block, smem, stream>>>(
         s, w.q_ext[cur], w.counters + cur, w.counters + CNT_FETCH_EXT, w.ray_o, w.ray_d, w.hit, w.ray_stats, refill,
-        w.counters + CNT_CLS0, w.q_cls, w.capacity, work);
+        w.counters + CNT_CLS0, w.q_cls, w.capacity, work, err);
   else if (kind == TK_SHADOW)
-    k_trace_sh<SMEM, COUNT><<<grid, block, smem, stream>>>(s, w.q_sh, w.counters + CNT_SH,
-                                                           w.counters + CNT_FETCH_SH, w.sh_o, w.sh_d, w.occluded,
-                                                           w.ray_stats + 1, refill_any, COUNT ? work + 1 : nullptr);
+    k_trace_sh<SMEM, COUNT, CAP><<<grid, block, smem, stream>>>(s, w.q_sh, w.counters + CNT_SH,
+                                                                w.counters + CNT_FETCH_SH, w.sh_o, w.sh_d, w.occluded,
+                                                                w.ray_stats + 1, refill_any,
+                                                                COUNT ? work + 1 : nullptr, err);
   else if (kind == TK_MIS_ENV)
-    k_trace_sh<SMEM, COUNT><<<grid, block, smem, stream>>>(s, w.q_mis_env, w.counters + CNT_MIS_ENV,
-                                                           w.counters + CNT_FETCH_MIS_ENV, w.mis_o, w.mis_d,
-                                                           w.mis_occluded, w.ray_stats + 2, refill_any,
-                                                           COUNT ? work + 2 : nullptr);
+    k_trace_sh<SMEM, COUNT, CAP><<<grid, block, smem, stream>>>(s, w.q_mis_env, w.counters + CNT_MIS_ENV,
+                                                                w.counters + CNT_FETCH_MIS_ENV, w.mis_o, w.mis_d,
+                                                                w.mis_occluded, w.ray_stats + 2, refill_any,
+                                                                COUNT ? work + 2 : nullptr, err);
   else
-    k_trace<SMEM, NeeF4, F4, COUNT><<<grid, block, smem, stream>>>(s, w.q_mis, w.counters + CNT_MIS,
-                                                                   w.counters + CNT_FETCH_MIS, w.mis_o, w.mis_d,
-                                                                   F4{w.mis_hit}, w.ray_stats + 2, refill, nullptr,
-                                                                   nullptr, 0, COUNT ? work + 2 : nullptr);
+    k_trace<SMEM, NeeF4, F4, COUNT, CAP><<<grid, block, smem, stream>>>(s, w.q_mis, w.counters + CNT_MIS,
+                                                                        w.counters + CNT_FETCH_MIS, w.mis_o, w.mis_d,
+                                                                        F4{w.mis_hit}, w.ray_stats + 2, refill,
+                                                                        nullptr, nullptr, 0,
+                                                                        COUNT ? work + 2 : nullptr, err);
 }
 
 void trace_dispatch(int kind, const SceneView& s, const WaveView& w, int cur, const LaunchConfig& cfg, int grid,
                     cudaStream_t stream) {
   if (w.trace_work) {  // counting render: the stack's split between shared and local memory is irrelevant
     launch_trace_kernels<0, true>(kind, s, w, cur, cfg, grid, stream);
+    return;
+  }
+  if (cfg.test_stack_entries) {  // orion_gpu_set_test_limits: kernels with a kTestStackEntries-entry stack
+    launch_trace_kernels<0, false, kTestStackEntries>(kind, s, w, cur, cfg, grid, stream);
     return;
   }
   switch (cfg.smem_stack) {
@@ -376,6 +419,15 @@ void launch_trace(const SceneView& s, int64_t n, const float* rays, int any_hit,
   int block = cfg.trace_block;
   int grid = grid_for(n, block, cfg.num_sms * cfg.blocks_per_sm * 2);
   k_trace_rays<16><<<grid, block, (size_t)16 * block * sizeof(int2), stream>>>(s, n, rays, any_hit, t, u, v, prim);
+}
+
+void launch_trace_wave(const SceneView& s, const WaveView& w, int n, const float* rays, int any_hit, float* t,
+                       float* u, float* v, int* prim, const LaunchConfig& cfg, cudaStream_t stream) {
+  k_reset_counters<<<1, 32, 0, stream>>>(w.counters, kCounterSlots, any_hit ? CNT_SH : CNT_EXT0, n);
+  k_load_rays<<<grid_for(n, 256, 4096), 256, 0, stream>>>(w, n, rays, any_hit);
+  const int tgrid = grid_for(n, cfg.trace_block, cfg.num_sms * cfg.blocks_per_sm * 2);
+  trace_dispatch(any_hit ? TK_SHADOW : TK_EXT, s, w, 0, cfg, tgrid, stream);
+  k_store_hits<<<grid_for(n, 256, 4096), 256, 0, stream>>>(w, n, any_hit, t, u, v, prim);
 }
 
 namespace {

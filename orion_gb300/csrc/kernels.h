@@ -99,6 +99,12 @@ struct WaveView {
   int capacity;
 };
 
+// Bits of a launch's error word (plain renders: WaveView::error_word; batches: BatchCtl::error).
+constexpr int kErrIterationCap = 1;    // a batch loop reached its iteration bound
+constexpr int kErrTraversalStack = 2;  // a traversal needed more stack entries than its capacity
+// Stack capacity of the test-only trace kernels (orion_gpu_set_test_limits).
+constexpr int kTestStackEntries = 2;
+
 enum CounterSlot { CNT_EXT0 = 0, CNT_EXT1 = 1, CNT_NEE = 2, CNT_SH = 3, CNT_MIS = 4, CNT_RETIRE = 5, CNT_FREE = 6,
                    CNT_FETCH_EXT = 8, CNT_FETCH_SH = 9, CNT_FETCH_MIS = 10, CNT_MIS_ENV = 11,
                    CNT_FETCH_MIS_ENV = 12, CNT_CLS0 = 16, kCounterSlots = 32 };
@@ -132,7 +138,7 @@ struct BatchCtl {
   int njobs;
   int iterations;
   int max_iterations;
-  int error;                     // 1: iteration cap reached
+  int error;                     // kErr* bits
   unsigned long long rays[3];    // ext, shadow, mis
   unsigned long long paths_done;
   int more;                      // host-driven loop: 1 while another iteration is needed
@@ -178,6 +184,9 @@ struct LaunchConfig {
   int blocks_per_sm; // persistent grid size factor
   int smem_stack;    // shared-memory stack entries per thread (0, 8, 16, 24, 32)
   int refill_below;  // a traversal warp refills idle lanes when fewer lanes than this hold a ray (1..32)
+  // Test knobs (orion_gpu_set_test_limits), 0 in normal operation:
+  int test_stack_entries;   // plain renders trace with kernels whose stack holds kTestStackEntries entries
+  int test_batch_iterations;  // batch loops stop (with an error) after this many iterations
 };
 
 enum Stage { ST_CAMERA = 0, ST_TRACE_EXT, ST_SHADE, ST_TRACE_SHADOW, ST_TRACE_MIS, ST_RESOLVE, ST_FILM, ST_OTHER,
@@ -239,6 +248,8 @@ void launch_batch_iteration(const WaveView& w, const BatchView& b, const uint32_
 void launch_batch_wave_begin(const WaveView& w, const BatchView& b, const uint32_t* sobol, unsigned long long base,
                              int n, int iteration_cap, int num_sms, cudaStream_t stream);
 void launch_batch_wave_film(const WaveView& w, const BatchView& b, int n, int num_sms, cudaStream_t stream);
+// dst[i] = (float)src[i] for i < n.
+void launch_film_to_f32(const double* src, float* dst, long long n, int num_sms, cudaStream_t stream);
 // Resets the batch control block and the free-slot list for `capacity` slots.
 void launch_batch_init(const WaveView& w, const BatchView& b, int capacity, cudaStream_t stream);
 
@@ -313,6 +324,10 @@ void launch_sobol(const uint32_t* sobol, int64_t n, const uint64_t* index, const
                   cudaStream_t stream);
 void launch_trace(const SceneView& s, int64_t n, const float* rays, int any_hit, float* t, float* u, float* v,
                   int* prim, const LaunchConfig& cfg, cudaStream_t stream);
+// The same queries through the renderer's persistent trace kernels: the rays
+// become wave `w`'s extension rays (closest hit) or shadow rays (any hit).
+void launch_trace_wave(const SceneView& s, const WaveView& w, int n, const float* rays, int any_hit, float* t,
+                       float* u, float* v, int* prim, const LaunchConfig& cfg, cudaStream_t stream);
 void launch_camera_rays(const SceneView& s, const uint32_t* sobol, int64_t n, const int64_t* index, float* rays,
                         cudaStream_t stream);
 void launch_bsdf_eval(const DevMaterial* mat, int64_t n, const float* frame, const float* wo, const float* wi,

@@ -66,9 +66,11 @@ int noalloc_trace_scratch(int device, unsigned char** out, std::string* err) {
   if (!a.ptr[device]) {
     int cur = -1;
     cudaError_t e = cudaGetDevice(&cur);
-    if (e == cudaSuccess && cur != device) e = cudaSetDevice(device);
+    const bool switched = e == cudaSuccess && cur != device;
+    if (switched) e = cudaSetDevice(device);
     void* p = nullptr;
     if (e == cudaSuccess) e = cudaGetSymbolAddress(&p, g_trace_scratch);
+    if (switched) cudaSetDevice(cur);  // the calling thread keeps its current device
     if (e != cudaSuccess) {
       *err = std::string("cudaGetSymbolAddress(trace scratch): ") + cudaGetErrorString(e);
       return e;

@@ -350,16 +350,17 @@ struct JobScene {
 // With `q_cls` (closest hit only), each finished ray's slot is also appended
 // to the queue of the shading class of what it hit (SC_MISS for a miss).
 // COUNT adds the kernel's node visits to work[0] and its triangle tests to
-// work[3].
-template <bool ANY, int SMEM, bool COUNT = false, class SceneOf, class RayView, class HitView>
+// work[3]. A ray whose traversal overflowed its stack (capacity CAP) is
+// reported as a miss (not occluded) and sets kErrTraversalStack in *err.
+template <bool ANY, int SMEM, bool COUNT = false, int CAP = kMaxStack, class SceneOf, class RayView, class HitView>
 __device__ __forceinline__ void trace_persistent(const SceneOf& scene_of, const int* queue, int n, int* fetch,
                                                  RayView ray_o, RayView ray_d, HitView hit, int* occluded,
-                                                 int2* stack_smem, int refill_below,
+                                                 int2* stack_smem, int refill_below, int* err,
                                                  int* cls_counters = nullptr, int* q_cls = nullptr,
                                                  int cls_stride = 0, unsigned long long* work = nullptr) {
   constexpr unsigned kFull = 0xffffffffu;
   const int lane = threadIdx.x & 31;
-  TraversalStack<SMEM> st;
+  TraversalStack<SMEM, CAP> st;
   st.smem = stack_smem + threadIdx.x;
   st.stride = blockDim.x;
   LaneRay r;
@@ -395,7 +396,11 @@ __device__ __forceinline__ void trace_persistent(const SceneOf& scene_of, const 
       continue;
     }
     if (active) {
-      if (lane_step<ANY, SMEM, COUNT>(r, ts, st, &wk)) {
+      if (lane_step<ANY, SMEM, COUNT, CAP>(r, ts, st, &wk)) {
+        if (r.tmax < 0.f) {  // poisoned by a stack overflow
+          r.tri = -1;
+          atomicOr(err, kErrTraversalStack);
+        }
         if (ANY) {
           occluded[pid] = r.tri >= 0;
         } else {

@@ -9,6 +9,16 @@
 // [entry][thread] so a warp's pushes hit 32 different banks; entries past the
 // shared part spill to a per-thread local array. Each entry is an 8-byte
 // node or triangle group, so popping needs no memory access.
+//
+// A push beyond the stack's capacity writes nothing: the entry is dropped and
+// the ray is poisoned (its tmax set to -1, so no further box or triangle test
+// passes and the traversal drains). The persistent trace kernels turn a
+// poisoned ray into a miss and set kErrTraversalStack (kernels.h) in the launch's
+// error word, so a render returns ORION_ERR_DEVICE instead of writing out of bounds.
+// The BVH builder bounds the wide tree's depth below 48, and one traversal
+// holds at most one entry per level, so the default capacity (96) is never
+// reached; the kernels built with kTestStackEntries (kernels.h) exist to exercise
+// the path.
 #pragma once
 #include "device_types.h"
 #include "dmath.cuh"
@@ -29,18 +39,23 @@ struct RayHit {
   int tri;  // leaf-order triangle index, -1 for a miss
 };
 
-template <int SMEM>
+template <int SMEM, int CAP = kMaxStack>
 struct TraversalStack {
+  static_assert(CAP >= SMEM, "the shared part is within the capacity");
   int2* smem;  // SMEM entries for this thread, stride `stride`
   int stride;
   int sp;
-  int2 local[kMaxStack - SMEM > 0 ? kMaxStack - SMEM : 1];
-  __device__ __forceinline__ void push(int2 e) {
+  int2 local[CAP - SMEM > 0 ? CAP - SMEM : 1];
+  // False (and nothing written) when the stack already holds CAP entries.
+  __device__ __forceinline__ bool push(int2 e) {
     if (sp < SMEM)
       smem[sp * stride] = e;
-    else
+    else if (sp < CAP)
       local[sp - SMEM] = e;
+    else
+      return false;
     ++sp;
+    return true;
   }
   __device__ __forceinline__ int2 pop() {
     --sp;
@@ -190,9 +205,10 @@ __device__ __forceinline__ int take_child(uint2& ng, uint32_t oct) {
 }
 
 // ANY = false: closest hit over (tnear, tfar]. ANY = true: first hit found.
-template <bool ANY, int SMEM>
+// A stack overflow ends the traversal with a miss (see the file comment).
+template <bool ANY, int SMEM, int CAP>
 __device__ __forceinline__ RayHit traverse(const TraceScene& s, V3 o, V3 d, float tnear, float tfar,
-                                           TraversalStack<SMEM>& st) {
+                                           TraversalStack<SMEM, CAP>& st) {
   RayHit h;
   h.t = tfar;
   h.u = h.v = 0.f;
@@ -205,7 +221,10 @@ __device__ __forceinline__ RayHit traverse(const TraceScene& s, V3 o, V3 d, floa
   while (true) {
     if (ng.y > 0x00ffffffu) {
       const int child = take_child(ng, oct);
-      if (ng.y) st.push(make_int2((int)ng.x, (int)ng.y));
+      if (ng.y && !st.push(make_int2((int)ng.x, (int)ng.y))) {
+        h.t = -1.f;  // poisoned: nothing passes a test against tmax < tnear
+        h.tri = -1;
+      }
       wide_node(s.nodes, child, o, idir, oct, tnear, h.t, ng, tg);
     } else {
       tg = ng;
@@ -238,6 +257,10 @@ __device__ __forceinline__ RayHit traverse(const TraceScene& s, V3 o, V3 d, floa
       const int2 e = st.pop();
       ng = make_uint2((uint32_t)e.x, (uint32_t)e.y);
     }
+  }
+  if (h.t < 0.f) {  // stack overflow: reported as a miss
+    h.t = tfar;
+    h.tri = -1;
   }
   return h;
 }
@@ -284,13 +307,15 @@ struct TraceWork {
 
 // One node visit and its triangles. Returns true when the lane's ray is done:
 // its stack ran empty, or (ANY) a hit was found. COUNT adds the node visit
-// and the triangle tests to `wk`; the traversal itself is the same.
-template <bool ANY, int SMEM, bool COUNT = false>
-__device__ __forceinline__ bool lane_step(LaneRay& r, const TraceScene& s, TraversalStack<SMEM>& st,
+// and the triangle tests to `wk`; the traversal itself is the same. A push
+// beyond the stack's capacity poisons the ray (r.tmax = -1; see the file
+// comment): the caller reports it when the ray is done.
+template <bool ANY, int SMEM, bool COUNT = false, int CAP = kMaxStack>
+__device__ __forceinline__ bool lane_step(LaneRay& r, const TraceScene& s, TraversalStack<SMEM, CAP>& st,
                                           TraceWork* wk = nullptr) {
   if (r.ng.y > 0x00ffffffu) {
     const int child = take_child(r.ng, r.oct);
-    if (r.ng.y) st.push(make_int2((int)r.ng.x, (int)r.ng.y));
+    if (r.ng.y && !st.push(make_int2((int)r.ng.x, (int)r.ng.y))) r.tmax = -1.f;
     wide_node(s.nodes, child, r.o, r.idir, r.oct, r.tnear, r.tmax, r.ng, r.tg);
     if (COUNT) ++wk->nodes;
   } else {

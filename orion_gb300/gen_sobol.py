@@ -40,5 +40,6 @@ def write(vals: list[int], out: str = OUT) -> str:
 
 
 if __name__ == "__main__":
-    src = sys.argv[1] if len(sys.argv) > 1 else "/root/reference/src/sampler/sobol.cpp"
-    print(write(extract(src)))
+    if len(sys.argv) != 2:
+        sys.exit("usage: python -m orion_gb300.gen_sobol /path/to/orion/src/sampler/sobol.cpp")
+    print(write(extract(sys.argv[1])))

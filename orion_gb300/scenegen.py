@@ -381,12 +381,14 @@ def displaced(res: int = 1024, spp: int = 64, subdiv: int = 8, max_depth: int = 
 
 
 def mixed(width: int = 1920, height: int = 1080, spp: int = 128, max_depth: int = 16, seed: int = 3,
-          subdivs=(5, 6, 7, 5, 6, 7, 6, 7)) -> Scene:
+          subdivs=(5, 6, 7, 5, 6, 7, 6, 7), plastic_distribution: str = "beckmann") -> Scene:
+    """plastic_distribution "ggx": the plastic coat with the reference's only microfacet distribution
+    (the reference ignores distribution="beckmann" and renders GGX)."""
     rng = Rng(seed)
     s = Scene("mixed", width, height, spp, max_depth, (0.0, 2.0, 12.0), (0.0, 0.0, 0.0), (0, 1, 0), 45.0,
               lens_radius=0.025, focal_distance=5.0, meta={"config": "mixed materials", "seed": seed})
     mats = [matte((0.6, 0.55, 0.5)), metal((0.2, 0.92, 1.1), (3.9, 2.45, 2.14), 0.2), glass(1.5, 0.1),
-            mirror(), plastic((0.4, 0.1, 0.1), (0.5, 0.5, 0.5), 0.15, distribution="beckmann")]
+            mirror(), plastic((0.4, 0.1, 0.1), (0.5, 0.5, 0.5), 0.15, distribution=plastic_distribution)]
     for i, sd in enumerate(subdivs):
         pos, f, n = displaced_sphere(sd, 1.0, 0.05, 4.0, seed * 100 + i)
         scale = rng.uniform(0.5, 1.5)
@@ -772,6 +774,19 @@ def to_host_scene(scene: Scene, text_rounding: bool = False):
     (within 1e-7 relative of the written text). Light frames agree with the loader's to float
     rounding (computed here in float64)."""
     import orion_gb300 as og
+    return og.HostScene.from_arrays(**scene_arrays(scene, text_rounding))
+
+
+def scene_desc(scene: Scene, text_rounding: bool = False):
+    """(orion_scene_desc, keep-alive) of the scene, built in Python without loading the library
+    (the same arrays to_host_scene hands it)."""
+    import orion_gb300 as og
+    return og.desc_from_arrays(**scene_arrays(scene, text_rounding))
+
+
+def scene_arrays(scene: Scene, text_rounding: bool = False) -> dict:
+    """Keyword arguments of HostScene.from_arrays / desc_from_arrays for the scene."""
+    import orion_gb300 as og
     P, N, mesh_of = scene.flat(text_rounding)
     images, image_ids = [], {}
 
@@ -840,8 +855,9 @@ def to_host_scene(scene: Scene, text_rounding: bool = False):
         lights.append(L)
     cam = og.look_at_camera(scene.eye, scene.look, scene.up, scene.fov, scene.width, scene.height,
                             scene.lens_radius, scene.focal_distance)
-    return og.HostScene.from_arrays(P, N, mesh_of, mats, lights, cam, scene.spp, scene.max_depth,
-                                    light_of_prim=light_of, uvs=uvs, images=images, sppm=scene.sppm)
+    return dict(positions=P, normals=N, material_of_prim=mesh_of, materials=mats, lights=lights, camera=cam,
+                spp=scene.spp, max_depth=scene.max_depth, light_of_prim=light_of, uvs=uvs, images=images,
+                sppm=scene.sppm)
 
 
 def job_views(s: Scene, views: int = 16):

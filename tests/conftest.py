@@ -16,8 +16,9 @@ def pytest_configure(config):
 @pytest.fixture(scope="session")
 def built():
     """Build the in-tree libraries once per session (no-op when up to date)."""
+    from oracle import build as oracle_build
     from orion_gb300 import build
-    return build.build_all(with_reference=True)
+    return {"product": build.build_product(), "sobol": build.sobol_table(), **oracle_build.build_all()}
 
 
 @pytest.fixture(scope="session")

@@ -15,9 +15,15 @@ records its outputs on fixed inputs:
   image_*_sppm.npz  SPPM::render film sums (src/integrator/sppm.cpp:58-322), one thread:
                caustics (every light type), envlit (image environment map), textured
   stats_*.npz  FP64 per-pixel mean and variance at high spp (for 3-sigma checks)
+  fullsize_*.npz  the 1024x1024 displaced-sphere and the 1920x1080 eight-sphere
+               workloads at their full sizes: per-pixel FP64 sums at the
+               workload's own spp on seeded pixels (path-for-path parity) and
+               at 65,536 spp on the same pixels (3-sigma and RMSE checks); the
+               eight-sphere scene with its Beckmann plastic (no Beckmann in the
+               reference) comes from the oracle restatement instead
   geometry.npz loader output digests
 
-    python tests/golden/make_golden.py [--quick]
+    python tests/golden/make_golden.py [--quick] [--only fullsize]
 """
 from __future__ import annotations
 
@@ -36,7 +42,8 @@ sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.join(ROOT, "tests"))
 
 import helpers  # noqa: E402
-from orion_gb300 import Material, build  # noqa: E402
+from oracle import build  # noqa: E402
+from orion_gb300 import Material  # noqa: E402
 
 
 def vp(a):
@@ -102,9 +109,13 @@ def sobol_grid():
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--quick", action="store_true")
+    ap.add_argument("--only", choices=["fullsize"], help="regenerate one group of fixtures only")
     args = ap.parse_args()
     ref = Ref()
     t0 = time.time()
+    if args.only == "fullsize":
+        fullsize(ref, args.quick)
+        return
 
     # Sobol
     idx, dim = sobol_grid()
@@ -232,6 +243,75 @@ def main():
                             hash=np.frombuffer(helpers.scene_hash(path).encode(), np.uint8))
         ref.lib.ref_scene_free(h)
         print("stats", time.time() - t0)
+    fullsize(ref, args.quick)
+
+
+# Full-size workloads: (scenegen function, its arguments, fixture name, seed of the pixel choice, renderer).
+# The reference has one microfacet distribution (GGX) and renders the eight-sphere scene's Beckmann plastic
+# as GGX, so its fixture is of the scene with a GGX plastic; the scene as specified (Beckmann) gets a
+# fixture from the oracle restatement, which implements Beckmann as an extension.
+FULLSIZE = [("cornell", {}, "fullsize_cornell.npz", 37, "reference"),
+            ("displaced", {}, "fullsize_displaced.npz", 41, "reference"),
+            ("mixed", {"plastic_distribution": "ggx"}, "fullsize_mixed.npz", 43, "reference"),
+            ("mixed", {}, "fullsize_mixed_beckmann.npz", 47, "oracle")]
+
+
+def seeded_pixels(n: int, W: int, H: int, seed: int) -> np.ndarray:
+    """n (x, y) pixels from SplitMix64, uniform over the image (tests recompute nothing: the fixture stores them)."""
+    u = helpers.splitmix_uniform(2 * n, seed).reshape(n, 2)
+    return np.stack([(u[:, 0] * W).astype(np.int32), (u[:, 1] * H).astype(np.int32)], 1).astype(np.int32)
+
+
+def fullsize(ref: Ref, quick: bool) -> None:
+    """Per-pixel FP64 sums of the reference's PathTracing::Li on the full-size workloads.
+
+    On 1024 seeded pixels (band_pix = pix):
+    band_*: the workload's own spp, sample passes [0, spp): the same Sobol samples the GPU
+    renderer and the oracle trace, so sums agree path for path, and the Monte Carlo error of
+    an image at the workload's spp (matched-RMSE checks);
+    sum/sumsq: 65,536 spp, passes [0, 65536): the converged per-pixel means and their
+    Monte Carlo variance (3-sigma checks, the reference image of the RMSE checks)."""
+    spp_hi = 4096 if quick else 65536
+    for name, kw, fixture, seed, renderer in FULLSIZE:
+        t0 = time.time()
+        with tempfile.TemporaryDirectory() as tmp:
+            path = helpers.write_scene(name, os.path.join(tmp, name), **kw)
+            spp = scene_spp(path)
+            if renderer == "reference":
+                h, info = ref.load(path)
+                W, H = int(info[0]), int(info[1])
+
+                def pixels(pix, first, n):
+                    s, q = np.zeros((len(pix), 3)), np.zeros((len(pix), 3))
+                    ref.lib.ref_scene_render_pixels(h, C.c_int64(len(pix)), vp(pix), C.c_int32(first), C.c_int32(n),
+                                                    vp(s), vp(q), C.c_int32(0))
+                    return s, q
+            else:
+                from oracle import port
+                sc = port.Scene.load(path)
+                W, H = sc.width, sc.height
+
+                def pixels(pix, first, n):
+                    return sc.render_pixels(pix, n, first_pass=first)
+            pix = band = seeded_pixels(1024, W, H, seed)
+            bs, bq = pixels(band, 0, spp)
+            s, q = pixels(pix, 0, spp_hi)
+            np.savez_compressed(os.path.join(HERE, fixture), band_pix=band, band_spp=spp, band_sum=bs, band_sumsq=bq,
+                                pix=pix, spp=spp_hi, sum=s, sumsq=q, width=W, height=H,
+                                renderer=np.frombuffer(renderer.encode(), np.uint8),
+                                hash=np.frombuffer(helpers.scene_hash(path).encode(), np.uint8))
+            if renderer == "reference":
+                ref.lib.ref_scene_free(h)
+        print(fixture, f"{time.time() - t0:.1f} s")
+
+
+def scene_spp(ori_path: str) -> int:
+    """The samples per pixel the scene file's integrator asks for (<Param nSamplesPerPixel=...>)."""
+    import re
+    m = re.search(r'nSamplesPerPixel="(\d+)"', open(ori_path).read())
+    if not m:
+        raise RuntimeError("no spp in " + ori_path)
+    return int(m.group(1))
 
 
 if __name__ == "__main__":

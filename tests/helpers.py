@@ -53,6 +53,23 @@ def random_rays(n: int, lo, hi, seed: int, pad: float = 0.1) -> np.ndarray:
     return r
 
 
+def t_tolerance(rays, t_ref, prim_ref, positions):
+    """Allowed |t - t_ref| of a hit: 1e-5 relative, or the float rounding of the ray-plane distance when
+    that is larger. Both the GPU's Woop test (t = -(r2.(o - v0)) / (r2.d)) and the oracle's Moller-Trumbore
+    test round the coordinates they combine, an error of a few units in the last place (2^-24 relative) of
+    the largest coordinate involved (|o|, |v0|, t|d|); the plane distance divides it by the cosine
+    between the ray and the triangle's normal, so grazing hits magnify it. 16 ulps of that scale over the
+    cosine covers both tests' roundings."""
+    o = rays[:, :3].astype(np.float64)
+    d = rays[:, 3:6].astype(np.float64)
+    tri = positions[np.maximum(prim_ref, 0)].reshape(-1, 3, 3).astype(np.float64)
+    nrm = np.cross(tri[:, 1] - tri[:, 0], tri[:, 2] - tri[:, 0])
+    nrm /= np.maximum(np.linalg.norm(nrm, axis=1, keepdims=True), 1e-300)
+    cos = np.abs((d * nrm).sum(1)) / np.linalg.norm(d, axis=1)
+    scale = np.maximum(np.abs(o).max(1), np.abs(tri).max((1, 2))) + np.abs(t_ref) * np.abs(d).max(1)
+    return 1e-5 * np.abs(t_ref) + 16 * 2.0 ** -24 * scale / np.maximum(cos, 1e-6)
+
+
 def random_frames(n: int, seed: int) -> np.ndarray:
     """n x 12 shading frames (ng, ns, u, v) built the way the reference builds them at a hit."""
     ng = unit_vectors(n, seed)
@@ -70,6 +87,27 @@ def random_frames(n: int, seed: int) -> np.ndarray:
 def write_scene(name: str, directory: str, **kw) -> str:
     s = getattr(scenegen, name)(**kw)
     return scenegen.write_ori(s, directory)
+
+
+# Full-size scenes of the parity fixtures: fixture -> (scenegen function, its arguments).
+FULLSIZE = {"fullsize_cornell.npz": ("cornell", {}),
+            "fullsize_displaced.npz": ("displaced", {}),
+            "fullsize_mixed.npz": ("mixed", {"plastic_distribution": "ggx"}),
+            "fullsize_mixed_beckmann.npz": ("mixed", {})}
+
+
+def fullsize_scene(name: str, **kw) -> str:
+    """The scene file of a workload at its full size (written once per machine into a cache directory,
+    then reused): the 1024x1024 displaced sphere or the 1920x1080 eight-sphere scene."""
+    import tempfile
+    tag = "_".join(f"{k}{v}" for k, v in sorted(kw.items()))
+    d = os.path.join(tempfile.gettempdir(), "orion_gb300_fullsize", name + ("_" + tag if tag else ""))
+    marker = os.path.join(d, "done")
+    if not os.path.exists(marker):
+        path = write_scene(name, d, **kw)
+        with open(marker, "w") as f:
+            f.write(path)
+    return open(marker).read().strip()
 
 
 def scene_hash(ori_path: str) -> str:

@@ -215,3 +215,16 @@ def test_sppm_integrator_parameters_load_and_round_trip(tmp_path):
     bad.write_text(open(scenegen.write_ori(sc, str(tmp_path))).read().replace('<Param initRadius="0.125"/>', ""))
     with pytest.raises(og.OrionError, match="initRadius"):
         og.HostScene.load(str(bad))
+
+
+def test_sobol_table_is_the_references():
+    """data/sobol_matrices.bin holds the direction numbers of src/sampler/sobol.cpp (where the reference tree
+    is present; elsewhere the committed table is what the GPU and the oracle load)."""
+    from oracle import build as oracle_build
+    from orion_gb300 import gen_sobol
+    ref = oracle_build.reference_root()
+    if ref is None:
+        pytest.skip("reference tree not present")
+    import struct
+    vals = gen_sobol.extract(os.path.join(ref, "src", "sampler", "sobol.cpp"))
+    assert open(gen_sobol.OUT, "rb").read() == struct.pack("<%dI" % len(vals), *vals)

@@ -158,3 +158,32 @@ def test_modes_give_the_same_films(ctx, scenes):
     for (a, q1, c1), (b, q2, c2) in zip(pooled, waves):
         assert np.array_equal(c1, c2)
         assert _close(a, b) and _close(q1, q2)
+
+
+def test_batch_iteration_cap_is_reported(ctx, scenes, mode):
+    """A batch loop stopped by its iteration bound returns ORION_ERR_DEVICE (no hang, no partial result
+    reported as success), and the next batch on the same context renders normally."""
+    import orion_gb300 as og
+    jobs = [_job(s) for s in scenes]
+    before, _ = ctx.render_batch(jobs)
+    try:
+        ctx.set_test_limits(batch_iterations=2)
+        with pytest.raises(og.OrionError, match="iteration cap") as e:
+            ctx.render_batch(jobs)
+        assert e.value.code == -7
+    finally:
+        ctx.set_test_limits()
+    after, _ = ctx.render_batch(jobs)
+    for (a, _, ca), (b, _, cb) in zip(before, after):
+        assert _close(a, b) and np.array_equal(ca, cb)
+
+
+def test_batch_fp32_readback(ctx, scenes, mode):
+    """orion_job.sum32: the FP64 sums rounded to FP32 on the device (FP64 atomics add in any order, so
+    two batches' sums agree to FP64 rounding and their FP32 roundings to one FP32 step)."""
+    jobs = [_job(s) for s in scenes]
+    f64, _ = ctx.render_batch(jobs, sumsq=False)
+    f32, _ = ctx.render_batch(jobs, fp32=True)
+    for (a, _, ca), (b, q, cb) in zip(f64, f32):
+        assert b.dtype == np.float32 and q is None
+        assert np.all(np.abs(a - b) <= 2.0 ** -23 * np.abs(a) + 1e-30) and np.array_equal(ca, cb)

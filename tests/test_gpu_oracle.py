@@ -1,11 +1,13 @@
 """GPU path vs the CPU oracle at sizes the oracle finishes in seconds.
 
-* 1M seeded rays: closest-hit primitive equal except ties, t within 1e-5
-  relative, occlusion equal to "closest hit exists" (the oracle's BVH is
-  checked equal to a brute-force loop in the CPU suite).
+* 1M seeded rays, through the test hook and through the renderer's own
+  persistent trace kernels: closest-hit primitive equal except ties, t within
+  1e-5 relative or the float rounding bound of helpers.t_tolerance, occlusion equal to
+  the oracle's (the oracle's BVH is checked equal to a brute-force loop in the
+  CPU suite).
 * images: the GPU and the oracle trace the same Sobol sample per path, so
   per-pixel sums match except where FP32 rounding sends a path down another
-  branch; at least 97% of pixels must match to 1e-4 relative.
+  branch; at least IMAGE_IDENTICAL of the pixels must match to 1e-4 relative.
 * statistics: a 1024-spp FP64 GPU render against the reference's 65,536-spp
   FP64 per-pixel means, |difference| <= 3 sigma for >= 95% of the tested
   pixels; relative RMSE is printed.
@@ -21,6 +23,11 @@ import helpers
 
 pytestmark = pytest.mark.gpu
 
+# Path-for-path image bars (fraction of pixels identical to 1e-4; relative RMSE of the film sums).
+# Measured on GB300: 0.9966 (displaced) to 0.9999 (Cornell) of pixels, RMSE 1.3e-6 to 1.4e-3.
+IMAGE_IDENTICAL = 0.995
+IMAGE_RMSE = 5e-3
+
 
 @pytest.fixture(scope="module")
 def port(built):
@@ -35,30 +42,81 @@ def _bounds(host):
 
 
 @pytest.mark.parametrize("name,kw", [("cornell", {}), ("displaced", dict(res=64, spp=4, subdiv=6))])
-def test_million_rays_match_oracle(ctx, port, tmp_path, name, kw):
+@pytest.mark.parametrize("kernel", ["hook", "production"])
+def test_million_rays_match_oracle(ctx, port, tmp_path, name, kw, kernel):
+    """1M seeded rays (origins in the scene's padded box, uniform directions) against the oracle's closest
+    hit. kernel "hook": orion_gpu_trace (one ray per thread, traverse()); "production": orion_gpu_trace_wave,
+    the renderer's own persistent k_trace / k_trace_sh launched on the rays as a wave's extension and shadow
+    rays. Same primitive unless the two are at equal distance (a tie), t within t_tolerance; a hit where
+    the oracle misses (or the reverse) only on rays through a shared edge, where the two triangle tests
+    round differently: at most 10 per million."""
     import orion_gb300 as og
     path = helpers.write_scene(name, str(tmp_path / name), **kw)
     host = og.HostScene.load(path)
     lo, hi = _bounds(host)
     n = 1 << 20
     rays = helpers.random_rays(n, lo, hi, seed=17)
-    rays[: n // 8, 7] = (helpers.splitmix_uniform(n // 8, 18) * float(np.max(hi - lo))).astype(np.float32)
+    finite = np.zeros(n, bool)
+    finite[: n // 8] = True  # the renderer's closest-hit rays are unbounded: finite tfar only for occlusion
+    rays[finite, 7] = (helpers.splitmix_uniform(n // 8, 18) * float(np.max(hi - lo))).astype(np.float32)
     sid = ctx.upload(host)
-    t, u, v, prim = ctx.trace(sid, rays)
-    _, _, _, occ = ctx.trace(sid, rays, any_hit=True)
+    trace = ctx.trace if kernel == "hook" else ctx.trace_wave
+    closest = rays.copy()
+    if kernel == "production":
+        closest[:, 7] = helpers.FLT_MAX
+    t, u, v, prim = trace(sid, closest)
+    _, _, _, occ = trace(sid, rays, any_hit=True)
     ctx.release(sid)
-    rt, ru, rv, rprim = port.Scene(host).trace(rays)
+    sc = port.Scene(host)
+    rt, ru, rv, rprim = sc.trace(closest)
+    _, _, _, rocc = sc.trace(rays) if kernel == "production" else (rt, ru, rv, rprim)
     hit = rprim >= 0
     miss_mismatch = np.count_nonzero((prim >= 0) != hit)
     assert miss_mismatch <= n * 1e-5, f"hit/miss differs on {miss_mismatch} rays"
-    assert np.count_nonzero((occ >= 0) != hit) <= n * 1e-5
+    occ_mismatch = np.count_nonzero((occ >= 0) != (rocc >= 0))
+    assert occ_mismatch <= n * 1e-5, f"occlusion differs on {occ_mismatch} rays"
     both = hit & (prim >= 0)
-    t_ok = np.abs(t - rt) <= 1e-5 * np.abs(rt) + 1e-7
+    tol = helpers.t_tolerance(closest, rt, rprim, host.arrays()["positions"])
+    t_ok = np.abs(t.astype(np.float64) - rt) <= tol
     same = prim == rprim
-    assert (same | t_ok)[both].all(), "a different primitive at a different distance"
-    assert t_ok[both].mean() > 0.99999, f"t differs on {np.count_nonzero(both & ~t_ok)} rays"
-    print(f"{name}: {n} rays, {hit.mean():.3f} hit, primitive identical on {same[both].mean():.6f} of hits "
-          f"(rest are ties), max rel t error {np.max(np.abs(t - rt)[both] / np.maximum(np.abs(rt[both]), 1e-30)):.2e}")
+    rel = np.abs(t - rt)[both] / np.maximum(np.abs(rt[both]), 1e-30)
+    print(f"{name} ({kernel}): {n} rays, {hit.mean():.3f} hit, primitive identical on {same[both].mean():.6f} "
+          f"of hits (rest are ties), t beyond 1e-5 relative on {np.count_nonzero(rel > 1e-5)} rays (max "
+          f"{rel.max():.2e}), all within the rounding bound: {bool(t_ok[both].all())}; hit/miss differs on "
+          f"{miss_mismatch}, occlusion on {occ_mismatch}")
+    assert t_ok[both].all(), f"t outside the tolerance on {np.count_nonzero(both & ~t_ok)} rays"
+    if kernel == "production":  # barycentrics of the same primitive (grazing hits round them further)
+        ok = same & both
+        uv_ok = (np.abs(u[ok] - ru[ok]) <= 1e-4) & (np.abs(v[ok] - rv[ok]) <= 1e-4)
+        assert uv_ok.mean() >= 0.9999, f"u, v differ beyond 1e-4 on {np.count_nonzero(~uv_ok)} hits"
+
+
+def test_traversal_stack_overflow_is_reported(ctx, tmp_path):
+    """A traversal whose stack would overflow writes nothing out of bounds and the call fails with
+    ORION_ERR_DEVICE; the context keeps working (test kernels with a 2-entry stack)."""
+    import orion_gb300 as og
+    path = helpers.write_scene("displaced", str(tmp_path / "d"), res=32, spp=1, subdiv=6)
+    host = og.HostScene.load(path)
+    sid = ctx.upload(host)
+    lo, hi = _bounds(host)
+    rays = helpers.random_rays(1 << 14, lo, hi, seed=23)
+    try:
+        good = ctx.trace_wave(sid, rays)
+        ref, _ = ctx.render(sid, 32, 32)
+        ctx.set_test_limits(stack_entries=2)
+        with pytest.raises(og.OrionError, match="overflowed its stack") as e:
+            ctx.trace_wave(sid, rays)
+        assert e.value.code == -7
+        with pytest.raises(og.OrionError, match="overflowed its stack"):
+            ctx.render(sid, 32, 32)
+        ctx.set_test_limits()
+        again = ctx.trace_wave(sid, rays)
+        img, _ = ctx.render(sid, 32, 32)
+        assert all(np.array_equal(a, b) for a, b in zip(good, again))
+        assert np.array_equal(img, ref)
+    finally:
+        ctx.set_test_limits()
+        ctx.release(sid)
 
 
 @pytest.mark.parametrize("name,kw", [
@@ -82,8 +140,8 @@ def test_image_matches_oracle_path_for_path(ctx, port, tmp_path, name, kw):
     close = (np.abs(gpu.astype(np.float64) - ref) <= 1e-4 * np.abs(ref) + 1e-5).all(2).mean()
     rmse = float(np.sqrt(np.mean((gpu.astype(np.float64) - ref) ** 2)) / max(np.sqrt(np.mean(ref.astype(np.float64) ** 2)), 1e-12))
     print(f"{name}: {close:.4f} of pixels identical path-for-path, relative RMSE {rmse:.2e}")
-    assert close >= 0.97
-    assert rmse < 0.05
+    assert close >= IMAGE_IDENTICAL
+    assert rmse < IMAGE_RMSE
 
 
 def test_render_statistics_within_3_sigma_of_reference(ctx, tmp_path):
