@@ -79,7 +79,7 @@ WORKLOADS = {
 # for the eight-sphere scene, whose Beckmann plastic the reference cannot render (it has GGX only): that
 # fixture comes from the oracle restatement (its "renderer" field says which).
 CONVERGED = {"displaced": "fullsize_displaced.npz", "mixed": "fullsize_mixed_beckmann.npz",
-             "cornell": "stats_cornell.npz"}
+             "cornell": "fullsize_cornell.npz"}
 
 
 def scene_path(workload: str, **override) -> str:

@@ -10,7 +10,7 @@ namespace orion_gb300 {
 
 struct BvhBuildOptions {
   int max_leaf = 4;        // triangles per leaf at most
-  int max_depth = 48;      // depth bound; deeper subtrees fall back to median splits
+  int max_depth = kMaxBvhDepth;  // depth bound; deeper subtrees fall back to median splits
   int bins = 32;           // SAH bins per axis
   int top_bfs_nodes = 0;   // the first N node slots hold the top levels in breadth-first order
   int threads = 0;         // build threads, 0 = hardware concurrency

@@ -299,7 +299,7 @@ extern "C" int orion_gpu_scene_upload(orion_gpu_ctx* ctx, const orion_host_scene
       bo.wide = true;
       bo.max_leaf = 3;
       build_bvh(hs.positions.data(), hs.num_prims(), bo, b.get());
-      if (b->depth >= 48) return fail(ORION_ERR_UNSUPPORTED, "BVH deeper than the traversal stack bound");
+      if (b->depth >= kMaxBvhDepth) return fail(ORION_ERR_UNSUPPORTED, "BVH deeper than the traversal stack bound");
       hsm->tri_class.resize(b->tri_prim.size());
       hsm->class_mask = 1u << SC_MISS;
       for (size_t i = 0; i < hsm->tri_class.size(); ++i) {

@@ -16,6 +16,10 @@
 
 namespace orion_gb300 {
 
+// Deepest BVH (levels of the binary tree below the root) a scene upload accepts;
+// the traversal stacks hold one entry per level.
+constexpr int kMaxBvhDepth = 48;
+
 // BxDFType bits (src/core/bsdf.h:16-24).
 enum : int32_t {
   BXDF_REFLECTION = 1,

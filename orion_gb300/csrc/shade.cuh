@@ -397,9 +397,11 @@ __device__ __forceinline__ void trace_persistent(const SceneOf& scene_of, const 
     }
     if (active) {
       if (lane_step<ANY, SMEM, COUNT, CAP>(r, ts, st, &wk)) {
-        if (r.tmax < 0.f) {  // poisoned by a stack overflow
-          r.tri = -1;
-          atomicOr(err, kErrTraversalStack);
+        if constexpr (CAP < kMaxStack) {
+          if (r.tmax < 0.f) {  // poisoned by a stack overflow
+            r.tri = -1;
+            atomicOr(err, kErrTraversalStack);
+          }
         }
         if (ANY) {
           occluded[pid] = r.tri >= 0;

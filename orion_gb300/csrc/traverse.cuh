@@ -10,22 +10,28 @@
 // shared part spill to a per-thread local array. Each entry is an 8-byte
 // node or triangle group, so popping needs no memory access.
 //
-// A push beyond the stack's capacity writes nothing: the entry is dropped and
-// the ray is poisoned (its tmax set to -1, so no further box or triangle test
-// passes and the traversal drains). The persistent trace kernels turn a
-// poisoned ray into a miss and set kErrTraversalStack (kernels.h) in the launch's
-// error word, so a render returns ORION_ERR_DEVICE instead of writing out of bounds.
-// The BVH builder bounds the wide tree's depth below 48, and one traversal
-// holds at most one entry per level, so the default capacity (96) is never
-// reached; the kernels built with kTestStackEntries (kernels.h) exist to exercise
-// the path.
+// Capacity. A traversal holds at most one stack entry per tree level: an
+// entry is the rest of one visited node's group of hit children, and popping
+// it replaces it by at most one entry of the same level. So the stack never
+// holds more entries than the wide tree has levels, which is at most the
+// binary tree's depth; the builder bounds that below kMaxBvhDepth (48) and
+// orion_gpu_scene_upload rejects any deeper tree, so kMaxStack (96) entries
+// cannot overflow and the production kernels carry no per-push check (a
+// checked push measured 2.7% slower on the 1024x1024 x 64 spp displaced
+// sphere). Kernels built with a smaller capacity (kTestStackEntries, kernels.h:
+// the failure-path tests) check every push: a push beyond the capacity writes
+// nothing, the entry is dropped and the ray poisoned (tmax = -1, so no further
+// box or triangle test passes and the traversal drains); the persistent trace
+// kernels report a poisoned ray as a miss and set kErrTraversalStack in the
+// launch's error word, and the render returns ORION_ERR_DEVICE.
 #pragma once
 #include "device_types.h"
 #include "dmath.cuh"
 
 namespace orion_gb300 {
 
-constexpr int kMaxStack = 96;  // >= wide-tree depth (< 48) + 1
+constexpr int kMaxStack = 96;  // entries; >= the deepest tree a scene upload accepts
+static_assert(kMaxStack > kMaxBvhDepth, "a traversal stack holds one entry per tree level");
 
 struct TraceScene {
   const float4* __restrict__ nodes;  // 5 float4 per WideNode
@@ -46,14 +52,16 @@ struct TraversalStack {
   int stride;
   int sp;
   int2 local[CAP - SMEM > 0 ? CAP - SMEM : 1];
-  // False (and nothing written) when the stack already holds CAP entries.
+  // False (and nothing written) when a test-capacity stack already holds CAP
+  // entries; a kMaxStack stack cannot overflow (see the file comment).
   __device__ __forceinline__ bool push(int2 e) {
+    if constexpr (CAP < kMaxStack) {
+      if (sp >= CAP) return false;
+    }
     if (sp < SMEM)
       smem[sp * stride] = e;
-    else if (sp < CAP)
-      local[sp - SMEM] = e;
     else
-      return false;
+      local[sp - SMEM] = e;
     ++sp;
     return true;
   }
