@@ -136,8 +136,8 @@ int orion_gb300::alloc_wave(Wave& wave, int capacity) {
   const size_t n = (size_t)capacity;
   auto round256 = [](size_t b) { return (b + 255) & ~(size_t)255; };
   const size_t recb = round256(n * sizeof(PathRec)), neeb = round256(n * sizeof(NeeRec));
-  const size_t f4 = round256(n * sizeof(float4)), i4 = round256(n * sizeof(int));
-  const size_t bytes = recb + neeb + f4 + (8 + kShadeClasses) * i4 + 256 + 4096;
+  const size_t f4 = round256(n * sizeof(float4)), i4 = round256(n * sizeof(int)), fb = round256(n);
+  const size_t bytes = recb + neeb + f4 + (8 + kShadeClasses) * i4 + fb + 256 + 4096;
   int rc = wave.block.alloc(bytes);
   if (rc != ORION_OK) {
     wave.capacity = 0;
@@ -181,6 +181,8 @@ int orion_gb300::alloc_wave(Wave& wave, int capacity) {
   }
   w.q_cls = reinterpret_cast<int*>(p);  // class c at q_cls + c * capacity
   p += kShadeClasses * i4;
+  w.qflags = reinterpret_cast<uint8_t*>(p);
+  p += fb;
   w.counters = reinterpret_cast<int*>(p);
   p += 128;
   w.ray_stats = reinterpret_cast<unsigned long long*>(p);  // [0, 3) rays, [4, 10) traversal work
@@ -468,7 +470,7 @@ static int render_impl(orion_gpu_ctx* ctx, orion_scene_id id, const orion_render
   StageTimer timer{nullptr, nullptr, 0, 0};
   if (ctx->profiling) {
     const int64_t waves = (total + wave - 1) / wave;
-    const int need = (int)std::min<int64_t>(waves * (6 * (max_depth + 1) + 4), 200000);
+    const int need = (int)std::min<int64_t>(waves * (8 * (max_depth + 1) + 4), 200000);
     while ((int)ctx->prof_events.size() < 2 * need) {
       cudaEvent_t e;
       CUDA_TRY(cudaEventCreate(&e));

@@ -45,6 +45,7 @@ __global__ void k_camera(SceneView s, WaveView w, WaveArgs a) {
     r.meta = make_int4((int)smp.dim, 0, 0, 0);
     w.rec[pid] = r;
     w.q_ext[0][pid] = pid;
+    w.qflags[pid] = 0;
   }
 }
 
@@ -58,11 +59,11 @@ template <int SMEM, class RayView, class HitView, bool COUNT = false, int CAP = 
 __global__ void __launch_bounds__(512, 2)
     k_trace(SceneView s, const int* queue, const int* count, int* fetch, RayView ray_o, RayView ray_d, HitView hit,
             unsigned long long* stat, int refill_below, int* cls_counters, int* q_cls, int cls_stride,
-            unsigned long long* work, int* err) {
+            unsigned long long* work, int* err, uint8_t* cls_flags) {
   extern __shared__ int2 stack_smem[];
   const int n = *count;
   trace_persistent<false, SMEM, COUNT, CAP>(SingleScene{&s}, queue, n, fetch, ray_o, ray_d, hit, nullptr, stack_smem,
-                                            refill_below, err, cls_counters, q_cls, cls_stride, work);
+                                            refill_below, err, cls_counters, q_cls, cls_stride, work, cls_flags);
   if (stat && blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(stat, (unsigned long long)n);
 }
 
@@ -80,21 +81,89 @@ __global__ void __launch_bounds__(512, 2)
 // One bounce for every path whose extension ray hit a material of shading
 // class SC (or, for SC_MISS, left the scene), with that class's BSDF code only.
 // Launch bounds: at most 96 registers (5 blocks of 128 threads per SM).
+// The queues a path goes to next (light-sample resolution, shadow ray, MIS
+// rays, next extension ray) are recorded as bits of its qflags byte, and
+// k_compact_queues lists them in slot order: the next trace launches then
+// take rays of neighbouring pixels together instead of in the order the
+// shading finished them.
 template <int SC>
 __global__ void __launch_bounds__(128, 5) k_shade(SceneView s, WaveView w, WaveArgs a, int bounce, int cur) {
-  int* out_q = w.q_ext[cur ^ 1];
-  int* out_cnt = w.counters + (cur ^ 1);
   const int n = w.counters[CNT_CLS0 + SC];
   const int* in_q = w.q_cls + (size_t)SC * w.capacity;
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
     const int pid = in_q[q];
     ShadeResult r = shade_one<lobes_of_class(SC), SC == SC_TEXTURED>(
         s, w, a.sobol_bitmajor, pid, (uint64_t)(a.base_index + pid), bounce, a.max_depth, a.rr_depth);
-    queue_append(w.counters + CNT_NEE, w.q_nee, pid, r.did_nee);
-    queue_append(w.counters + CNT_SH, w.q_sh, pid, r.want_sh);
-    queue_append(w.counters + CNT_MIS, w.q_mis, pid, r.want_mis);
-    queue_append(w.counters + CNT_MIS_ENV, w.q_mis_env, pid, r.want_mis_env);
-    queue_append(out_cnt, out_q, pid, r.alive);
+    w.qflags[pid] = (uint8_t)((r.alive ? kQfExt : 0) | (r.did_nee ? kQfNee : 0) | (r.want_sh ? kQfShadow : 0) |
+                              (r.want_mis ? kQfMis : 0) | (r.want_mis_env ? kQfMisEnv : 0));
+  }
+}
+
+// Lists slots in queues from their qflags bytes: bit b of a slot's byte puts
+// the slot in queue b. Slot order within each block's span of kCompactSpan
+// slots (a block reserves its part of each queue with one atomicAdd, so spans
+// land in any order); the bytes are cleared for the next pass. Used twice a
+// bounce: the extension trace marks each slot's shading class (one queue per
+// class), and the shading marks the queues a path goes to next.
+constexpr int kCompactItems = 16, kCompactThreads = 256, kCompactSpan = kCompactItems * kCompactThreads;
+
+struct CompactTargets {
+  int* queue[8];
+  int* counter[8];
+};
+
+template <int NQ>
+__global__ void __launch_bounds__(kCompactThreads) k_compact_queues(uint8_t* flags, int n, CompactTargets tg) {
+  __shared__ int s_warp[kCompactThreads / 32][NQ];
+  __shared__ int s_base[NQ];
+  const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+  const int p0 = blockIdx.x * kCompactSpan + t * kCompactItems;
+  uint32_t words[4] = {0u, 0u, 0u, 0u};
+  if (p0 + kCompactItems <= n) {  // p0 is a multiple of 16: one aligned 16-byte load and store
+    const uint4 v = *reinterpret_cast<const uint4*>(flags + p0);
+    words[0] = v.x, words[1] = v.y, words[2] = v.z, words[3] = v.w;
+    if (v.x | v.y | v.z | v.w) *reinterpret_cast<uint4*>(flags + p0) = make_uint4(0u, 0u, 0u, 0u);
+  } else {
+    for (int j = 0; j < kCompactItems && p0 + j < n; ++j) {
+      words[j >> 2] |= (uint32_t)flags[p0 + j] << (8 * (j & 3));
+      flags[p0 + j] = 0;
+    }
+  }
+  // Late bounces leave most spans empty.
+  if (!__syncthreads_or((words[0] | words[1] | words[2] | words[3]) != 0u)) return;
+  int off[NQ];
+#pragma unroll
+  for (int b = 0; b < NQ; ++b) {
+    int c = 0;
+#pragma unroll
+    for (int k = 0; k < 4; ++k) c += __popc(words[k] & (0x01010101u << b));
+    int x = c;  // inclusive scan over the warp
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    off[b] = x - c;
+    if (lane == 31) s_warp[wid][b] = x;
+  }
+  __syncthreads();
+  if (t < NQ) {
+    int total = 0;
+    for (int k = 0; k < kCompactThreads / 32; ++k) {
+      const int c = s_warp[k][t];
+      s_warp[k][t] = total;
+      total += c;
+    }
+    s_base[t] = total ? atomicAdd(tg.counter[t], total) : 0;
+  }
+  __syncthreads();
+#pragma unroll
+  for (int b = 0; b < NQ; ++b) {
+    int o = s_base[b] + s_warp[wid][b] + off[b];
+    int* q = tg.queue[b];
+#pragma unroll
+    for (int j = 0; j < kCompactItems; ++j)
+      if ((words[j >> 2] >> (8 * (j & 3) + b)) & 1u) q[o++] = p0 + j;
   }
 }
 
@@ -291,7 +360,7 @@ void launch_trace_kernels(int kind, const SceneView& s, const WaveView& w, int c
   if (kind == TK_EXT)
     k_trace<SMEM, RecF4, RecF4, COUNT, CAP><<<grid, block, smem, stream>>>(
         s, w.q_ext[cur], w.counters + cur, w.counters + CNT_FETCH_EXT, w.ray_o, w.ray_d, w.hit, w.ray_stats, refill,
-        w.counters + CNT_CLS0, w.q_cls, w.capacity, work, err);
+        w.counters + CNT_CLS0, w.q_cls, w.capacity, work, err, w.qflags);
   else if (kind == TK_SHADOW)
     k_trace_sh<SMEM, COUNT, CAP><<<grid, block, smem, stream>>>(s, w.q_sh, w.counters + CNT_SH,
                                                                 w.counters + CNT_FETCH_SH, w.sh_o, w.sh_d, w.occluded,
@@ -307,7 +376,7 @@ void launch_trace_kernels(int kind, const SceneView& s, const WaveView& w, int c
                                                                         w.counters + CNT_FETCH_MIS, w.mis_o, w.mis_d,
                                                                         F4{w.mis_hit}, w.ray_stats + 2, refill,
                                                                         nullptr, nullptr, 0,
-                                                                        COUNT ? work + 2 : nullptr, err);
+                                                                        COUNT ? work + 2 : nullptr, err, nullptr);
 }
 
 void trace_dispatch(int kind, const SceneView& s, const WaveView& w, int cur, const LaunchConfig& cfg, int grid,
@@ -351,6 +420,10 @@ void launch_wave(const SceneView& s, const WaveView& w, const WaveArgs& a, const
   end();
   const int tgrid = grid_for(a.n_paths, cfg.trace_block, persistent * 2);
   const int sgrid = grid_for(a.n_paths, cfg.shade_block, persistent * 2);
+  const int compact_grid = (a.n_paths + kCompactSpan - 1) / kCompactSpan;
+  CompactTargets class_tg{};
+  for (int c = 0; c < kShadeClasses; ++c)
+    class_tg.queue[c] = w.q_cls + (size_t)c * w.capacity, class_tg.counter[c] = w.counters + CNT_CLS0 + c;
   int cur = 0;
   for (int bounce = 0; bounce <= a.max_depth; ++bounce) {
     begin(ST_OTHER);
@@ -358,6 +431,10 @@ void launch_wave(const SceneView& s, const WaveView& w, const WaveArgs& a, const
     end();
     begin(ST_TRACE_EXT);
     trace_dispatch(TK_EXT, s, w, cur, cfg, tgrid, stream);
+    end();
+    // The trace marked each finished ray's shading class; list them by class in slot order.
+    begin(ST_OTHER);
+    k_compact_queues<kShadeClasses><<<compact_grid, kCompactThreads, 0, stream>>>(w.qflags, a.n_paths, class_tg);
     end();
     begin(ST_SHADE);
     for (int sc = 0; sc < kShadeClasses; ++sc) {
@@ -377,6 +454,16 @@ void launch_wave(const SceneView& s, const WaveView& w, const WaveArgs& a, const
     }
     --nl;  // end() counts one of them
     end();
+    if (bounce < a.max_depth) {  // after the last bounce no path goes on and no queue is read
+      begin(ST_OTHER);
+      CompactTargets tg{};
+      int* qs[5] = {w.q_ext[cur ^ 1], w.q_nee, w.q_sh, w.q_mis, w.q_mis_env};
+      int* cs[5] = {w.counters + (cur ^ 1), w.counters + CNT_NEE, w.counters + CNT_SH, w.counters + CNT_MIS,
+                    w.counters + CNT_MIS_ENV};
+      for (int q = 0; q < 5; ++q) tg.queue[q] = qs[q], tg.counter[q] = cs[q];
+      k_compact_queues<5><<<compact_grid, kCompactThreads, 0, stream>>>(w.qflags, a.n_paths, tg);
+      end();
+    }
     if (bounce < a.max_depth) {
       begin(ST_TRACE_SHADOW);
       trace_dispatch(TK_SHADOW, s, w, cur, cfg, tgrid, stream);

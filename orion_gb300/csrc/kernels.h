@@ -96,8 +96,15 @@ struct WaveView {
   // visits of the extension, shadow and MIS rays, then their triangle tests.
   unsigned long long* trace_work;
   int* error_word;
+  // Plain renders: per slot, the queues its shading appended it to this
+  // bounce (kQueueFlag* bits); k_compact_queues turns them into the queues,
+  // in slot order, and clears them.
+  uint8_t* qflags;
   int capacity;
 };
+
+// Bits of WaveView::qflags: the queues a shaded path goes to.
+enum QueueFlag { kQfExt = 1, kQfNee = 2, kQfShadow = 4, kQfMis = 8, kQfMisEnv = 16 };
 
 // Bits of a launch's error word (plain renders: WaveView::error_word; batches: BatchCtl::error).
 constexpr int kErrIterationCap = 1;    // a batch loop reached its iteration bound

@@ -348,8 +348,9 @@ struct JobScene {
 // in the kernel and refill idle lanes from the queue through `fetch`, a
 // counter that must be zero at launch. Block size must be a multiple of 32.
 // With `q_cls` (closest hit only), each finished ray's slot is also appended
-// to the queue of the shading class of what it hit (SC_MISS for a miss).
-// COUNT adds the kernel's node visits to work[0] and its triangle tests to
+// to the queue of the shading class of what it hit (SC_MISS for a miss), or,
+// given `cls_flags`, that class's bit is set in the slot's byte there for a
+// compaction pass to list the slots in slot order. COUNT adds the kernel's node visits to work[0] and its triangle tests to
 // work[3]. A ray whose traversal overflowed its stack (capacity CAP) is
 // reported as a miss (not occluded) and sets kErrTraversalStack in *err.
 template <bool ANY, int SMEM, bool COUNT = false, int CAP = kMaxStack, class SceneOf, class RayView, class HitView>
@@ -357,7 +358,8 @@ __device__ __forceinline__ void trace_persistent(const SceneOf& scene_of, const 
                                                  RayView ray_o, RayView ray_d, HitView hit, int* occluded,
                                                  int2* stack_smem, int refill_below, int* err,
                                                  int* cls_counters = nullptr, int* q_cls = nullptr,
-                                                 int cls_stride = 0, unsigned long long* work = nullptr) {
+                                                 int cls_stride = 0, unsigned long long* work = nullptr,
+                                                 uint8_t* cls_flags = nullptr) {
   constexpr unsigned kFull = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   TraversalStack<SMEM, CAP> st;
@@ -408,9 +410,13 @@ __device__ __forceinline__ void trace_persistent(const SceneOf& scene_of, const 
         } else {
           hit[pid] = make_float4(r.tri >= 0 ? r.tmax : kFloatMax, r.u, r.v,
                                  __int_as_float(r.tri >= 0 ? __ldg(ts.tri_prim + r.tri) : -1));
-          if (q_cls)
-            class_append(cls_counters, q_cls, cls_stride, r.tri >= 0 ? (int)__ldg(ts.tri_class + r.tri) : SC_MISS,
-                         pid);
+          if (q_cls) {
+            const int cls = r.tri >= 0 ? (int)__ldg(ts.tri_class + r.tri) : SC_MISS;
+            if (cls_flags)
+              cls_flags[pid] = (uint8_t)(1u << cls);
+            else
+              class_append(cls_counters, q_cls, cls_stride, cls, pid);
+          }
         }
         active = false;
       }
