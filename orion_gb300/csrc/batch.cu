@@ -99,8 +99,11 @@ __global__ void k_b_regen(WaveView w, BatchView b, const uint32_t* sobol) {
 
 // kind 0: extension rays (current queue), 1: shadow rays, 2: MIS rays towards
 // area lights, 3: MIS rays towards environment lights (occlusion).
+// cls_flags (wave mode): extension hits mark their slot's shading class there
+// for k_b_compact instead of appending to the class queues.
 template <int SMEM>
-__global__ void __launch_bounds__(512, 2) k_b_trace(WaveView w, BatchView b, int kind, int refill_below) {
+__global__ void __launch_bounds__(512, 2) k_b_trace(WaveView w, BatchView b, int kind, int refill_below,
+                                                     uint8_t* cls_flags) {
   extern __shared__ int2 stack_smem[];
   BatchCtl& c = *b.ctl;
   JobScene js{b.jobs, w.job};
@@ -109,7 +112,7 @@ __global__ void __launch_bounds__(512, 2) k_b_trace(WaveView w, BatchView b, int
     n = c.counters[CNT_EXT0 + c.cur];
     trace_persistent<false, SMEM>(js, w.q_ext[c.cur], n, &c.counters[CNT_FETCH_EXT], w.ray_o, w.ray_d, w.hit,
                                   nullptr, stack_smem, refill_below, &c.error, &c.counters[CNT_CLS0], w.q_cls,
-                                  w.capacity);
+                                  w.capacity, nullptr, cls_flags);
   } else if (kind == 1) {
     n = c.counters[CNT_SH];
     trace_persistent<true, SMEM>(js, w.q_sh, n, &c.counters[CNT_FETCH_SH], w.sh_o, w.sh_d,
@@ -128,8 +131,12 @@ __global__ void __launch_bounds__(512, 2) k_b_trace(WaveView w, BatchView b, int
 
 // Shading of the slots whose extension ray hit a material of class SC (or
 // missed, SC_MISS), each against its job's scene.
+// waves: a wave's paths are never retired one by one, and the queues they go
+// to are marked in the slots' qflags bytes for k_b_compact (slot order, as in
+// plain renders); pooled mode appends to the queues directly.
 template <int SC>
-__global__ void __launch_bounds__(128, 5) k_b_shade(WaveView w, BatchView b, const uint32_t* sobol_bitmajor) {
+__global__ void __launch_bounds__(128, 5) k_b_shade(WaveView w, BatchView b, const uint32_t* sobol_bitmajor,
+                                                    int waves) {
   BatchCtl& c = *b.ctl;
   const int cur = c.cur;
   const int n = c.counters[CNT_CLS0 + SC];
@@ -142,12 +149,42 @@ __global__ void __launch_bounds__(128, 5) k_b_shade(WaveView w, BatchView b, con
     ShadeResult r = shade_one<lobes_of_class(SC), SC == SC_TEXTURED>(
         J.scene, w, sobol_bitmajor, pid, (uint64_t)slot_index(w, pid), bounce, J.max_depth, J.rr_depth);
     if (r.alive) w.bounce[pid] = bounce + 1;
+    if (waves) {
+      w.qflags[pid] = (uint8_t)((r.alive ? kQfExt : 0) | (r.did_nee ? kQfNee : 0) | (r.want_sh ? kQfShadow : 0) |
+                                (r.want_mis ? kQfMis : 0) | (r.want_mis_env ? kQfMisEnv : 0));
+      continue;
+    }
     queue_append(&c.counters[CNT_NEE], w.q_nee, pid, r.did_nee);
     queue_append(&c.counters[CNT_SH], w.q_sh, pid, r.want_sh);
     queue_append(&c.counters[CNT_MIS], w.q_mis, pid, r.want_mis);
     queue_append(&c.counters[CNT_MIS_ENV], w.q_mis_env, pid, r.want_mis_env);
     queue_append(&c.counters[CNT_EXT0 + (cur ^ 1)], w.q_ext[cur ^ 1], pid, r.alive);
     queue_append(&c.counters[CNT_RETIRE], b.q_retire, pid, !r.alive);
+  }
+}
+
+// Wave mode: the slots' qflags bytes into queues in slot order (plain
+// renders' compaction, compact_queues). which 0: shading classes, after the
+// extension trace; 1: the queues the shading sent paths to (next extension
+// queue by the current parity, which only the device knows inside a graph).
+__global__ void __launch_bounds__(kCompactThreads) k_b_compact(WaveView w, BatchView b, int which) {
+  BatchCtl& c = *b.ctl;
+  const int n = c.wave_n;
+  if (blockIdx.x * kCompactSpan >= n) return;
+  CompactTargets tg{};
+  if (which == 0) {
+    for (int k = 0; k < kShadeClasses; ++k) {
+      tg.queue[k] = w.q_cls + (size_t)k * w.capacity;
+      tg.counter[k] = &c.counters[CNT_CLS0 + k];
+    }
+    compact_queues<kShadeClasses>(w.qflags, n, tg);
+  } else {
+    const int next = c.cur ^ 1;
+    int* qs[5] = {w.q_ext[next], w.q_nee, w.q_sh, w.q_mis, w.q_mis_env};
+    int* cs[5] = {&c.counters[CNT_EXT0 + next], &c.counters[CNT_NEE], &c.counters[CNT_SH], &c.counters[CNT_MIS],
+                  &c.counters[CNT_MIS_ENV]};
+    for (int k = 0; k < 5; ++k) tg.queue[k] = qs[k], tg.counter[k] = cs[k];
+    compact_queues<5>(w.qflags, n, tg);
   }
 }
 
@@ -202,6 +239,7 @@ __global__ void k_b_wave_begin(BatchView b, int n, int iteration_cap) {
   c.cur = 0;
   for (int k = 0; k < kCounterSlots; ++k) c.counters[k] = 0;
   c.counters[CNT_EXT0] = n;
+  c.wave_n = n;
   c.max_iterations = c.iterations + iteration_cap;
   c.more = 1;
 }
@@ -227,6 +265,7 @@ __global__ void k_b_wave_camera(WaveView w, BatchView b, const uint32_t* sobol, 
     r.meta = make_int4((int)smp.dim, job, 0, (int)((unsigned long long)index >> 32));
     w.rec[i] = r;
     w.q_ext[0][i] = i;
+    w.qflags[i] = 0;
   }
 }
 
@@ -270,19 +309,21 @@ __global__ void k_b_control(BatchView b, cudaGraphConditionalHandle cond, int in
 }
 
 template <int SMEM>
-void launch_b_trace(const WaveView& w, const BatchView& b, int kind, int grid, int block, int refill, cudaStream_t s) {
-  k_b_trace<SMEM><<<grid, block, (size_t)SMEM * block * sizeof(int2), s>>>(w, b, kind, refill);
+void launch_b_trace(const WaveView& w, const BatchView& b, int kind, int grid, int block, int refill,
+                    uint8_t* cls_flags, cudaStream_t s) {
+  k_b_trace<SMEM><<<grid, block, (size_t)SMEM * block * sizeof(int2), s>>>(w, b, kind, refill, cls_flags);
 }
 
-void b_trace(const LaunchConfig& cfg, const WaveView& w, const BatchView& b, int kind, int grid, cudaStream_t s) {
+void b_trace(const LaunchConfig& cfg, const WaveView& w, const BatchView& b, int kind, int grid, uint8_t* cls_flags,
+             cudaStream_t s) {
   const int block = cfg.trace_block;
   const int refill = cfg.refill_below < 1 ? 1 : (cfg.refill_below > 32 ? 32 : cfg.refill_below);
   switch (cfg.smem_stack) {
-    case 0: launch_b_trace<0>(w, b, kind, grid, block, refill, s); break;
-    case 8: launch_b_trace<8>(w, b, kind, grid, block, refill, s); break;
-    case 24: launch_b_trace<24>(w, b, kind, grid, block, refill, s); break;
-    case 32: launch_b_trace<32>(w, b, kind, grid, block, refill, s); break;
-    default: launch_b_trace<16>(w, b, kind, grid, block, refill, s); break;
+    case 0: launch_b_trace<0>(w, b, kind, grid, block, refill, cls_flags, s); break;
+    case 8: launch_b_trace<8>(w, b, kind, grid, block, refill, cls_flags, s); break;
+    case 24: launch_b_trace<24>(w, b, kind, grid, block, refill, cls_flags, s); break;
+    case 32: launch_b_trace<32>(w, b, kind, grid, block, refill, cls_flags, s); break;
+    default: launch_b_trace<16>(w, b, kind, grid, block, refill, cls_flags, s); break;
   }
 }
 
@@ -349,30 +390,41 @@ void enqueue_iteration(const WaveView& w, const BatchView& b, const uint32_t* so
   k_b_plan<<<1, 32, 0, stream>>>(b);  // wave mode: counters reset, nothing to take
   if (!waves) k_b_regen<<<grid_cap(cap, 256, persistent * 4), 256, 0, stream>>>(w, b, sobol);
   end();
+  const int cgrid = (cap + kCompactSpan - 1) / kCompactSpan;
   begin(ST_TRACE_EXT);
-  b_trace(cfg, w, b, 0, tgrid, stream);
+  b_trace(cfg, w, b, 0, tgrid, waves ? w.qflags : nullptr, stream);
   end();
+  if (waves) {  // the trace marked the slots' shading classes: list them in slot order
+    begin(ST_OTHER);
+    k_b_compact<<<cgrid, kCompactThreads, 0, stream>>>(w, b, 0);
+    end();
+  }
   begin(ST_SHADE);
   for (int sc = 0; sc < kShadeClasses; ++sc) {
     if (!((class_mask >> sc) & 1u)) continue;
     switch (sc) {
-      case SC_DIFFUSE: k_b_shade<SC_DIFFUSE><<<sgrid, cfg.shade_block, 0, stream>>>(w, b, sobol_bitmajor); break;
-      case SC_CONDUCTOR: k_b_shade<SC_CONDUCTOR><<<sgrid, cfg.shade_block, 0, stream>>>(w, b, sobol_bitmajor); break;
-      case SC_SPECULAR: k_b_shade<SC_SPECULAR><<<sgrid, cfg.shade_block, 0, stream>>>(w, b, sobol_bitmajor); break;
-      case SC_DIELECTRIC: k_b_shade<SC_DIELECTRIC><<<sgrid, cfg.shade_block, 0, stream>>>(w, b, sobol_bitmajor); break;
-      case SC_PLASTIC: k_b_shade<SC_PLASTIC><<<sgrid, cfg.shade_block, 0, stream>>>(w, b, sobol_bitmajor); break;
-      case SC_GENERAL: k_b_shade<SC_GENERAL><<<sgrid, cfg.shade_block, 0, stream>>>(w, b, sobol_bitmajor); break;
-      case SC_TEXTURED: k_b_shade<SC_TEXTURED><<<sgrid, cfg.shade_block, 0, stream>>>(w, b, sobol_bitmajor); break;
-      case SC_MISS: k_b_shade<SC_MISS><<<sgrid, cfg.shade_block, 0, stream>>>(w, b, sobol_bitmajor); break;
+      case SC_DIFFUSE: k_b_shade<SC_DIFFUSE><<<sgrid, cfg.shade_block, 0, stream>>>(w, b, sobol_bitmajor, waves); break;
+      case SC_CONDUCTOR: k_b_shade<SC_CONDUCTOR><<<sgrid, cfg.shade_block, 0, stream>>>(w, b, sobol_bitmajor, waves); break;
+      case SC_SPECULAR: k_b_shade<SC_SPECULAR><<<sgrid, cfg.shade_block, 0, stream>>>(w, b, sobol_bitmajor, waves); break;
+      case SC_DIELECTRIC: k_b_shade<SC_DIELECTRIC><<<sgrid, cfg.shade_block, 0, stream>>>(w, b, sobol_bitmajor, waves); break;
+      case SC_PLASTIC: k_b_shade<SC_PLASTIC><<<sgrid, cfg.shade_block, 0, stream>>>(w, b, sobol_bitmajor, waves); break;
+      case SC_GENERAL: k_b_shade<SC_GENERAL><<<sgrid, cfg.shade_block, 0, stream>>>(w, b, sobol_bitmajor, waves); break;
+      case SC_TEXTURED: k_b_shade<SC_TEXTURED><<<sgrid, cfg.shade_block, 0, stream>>>(w, b, sobol_bitmajor, waves); break;
+      case SC_MISS: k_b_shade<SC_MISS><<<sgrid, cfg.shade_block, 0, stream>>>(w, b, sobol_bitmajor, waves); break;
     }
   }
   end();
+  if (waves) {  // the shading marked the queues its paths go to
+    begin(ST_OTHER);
+    k_b_compact<<<cgrid, kCompactThreads, 0, stream>>>(w, b, 1);
+    end();
+  }
   begin(ST_TRACE_SHADOW);
-  b_trace(cfg, w, b, 1, tgrid, stream);
+  b_trace(cfg, w, b, 1, tgrid, nullptr, stream);
   end();
   begin(ST_TRACE_MIS);
-  b_trace(cfg, w, b, 2, tgrid, stream);
-  b_trace(cfg, w, b, 3, tgrid, stream);
+  b_trace(cfg, w, b, 2, tgrid, nullptr, stream);
+  b_trace(cfg, w, b, 3, tgrid, nullptr, stream);
   end();
   begin(ST_RESOLVE);
   k_b_resolve<<<sgrid, cfg.shade_block, 0, stream>>>(w, b);

@@ -288,13 +288,15 @@ static int run_batch_waves_locked(orion_gpu_ctx* ctx, std::vector<DevJob>& dj, u
     cudaStream_t es = engine_stream(ctx, e);
     CUDA_TRY(cudaMemcpyAsync(bvs[e].jobs, dj.data(), (size_t)njobs * sizeof(DevJob), cudaMemcpyHostToDevice, es));
     CUDA_TRY(cudaMemcpyAsync(bvs[e].ctl, &zero, sizeof(BatchCtl), cudaMemcpyHostToDevice, es));
+    // The queue-compaction bytes start clear (other entry points share the slots' memory).
+    CUDA_TRY(cudaMemsetAsync(engine_wave(ctx, e).view.qflags, 0, (size_t)caps[e], es));
   }
   // Every live path advances one bounce per iteration: a bound on each wave's loop.
   const int iteration_cap =
       ctx->cfg.test_batch_iterations > 0 ? ctx->cfg.test_batch_iterations : 2 * (max_depth_all + 2) + 8;
   StageTimer timer{nullptr, nullptr, 0, 0};
   if (ctx->profiling) {
-    const int need = (int)std::min<int64_t>(nwaves * iteration_cap * 8, 200000);
+    const int need = (int)std::min<int64_t>(nwaves * iteration_cap * 10, 200000);
     while ((int)ctx->prof_events.size() < 2 * need) {
       cudaEvent_t e;
       CUDA_TRY(cudaEventCreate(&e));
@@ -359,9 +361,9 @@ static int run_batch_waves_locked(orion_gpu_ctx* ctx, std::vector<DevJob>& dj, u
       out.iterations += o.iterations;
     }
     error_bits |= o.error;
-    // Per iteration: plan, 4 traces, one shade per class, resolve, control.
+    // Per iteration: plan, 4 traces, 2 queue compactions, one shade per class, resolve, control.
     const unsigned launched = ctx->profiling ? mask : ctx->beng[e].loop[ORION_BATCH_WAVES].mask;
-    launches += (7LL + __builtin_popcount(launched)) * o.iterations;
+    launches += (9LL + __builtin_popcount(launched)) * o.iterations;
   }
   launches += 3 * nwaves;  // begin, camera, film per wave
   out.error = error_bits;

@@ -99,72 +99,9 @@ __global__ void __launch_bounds__(128, 5) k_shade(SceneView s, WaveView w, WaveA
   }
 }
 
-// Lists slots in queues from their qflags bytes: bit b of a slot's byte puts
-// the slot in queue b. Slot order within each block's span of kCompactSpan
-// slots (a block reserves its part of each queue with one atomicAdd, so spans
-// land in any order); the bytes are cleared for the next pass. Used twice a
-// bounce: the extension trace marks each slot's shading class (one queue per
-// class), and the shading marks the queues a path goes to next.
-constexpr int kCompactItems = 16, kCompactThreads = 256, kCompactSpan = kCompactItems * kCompactThreads;
-
-struct CompactTargets {
-  int* queue[8];
-  int* counter[8];
-};
-
 template <int NQ>
 __global__ void __launch_bounds__(kCompactThreads) k_compact_queues(uint8_t* flags, int n, CompactTargets tg) {
-  __shared__ int s_warp[kCompactThreads / 32][NQ];
-  __shared__ int s_base[NQ];
-  const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
-  const int p0 = blockIdx.x * kCompactSpan + t * kCompactItems;
-  uint32_t words[4] = {0u, 0u, 0u, 0u};
-  if (p0 + kCompactItems <= n) {  // p0 is a multiple of 16: one aligned 16-byte load and store
-    const uint4 v = *reinterpret_cast<const uint4*>(flags + p0);
-    words[0] = v.x, words[1] = v.y, words[2] = v.z, words[3] = v.w;
-    if (v.x | v.y | v.z | v.w) *reinterpret_cast<uint4*>(flags + p0) = make_uint4(0u, 0u, 0u, 0u);
-  } else {
-    for (int j = 0; j < kCompactItems && p0 + j < n; ++j) {
-      words[j >> 2] |= (uint32_t)flags[p0 + j] << (8 * (j & 3));
-      flags[p0 + j] = 0;
-    }
-  }
-  // Late bounces leave most spans empty.
-  if (!__syncthreads_or((words[0] | words[1] | words[2] | words[3]) != 0u)) return;
-  int off[NQ];
-#pragma unroll
-  for (int b = 0; b < NQ; ++b) {
-    int c = 0;
-#pragma unroll
-    for (int k = 0; k < 4; ++k) c += __popc(words[k] & (0x01010101u << b));
-    int x = c;  // inclusive scan over the warp
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const int y = __shfl_up_sync(0xffffffffu, x, o);
-      if (lane >= o) x += y;
-    }
-    off[b] = x - c;
-    if (lane == 31) s_warp[wid][b] = x;
-  }
-  __syncthreads();
-  if (t < NQ) {
-    int total = 0;
-    for (int k = 0; k < kCompactThreads / 32; ++k) {
-      const int c = s_warp[k][t];
-      s_warp[k][t] = total;
-      total += c;
-    }
-    s_base[t] = total ? atomicAdd(tg.counter[t], total) : 0;
-  }
-  __syncthreads();
-#pragma unroll
-  for (int b = 0; b < NQ; ++b) {
-    int o = s_base[b] + s_warp[wid][b] + off[b];
-    int* q = tg.queue[b];
-#pragma unroll
-    for (int j = 0; j < kCompactItems; ++j)
-      if ((words[j >> 2] >> (8 * (j & 3) + b)) & 1u) q[o++] = p0 + j;
-  }
+  compact_queues<NQ>(flags, n, tg);
 }
 
 __global__ void k_resolve(SceneView s, WaveView w) {
