@@ -208,6 +208,15 @@ extern "C" int orion_gpu_create(const orion_gpu_opts* opts, orion_gpu_ctx** out)
   CUDA_TRY(cudaGetDeviceProperties(&prop, c->device));
   c->num_sms = prop.multiProcessorCount;
   CUDA_TRY(cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking));
+  {
+    cudaMemPoolProps props = {};
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = c->device;
+    CUDA_TRY(cudaMemPoolCreate(&c->scene_pool, &props));
+    uint64_t keep = UINT64_MAX;  // freed scene memory stays with the pool for the next upload
+    CUDA_TRY(cudaMemPoolSetAttribute(c->scene_pool, cudaMemPoolAttrReleaseThreshold, &keep));
+  }
   for (cudaStream_t& x : c->xstream) CUDA_TRY(cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking));
   CUDA_TRY(cudaEventCreate(&c->ev0));
   CUDA_TRY(cudaEventCreate(&c->ev1));
@@ -253,6 +262,7 @@ extern "C" int orion_gpu_destroy(orion_gpu_ctx* ctx) {
   for (cudaStream_t x : ctx->xstream)
     if (x) cudaStreamSynchronize(x);
   ctx->scenes.clear();
+  cudaStreamSynchronize(ctx->stream);  // the scenes' pooled memory is back in the pool
   ctx->wave.block.alloc(0);
   for (Wave& w : ctx->xwave) w.block.alloc(0);
   for (BatchEngine& e : ctx->beng) e.drop_graph();
@@ -267,13 +277,14 @@ extern "C" int orion_gpu_destroy(orion_gpu_ctx* ctx) {
   for (cudaStream_t x : ctx->xstream)
     if (x) cudaStreamDestroy(x);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  if (ctx->scene_pool) cudaMemPoolDestroy(ctx->scene_pool);
   delete ctx;
   return ORION_OK;
 }
 
 template <class T>
-static int upload(DevBuf& b, const std::vector<T>& v, cudaStream_t s, int64_t* bytes) {
-  int rc = b.alloc(v.size() * sizeof(T));
+static int upload(DevBuf& b, const std::vector<T>& v, cudaMemPool_t pool, cudaStream_t s, int64_t* bytes) {
+  int rc = b.alloc_pooled(v.size() * sizeof(T), pool, s);
   if (rc != ORION_OK) return rc;
   if (!v.empty()) CUDA_TRY(cudaMemcpyAsync(b.p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice, s));
   *bytes += (int64_t)b.bytes;
@@ -321,32 +332,32 @@ extern "C" int orion_gpu_scene_upload(orion_gpu_ctx* ctx, const orion_host_scene
   std::unique_ptr<DeviceScene> d(new DeviceScene());
   int64_t bytes = 0;
   int rc;
-  if ((rc = upload(d->nodes, bvh.wide, ctx->stream, &bytes)) != ORION_OK) return rc;
-  if ((rc = upload(d->woop, bvh.woop, ctx->stream, &bytes)) != ORION_OK) return rc;
-  if ((rc = upload(d->tri_prim, bvh.tri_prim, ctx->stream, &bytes)) != ORION_OK) return rc;
+  if ((rc = upload(d->nodes, bvh.wide, ctx->scene_pool, ctx->stream, &bytes)) != ORION_OK) return rc;
+  if ((rc = upload(d->woop, bvh.woop, ctx->scene_pool, ctx->stream, &bytes)) != ORION_OK) return rc;
+  if ((rc = upload(d->tri_prim, bvh.tri_prim, ctx->scene_pool, ctx->stream, &bytes)) != ORION_OK) return rc;
   d->class_mask = hsm->class_mask;
-  if ((rc = upload(d->tri_class, hsm->tri_class, ctx->stream, &bytes)) != ORION_OK) return rc;
-  if ((rc = upload(d->prims, ps.prims, ctx->stream, &bytes)) != ORION_OK) return rc;
-  if ((rc = upload(d->mats, ps.mats, ctx->stream, &bytes)) != ORION_OK) return rc;
-  if ((rc = upload(d->lights, ps.lights, ctx->stream, &bytes)) != ORION_OK) return rc;
-  if ((rc = upload(d->lfunc, ps.light_func, ctx->stream, &bytes)) != ORION_OK) return rc;
-  if ((rc = upload(d->lcdf, ps.light_cdf, ctx->stream, &bytes)) != ORION_OK) return rc;
+  if ((rc = upload(d->tri_class, hsm->tri_class, ctx->scene_pool, ctx->stream, &bytes)) != ORION_OK) return rc;
+  if ((rc = upload(d->prims, ps.prims, ctx->scene_pool, ctx->stream, &bytes)) != ORION_OK) return rc;
+  if ((rc = upload(d->mats, ps.mats, ctx->scene_pool, ctx->stream, &bytes)) != ORION_OK) return rc;
+  if ((rc = upload(d->lights, ps.lights, ctx->scene_pool, ctx->stream, &bytes)) != ORION_OK) return rc;
+  if ((rc = upload(d->lfunc, ps.light_func, ctx->scene_pool, ctx->stream, &bytes)) != ORION_OK) return rc;
+  if ((rc = upload(d->lcdf, ps.light_cdf, ctx->scene_pool, ctx->stream, &bytes)) != ORION_OK) return rc;
   // Image environment maps: the float block, then their records pointing into it.
-  if ((rc = upload(d->env_data, ps.env_data, ctx->stream, &bytes)) != ORION_OK) return rc;
+  if ((rc = upload(d->env_data, ps.env_data, ctx->scene_pool, ctx->stream, &bytes)) != ORION_OK) return rc;
   std::vector<DevEnvMap> envs;
   const float* eb = d->env_data.as<float>();
   for (const PreparedScene::EnvMapLayout& e : ps.envmaps)
     envs.push_back(DevEnvMap{e.width, e.height, e.marg_int, 0, eb + e.texels, eb + e.cond_func, eb + e.cond_cdf,
                              eb + e.cond_int, eb + e.marg_func, eb + e.marg_cdf});
-  if ((rc = upload(d->envmaps, envs, ctx->stream, &bytes)) != ORION_OK) return rc;
+  if ((rc = upload(d->envmaps, envs, ctx->scene_pool, ctx->stream, &bytes)) != ORION_OK) return rc;
   // Image textures: records pointing into the same block, the materials'
   // builder inputs, and per-primitive texture coordinates.
   std::vector<DevTexture> texs;
   for (const PreparedScene::TextureLayout& t : ps.textures) texs.push_back(DevTexture{t.width, t.height, eb + t.texels});
   if (!texs.empty()) {
-    if ((rc = upload(d->textures, texs, ctx->stream, &bytes)) != ORION_OK) return rc;
-    if ((rc = upload(d->mat_src, ps.mat_src, ctx->stream, &bytes)) != ORION_OK) return rc;
-    if ((rc = upload(d->prim_uv, ps.prim_uv, ctx->stream, &bytes)) != ORION_OK) return rc;
+    if ((rc = upload(d->textures, texs, ctx->scene_pool, ctx->stream, &bytes)) != ORION_OK) return rc;
+    if ((rc = upload(d->mat_src, ps.mat_src, ctx->scene_pool, ctx->stream, &bytes)) != ORION_OK) return rc;
+    if ((rc = upload(d->prim_uv, ps.prim_uv, ctx->scene_pool, ctx->stream, &bytes)) != ORION_OK) return rc;
   }
   CUDA_TRY(cudaStreamSynchronize(ctx->stream));
   SceneView& v = d->view;

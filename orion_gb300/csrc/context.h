@@ -53,13 +53,23 @@ int fail(int code, const std::string& msg);
 struct DevBuf {
   void* p = nullptr;
   size_t bytes = 0;
-  ~DevBuf() {
-    if (p) cudaFree(p);
-  }
-  int alloc(size_t n) {
-    if (p) cudaFree(p);
+  // Non-null: p came from a memory pool in this stream's order (alloc_pooled)
+  // and goes back to it in the same order, without a device-wide sync.
+  cudaStream_t pool_stream = nullptr;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) {
+      if (pool_stream)
+        cudaFreeAsync(p, pool_stream);
+      else
+        cudaFree(p);
+    }
     p = nullptr;
     bytes = 0;
+    pool_stream = nullptr;
+  }
+  int alloc(size_t n) {
+    release();
     if (n == 0) n = 16;
     cudaError_t e = cudaMalloc(&p, n);
     if (e != cudaSuccess) {
@@ -68,6 +78,20 @@ struct DevBuf {
                   std::string("cudaMalloc(") + std::to_string(n) + "): " + cudaGetErrorString(e));
     }
     bytes = n;
+    return ORION_OK;
+  }
+  // From `pool`, in the order of stream `s` (usable by work later on `s`).
+  int alloc_pooled(size_t n, cudaMemPool_t pool, cudaStream_t s) {
+    release();
+    if (n == 0) n = 16;
+    cudaError_t e = cudaMallocFromPoolAsync(&p, n, pool, s);
+    if (e != cudaSuccess) {
+      p = nullptr;
+      return fail(e == cudaErrorMemoryAllocation ? ORION_ERR_NOMEM : ORION_ERR_CUDA,
+                  std::string("cudaMallocFromPoolAsync(") + std::to_string(n) + "): " + cudaGetErrorString(e));
+    }
+    bytes = n;
+    pool_stream = s;
     return ORION_OK;
   }
   template <class T>
@@ -133,6 +157,10 @@ struct orion_gpu_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
   int num_sms = 0;
+  // Resident scenes' arrays come from this pool in the order of `stream`:
+  // uploading and releasing scenes (serving evicts and re-uploads them) then
+  // reuses the memory with no cudaMalloc or device-wide cudaFree sync.
+  cudaMemPool_t scene_pool = nullptr;
   DevBuf sobol, sobol_bitmajor;
   std::map<int, std::unique_ptr<DeviceScene>> scenes;
   int next_id = 1;
