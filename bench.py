@@ -833,7 +833,8 @@ def main():
     ap.add_argument("--serve-views", type=int, default=16)
     ap.add_argument("--serve-rates", type=float, nargs="+", default=[5.0, 20.0, 50.0, 100.0, 200.0])
     ap.add_argument("--serve-requests", type=int, default=2000, help="served leg: requests over all arrival rates")
-    ap.add_argument("--spp-chunk", type=int, default=4, help="served leg: progressive spp per pass")
+    # 16: 146 req/s saturated and p50 8.5 ms at 50 req/s, against 137 req/s and 16.4 ms with chunks of 4
+    ap.add_argument("--spp-chunk", type=int, default=16, help="served leg: progressive spp per pass")
     ap.add_argument("--plain-requests", type=int, default=32, help="served leg: requests timed on the plain path")
     ap.add_argument("--batch-only", action="store_true", help="run the batched leg alone (profiling)")
     ap.add_argument("--sppm-res", type=int, default=512, help="SPPM leg: image side (0 = skip)")

@@ -293,6 +293,7 @@ static int upload(DevBuf& b, const std::vector<T>& v, cudaMemPool_t pool, cudaSt
 
 extern "C" int orion_gpu_scene_upload(orion_gpu_ctx* ctx, const orion_host_scene* scene, orion_scene_id* out) {
   if (!ctx || !scene || !out) return fail(ORION_ERR_INVALID, "null argument");
+  NvtxRange range("orion_gpu_scene_upload");
   std::lock_guard<std::mutex> g(ctx->mu);
   CUDA_TRY(cudaSetDevice(ctx->device));
   const HostScene& hs = scene->s;
@@ -420,6 +421,7 @@ extern "C" int orion_gpu_scene_bytes(orion_gpu_ctx* ctx, orion_scene_id id, int6
 static int render_impl(orion_gpu_ctx* ctx, orion_scene_id id, const orion_render_params* params, float* film_rgb,
                        uint32_t* film_count, double* sum64, double* sumsq64, bool take_lock = true) {
   if (!ctx) return fail(ORION_ERR_INVALID, "null context");
+  NvtxRange range("orion_gpu_render");
   std::unique_lock<std::mutex> g(ctx->mu, std::defer_lock);
   if (take_lock) g.lock();
   CUDA_TRY(cudaSetDevice(ctx->device));

@@ -435,6 +435,7 @@ static int plan_batch(orion_gpu_ctx* ctx, int32_t njobs, const orion_job* jobs, 
 extern "C" int orion_gpu_render_batch(orion_gpu_ctx* ctx, int32_t njobs, const orion_job* jobs,
                                       orion_batch_stats* stats) {
   if (!ctx || njobs < 0 || (njobs > 0 && !jobs)) return fail(ORION_ERR_INVALID, "bad argument");
+  NvtxRange range("orion_gpu_render_batch");
   std::lock_guard<std::mutex> g(ctx->mu);
   CUDA_TRY(cudaSetDevice(ctx->device));
   if (njobs == 0) {
@@ -617,6 +618,7 @@ namespace orion_gb300 {
 
 int ctx_run_device_jobs(orion_gpu_ctx* ctx, const DeviceFilmJob* jobs, int njobs, double* device_ms,
                         int64_t* paths) {
+  NvtxRange range("orion_server launch");
   std::lock_guard<std::mutex> g(ctx->mu);
   CUDA_TRY(cudaSetDevice(ctx->device));
   std::vector<DevJob> dj(njobs);

@@ -13,6 +13,7 @@ using namespace orion_gb300;
 extern "C" int orion_gpu_render_sppm(orion_gpu_ctx* ctx, orion_scene_id id, const orion_sppm_params* params,
                                      float* film_rgb_sum, uint32_t* film_count) {
   if (!ctx || !film_rgb_sum) return fail(ORION_ERR_INVALID, "null argument");
+  NvtxRange range("orion_gpu_render_sppm");
   std::lock_guard<std::mutex> g(ctx->mu);
   CUDA_TRY(cudaSetDevice(ctx->device));
   auto it = ctx->scenes.find(id);

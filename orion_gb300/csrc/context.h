@@ -2,6 +2,7 @@
 // device context and the helpers they share. Not part of the ABI.
 #pragma once
 #include <cuda_runtime.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include <map>
 #include <memory>
@@ -43,6 +44,16 @@ int fail(int code, const std::string& msg);
     cudaError_t e_ = (call);                                                                           \
     if (e_ != cudaSuccess) return fail(ORION_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
   } while (0)
+
+// A named NVTX range over a scope: the entry points mark their host work so a
+// timeline profiler shows renders, uploads and batches beside the kernels
+// (header-only NVTX: a no-op unless a profiler is attached).
+struct NvtxRange {
+  explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+  ~NvtxRange() { nvtxRangePop(); }
+  NvtxRange(const NvtxRange&) = delete;
+  NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 #define RC(x)                        \
   do {                               \
