@@ -169,22 +169,21 @@ __global__ void __launch_bounds__(128, 5) k_b_shade(WaveView w, BatchView b, con
 // queue by the current parity, which only the device knows inside a graph).
 __global__ void __launch_bounds__(kCompactThreads) k_b_compact(WaveView w, BatchView b, int which) {
   BatchCtl& c = *b.ctl;
-  const int n = c.wave_n;
-  if (blockIdx.x * kCompactSpan >= n) return;
+  const int cur = c.cur;
   CompactTargets tg{};
   if (which == 0) {
     for (int k = 0; k < kShadeClasses; ++k) {
       tg.queue[k] = w.q_cls + (size_t)k * w.capacity;
       tg.counter[k] = &c.counters[CNT_CLS0 + k];
     }
-    compact_queues<kShadeClasses>(w.qflags, n, tg);
+    compact_queues<kShadeClasses>(w.qflags, w.q_ext[cur], &c.counters[CNT_EXT0 + cur], tg);
   } else {
-    const int next = c.cur ^ 1;
+    const int next = cur ^ 1;
     int* qs[5] = {w.q_ext[next], w.q_nee, w.q_sh, w.q_mis, w.q_mis_env};
     int* cs[5] = {&c.counters[CNT_EXT0 + next], &c.counters[CNT_NEE], &c.counters[CNT_SH], &c.counters[CNT_MIS],
                   &c.counters[CNT_MIS_ENV]};
     for (int k = 0; k < 5; ++k) tg.queue[k] = qs[k], tg.counter[k] = cs[k];
-    compact_queues<5>(w.qflags, n, tg);
+    compact_queues<5>(w.qflags, w.q_ext[cur], &c.counters[CNT_EXT0 + cur], tg);
   }
 }
 
@@ -239,7 +238,6 @@ __global__ void k_b_wave_begin(BatchView b, int n, int iteration_cap) {
   c.cur = 0;
   for (int k = 0; k < kCounterSlots; ++k) c.counters[k] = 0;
   c.counters[CNT_EXT0] = n;
-  c.wave_n = n;
   c.max_iterations = c.iterations + iteration_cap;
   c.more = 1;
 }
@@ -390,7 +388,7 @@ void enqueue_iteration(const WaveView& w, const BatchView& b, const uint32_t* so
   k_b_plan<<<1, 32, 0, stream>>>(b);  // wave mode: counters reset, nothing to take
   if (!waves) k_b_regen<<<grid_cap(cap, 256, persistent * 4), 256, 0, stream>>>(w, b, sobol);
   end();
-  const int cgrid = (cap + kCompactSpan - 1) / kCompactSpan;
+  const int cgrid = grid_cap(cap, kCompactSpan, cfg.num_sms * 8);
   begin(ST_TRACE_EXT);
   b_trace(cfg, w, b, 0, tgrid, waves ? w.qflags : nullptr, stream);
   end();

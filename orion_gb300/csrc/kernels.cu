@@ -100,8 +100,9 @@ __global__ void __launch_bounds__(128, 5) k_shade(SceneView s, WaveView w, WaveA
 }
 
 template <int NQ>
-__global__ void __launch_bounds__(kCompactThreads) k_compact_queues(uint8_t* flags, int n, CompactTargets tg) {
-  compact_queues<NQ>(flags, n, tg);
+__global__ void __launch_bounds__(kCompactThreads) k_compact_queues(uint8_t* flags, const int* list, const int* count,
+                                                                    CompactTargets tg) {
+  compact_queues<NQ>(flags, list, count, tg);
 }
 
 __global__ void k_resolve(SceneView s, WaveView w) {
@@ -357,7 +358,7 @@ void launch_wave(const SceneView& s, const WaveView& w, const WaveArgs& a, const
   end();
   const int tgrid = grid_for(a.n_paths, cfg.trace_block, persistent * 2);
   const int sgrid = grid_for(a.n_paths, cfg.shade_block, persistent * 2);
-  const int compact_grid = (a.n_paths + kCompactSpan - 1) / kCompactSpan;
+  const int compact_grid = grid_for(a.n_paths, kCompactSpan, cfg.num_sms * 8);
   CompactTargets class_tg{};
   for (int c = 0; c < kShadeClasses; ++c)
     class_tg.queue[c] = w.q_cls + (size_t)c * w.capacity, class_tg.counter[c] = w.counters + CNT_CLS0 + c;
@@ -371,7 +372,8 @@ void launch_wave(const SceneView& s, const WaveView& w, const WaveArgs& a, const
     end();
     // The trace marked each finished ray's shading class; list them by class in slot order.
     begin(ST_OTHER);
-    k_compact_queues<kShadeClasses><<<compact_grid, kCompactThreads, 0, stream>>>(w.qflags, a.n_paths, class_tg);
+    k_compact_queues<kShadeClasses><<<compact_grid, kCompactThreads, 0, stream>>>(w.qflags, w.q_ext[cur],
+                                                                                  w.counters + cur, class_tg);
     end();
     begin(ST_SHADE);
     for (int sc = 0; sc < kShadeClasses; ++sc) {
@@ -398,7 +400,8 @@ void launch_wave(const SceneView& s, const WaveView& w, const WaveArgs& a, const
       int* cs[5] = {w.counters + (cur ^ 1), w.counters + CNT_NEE, w.counters + CNT_SH, w.counters + CNT_MIS,
                     w.counters + CNT_MIS_ENV};
       for (int q = 0; q < 5; ++q) tg.queue[q] = qs[q], tg.counter[q] = cs[q];
-      k_compact_queues<5><<<compact_grid, kCompactThreads, 0, stream>>>(w.qflags, a.n_paths, tg);
+      k_compact_queues<5><<<compact_grid, kCompactThreads, 0, stream>>>(w.qflags, w.q_ext[cur], w.counters + cur,
+                                                                           tg);
       end();
     }
     if (bounce < a.max_depth) {

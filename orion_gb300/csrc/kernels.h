@@ -149,7 +149,6 @@ struct BatchCtl {
   unsigned long long rays[3];    // ext, shadow, mis
   unsigned long long paths_done;
   int more;                      // host-driven loop: 1 while another iteration is needed
-  int wave_n;                    // wave mode: slots of the current wave
 };
 
 struct BatchView {

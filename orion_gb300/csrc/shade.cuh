@@ -435,12 +435,15 @@ __device__ __forceinline__ void trace_persistent(const SceneOf& scene_of, const 
 }
 
 // Lists slots in queues from their qflags bytes: bit b of a slot's byte puts
-// the slot in queue b. Run by blocks of kCompactThreads threads, each over a
-// span of kCompactSpan slots: slot order within a span (a block reserves its
-// part of each queue with one atomicAdd, so spans land in any order); the
-// bytes are cleared for the next pass. Used twice a bounce: the extension
-// trace marks each slot's shading class (one queue per class), and the
-// shading marks the queues a path goes to next.
+// the slot in queue b. The slots looked at are list[0 .. *count) (the bounce's
+// extension queue: every slot traced and shaded this bounce), so the cost
+// follows the live paths, not the wave. Blocks of kCompactThreads threads take
+// spans of kCompactSpan list entries in turn: list order within a span (a
+// block reserves its part of each queue with one atomicAdd, so spans land in
+// any order), and the list is itself in slot order span by span, so the
+// queues come out in slot order too. The bytes are cleared for the next pass.
+// Used twice a bounce: the extension trace marks each slot's shading class
+// (one queue per class), and the shading marks the queues a path goes to next.
 constexpr int kCompactItems = 16, kCompactThreads = 256, kCompactSpan = kCompactItems * kCompactThreads;
 
 struct CompactTargets {
@@ -449,57 +452,72 @@ struct CompactTargets {
 };
 
 template <int NQ>
-__device__ __forceinline__ void compact_queues(uint8_t* flags, int n, const CompactTargets& tg) {
+__device__ __forceinline__ void compact_queues(uint8_t* flags, const int* list, const int* count,
+                                               const CompactTargets& tg) {
   __shared__ int s_warp[kCompactThreads / 32][NQ];
   __shared__ int s_base[NQ];
   const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
-  const int p0 = blockIdx.x * kCompactSpan + t * kCompactItems;
-  uint32_t words[4] = {0u, 0u, 0u, 0u};
-  if (p0 + kCompactItems <= n) {  // p0 is a multiple of 16: one aligned 16-byte load and store
-    const uint4 v = *reinterpret_cast<const uint4*>(flags + p0);
-    words[0] = v.x, words[1] = v.y, words[2] = v.z, words[3] = v.w;
-    if (v.x | v.y | v.z | v.w) *reinterpret_cast<uint4*>(flags + p0) = make_uint4(0u, 0u, 0u, 0u);
-  } else {
-    for (int j = 0; j < kCompactItems && p0 + j < n; ++j) {
-      words[j >> 2] |= (uint32_t)flags[p0 + j] << (8 * (j & 3));
-      flags[p0 + j] = 0;
+  const int n = *count;
+  for (int span = blockIdx.x; span * kCompactSpan < n; span += gridDim.x) {
+    const int p0 = span * kCompactSpan + t * kCompactItems;
+    int slot[kCompactItems];
+    uint32_t words[4] = {0u, 0u, 0u, 0u};
+    if (p0 + kCompactItems <= n) {  // p0 is a multiple of 16: four aligned 16-byte loads of the list
+      const int4* l4 = reinterpret_cast<const int4*>(list + p0);
+#pragma unroll
+      for (int k = 0; k < 4; ++k) {
+        const int4 v = l4[k];
+        slot[4 * k] = v.x, slot[4 * k + 1] = v.y, slot[4 * k + 2] = v.z, slot[4 * k + 3] = v.w;
+      }
+    } else {
+#pragma unroll
+      for (int j = 0; j < kCompactItems; ++j) slot[j] = p0 + j < n ? list[p0 + j] : -1;
     }
-  }
-  // Late bounces leave most spans empty.
-  if (!__syncthreads_or((words[0] | words[1] | words[2] | words[3]) != 0u)) return;
-  int off[NQ];
-#pragma unroll
-  for (int b = 0; b < NQ; ++b) {
-    int c = 0;
-#pragma unroll
-    for (int k = 0; k < 4; ++k) c += __popc(words[k] & (0x01010101u << b));
-    int x = c;  // inclusive scan over the warp
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const int y = __shfl_up_sync(0xffffffffu, x, o);
-      if (lane >= o) x += y;
-    }
-    off[b] = x - c;
-    if (lane == 31) s_warp[wid][b] = x;
-  }
-  __syncthreads();
-  if (t < NQ) {
-    int total = 0;
-    for (int k = 0; k < kCompactThreads / 32; ++k) {
-      const int c = s_warp[k][t];
-      s_warp[k][t] = total;
-      total += c;
-    }
-    s_base[t] = total ? atomicAdd(tg.counter[t], total) : 0;
-  }
-  __syncthreads();
-#pragma unroll
-  for (int b = 0; b < NQ; ++b) {
-    int o = s_base[b] + s_warp[wid][b] + off[b];
-    int* q = tg.queue[b];
 #pragma unroll
     for (int j = 0; j < kCompactItems; ++j)
-      if ((words[j >> 2] >> (8 * (j & 3) + b)) & 1u) q[o++] = p0 + j;
+      if (slot[j] >= 0) {
+        const uint32_t f = flags[slot[j]];
+        if (f) {
+          words[j >> 2] |= f << (8 * (j & 3));
+          flags[slot[j]] = 0;
+        }
+      }
+    if (!__syncthreads_or((words[0] | words[1] | words[2] | words[3]) != 0u)) continue;
+    int off[NQ];
+#pragma unroll
+    for (int b = 0; b < NQ; ++b) {
+      int c = 0;
+#pragma unroll
+      for (int k = 0; k < 4; ++k) c += __popc(words[k] & (0x01010101u << b));
+      int x = c;  // inclusive scan over the warp
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+      }
+      off[b] = x - c;
+      if (lane == 31) s_warp[wid][b] = x;
+    }
+    __syncthreads();
+    if (t < NQ) {
+      int total = 0;
+      for (int k = 0; k < kCompactThreads / 32; ++k) {
+        const int c = s_warp[k][t];
+        s_warp[k][t] = total;
+        total += c;
+      }
+      s_base[t] = total ? atomicAdd(tg.counter[t], total) : 0;
+    }
+    __syncthreads();
+#pragma unroll
+    for (int b = 0; b < NQ; ++b) {
+      int o = s_base[b] + s_warp[wid][b] + off[b];
+      int* q = tg.queue[b];
+#pragma unroll
+      for (int j = 0; j < kCompactItems; ++j)
+        if ((words[j >> 2] >> (8 * (j & 3) + b)) & 1u) q[o++] = slot[j];
+    }
+    __syncthreads();  // s_warp and s_base are reused by the block's next span
   }
 }
 
