@@ -251,16 +251,16 @@ __global__ void k_b_wave_camera(WaveView w, BatchView b, const uint32_t* sobol, 
     const long long index = J.first_index + (long long)(work - (unsigned long long)J.work_begin);
     const long long wh = (long long)J.width * J.height;
     const long long pix = index % wh;
-    PathSampler smp{sobol, (uint64_t)index, 5u};
     V3 o, d;
-    camera_ray(J.scene.cam, smp, (int)(pix % J.width), (int)(pix / J.width), &o, &d);
+    const uint32_t dim = camera_ray_block(J.scene.cam, sobol, (uint64_t)index, (int)(pix % J.width),
+                                          (int)(pix / J.width), &o, &d);
     PathRec r;
     r.o = f4(o, 0.f);
     r.d = f4(d, 0.f);
     r.beta = make_float4(1.f, 1.f, 1.f, 0.f);
     r.L = make_float4(0.f, 0.f, 0.f, __uint_as_float((uint32_t)(unsigned long long)index));
     r.hit = make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
-    r.meta = make_int4((int)smp.dim, job, 0, (int)((unsigned long long)index >> 32));
+    r.meta = make_int4((int)dim, job, 0, (int)((unsigned long long)index >> 32));
     w.rec[i] = r;
     w.q_ext[0][i] = i;
     w.qflags[i] = 0;
@@ -459,8 +459,8 @@ void launch_batch_iteration(const WaveView& w, const BatchView& b, const uint32_
                     timer);
 }
 
-void launch_batch_wave_begin(const WaveView& w, const BatchView& b, const uint32_t* sobol, unsigned long long base,
-                             int n, int iteration_cap, int num_sms, cudaStream_t stream) {
+void launch_batch_wave_begin(const WaveView& w, const BatchView& b, const uint32_t* sobol,
+                             unsigned long long base, int n, int iteration_cap, int num_sms, cudaStream_t stream) {
   k_b_wave_begin<<<1, 32, 0, stream>>>(b, n, iteration_cap);
   k_b_wave_camera<<<grid_cap(n, 256, num_sms * 32), 256, 0, stream>>>(w, b, sobol, base, n);
 }

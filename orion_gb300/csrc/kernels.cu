@@ -33,16 +33,15 @@ __global__ void k_camera(SceneView s, WaveView w, WaveArgs a) {
     int64_t index = a.base_index + pid;
     int64_t pix = index % wh;
     int i = (int)(pix % a.width), j = (int)(pix / a.width);
-    PathSampler smp{a.sobol, (uint64_t)index, 5u};
     V3 o, d;
-    camera_ray(s.cam, smp, i, j, &o, &d);
+    const uint32_t dim = camera_ray_block(s.cam, a.sobol, (uint64_t)index, i, j, &o, &d);
     PathRec r;  // written whole: three full sectors
     r.o = f4(o, 0.f);
     r.d = f4(d, 0.f);
     r.beta = make_float4(1.f, 1.f, 1.f, 0.f);
     r.L = make_float4(0.f, 0.f, 0.f, 0.f);
     r.hit = make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
-    r.meta = make_int4((int)smp.dim, 0, 0, 0);
+    r.meta = make_int4((int)dim, 0, 0, 0);
     w.rec[pid] = r;
     w.q_ext[0][pid] = pid;
     w.qflags[pid] = 0;

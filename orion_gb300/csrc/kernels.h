@@ -252,8 +252,8 @@ void launch_batch_iteration(const WaveView& w, const BatchView& b, const uint32_
 // Wave mode: starts a wave of work items [base, base + n) on slots 0..n-1
 // (at most `iteration_cap` more loop iterations), and after its loop adds
 // the n paths' radiance to their jobs' films.
-void launch_batch_wave_begin(const WaveView& w, const BatchView& b, const uint32_t* sobol, unsigned long long base,
-                             int n, int iteration_cap, int num_sms, cudaStream_t stream);
+void launch_batch_wave_begin(const WaveView& w, const BatchView& b, const uint32_t* sobol,
+                             unsigned long long base, int n, int iteration_cap, int num_sms, cudaStream_t stream);
 void launch_batch_wave_film(const WaveView& w, const BatchView& b, int n, int num_sms, cudaStream_t stream);
 // dst[i] = (float)src[i] for i < n.
 void launch_film_to_f32(const double* src, float* dst, long long n, int num_sms, cudaStream_t stream);

@@ -124,8 +124,9 @@ __device__ __forceinline__ TraceScene trace_scene(const SceneView& s) { return T
 // Sampler::next2() builds Point2f(next(), next()) (src/core/sampler.h:29); the
 // two calls are unsequenced and the compiled reference evaluates the second
 // first, so .x holds the later dimension. All 2-D samples follow that order.
-__device__ __forceinline__ void camera_ray(const DevCamera& c, PathSampler& smp, int i, int j, V3* o, V3* d) {
-  float s0 = smp.next(), s1 = smp.next();
+// u: the path's sample dimensions 5..8 in order (pixel jitter, then lens).
+__device__ __forceinline__ void camera_ray_u(const DevCamera& c, const float u[4], int i, int j, V3* o, V3* d) {
+  float s0 = u[0], s1 = u[1];
   float rx = (float)i + s1;
   float ry = (float)j + s0;
   float xx = (2.f * rx / (float)c.width - 1.f) * c.aspect * c.tan_half_fov;
@@ -135,7 +136,7 @@ __device__ __forceinline__ void camera_ray(const DevCamera& c, PathSampler& smp,
   if (c.lens_radius > 0.f) {
     V3 target = org + dir * c.focal_distance;
     float lx, ly;
-    float l0 = smp.next(), l1 = smp.next();
+    float l0 = u[2], l1 = u[3];
     concentric_sample_disk(l1, l0, &lx, &ly);
     org = V3{lx * c.lens_radius, ly * c.lens_radius, 0.f};
     dir = normalize(target - org);
@@ -151,6 +152,33 @@ __device__ __forceinline__ void camera_ray(const DevCamera& c, PathSampler& smp,
     *o = vdiv(V3{xp, yp, zp}, wp);
   *d = V3{m[0] * dir.x + m[1] * dir.y + m[2] * dir.z, m[4] * dir.x + m[5] * dir.y + m[6] * dir.z,
           m[8] * dir.x + m[9] * dir.y + m[10] * dir.z};
+}
+
+// Pinhole::generateRay from a path's sampler (dimensions consumed in order).
+__device__ __forceinline__ void camera_ray(const DevCamera& c, PathSampler& smp, int i, int j, V3* o, V3* d) {
+  float u[4];
+  u[0] = smp.next();
+  u[1] = smp.next();
+  if (c.lens_radius > 0.f) {
+    u[2] = smp.next();
+    u[3] = smp.next();
+  }
+  camera_ray_u(c, u, i, j, o, d);
+}
+
+// The same with its 2 (pinhole) or 4 (thin lens) sample dimensions taken in
+// one pass over the index bits; returns the next sample dimension (7 or 9).
+__device__ __forceinline__ uint32_t camera_ray_block(const DevCamera& c, const uint32_t* __restrict__ matrices,
+                                                     uint64_t index, int i, int j, V3* o, V3* d) {
+  float u[4];
+  if (c.lens_radius > 0.f) {
+    sobol_dims<4>(matrices, index, 5u, u);
+  } else {
+    sobol_dims<2>(matrices, index, 5u, u);
+    u[2] = u[3] = 0.f;
+  }
+  camera_ray_u(c, u, i, j, o, d);
+  return c.lens_radius > 0.f ? 9u : 7u;
 }
 
 // One bounce of PathTracing::Li (src/integrator/path.cpp:56-97) for path slot
