@@ -135,7 +135,7 @@ __global__ void __launch_bounds__(512, 2) k_b_trace(WaveView w, BatchView b, int
 // to are marked in the slots' qflags bytes for k_b_compact (slot order, as in
 // plain renders); pooled mode appends to the queues directly.
 template <int SC>
-__global__ void __launch_bounds__(128, 5) k_b_shade(WaveView w, BatchView b, const uint32_t* sobol_bitmajor,
+__global__ void __launch_bounds__(128, 5) k_b_shade(WaveView w, BatchView b, const uint32_t* sobol,
                                                     int waves) {
   BatchCtl& c = *b.ctl;
   const int cur = c.cur;
@@ -147,7 +147,7 @@ __global__ void __launch_bounds__(128, 5) k_b_shade(WaveView w, BatchView b, con
     const DevJob& J = b.jobs[meta.y];
     const int bounce = meta.z;
     ShadeResult r = shade_one<lobes_of_class(SC), SC == SC_TEXTURED>(
-        J.scene, w, sobol_bitmajor, pid, (uint64_t)slot_index(w, pid), bounce, J.max_depth, J.rr_depth);
+        J.scene, w, sobol, pid, (uint64_t)slot_index(w, pid), bounce, J.max_depth, J.rr_depth);
     if (r.alive) w.bounce[pid] = bounce + 1;
     if (waves) {
       w.qflags[pid] = (uint8_t)((r.alive ? kQfExt : 0) | (r.did_nee ? kQfNee : 0) | (r.want_sh ? kQfShadow : 0) |
@@ -371,7 +371,7 @@ void launch_batch_init(const WaveView& w, const BatchView& b, int capacity, cuda
 namespace {
 
 // One loop iteration's kernels on `stream`, optionally timed per stage.
-void enqueue_iteration(const WaveView& w, const BatchView& b, const uint32_t* sobol, const uint32_t* sobol_bitmajor,
+void enqueue_iteration(const WaveView& w, const BatchView& b, const uint32_t* sobol,
                        const LaunchConfig& cfg, unsigned class_mask, bool waves, cudaGraphConditionalHandle cond,
                        int in_graph, cudaStream_t stream, StageTimer* timer) {
   const int cap = w.capacity;
@@ -401,14 +401,14 @@ void enqueue_iteration(const WaveView& w, const BatchView& b, const uint32_t* so
   for (int sc = 0; sc < kShadeClasses; ++sc) {
     if (!((class_mask >> sc) & 1u)) continue;
     switch (sc) {
-      case SC_DIFFUSE: k_b_shade<SC_DIFFUSE><<<sgrid, cfg.shade_block, 0, stream>>>(w, b, sobol_bitmajor, waves); break;
-      case SC_CONDUCTOR: k_b_shade<SC_CONDUCTOR><<<sgrid, cfg.shade_block, 0, stream>>>(w, b, sobol_bitmajor, waves); break;
-      case SC_SPECULAR: k_b_shade<SC_SPECULAR><<<sgrid, cfg.shade_block, 0, stream>>>(w, b, sobol_bitmajor, waves); break;
-      case SC_DIELECTRIC: k_b_shade<SC_DIELECTRIC><<<sgrid, cfg.shade_block, 0, stream>>>(w, b, sobol_bitmajor, waves); break;
-      case SC_PLASTIC: k_b_shade<SC_PLASTIC><<<sgrid, cfg.shade_block, 0, stream>>>(w, b, sobol_bitmajor, waves); break;
-      case SC_GENERAL: k_b_shade<SC_GENERAL><<<sgrid, cfg.shade_block, 0, stream>>>(w, b, sobol_bitmajor, waves); break;
-      case SC_TEXTURED: k_b_shade<SC_TEXTURED><<<sgrid, cfg.shade_block, 0, stream>>>(w, b, sobol_bitmajor, waves); break;
-      case SC_MISS: k_b_shade<SC_MISS><<<sgrid, cfg.shade_block, 0, stream>>>(w, b, sobol_bitmajor, waves); break;
+      case SC_DIFFUSE: k_b_shade<SC_DIFFUSE><<<sgrid, cfg.shade_block, 0, stream>>>(w, b, sobol, waves); break;
+      case SC_CONDUCTOR: k_b_shade<SC_CONDUCTOR><<<sgrid, cfg.shade_block, 0, stream>>>(w, b, sobol, waves); break;
+      case SC_SPECULAR: k_b_shade<SC_SPECULAR><<<sgrid, cfg.shade_block, 0, stream>>>(w, b, sobol, waves); break;
+      case SC_DIELECTRIC: k_b_shade<SC_DIELECTRIC><<<sgrid, cfg.shade_block, 0, stream>>>(w, b, sobol, waves); break;
+      case SC_PLASTIC: k_b_shade<SC_PLASTIC><<<sgrid, cfg.shade_block, 0, stream>>>(w, b, sobol, waves); break;
+      case SC_GENERAL: k_b_shade<SC_GENERAL><<<sgrid, cfg.shade_block, 0, stream>>>(w, b, sobol, waves); break;
+      case SC_TEXTURED: k_b_shade<SC_TEXTURED><<<sgrid, cfg.shade_block, 0, stream>>>(w, b, sobol, waves); break;
+      case SC_MISS: k_b_shade<SC_MISS><<<sgrid, cfg.shade_block, 0, stream>>>(w, b, sobol, waves); break;
     }
   }
   end();
@@ -440,23 +440,20 @@ void enqueue_iteration(const WaveView& w, const BatchView& b, const uint32_t* so
 }  // namespace
 
 cudaError_t capture_batch_iteration(const WaveView& w, const BatchView& b, const uint32_t* sobol,
-                                    const uint32_t* sobol_bitmajor, const LaunchConfig& cfg, unsigned class_mask,
-                                    bool waves, cudaGraphConditionalHandle cond, cudaStream_t stream,
+                                    const LaunchConfig& cfg, unsigned class_mask, bool waves, cudaGraphConditionalHandle cond, cudaStream_t stream,
                                     cudaGraph_t body) {
   cudaError_t e = cudaStreamBeginCaptureToGraph(stream, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal);
   if (e != cudaSuccess) return e;
-  enqueue_iteration(w, b, sobol, sobol_bitmajor, cfg, class_mask, waves, cond, 1, stream, nullptr);
+  enqueue_iteration(w, b, sobol, cfg, class_mask, waves, cond, 1, stream, nullptr);
   cudaGraph_t out = body;
   cudaError_t e2 = cudaStreamEndCapture(stream, &out);
   cudaError_t e3 = cudaGetLastError();
   return e2 != cudaSuccess ? e2 : e3;
 }
 
-void launch_batch_iteration(const WaveView& w, const BatchView& b, const uint32_t* sobol,
-                            const uint32_t* sobol_bitmajor, const LaunchConfig& cfg, unsigned class_mask, bool waves,
-                            cudaStream_t stream, StageTimer* timer) {
-  enqueue_iteration(w, b, sobol, sobol_bitmajor, cfg, class_mask, waves, cudaGraphConditionalHandle{}, 0, stream,
-                    timer);
+void launch_batch_iteration(const WaveView& w, const BatchView& b, const uint32_t* sobol, const LaunchConfig& cfg,
+                            unsigned class_mask, bool waves, cudaStream_t stream, StageTimer* timer) {
+  enqueue_iteration(w, b, sobol, cfg, class_mask, waves, cudaGraphConditionalHandle{}, 0, stream, timer);
 }
 
 void launch_batch_wave_begin(const WaveView& w, const BatchView& b, const uint32_t* sobol,

@@ -236,11 +236,6 @@ extern "C" int orion_gpu_create(const orion_gpu_opts* opts, orion_gpu_ctx** out)
   int rc = c->sobol.alloc(m.size() * sizeof(uint32_t));
   if (rc != ORION_OK) return rc;
   CUDA_TRY(cudaMemcpy(c->sobol.p, m.data(), m.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
-  std::vector<uint32_t> bm(m.size());
-  for (int d = 0; d < 1024; ++d)
-    for (int b = 0; b < 52; ++b) bm[(size_t)b * 1024 + d] = m[(size_t)d * 52 + b];
-  if ((rc = c->sobol_bitmajor.alloc(bm.size() * sizeof(uint32_t))) != ORION_OK) return rc;
-  CUDA_TRY(cudaMemcpy(c->sobol_bitmajor.p, bm.data(), bm.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
   c->cfg.num_sms = c->num_sms;
   c->cfg.trace_block = 128;
   c->cfg.shade_block = 128;
@@ -502,7 +497,6 @@ static int render_impl(orion_gpu_ctx* ctx, orion_scene_id id, const orion_render
     const int slot = (int)(k % ns);
     WaveArgs a;
     a.sobol = ctx->sobol.as<uint32_t>();
-    a.sobol_bitmajor = ctx->sobol_bitmajor.as<uint32_t>();
     a.base_index = first + off;
     a.n_paths = (int)std::min<int64_t>(wave, total - off);
     a.width = d.width;

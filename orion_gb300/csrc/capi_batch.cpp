@@ -53,8 +53,7 @@ static int build_batch_graph(orion_gpu_ctx* ctx, int e, int mode, const BatchVie
   cudaGraphNode_t node;
   CUDA_TRY(cudaGraphAddNode(&node, be.graph, nullptr, nullptr, 0, &np));
   cudaGraph_t body = np.conditional.phGraph_out[0];
-  cudaError_t ce = capture_batch_iteration(wave.view, bv, ctx->sobol.as<uint32_t>(), ctx->sobol_bitmajor.as<uint32_t>(),
-                                           ctx->cfg, mask, mode == ORION_BATCH_WAVES, cond, engine_stream(ctx, e), body);
+  cudaError_t ce = capture_batch_iteration(wave.view, bv, ctx->sobol.as<uint32_t>(), ctx->cfg, mask, mode == ORION_BATCH_WAVES, cond, engine_stream(ctx, e), body);
   if (ce != cudaSuccess) {
     // A graph whose loop-body capture was invalidated is dropped, not
     // destroyed: nothing is assumed about its state after the failure.
@@ -193,8 +192,8 @@ static int run_batch_pooled_locked(orion_gpu_ctx* ctx, std::vector<DevJob>& dj, 
     StageTimer timer{ctx->prof_events.data(), ctx->prof_stage.data(), need, 0};
     int more = 1;
     for (int it = 0; more && it < init[0].max_iterations; ++it) {
-      launch_batch_iteration(ctx->wave.view, bvs[0], ctx->sobol.as<uint32_t>(), ctx->sobol_bitmajor.as<uint32_t>(),
-                             ctx->cfg, masks[0], false, s, &timer);
+      launch_batch_iteration(ctx->wave.view, bvs[0], ctx->sobol.as<uint32_t>(), ctx->cfg, masks[0], false, s,
+                             &timer);
       CUDA_TRY(cudaGetLastError());
       CUDA_TRY(cudaMemcpyAsync(&more, &bvs[0].ctl->more, sizeof(int), cudaMemcpyDeviceToHost, s));
       CUDA_TRY(cudaStreamSynchronize(s));
@@ -317,8 +316,7 @@ static int run_batch_waves_locked(orion_gpu_ctx* ctx, std::vector<DevJob>& dj, u
     if (ctx->profiling) {
       int more = 1;
       for (int it = 0; more && it < iteration_cap; ++it) {
-        launch_batch_iteration(wv, bvs[e], ctx->sobol.as<uint32_t>(), ctx->sobol_bitmajor.as<uint32_t>(), ctx->cfg,
-                               mask, true, es, &timer);
+        launch_batch_iteration(wv, bvs[e], ctx->sobol.as<uint32_t>(), ctx->cfg, mask, true, es, &timer);
         CUDA_TRY(cudaGetLastError());
         CUDA_TRY(cudaMemcpyAsync(&more, &bvs[e].ctl->more, sizeof(int), cudaMemcpyDeviceToHost, es));
         CUDA_TRY(cudaStreamSynchronize(es));

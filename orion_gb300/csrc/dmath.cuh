@@ -213,25 +213,6 @@ __device__ __forceinline__ float sobol_sample(const uint32_t* __restrict__ matri
   return __uint2float_rn(r) * 2.3283064365386963e-10f;
 }
 
-// Eight consecutive dimensions d0..d0+7 of one sample index in a single pass
-// over the index bits, from the bit-major copy of the matrices (word (b, d)
-// at b * kSobolDims + d): per set bit, eight independent loads from one or
-// two 32-byte sectors instead of eight dependent lookup chains. Requires
-// d0 + 8 <= kSobolDims. Values are identical to sobol_sample.
-__device__ __forceinline__ void sobol_block8(const uint32_t* __restrict__ bitmajor, uint64_t index, uint32_t d0,
-                                             float out[8]) {
-  uint32_t r[8] = {0, 0, 0, 0, 0, 0, 0, 0};
-  while (index) {
-    int b = __ffsll((long long)index) - 1;
-    index &= index - 1;
-    const uint32_t* row = bitmajor + (size_t)b * kSobolDims + d0;
-#pragma unroll
-    for (int k = 0; k < 8; ++k) r[k] ^= __ldg(row + k);
-  }
-#pragma unroll
-  for (int k = 0; k < 8; ++k) out[k] = __uint2float_rn(r[k]) * 2.3283064365386963e-10f;
-}
-
 // N consecutive dimensions d0..d0+N-1 in one pass over the index bits, from
 // the dimension-major matrices (N short rows that stay in L1): N independent
 // lookups per set bit instead of N dependent chains (camera rays: pixel

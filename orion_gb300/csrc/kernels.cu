@@ -92,7 +92,7 @@ __global__ void __launch_bounds__(128, 5) k_shade(SceneView s, WaveView w, WaveA
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
     const int pid = in_q[q];
     ShadeResult r = shade_one<lobes_of_class(SC), SC == SC_TEXTURED>(
-        s, w, a.sobol_bitmajor, pid, (uint64_t)(a.base_index + pid), bounce, a.max_depth, a.rr_depth);
+        s, w, a.sobol, pid, (uint64_t)(a.base_index + pid), bounce, a.max_depth, a.rr_depth);
     w.qflags[pid] = (uint8_t)((r.alive ? kQfExt : 0) | (r.did_nee ? kQfNee : 0) | (r.want_sh ? kQfShadow : 0) |
                               (r.want_mis ? kQfMis : 0) | (r.want_mis_env ? kQfMisEnv : 0));
   }

@@ -168,7 +168,6 @@ __device__ __forceinline__ long long slot_index(const WaveView& w, int pid) {
 
 struct WaveArgs {
   const uint32_t* sobol;          // dimension-major Sobol matrices (1024 x 52)
-  const uint32_t* sobol_bitmajor; // the same words bit-major (52 x 1024)
   int64_t base_index;  // sample index of path slot 0
   int n_paths;
   int width, height;
@@ -241,14 +240,12 @@ cudaError_t configure_batch_kernels(int smem_bytes, KernelLimits* lim);
 // Shading kernels are launched for the classes in `class_mask` only.
 // waves: the iteration of wave mode (no refills, no per-iteration film).
 cudaError_t capture_batch_iteration(const WaveView& w, const BatchView& b, const uint32_t* sobol,
-                                    const uint32_t* sobol_bitmajor, const LaunchConfig& cfg, unsigned class_mask,
-                                    bool waves, cudaGraphConditionalHandle cond, cudaStream_t stream,
-                                    cudaGraph_t body);
+                                    const LaunchConfig& cfg, unsigned class_mask, bool waves,
+                                    cudaGraphConditionalHandle cond, cudaStream_t stream, cudaGraph_t body);
 // The same iteration launched directly (a host-driven loop reading ctl->more),
 // each stage timed by `timer`: the profiling path of the batched engine.
-void launch_batch_iteration(const WaveView& w, const BatchView& b, const uint32_t* sobol,
-                            const uint32_t* sobol_bitmajor, const LaunchConfig& cfg, unsigned class_mask, bool waves,
-                            cudaStream_t stream, StageTimer* timer);
+void launch_batch_iteration(const WaveView& w, const BatchView& b, const uint32_t* sobol, const LaunchConfig& cfg,
+                            unsigned class_mask, bool waves, cudaStream_t stream, StageTimer* timer);
 // Wave mode: starts a wave of work items [base, base + n) on slots 0..n-1
 // (at most `iteration_cap` more loop iterations), and after its loop adds
 // the n paths' radiance to their jobs' films.
