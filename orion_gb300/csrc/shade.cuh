@@ -417,7 +417,7 @@ __device__ __forceinline__ void trace_persistent(const SceneOf& scene_of, const 
           ts = TraceScene{s.nodes, s.woop, s.tri_prim, s.tri_class};
           const float4 o4 = ray_o[pid], d4 = ray_d[pid];
           st.sp = 0;
-          lane_start(r, o4, d4, ANY ? o4.w : kFloatMax);
+          lane_start(r, o4, d4, ANY ? o4.w : kFloatMax, ANY);
           active = true;
         }
       }

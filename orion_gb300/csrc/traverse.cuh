@@ -157,8 +157,11 @@ __device__ __forceinline__ uint32_t octant_permute(uint32_t x, uint32_t oct) {
   return x;
 }
 
+// oct: the ray's octant (which box planes are near); ord: the octant whose
+// near-to-far child order the node group lists (oct for closest hit, its
+// opposite for occlusion: far children first).
 __device__ __forceinline__ void wide_node(const float4* __restrict__ nodes, int idx, V3 o, V3 idir, uint32_t oct,
-                                          float tnear, float tmax, uint2& ng, uint2& tg) {
+                                          float tnear, float tmax, uint2& ng, uint2& tg, uint32_t ord) {
   const float4* n = nodes + 5 * (size_t)idx;
   const float4 n0 = __ldg(n), n1 = __ldg(n + 1), n2 = __ldg(n + 2), n3 = __ldg(n + 3), n4 = __ldg(n + 4);
   const uint32_t ew = __float_as_uint(n0.w);
@@ -190,7 +193,7 @@ __device__ __forceinline__ void wide_node(const float4* __restrict__ nodes, int 
                            fminf(fmaf(q8(zf[h], b), sz, oz), tmax));
     hm |= (tn <= tf ? 1u : 0u) << s;
   }
-  const uint32_t hits = octant_permute(hm & imask, oct);
+  const uint32_t hits = octant_permute(hm & imask, ord);
   uint32_t tris = 0u;
   const uint32_t meta[2] = {__float_as_uint(n1.z), __float_as_uint(n1.w)};
   for (uint32_t lh = hm & ~imask; lh; lh &= lh - 1u) {
@@ -212,8 +215,9 @@ __device__ __forceinline__ int take_child(uint2& ng, uint32_t oct) {
   return child;
 }
 
-// ANY = false: closest hit over (tnear, tfar]. ANY = true: first hit found.
-// A stack overflow ends the traversal with a miss (see the file comment).
+// ANY = false: closest hit over (tnear, tfar]. ANY = true: first hit found,
+// children visited far to near (see lane_step). A stack overflow ends the
+// traversal with a miss (see the file comment).
 template <bool ANY, int SMEM, int CAP>
 __device__ __forceinline__ RayHit traverse(const TraceScene& s, V3 o, V3 d, float tnear, float tfar,
                                            TraversalStack<SMEM, CAP>& st) {
@@ -223,17 +227,18 @@ __device__ __forceinline__ RayHit traverse(const TraceScene& s, V3 o, V3 d, floa
   h.tri = -1;
   const V3 idir = V3{safe_inv(d.x), safe_inv(d.y), safe_inv(d.z)};
   const uint32_t oct = ray_octant(idir);
+  const uint32_t ord = ANY ? oct ^ 7u : oct;
   int best_prim = 0x7fffffff;
   st.sp = 0;
-  uint2 ng = root_group(oct), tg = make_uint2(0u, 0u);
+  uint2 ng = root_group(ord), tg = make_uint2(0u, 0u);
   while (true) {
     if (ng.y > 0x00ffffffu) {
-      const int child = take_child(ng, oct);
+      const int child = take_child(ng, ord);
       if (ng.y && !st.push(make_int2((int)ng.x, (int)ng.y))) {
         h.t = -1.f;  // poisoned: nothing passes a test against tmax < tnear
         h.tri = -1;
       }
-      wide_node(s.nodes, child, o, idir, oct, tnear, h.t, ng, tg);
+      wide_node(s.nodes, child, o, idir, oct, tnear, h.t, ng, tg, ord);
     } else {
       tg = ng;
       ng = make_uint2(0u, 0u);
@@ -294,7 +299,8 @@ struct LaneRay {
   uint2 ng, tg;
 };
 
-__device__ __forceinline__ void lane_start(LaneRay& r, float4 o4, float4 d4, float tmax) {
+// any: an occlusion ray (its node groups list children far to near, lane_step).
+__device__ __forceinline__ void lane_start(LaneRay& r, float4 o4, float4 d4, float tmax, bool any) {
   r.o = xyz(o4);
   r.d = xyz(d4);
   r.idir = V3{safe_inv(r.d.x), safe_inv(r.d.y), safe_inv(r.d.z)};
@@ -304,7 +310,7 @@ __device__ __forceinline__ void lane_start(LaneRay& r, float4 o4, float4 d4, flo
   r.u = r.v = 0.f;
   r.tri = -1;
   r.best_prim = 0x7fffffff;
-  r.ng = root_group(r.oct);
+  r.ng = root_group(any ? r.oct ^ 7u : r.oct);
   r.tg = make_uint2(0u, 0u);
 }
 
@@ -322,9 +328,14 @@ template <bool ANY, int SMEM, bool COUNT = false, int CAP = kMaxStack>
 __device__ __forceinline__ bool lane_step(LaneRay& r, const TraceScene& s, TraversalStack<SMEM, CAP>& st,
                                           TraceWork* wk = nullptr) {
   if (r.ng.y > 0x00ffffffu) {
-    const int child = take_child(r.ng, r.oct);
+    // Occlusion rays take far children first: a shadow ray leaves the surface
+    // it starts on, and the subtrees around its origin seldom hold its
+    // occluder (shadow traversal of the 1024x1024 x 64 spp displaced sphere
+    // 19.0 -> 15.5 ms against near first).
+    const uint32_t ord = ANY ? (r.oct ^ 7u) : r.oct;
+    const int child = take_child(r.ng, ord);
     if (r.ng.y && !st.push(make_int2((int)r.ng.x, (int)r.ng.y))) r.tmax = -1.f;
-    wide_node(s.nodes, child, r.o, r.idir, r.oct, r.tnear, r.tmax, r.ng, r.tg);
+    wide_node(s.nodes, child, r.o, r.idir, r.oct, r.tnear, r.tmax, r.ng, r.tg, ord);
     if (COUNT) ++wk->nodes;
   } else {
     r.tg = r.ng;
