@@ -43,6 +43,16 @@ int fail(int code, const std::string& msg) {
   return code;
 }
 
+namespace {
+std::mutex g_pools_mu;
+std::vector<cudaMemPool_t> g_pools;  // every live context's scene pool
+}  // namespace
+
+void trim_scene_pools() {
+  std::lock_guard<std::mutex> g(g_pools_mu);
+  for (cudaMemPool_t pool : g_pools) cudaMemPoolTrimTo(pool, 0);
+}
+
 }  // namespace orion_gb300
 
 // Why a launch configuration cannot run on this context ("" if it can).
@@ -216,6 +226,8 @@ extern "C" int orion_gpu_create(const orion_gpu_opts* opts, orion_gpu_ctx** out)
     CUDA_TRY(cudaMemPoolCreate(&c->scene_pool, &props));
     uint64_t keep = UINT64_MAX;  // freed scene memory stays with the pool for the next upload
     CUDA_TRY(cudaMemPoolSetAttribute(c->scene_pool, cudaMemPoolAttrReleaseThreshold, &keep));
+    std::lock_guard<std::mutex> g(g_pools_mu);
+    g_pools.push_back(c->scene_pool);
   }
   for (cudaStream_t& x : c->xstream) CUDA_TRY(cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking));
   CUDA_TRY(cudaEventCreate(&c->ev0));
@@ -272,7 +284,13 @@ extern "C" int orion_gpu_destroy(orion_gpu_ctx* ctx) {
   for (cudaStream_t x : ctx->xstream)
     if (x) cudaStreamDestroy(x);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
-  if (ctx->scene_pool) cudaMemPoolDestroy(ctx->scene_pool);
+  if (ctx->scene_pool) {
+    {
+      std::lock_guard<std::mutex> g(g_pools_mu);
+      g_pools.erase(std::remove(g_pools.begin(), g_pools.end(), ctx->scene_pool), g_pools.end());
+    }
+    cudaMemPoolDestroy(ctx->scene_pool);
+  }
   delete ctx;
   return ORION_OK;
 }

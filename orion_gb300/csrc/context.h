@@ -39,6 +39,10 @@ namespace orion_gb300 {
 // Records `msg` as this thread's last error (orion_last_error) and returns `code`.
 int fail(int code, const std::string& msg);
 
+// Returns the unused memory every context's scene pool keeps (released scenes)
+// to the device, so that a cudaMalloc that ran out of memory can be retried.
+void trim_scene_pools();
+
 #define CUDA_TRY(call)                                                                                 \
   do {                                                                                                 \
     cudaError_t e_ = (call);                                                                           \
@@ -83,6 +87,11 @@ struct DevBuf {
     release();
     if (n == 0) n = 16;
     cudaError_t e = cudaMalloc(&p, n);
+    if (e == cudaErrorMemoryAllocation) {  // memory of released scenes may still sit in a pool
+      cudaGetLastError();
+      trim_scene_pools();
+      e = cudaMalloc(&p, n);
+    }
     if (e != cudaSuccess) {
       p = nullptr;
       return fail(e == cudaErrorMemoryAllocation ? ORION_ERR_NOMEM : ORION_ERR_CUDA,
