@@ -415,7 +415,9 @@ __device__ __forceinline__ void trace_persistent(const SceneOf& scene_of, const 
           pid = queue[my];
           const SceneView& s = scene_of(pid);
           ts = TraceScene{s.nodes, s.woop, s.tri_prim, s.tri_class};
-          const float4 o4 = ray_o[pid], d4 = ray_d[pid];
+          // The ray and its result pass through once: streaming (evict-first) accesses
+          // leave L1 and L2 to the BVH nodes and triangles (displaced sphere +1.2%).
+          const float4 o4 = __ldcs(&ray_o[pid]), d4 = __ldcs(&ray_d[pid]);
           st.sp = 0;
           lane_start(r, o4, d4, ANY ? o4.w : kFloatMax, ANY);
           active = true;
@@ -436,10 +438,10 @@ __device__ __forceinline__ void trace_persistent(const SceneOf& scene_of, const 
           }
         }
         if (ANY) {
-          occluded[pid] = r.tri >= 0;
+          __stcs(&occluded[pid], r.tri >= 0 ? 1 : 0);
         } else {
-          hit[pid] = make_float4(r.tri >= 0 ? r.tmax : kFloatMax, r.u, r.v,
-                                 __int_as_float(r.tri >= 0 ? __ldg(ts.tri_prim + r.tri) : -1));
+          __stcs(&hit[pid], make_float4(r.tri >= 0 ? r.tmax : kFloatMax, r.u, r.v,
+                                        __int_as_float(r.tri >= 0 ? __ldg(ts.tri_prim + r.tri) : -1)));
           if (q_cls) {
             const int cls = r.tri >= 0 ? (int)__ldg(ts.tri_class + r.tri) : SC_MISS;
             if (cls_flags)
