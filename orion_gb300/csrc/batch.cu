@@ -309,7 +309,7 @@ __global__ void k_b_control(BatchView b, cudaGraphConditionalHandle cond, int in
 template <int SMEM>
 void launch_b_trace(const WaveView& w, const BatchView& b, int kind, int grid, int block, int refill,
                     uint8_t* cls_flags, cudaStream_t s) {
-  k_b_trace<SMEM><<<grid, block, (size_t)SMEM * block * sizeof(int2), s>>>(w, b, kind, refill, cls_flags);
+  k_b_trace<SMEM><<<grid, block, trace_smem_bytes(SMEM, block), s>>>(w, b, kind, refill, cls_flags);
 }
 
 void b_trace(const LaunchConfig& cfg, const WaveView& w, const BatchView& b, int kind, int grid, uint8_t* cls_flags,

@@ -63,9 +63,9 @@ std::string orion_gb300::config_problem(const orion_gpu_ctx* ctx, const LaunchCo
   if (c.shade_block < 32 || c.shade_block % 32 || c.shade_block > ctx->limits.max_shade_block)
     return "shade_block must be a multiple of 32 up to " + std::to_string(ctx->limits.max_shade_block);
   if (!(st == 0 || st == 8 || st == 16 || st == 24 || st == 32)) return "smem_stack must be 0, 8, 16, 24 or 32";
-  if ((int64_t)st * c.trace_block * 8 > ctx->smem_limit)
-    return "traversal stack (smem_stack x trace_block x 8 bytes) exceeds " + std::to_string(ctx->smem_limit) +
-           " bytes of shared memory";
+  if ((int64_t)st * c.trace_block * 8 + (int64_t)(c.trace_block / 32) * kTriScratchBytes > ctx->smem_limit)
+    return "traversal stack (smem_stack x trace_block x 8 bytes) and triangle scratch exceed " +
+           std::to_string(ctx->smem_limit) + " bytes of shared memory";
   if (c.blocks_per_sm < 1 || c.blocks_per_sm > 64) return "blocks_per_sm out of range (1..64)";
   if (c.refill_below < 1 || c.refill_below > 32) return "refill_below out of range (1..32)";
   return std::string();

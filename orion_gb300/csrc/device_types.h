@@ -20,6 +20,10 @@ namespace orion_gb300 {
 // the traversal stacks hold one entry per level.
 constexpr int kMaxBvhDepth = 48;
 
+// Shared memory a persistent trace block needs per warp beside its stacks:
+// the scratch of the warp-cooperative triangle tests (TriScratch).
+constexpr int kTriScratchBytes = 288;
+
 // BxDFType bits (src/core/bsdf.h:16-24).
 enum : int32_t {
   BXDF_REFLECTION = 1,

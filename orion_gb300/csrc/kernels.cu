@@ -291,7 +291,7 @@ void launch_trace_kernels(int kind, const SceneView& s, const WaveView& w, int c
   // (1024x1024 x 64 spp displaced sphere: 804 Mpaths/s against 798 at the
   // closest-hit threshold of 20, 787 at 16).
   const int refill_any = refill + 4 > 32 ? 32 : refill + 4;
-  size_t smem = (size_t)SMEM * block * sizeof(int2);
+  const size_t smem = trace_smem_bytes(SMEM, block);
   unsigned long long* work = w.trace_work;  // nodes[ext, shadow, mis], then tris[ext, shadow, mis]
   int* err = w.error_word;
   if (kind == TK_EXT)

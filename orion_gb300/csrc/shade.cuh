@@ -8,6 +8,8 @@
 #include "material_build.h"
 #include "traverse.cuh"
 
+#include <type_traits>
+
 namespace orion_gb300 {
 
 constexpr int kNonSpecular = BXDF_ALL & ~BXDF_SPECULAR;
@@ -391,12 +393,21 @@ __device__ __forceinline__ void trace_persistent(const SceneOf& scene_of, const 
                                                  int cls_stride = 0, unsigned long long* work = nullptr,
                                                  uint8_t* cls_flags = nullptr) {
   constexpr unsigned kFull = 0xffffffffu;
+  constexpr bool kUniform = std::is_same<SceneOf, SingleScene>::value;
   const int lane = threadIdx.x & 31;
   TraversalStack<SMEM, CAP> st;
   st.smem = stack_smem + threadIdx.x;
   st.stride = blockDim.x;
+  TriScratch* tsc = reinterpret_cast<TriScratch*>(stack_smem + (size_t)SMEM * blockDim.x) + (threadIdx.x >> 5);
   LaneRay r;
+  r.tg = make_uint2(0u, 0u);
+  // Every lane may test triangles for the others (warp_triangles): with one
+  // scene for all rays, a lane holds its arrays before its first ray.
   TraceScene ts{nullptr, nullptr, nullptr, nullptr};
+  if constexpr (kUniform) {
+    const SceneView& s0 = scene_of(0);
+    ts = TraceScene{s0.nodes, s0.woop, s0.tri_prim, s0.tri_class};
+  }
   int pid = -1;
   bool active = false, exhausted = false;
   TraceWork wk;
@@ -429,8 +440,10 @@ __device__ __forceinline__ void trace_persistent(const SceneOf& scene_of, const 
       if (exhausted) break;
       continue;
     }
+    if (active) lane_visit<ANY, SMEM, COUNT, CAP>(r, ts, st, &wk);
+    const bool occl = warp_triangles<ANY, COUNT, kUniform>(r, ts, tsc, &wk);
     if (active) {
-      if (lane_step<ANY, SMEM, COUNT, CAP>(r, ts, st, &wk)) {
+      if ((ANY && occl) || lane_pop(r, st)) {
         if constexpr (CAP < kMaxStack) {
           if (r.tmax < 0.f) {  // poisoned by a stack overflow
             r.tri = -1;

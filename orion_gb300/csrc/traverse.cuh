@@ -281,31 +281,31 @@ __device__ __forceinline__ RayHit traverse(const TraceScene& s, V3 o, V3 d, floa
 // ------------------------------------------------ persistent warp traversal
 //
 // The kernels below trace a queue of rays with warps that stay resident.
-// Each loop iteration visits one node per lane and then tests the triangles
-// it yielded. (Postponing the triangles of lanes that are few in their warp,
-// to keep descending with the rest, was measured 11% slower on the 8-wide
-// tree: a leaf visit costs about as much as the node visits it waits for.)
-// When fewer than
-// `refill_below` lanes still hold a ray, the warp takes new rays for its idle
-// lanes from the queue with one atomicAdd. Warp votes only steer scheduling;
-// each ray's result does not depend on them.
+// Each loop iteration visits one node per lane; the triangles those visits
+// yield are then tested by the whole warp together (warp_triangles), and
+// each lane pops its next node group. (Postponing the triangles of lanes
+// that are few in their warp, to keep descending with the rest, was measured
+// 11% slower on the 8-wide tree: a leaf visit costs about as much as the
+// node visits it waits for.) When fewer than `refill_below` lanes still hold
+// a ray, the warp takes new rays for its idle lanes from the queue with one
+// atomicAdd. Warp votes and the dealing of triangle tests only steer
+// scheduling; each ray's result does not depend on them.
 
 struct LaneRay {
   V3 o, d, idir;
-  float tnear, tmax;  // tmax shrinks to the closest hit found so far
+  float tmax;  // shrinks to the closest hit found so far; the ray starts at t = 0
   float u, v;
   int tri, best_prim;
   uint32_t oct;
   uint2 ng, tg;
 };
 
-// any: an occlusion ray (its node groups list children far to near, lane_step).
+// any: an occlusion ray (its node groups list children far to near, lane_visit).
 __device__ __forceinline__ void lane_start(LaneRay& r, float4 o4, float4 d4, float tmax, bool any) {
   r.o = xyz(o4);
   r.d = xyz(d4);
   r.idir = V3{safe_inv(r.d.x), safe_inv(r.d.y), safe_inv(r.d.z)};
   r.oct = ray_octant(r.idir);
-  r.tnear = 0.f;
   r.tmax = tmax;
   r.u = r.v = 0.f;
   r.tri = -1;
@@ -319,14 +319,13 @@ struct TraceWork {
   unsigned long long nodes = 0, tris = 0;
 };
 
-// One node visit and its triangles. Returns true when the lane's ray is done:
-// its stack ran empty, or (ANY) a hit was found. COUNT adds the node visit
-// and the triangle tests to `wk`; the traversal itself is the same. A push
-// beyond the stack's capacity poisons the ray (r.tmax = -1; see the file
-// comment): the caller reports it when the ray is done.
+// One node visit: the lane's next node group yields its hit children (r.ng)
+// and the triangles of its hit leaves (r.tg). COUNT adds the visit to `wk`.
+// A push beyond the stack's capacity poisons the ray (r.tmax = -1; see the
+// file comment): the caller reports it when the ray is done.
 template <bool ANY, int SMEM, bool COUNT = false, int CAP = kMaxStack>
-__device__ __forceinline__ bool lane_step(LaneRay& r, const TraceScene& s, TraversalStack<SMEM, CAP>& st,
-                                          TraceWork* wk = nullptr) {
+__device__ __forceinline__ void lane_visit(LaneRay& r, const TraceScene& s, TraversalStack<SMEM, CAP>& st,
+                                           TraceWork* wk) {
   if (r.ng.y > 0x00ffffffu) {
     // Occlusion rays take far children first: a shadow ray leaves the surface
     // it starts on, and the subtrees around its origin seldom hold its
@@ -335,33 +334,18 @@ __device__ __forceinline__ bool lane_step(LaneRay& r, const TraceScene& s, Trave
     const uint32_t ord = ANY ? (r.oct ^ 7u) : r.oct;
     const int child = take_child(r.ng, ord);
     if (r.ng.y && !st.push(make_int2((int)r.ng.x, (int)r.ng.y))) r.tmax = -1.f;
-    wide_node(s.nodes, child, r.o, r.idir, r.oct, r.tnear, r.tmax, r.ng, r.tg, ord);
+    wide_node(s.nodes, child, r.o, r.idir, r.oct, 0.f, r.tmax, r.ng, r.tg, ord);
     if (COUNT) ++wk->nodes;
   } else {
     r.tg = r.ng;
     r.ng = make_uint2(0u, 0u);
   }
-  while (r.tg.y != 0u) {
-    const int k = (int)r.tg.x + __ffs(r.tg.y) - 1;
-    r.tg.y &= r.tg.y - 1u;
-    float t, u, v;
-    if (COUNT) ++wk->tris;
-    if (woop_hit(s.woop, k, r.o, r.d, r.tnear, r.tmax, &t, &u, &v)) {
-      if (ANY) {
-        r.tmax = t;
-        r.tri = k;
-        return true;
-      }
-      const int prim = __ldg(s.tri_prim + k);
-      if (t < r.tmax || r.tri < 0 || prim < r.best_prim) {
-        r.tmax = t;
-        r.u = u;
-        r.v = v;
-        r.tri = k;
-        r.best_prim = prim;
-      }
-    }
-  }
+}
+
+// After a visit and its triangles: pops the lane's next node group. Returns
+// true when the stack ran empty (the ray is done).
+template <int SMEM, int CAP>
+__device__ __forceinline__ bool lane_pop(LaneRay& r, TraversalStack<SMEM, CAP>& st) {
   if (r.ng.y == 0u) {
     if (st.sp == 0) return true;
     const int2 e = st.pop();
@@ -370,5 +354,157 @@ __device__ __forceinline__ bool lane_step(LaneRay& r, const TraceScene& s, Trave
   return false;
 }
 
+// Position of the n-th (from 0) set bit of m; n < popc(m).
+__device__ __forceinline__ uint32_t nth_set_bit(uint32_t m, uint32_t n) {
+  uint32_t p = 0u, c = (uint32_t)__popc(m & 0xffffu);
+  if (n >= c) n -= c, m >>= 16, p += 16u;
+  c = (uint32_t)__popc(m & 0xffu);
+  if (n >= c) n -= c, m >>= 8, p += 8u;
+  c = (uint32_t)__popc(m & 0xfu);
+  if (n >= c) n -= c, m >>= 4, p += 4u;
+  c = (uint32_t)__popc(m & 0x3u);
+  if (n >= c) n -= c, m >>= 2, p += 2u;
+  return p + (n >= (m & 1u) ? 1u : 0u);
+}
+
+// Shared scratch of one warp for warp_triangles.
+struct TriScratch {
+  unsigned long long key[32];  // owner lane -> least (t bits, primID) of its ray so far
+  uint8_t owner[32];           // first pair of a segment -> its owner lane
+};
+static_assert(sizeof(TriScratch) == kTriScratchBytes, "per-warp triangle scratch");
+
+// Dynamic shared memory of a persistent trace block: the stacks' shared
+// entries, then one TriScratch per warp.
+__host__ __device__ constexpr size_t trace_smem_bytes(int smem_entries, int block) {
+  return (size_t)smem_entries * block * sizeof(int2) + (size_t)(block / 32) * kTriScratchBytes;
+}
+
+// Dealing a lane's triangle tests to the whole warp pays when one lane holds
+// many more than the others: a dealt round costs about as much as this many
+// one-by-one tests (closest hit: keeping the least hit takes shared-memory
+// atomics; occlusion: one vote).
+constexpr int kDealClosest = 4, kDealAny = 2;
+
+// Tests the triangles of every lane's r.tg (all 32 lanes call it; lanes
+// without a ray have r.tg.y == 0), with the same result as each lane testing
+// its own one by one, which it does when the warp's tests are even. When a
+// few lanes hold most of them (the largest count at least kDealClosest /
+// kDealAny times the rounds dealing takes), the warp's (ray, triangle) pairs,
+// listed lane by lane in bit order, are dealt to the lanes 32 at a time: a
+// lane tests its pair against the owning lane's ray (fetched by shuffles), and
+// each owner keeps the least (t, primID) of its hits in (0, tmax] or, ANY,
+// any hit. UNIFORM: every lane traces the same scene (otherwise each pair
+// uses its owner's triangle arrays). Returns true for an ANY lane whose ray
+// hit.
+template <bool ANY, bool COUNT, bool UNIFORM>
+__device__ __forceinline__ bool warp_triangles(LaneRay& r, const TraceScene& s, TriScratch* sc, TraceWork* wk) {
+  constexpr unsigned kFull = 0xffffffffu;
+  constexpr int kDeal = ANY ? kDealAny : kDealClosest;
+  const int lane = threadIdx.x & 31;
+  bool found = false;
+  while (true) {
+    const int c = __popc(r.tg.y);
+    const int total = (int)__reduce_add_sync(kFull, (unsigned)c);
+    if (total == 0) break;
+    if ((int)__reduce_max_sync(kFull, (unsigned)c) < kDeal * ((total + 31) >> 5)) {
+      while (r.tg.y != 0u) {  // one by one
+        const int k = (int)r.tg.x + __ffs(r.tg.y) - 1;
+        r.tg.y &= r.tg.y - 1u;
+        float t, u, v;
+        if (COUNT) ++wk->tris;
+        if (woop_hit(s.woop, k, r.o, r.d, 0.f, r.tmax, &t, &u, &v)) {
+          if (ANY) {
+            r.tri = k;
+            r.tg.y = 0u;
+            found = true;
+            break;
+          }
+          const int prim = __ldg(s.tri_prim + k);
+          if (t < r.tmax || r.tri < 0 || prim < r.best_prim) {
+            r.tmax = t;
+            r.u = u;
+            r.v = v;
+            r.tri = k;
+            r.best_prim = prim;
+          }
+        }
+      }
+      break;
+    }
+    // Dealt: this lane's pairs are [first, first + c) of the warp's list.
+    int incl = c;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(kFull, incl, o);
+      if (lane >= o) incl += y;
+    }
+    const int first = incl - c;
+    const bool owns = c > 0 && first < 32;
+    const int dealt = owns ? min(c, 32 - first) : 0;  // pairs of this lane tested this round
+    const unsigned starts = __reduce_or_sync(kFull, owns ? 1u << first : 0u);
+    if (owns) sc->owner[first] = (uint8_t)lane;
+    __syncwarp();
+    // The pair at position `lane`: segment start at or below it (position 0
+    // always starts one), its owner, and the triangle's index there.
+    const int seg = 31 - __clz(starts & (kFull >> (31 - lane)));
+    const int ow = sc->owner[seg];
+    const float ox = __shfl_sync(kFull, r.o.x, ow), oy = __shfl_sync(kFull, r.o.y, ow);
+    const float oz = __shfl_sync(kFull, r.o.z, ow), dx = __shfl_sync(kFull, r.d.x, ow);
+    const float dy = __shfl_sync(kFull, r.d.y, ow), dz = __shfl_sync(kFull, r.d.z, ow);
+    const float tmax = __shfl_sync(kFull, r.tmax, ow);
+    const uint32_t obase = __shfl_sync(kFull, r.tg.x, ow), omask = __shfl_sync(kFull, r.tg.y, ow);
+    const float4* woop = s.woop;
+    const int* tri_prim = s.tri_prim;
+    if constexpr (!UNIFORM) {
+      woop = (const float4*)__shfl_sync(kFull, (unsigned long long)s.woop, ow);
+      tri_prim = (const int*)__shfl_sync(kFull, (unsigned long long)s.tri_prim, ow);
+    }
+    bool hit = false;
+    float t = 0.f, u = 0.f, v = 0.f;
+    int k = 0;
+    if (lane < total) {
+      k = (int)(obase + nth_set_bit(omask, (uint32_t)(lane - seg)));
+      hit = woop_hit(woop, k, V3{ox, oy, oz}, V3{dx, dy, dz}, 0.f, tmax, &t, &u, &v);
+    }
+    const unsigned span = dealt == 32 ? kFull : (((1u << dealt) - 1u) << (first & 31));
+    if (ANY) {
+      if (__ballot_sync(kFull, hit) & span) {
+        r.tri = 0;  // occluded; which triangle is not reported
+        found = true;
+      }
+    } else {
+      if (owns)
+        sc->key[lane] = ((unsigned long long)__float_as_uint(r.tmax) << 32) |
+                        (r.tri >= 0 ? (uint32_t)r.best_prim : 0xffffffffu);
+      __syncwarp();
+      unsigned long long key = 0ull;
+      if (hit) {
+        key = ((unsigned long long)__float_as_uint(t) << 32) | (uint32_t)__ldg(tri_prim + k);
+        atomicMin(&sc->key[ow], key);
+      }
+      __syncwarp();
+      const unsigned wins = __ballot_sync(kFull, hit && sc->key[ow] == key) & span;
+      const int wl = wins ? __ffs(wins) - 1 : lane;
+      const float wu = __shfl_sync(kFull, u, wl), wv = __shfl_sync(kFull, v, wl);
+      const int wt = __shfl_sync(kFull, k, wl);
+      if (wins) {
+        const unsigned long long best = sc->key[lane];
+        r.tmax = __uint_as_float((uint32_t)(best >> 32));
+        r.best_prim = (int)(uint32_t)best;
+        r.tri = wt;
+        r.u = wu;
+        r.v = wv;
+      }
+    }
+    if (COUNT) wk->tris += (unsigned long long)dealt;
+    if (found || dealt == c)
+      r.tg.y = 0u;
+    else if (dealt > 0)
+      r.tg.y &= kFull << nth_set_bit(r.tg.y, (uint32_t)dealt);
+    __syncwarp();
+  }
+  return found;
+}
 
 }  // namespace orion_gb300
