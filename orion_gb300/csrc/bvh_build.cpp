@@ -563,7 +563,8 @@ struct WideCollapser {
     // Empty slots get inverted boxes (lo = 255 > hi = 0 on every axis), which
     // no ray hits whatever its direction.
     std::memset(w.qlo, 0xff, sizeof(w.qlo));
-    // Quantisation grid per axis: the smallest power-of-two cell with 255 cells covering the node.
+    // Quantisation grid per axis: the smallest power-of-two cell with 255 cells
+    // covering the node, at most 2^112 (the traversal scales cells by 2^15).
     double cell[3];
     for (int k = 0; k < 3; ++k) {
       w.p[k] = (float)nlo[k];
@@ -573,9 +574,9 @@ struct WideCollapser {
       if (ext > 0.0) {
         int ex;
         const double m = std::frexp(ext / 255.0, &ex);  // ext / 255 = m * 2^ex, m in [0.5, 1)
-        e = std::max(-126, std::min(127, m == 0.5 ? ex - 1 : ex));
+        e = std::max(-126, std::min(112, m == 0.5 ? ex - 1 : ex));
       }
-      while (e < 127 && std::ldexp(255.0, e) < ext) ++e;  // guards the rounding of ext / 255
+      while (e < 112 && std::ldexp(255.0, e) < ext) ++e;  // guards the rounding of ext / 255
       w.e[k] = (uint8_t)(e + 127);
       cell[k] = std::ldexp(1.0, e);
     }

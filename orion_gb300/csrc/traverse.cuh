@@ -131,10 +131,10 @@ __device__ __forceinline__ uint32_t ray_octant(V3 idir) {
 
 __device__ __forceinline__ uint2 root_group(uint32_t oct) { return make_uint2(0u, (1u << (24 + oct)) | 1u); }
 
-// Byte `b` of `w` as a float: the byte is placed in the mantissa of 2^23 with
-// one byte permute, and 2^23 subtracted (exact).
+// Byte `b` of `w` as the float 1 + byte * 2^-15 (exact): one byte permute
+// places the byte in mantissa bits 8..15 of 1.0.
 __device__ __forceinline__ float q8(uint32_t w, int b) {
-  return __uint_as_float(__byte_perm(w, 0x4b000000u, 0x7440u + (uint32_t)b)) - 8388608.f;
+  return __uint_as_float(__byte_perm(w, 0x3f800000u, 0x7604u + ((uint32_t)b << 4)));
 }
 
 __device__ __forceinline__ float max3f(float a, float b, float c) {
@@ -164,12 +164,19 @@ __device__ __forceinline__ void wide_node(const float4* __restrict__ nodes, int 
                                           float tnear, float tmax, uint2& ng, uint2& tg, uint32_t ord) {
   const float4* n = nodes + 5 * (size_t)idx;
   const float4 n0 = __ldg(n), n1 = __ldg(n + 1), n2 = __ldg(n + 2), n3 = __ldg(n + 3), n4 = __ldg(n + 4);
+  // A child plane p + q * cell is met at ray distance (p - o + q * cell) / d,
+  // computed as fma(1 + q * 2^-15, S, C) with S = 2^15 * cell / d (a power-of-
+  // two scaling, exact) and C = (p - o) / d - S: one byte permute and one fma
+  // per plane. C rounds once per node; beyond the rounding of (p - o) / d that
+  // costs at most 2^-9 of a cell, well inside the outward quantisation. (The
+  // builder keeps cells at or below 2^112, so S stays finite.)
   const uint32_t ew = __float_as_uint(n0.w);
-  const float sx = __uint_as_float((ew & 0xffu) << 23) * idir.x;
-  const float sy = __uint_as_float(((ew >> 8) & 0xffu) << 23) * idir.y;
-  const float sz = __uint_as_float(((ew >> 16) & 0xffu) << 23) * idir.z;
+  const float sx = __uint_as_float(((ew & 0xffu) + 15u) << 23) * idir.x;
+  const float sy = __uint_as_float((((ew >> 8) & 0xffu) + 15u) << 23) * idir.y;
+  const float sz = __uint_as_float((((ew >> 16) & 0xffu) + 15u) << 23) * idir.z;
   const uint32_t imask = ew >> 24;
-  const float ox = (n0.x - o.x) * idir.x, oy = (n0.y - o.y) * idir.y, oz = (n0.z - o.z) * idir.z;
+  const float ox = fmaf(n0.x - o.x, idir.x, -sx), oy = fmaf(n0.y - o.y, idir.y, -sy);
+  const float oz = fmaf(n0.z - o.z, idir.z, -sz);
   // Quantised bounds: lo x = (n2.x, n2.y), lo y = (n2.z, n2.w), lo z = (n3.x, n3.y),
   // hi x = (n3.z, n3.w), hi y = (n4.x, n4.y), hi z = (n4.z, n4.w); the near plane
   // along a negative direction is the upper bound.
@@ -384,7 +391,7 @@ __host__ __device__ constexpr size_t trace_smem_bytes(int smem_entries, int bloc
 // many more than the others: a dealt round costs about as much as this many
 // one-by-one tests (closest hit: keeping the least hit takes shared-memory
 // atomics; occlusion: one vote).
-constexpr int kDealClosest = 4, kDealAny = 2;
+constexpr int kDealClosest = 4, kDealAny = 3;
 
 // Tests the triangles of every lane's r.tg (all 32 lanes call it; lanes
 // without a ray have r.tg.y == 0), with the same result as each lane testing
