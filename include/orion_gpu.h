@@ -313,7 +313,7 @@ typedef struct orion_launch_config {
   int32_t trace_block;    /* threads per block of the traversal kernels (64..512) */
   int32_t shade_block;    /* threads per block of the shading kernels (64..512) */
   int32_t smem_stack;     /* traversal stack entries kept in shared memory: 0, 8, 16, 24 or 32 */
-  int32_t blocks_per_sm;  /* grid size factor of the grid-stride kernels */
+  int32_t blocks_per_sm;  /* persistent trace blocks per SM; the grid-stride kernels launch twice as many */
   int32_t wave_paths;     /* paths per plain-render wave */
   int32_t batch_slots;    /* batches: path slots of the pool (pooled mode) or paths per wave (wave mode) */
   int32_t refill_below;   /* a traversal warp takes new rays once fewer lanes than this hold one (1..32);

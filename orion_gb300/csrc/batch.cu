@@ -376,7 +376,7 @@ void enqueue_iteration(const WaveView& w, const BatchView& b, const uint32_t* so
                        int in_graph, cudaStream_t stream, StageTimer* timer) {
   const int cap = w.capacity;
   const int persistent = cfg.num_sms * cfg.blocks_per_sm;
-  const int tgrid = grid_cap(cap, cfg.trace_block, persistent * 2);
+  const int tgrid = grid_cap(cap, cfg.trace_block, persistent);
   const int sgrid = grid_cap(cap, cfg.shade_block, persistent * 2);
   auto begin = [&](int st) {
     if (timer) timer->begin(st, stream);

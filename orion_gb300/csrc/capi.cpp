@@ -251,7 +251,7 @@ extern "C" int orion_gpu_create(const orion_gpu_opts* opts, orion_gpu_ctx** out)
   c->cfg.num_sms = c->num_sms;
   c->cfg.trace_block = 128;
   c->cfg.shade_block = 128;
-  c->cfg.blocks_per_sm = 8;
+  c->cfg.blocks_per_sm = 6;
   c->cfg.smem_stack = 8;  // C2: 798 Mpaths/s against 793 at 16, 781 at 0, 721 at 24
   c->cfg.refill_below = 20;
   c->smem_limit = (int)prop.sharedMemPerBlockOptin;
@@ -742,12 +742,12 @@ extern "C" int orion_gpu_autotune(orion_gpu_ctx* ctx, orion_scene_id id, int32_t
   const int trace_blocks[] = {64, 128, 256};
   const int stacks[] = {8, 16, 32};
   const int shade_blocks[] = {64, 128, 256};
-  const int bpsm[] = {4, 8, 16};
+  const int bpsm[] = {4, 6, 8, 12};
   const int waves[] = {1 << 22, 1 << 23, 1 << 24, 1 << 25};
   const int refills[] = {8, 16, 24, 32};
   const int stream_counts[] = {1, 2, 3, 4};
   for (int knob = 0; knob < 7 && used < budget_ms; ++knob) {
-    int n = knob >= 4 ? 4 : 3;
+    int n = knob >= 3 ? 4 : 3;
     for (int v = 0; v < n && used < budget_ms; ++v) {
       LaunchConfig c = best;
       int wave = best_wave, streams = best_streams;

@@ -558,13 +558,13 @@ extern "C" int orion_gpu_autotune_batch(orion_gpu_ctx* ctx, int32_t njobs, const
   const int trace_blocks[] = {64, 128, 256};
   const int stacks[] = {8, 16, 32};
   const int shade_blocks[] = {64, 128, 256};
-  const int bpsm[] = {4, 8, 16};
+  const int bpsm[] = {4, 6, 8, 12};
   const int slot_counts[] = {1 << 22, 1 << 23, 1 << 24, 1 << 25};
   const int refills[] = {8, 16, 24, 32};
   const int engine_counts[] = {1, 2};
   const int modes[] = {ORION_BATCH_POOLED, ORION_BATCH_WAVES};
   for (int knob = 0; knob < 8 && used < budget_ms; ++knob) {
-    const int n = knob >= 6 ? 2 : (knob >= 4 ? 4 : 3);
+    const int n = knob >= 6 ? 2 : (knob >= 3 ? 4 : 3);
     for (int v = 0; v < n && used < budget_ms; ++v) {
       LaunchConfig c = best;
       int slots = best_slots, streams = best_streams, mode = best_mode;
