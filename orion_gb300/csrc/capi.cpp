@@ -241,13 +241,26 @@ extern "C" int orion_gpu_create(const orion_gpu_opts* opts, orion_gpu_ctx** out)
   std::string path = (opts && opts->sobol_path) ? std::string(opts->sobol_path) : default_sobol_path();
   FILE* f = std::fopen(path.c_str(), "rb");
   if (!f) return fail(ORION_ERR_IO, "cannot open Sobol matrices " + path);
-  std::vector<uint32_t> m((size_t)1024 * 52);
+  std::vector<uint32_t> m((size_t)kSobolDims * kSobolBits);
   size_t got = std::fread(m.data(), sizeof(uint32_t), m.size(), f);
   std::fclose(f);
   if (got != m.size()) return fail(ORION_ERR_IO, "short Sobol matrix file " + path);
-  int rc = c->sobol.alloc(m.size() * sizeof(uint32_t));
+  // Device form: for each dimension and each byte of the sample index, the XOR
+  // of that byte's direction numbers for all 256 byte values, so a sample is
+  // one lookup per non-zero index byte (sobol_sample, dmath.cuh).
+  std::vector<uint32_t> tab((size_t)kSobolDims * kSobolBytes * 256);
+  for (int d = 0; d < kSobolDims; ++d)
+    for (int k = 0; k < kSobolBytes; ++k) {
+      uint32_t* t = tab.data() + ((size_t)d * kSobolBytes + k) * 256;
+      t[0] = 0u;
+      for (int v = 1; v < 256; ++v) {  // v's lowest set bit j, and v without it
+        const int j = __builtin_ctz((unsigned)v), b = 8 * k + j;
+        t[v] = t[v & (v - 1)] ^ (b < kSobolBits ? m[(size_t)d * kSobolBits + b] : 0u);
+      }
+    }
+  int rc = c->sobol.alloc(tab.size() * sizeof(uint32_t));
   if (rc != ORION_OK) return rc;
-  CUDA_TRY(cudaMemcpy(c->sobol.p, m.data(), m.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
+  CUDA_TRY(cudaMemcpy(c->sobol.p, tab.data(), tab.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
   c->cfg.num_sms = c->num_sms;
   c->cfg.trace_block = 128;
   c->cfg.shade_block = 128;

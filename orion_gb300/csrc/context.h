@@ -181,7 +181,7 @@ struct orion_gpu_ctx {
   // uploading and releasing scenes (serving evicts and re-uploads them) then
   // reuses the memory with no cudaMalloc or device-wide cudaFree sync.
   cudaMemPool_t scene_pool = nullptr;
-  DevBuf sobol;  // Sobol direction numbers, dimension-major (1024 x 52)
+  DevBuf sobol;  // Sobol tables: per dimension and index byte, the XOR of every byte value's direction numbers
   std::map<int, std::unique_ptr<DeviceScene>> scenes;
   int next_id = 1;
   Wave wave;

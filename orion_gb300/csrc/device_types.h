@@ -24,6 +24,12 @@ constexpr int kMaxBvhDepth = 48;
 // the scratch of the warp-cooperative triangle tests (TriScratch).
 constexpr int kTriScratchBytes = 288;
 
+// Sobol direction numbers (src/sampler/sobol.cpp): dimensions, numbers per
+// dimension, and the index bytes those numbers cover.
+constexpr int kSobolBits = 52;
+constexpr int kSobolDims = 1024;
+constexpr int kSobolBytes = (kSobolBits + 7) / 8;
+
 // BxDFType bits (src/core/bsdf.h:16-24).
 enum : int32_t {
   BXDF_REFLECTION = 1,

@@ -10,6 +10,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include "device_types.h"
+
 namespace orion_gb300 {
 
 constexpr float kPi = 3.14159265358979323846f;
@@ -196,51 +198,47 @@ __device__ __forceinline__ V3 offset_ray_origin(V3 p, V3 n, V3 w) {
 
 // ----------------------------------------------------------------- Sobol
 
-constexpr int kSobolBits = 52;     // direction numbers per dimension
-constexpr int kSobolDims = 1024;
-
 // sobol::sample (src/sampler/sobol.h:28-43): XOR of the dimension's
 // direction numbers for the set bits of the index, scaled by 2^-32.
-// Unscrambled; can return exactly 1.0f like the reference.
-__device__ __forceinline__ float sobol_sample(const uint32_t* __restrict__ matrices, uint64_t index, uint32_t dim) {
-  const uint32_t* row = matrices + (size_t)dim * kSobolBits;
-  uint32_t r = 0;
-  while (index) {
-    int b = __ffsll((long long)index) - 1;
-    r ^= __ldg(row + b);
-    index &= index - 1;
+// Unscrambled; can return exactly 1.0f like the reference. The device holds
+// the direction numbers as tables: entry [dim][k][v] is the XOR of the
+// numbers of the set bits of v placed at index bits 8k..8k+7, so the XOR over
+// the index's set bits is one lookup per index byte (four for an index below
+// 2^32, against one per set bit: 13 on average for 26-bit indices). Indices
+// of 2^52 and above, beyond the reference's direction numbers, get none for
+// their bits 52 and up.
+__device__ __forceinline__ uint32_t sobol_bits(const uint32_t* __restrict__ t, uint64_t index) {
+  uint32_t r = __ldg(t + (uint32_t)(index & 0xffu)) ^ __ldg(t + 256 + (uint32_t)((index >> 8) & 0xffu)) ^
+               __ldg(t + 512 + (uint32_t)((index >> 16) & 0xffu)) ^ __ldg(t + 768 + (uint32_t)((index >> 24) & 0xffu));
+  if (index >> 32) {
+#pragma unroll
+    for (int k = 4; k < kSobolBytes; ++k) r ^= __ldg(t + 256 * k + (uint32_t)((index >> (8 * k)) & 0xffu));
   }
-  return __uint2float_rn(r) * 2.3283064365386963e-10f;
+  return r;
 }
 
-// N consecutive dimensions d0..d0+N-1 in one pass over the index bits, from
-// the dimension-major matrices (N short rows that stay in L1): N independent
-// lookups per set bit instead of N dependent chains (camera rays: pixel
-// jitter, and the lens sample). Values are identical to sobol_sample.
+__device__ __forceinline__ float sobol_sample(const uint32_t* __restrict__ tables, uint64_t index, uint32_t dim) {
+  return __uint2float_rn(sobol_bits(tables + (size_t)dim * kSobolBytes * 256, index)) * 2.3283064365386963e-10f;
+}
+
+// N consecutive dimensions d0..d0+N-1 of one index (their lookups are
+// independent and issue together). Values are identical to sobol_sample.
 template <int N>
-__device__ __forceinline__ void sobol_dims(const uint32_t* __restrict__ matrices, uint64_t index, uint32_t d0,
+__device__ __forceinline__ void sobol_dims(const uint32_t* __restrict__ tables, uint64_t index, uint32_t d0,
                                            float out[N]) {
-  uint32_t r[N];
+  const uint32_t* t = tables + (size_t)d0 * kSobolBytes * 256;
 #pragma unroll
-  for (int k = 0; k < N; ++k) r[k] = 0u;
-  const uint32_t* row = matrices + (size_t)d0 * kSobolBits;
-  while (index) {
-    int b = __ffsll((long long)index) - 1;
-    index &= index - 1;
-#pragma unroll
-    for (int k = 0; k < N; ++k) r[k] ^= __ldg(row + k * kSobolBits + b);
-  }
-#pragma unroll
-  for (int k = 0; k < N; ++k) out[k] = __uint2float_rn(r[k]) * 2.3283064365386963e-10f;
+  for (int k = 0; k < N; ++k)
+    out[k] = __uint2float_rn(sobol_bits(t + (size_t)k * kSobolBytes * 256, index)) * 2.3283064365386963e-10f;
 }
 
 // A path's sampler: fixed sample index, advancing dimension
 // (src/core/sampler.h:15-34, dimension starts at 5).
 struct PathSampler {
-  const uint32_t* matrices;
+  const uint32_t* tables;
   uint64_t index;
   uint32_t dim;
-  __device__ __forceinline__ float next() { return sobol_sample(matrices, index, dim++); }
+  __device__ __forceinline__ float next() { return sobol_sample(tables, index, dim++); }
 };
 
 }  // namespace orion_gb300

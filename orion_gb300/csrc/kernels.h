@@ -167,7 +167,7 @@ __device__ __forceinline__ long long slot_index(const WaveView& w, int pid) {
 #endif
 
 struct WaveArgs {
-  const uint32_t* sobol;          // dimension-major Sobol matrices (1024 x 52)
+  const uint32_t* sobol;          // Sobol tables (sobol_sample, dmath.cuh)
   int64_t base_index;  // sample index of path slot 0
   int n_paths;
   int width, height;
@@ -275,7 +275,7 @@ struct SppmGrid {
 struct SppmView {
   int width, height, npix;
   int max_depth, iterations, photons;  // photons per iteration
-  const uint32_t* sobol;               // dimension-major Sobol matrices
+  const uint32_t* sobol;               // Sobol tables (sobol_sample, dmath.cuh)
   // per pixel
   float4* vp_pr;    // visible point p, search radius (kept across iterations)
   float4* vp_wo;    // wo, material index (int bits; -1: no visible point)

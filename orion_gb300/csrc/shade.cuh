@@ -168,15 +168,15 @@ __device__ __forceinline__ void camera_ray(const DevCamera& c, PathSampler& smp,
   camera_ray_u(c, u, i, j, o, d);
 }
 
-// The same with its 2 (pinhole) or 4 (thin lens) sample dimensions taken in
-// one pass over the index bits; returns the next sample dimension (7 or 9).
-__device__ __forceinline__ uint32_t camera_ray_block(const DevCamera& c, const uint32_t* __restrict__ matrices,
+// The same with its 2 (pinhole) or 4 (thin lens) sample dimensions drawn
+// together; returns the next sample dimension (7 or 9).
+__device__ __forceinline__ uint32_t camera_ray_block(const DevCamera& c, const uint32_t* __restrict__ tables,
                                                      uint64_t index, int i, int j, V3* o, V3* d) {
   float u[4];
   if (c.lens_radius > 0.f) {
-    sobol_dims<4>(matrices, index, 5u, u);
+    sobol_dims<4>(tables, index, 5u, u);
   } else {
-    sobol_dims<2>(matrices, index, 5u, u);
+    sobol_dims<2>(tables, index, 5u, u);
     u[2] = u[3] = 0.f;
   }
   camera_ray_u(c, u, i, j, o, d);
@@ -247,10 +247,8 @@ __device__ __forceinline__ ShadeResult shade_one(const SceneView& s, const WaveV
       const DevMaterial& m = *mp;
       Frame fr{h.ng, h.ns, h.su, h.sv};
       // This bounce consumes at most 8 sample dimensions (light choice 1,
-      // light point 2, BSDF for MIS 2, continuation 2, roulette 1), all from
-      // one pass over the sample index (eight interleaved lookups per set bit
-      // in the dimension-major matrices: 21.8 -> 18.8 ms of shading per
-      // displaced-sphere render against eight words per bit of a bit-major copy).
+      // light point 2, BSDF for MIS 2, continuation 2, roulette 1), drawn
+      // together: their table lookups are independent.
       const uint32_t d0 = (uint32_t)w.dim[pid];
       float u[8];
       sobol_dims<8>(sobol, index, d0, u);
