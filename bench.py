@@ -306,16 +306,20 @@ def run_ours(args) -> dict:
 
     # End to end through the C ABI: upload scene arrays, render, read the film back (into the
     # caller's film buffers, allocated once as a caller rendering repeatedly would).
-    e2e_ms = []
+    e2e_ms, e2e_parts = [], []
     film_bytes = W * H * (3 * 4 + 4)
     e2e_out = (np.zeros((H, W, 3), np.float32), np.zeros((H, W), np.uint32))
-    for i in range(0 if args.quick else max(1, min(args.steps, 5))):
+    for i in range(0 if args.quick else max(1, min(args.steps, 7))):
         t = time.time()
         sid2 = ctx.upload(host)
+        t1 = time.time()
         ctx.render(sid2, W, H, out=e2e_out, **kw)
+        t2 = time.time()
         ctx.release(sid2)
         e2e_ms.append((time.time() - t) * 1e3)
+        e2e_parts.append([(t1 - t) * 1e3, (t2 - t1) * 1e3, ctx.last_stats()["device_ms"]])
     e2e_step = float(np.median(e2e_ms)) if e2e_ms else float("nan")
+    e2e_split = np.median(np.array(e2e_parts), 0) if e2e_parts else [float("nan")] * 3
 
     if args.quick:
         ctx.close()
@@ -372,7 +376,9 @@ def run_ours(args) -> dict:
         "rays_per_path": round(rays / (paths_per_step * args.steps), 4),
         "e2e": {"value": round(paths_per_step / (e2e_step * 1e-3) / 1e6, 3), "unit": "Mpaths/s",
                 "ms_per_step": round(e2e_step, 2), "h2d_bytes_per_step": int(scene_bytes),
-                "d2h_bytes_per_step": int(film_bytes)},
+                "d2h_bytes_per_step": int(film_bytes), "steps": len(e2e_ms),
+                "median_split_ms": {"upload": round(float(e2e_split[0]), 2), "render_and_readback": round(float(e2e_split[1]), 2),
+                                    "render_device": round(float(e2e_split[2]), 2)}},
         "roofline": roofline,
         "stages_ms": {k: round(v["ms"], 3) for k, v in stages.items()},
         "clocks": clk,

@@ -189,7 +189,10 @@ struct orion_gpu_ctx {
   // per extra stream its wave state, the stream, its join event; the events
   // that order the film writes wave after wave.
   static constexpr int kWaveStreams = orion_gb300::kMaxWaveStreams;
-  int wave_streams = 2;
+  // Four: the eight-sphere 1080p render (eight waves) 2583 -> 2822 Mpaths/s
+  // against two; the displaced sphere (two waves of 32M paths, split into four
+  // of 16M) 1025 -> 1026.
+  int wave_streams = 4;
   Wave xwave[kWaveStreams - 1];
   cudaStream_t xstream[kWaveStreams - 1] = {};
   cudaEvent_t ev_fork = nullptr, ev_join[kWaveStreams - 1] = {}, ev_film[kWaveStreams] = {};
