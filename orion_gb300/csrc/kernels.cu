@@ -35,14 +35,15 @@ __global__ void k_camera(SceneView s, WaveView w, WaveArgs a) {
     int i = (int)(pix % a.width), j = (int)(pix / a.width);
     V3 o, d;
     const uint32_t dim = camera_ray_block(s.cam, a.sobol, (uint64_t)index, i, j, &o, &d);
-    PathRec r;  // written whole: three full sectors
+    // Whole 32-byte sectors only (a partly written sector costs L2 a DRAM
+    // read): the ray, then the hit and meta sector. The throughput and
+    // radiance sector is left out: bounce 0's shading takes 1 and 0 for them
+    // (shade_one, FRESH) and writes them.
+    PathRec& r = w.rec[pid];
     r.o = f4(o, 0.f);
     r.d = f4(d, 0.f);
-    r.beta = make_float4(1.f, 1.f, 1.f, 0.f);
-    r.L = make_float4(0.f, 0.f, 0.f, 0.f);
     r.hit = make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
     r.meta = make_int4((int)dim, 0, 0, 0);
-    w.rec[pid] = r;
     w.q_ext[0][pid] = pid;
     w.qflags[pid] = 0;
   }
@@ -91,7 +92,7 @@ __global__ void __launch_bounds__(128, 5) k_shade(SceneView s, WaveView w, WaveA
   const int* in_q = w.q_cls + (size_t)SC * w.capacity;
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
     const int pid = in_q[q];
-    ShadeResult r = shade_one<lobes_of_class(SC), SC == SC_TEXTURED>(
+    ShadeResult r = shade_one<lobes_of_class(SC), SC == SC_TEXTURED, true>(
         s, w, a.sobol, pid, (uint64_t)(a.base_index + pid), bounce, a.max_depth, a.rr_depth);
     w.qflags[pid] = (uint8_t)((r.alive ? kQfExt : 0) | (r.did_nee ? kQfNee : 0) | (r.want_sh ? kQfShadow : 0) |
                               (r.want_mis ? kQfMis : 0) | (r.want_mis_env ? kQfMisEnv : 0));

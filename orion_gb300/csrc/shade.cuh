@@ -205,7 +205,9 @@ __host__ __device__ constexpr unsigned lobes_of_class(int sc) {
 
 // One bounce of PathTracing::Li for the path in slot `pid`, whose material
 // (if it hit one) holds only lobe kinds in KM; TEX: the material is textured.
-template <unsigned KM = kLobeAll, bool TEX = false>
+// FRESH: at bounce 0 the path's throughput is 1 and its radiance 0, and its
+// record does not hold them (plain waves: k_camera leaves them out).
+template <unsigned KM = kLobeAll, bool TEX = false, bool FRESH = false>
 __device__ __forceinline__ ShadeResult shade_one(const SceneView& s, const WaveView& w, const uint32_t* sobol,
                                                  int pid, uint64_t index, int bounce, int max_depth, int rr_depth) {
   LightDistrib distrib{s.light_func, s.light_cdf, s.light_func_int, s.num_lights};
@@ -213,10 +215,11 @@ __device__ __forceinline__ ShadeResult shade_one(const SceneView& s, const WaveV
     const int prim = __float_as_int(hv.w);  // the trace stores the primitive, -1 for a miss
     const V3 ro = xyz(w.ray_o[pid]);
     const V3 rd = xyz(w.ray_d[pid]);
-    float4 b4 = w.beta[pid];
+    const bool fresh = FRESH && bounce == 0;
+    float4 b4 = fresh ? make_float4(1.f, 1.f, 1.f, 0.f) : w.beta[pid];
     V3 beta = xyz(b4);
     const bool spec_prev = b4.w != 0.f;
-    const float4 L4 = w.L[pid];
+    const float4 L4 = fresh ? make_float4(0.f, 0.f, 0.f, 0.f) : w.L[pid];
     V3 L = xyz(L4);
 
     // Emission on the first hit or after a specular bounce (path.cpp:61-69).
