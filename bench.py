@@ -496,9 +496,11 @@ def run_batched(ctx, n_jobs: int, steps: int, tune_ms: float, oracle_jobs: int =
 
     plain_pass()  # warm-up
     plain = [plain_pass() for _ in range(steps)]
+    plain_cfg = ctx.get_config()
     tuned, tuned_mp = ctx.autotune_batch(specs, spp_cap=4, budget_ms=tune_ms)
     batch_pass()  # warm-up (graph instantiation at the tuned configuration; the output buffers)
     batched = [batch_pass() for _ in range(steps)]
+    ctx.set_config(**plain_cfg)  # the legs after this one run at the context's defaults
     p_wall = float(np.median([p[0] for p in plain]))
     b_wall = float(np.median([b[0] for b in batched]))
     p_dev = float(np.median([p[1] for p in plain]))

@@ -319,7 +319,9 @@ typedef struct orion_launch_config {
   int32_t refill_below;   /* a traversal warp takes new rays once fewer lanes than this hold one (1..32);
                              plain renders' any-hit launches use this + 4 (at most 32) */
   int32_t streams;        /* plain renders: waves in flight at once, each on its own stream (1..4);
-                             batches: concurrent pooled engines, min(streams, 2); 0 = keep */
+                             batches: concurrent engines, set to min(streams, 2) here; 0 = keep.
+                             orion_gpu_autotune_batch tunes the engine count alone (reported here
+                             by it) and leaves plain renders' waves as they were */
 } orion_launch_config;
 
 /* How orion_gpu_render_batch (and the server) run a batch:

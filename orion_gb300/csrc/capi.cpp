@@ -708,7 +708,10 @@ extern "C" int orion_gpu_set_config(orion_gpu_ctx* ctx, const orion_launch_confi
   if (cfg->streams < 0 || cfg->streams > kMaxWaveStreams)
     return fail(ORION_ERR_INVALID, "launch configuration: streams must be 0.." + std::to_string(kMaxWaveStreams));
   std::lock_guard<std::mutex> g(ctx->mu);
-  if (cfg->streams > 0) ctx->wave_streams = cfg->streams;
+  if (cfg->streams > 0) {
+    ctx->wave_streams = cfg->streams;
+    ctx->batch_engines = std::min(cfg->streams, (int)orion_gpu_ctx::kBatchEngines);
+  }
   ctx->cfg = c;
   ctx->default_wave = cfg->wave_paths;
   ctx->default_batch_slots = cfg->batch_slots;

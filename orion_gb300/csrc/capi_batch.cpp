@@ -129,7 +129,7 @@ static int run_batch_pooled_locked(orion_gpu_ctx* ctx, std::vector<DevJob>& dj, 
                                    int max_depth_all, BatchCtl* out_ctl, float* ms_out) {
   const int njobs = (int)dj.size();
   int rc;
-  const int ne = ctx->profiling ? 1 : std::min(std::min(ctx->wave_streams, (int)orion_gpu_ctx::kBatchEngines), njobs);
+  const int ne = ctx->profiling ? 1 : std::min(std::min(ctx->batch_engines, (int)orion_gpu_ctx::kBatchEngines), njobs);
   // Split by path count: largest jobs first, each to the lighter group.
   std::vector<std::vector<DevJob>> group(ne);
   std::vector<unsigned long long> gtotal(ne, 0);
@@ -262,7 +262,7 @@ static int run_batch_waves_locked(orion_gpu_ctx* ctx, std::vector<DevJob>& dj, u
   int rc;
   const int64_t wave = std::max<int64_t>(1024, std::min<int64_t>(ctx->default_batch_slots, (int64_t)total));
   const int64_t nwaves = std::max<int64_t>(1, ((int64_t)total + wave - 1) / wave);
-  const int ne = ctx->profiling ? 1 : (int)std::min<int64_t>(std::min(ctx->wave_streams, (int)orion_gpu_ctx::kBatchEngines),
+  const int ne = ctx->profiling ? 1 : (int)std::min<int64_t>(std::min(ctx->batch_engines, (int)orion_gpu_ctx::kBatchEngines),
                                                             nwaves);
   std::vector<BatchView> bvs(ne);
   std::vector<int> caps(ne);
@@ -531,22 +531,22 @@ extern "C" int orion_gpu_autotune_batch(orion_gpu_ctx* ctx, int32_t njobs, const
   // batch_slots is the pool size (pooled mode) or the wave size (wave mode).
   LaunchConfig best = ctx->cfg;
   int best_slots = ctx->default_batch_slots;
-  int best_streams = ctx->wave_streams, best_mode = ctx->batch_mode;
+  int best_streams = ctx->batch_engines, best_mode = ctx->batch_mode;
   double best_ms = 1e30, used = 0;
   auto trial = [&](const LaunchConfig& c, int slots, int streams, int mode, double* ms) -> int {
     LaunchConfig saved = ctx->cfg;
-    int saved_slots = ctx->default_batch_slots, saved_streams = ctx->wave_streams;
+    int saved_slots = ctx->default_batch_slots, saved_streams = ctx->batch_engines;
     int saved_mode = ctx->batch_mode;
     ctx->cfg = c;
     ctx->default_batch_slots = slots;
-    ctx->wave_streams = streams;
+    ctx->batch_engines = streams;
     ctx->batch_mode = mode;
     BatchCtl out;
     float fms = 0.f;
     int rc = run_batch_locked(ctx, dj, total, max_depth_all, &out, &fms);
     ctx->cfg = saved;
     ctx->default_batch_slots = saved_slots;
-    ctx->wave_streams = saved_streams;
+    ctx->batch_engines = saved_streams;
     ctx->batch_mode = saved_mode;
     *ms = fms;
     used += fms;
@@ -594,7 +594,7 @@ extern "C" int orion_gpu_autotune_batch(orion_gpu_ctx* ctx, int32_t njobs, const
   }
   ctx->cfg = best;
   ctx->default_batch_slots = best_slots;
-  ctx->wave_streams = best_streams;
+  ctx->batch_engines = best_streams;
   ctx->batch_mode = best_mode;
   if (best_out) {
     best_out->trace_block = best.trace_block;
@@ -604,7 +604,7 @@ extern "C" int orion_gpu_autotune_batch(orion_gpu_ctx* ctx, int32_t njobs, const
     best_out->wave_paths = ctx->default_wave;
     best_out->batch_slots = best_slots;
     best_out->refill_below = best.refill_below;
-    best_out->streams = ctx->wave_streams;
+    best_out->streams = ctx->batch_engines;
   }
   if (best_mpaths) *best_mpaths = (double)total / (best_ms * 1e-3) / 1e6;
   return ORION_OK;

@@ -193,6 +193,10 @@ struct orion_gpu_ctx {
   // against two; the displaced sphere (two waves of 32M paths, split into four
   // of 16M) 1025 -> 1026.
   int wave_streams = 4;
+  // Pooled or wave-mode batch engines running at once (at most kBatchEngines):
+  // orion_gpu_set_config sets min(streams, kBatchEngines), the batch
+  // autotuner tunes it alone, so tuning batches leaves plain renders' waves be.
+  int batch_engines = 2;
   Wave xwave[kWaveStreams - 1];
   cudaStream_t xstream[kWaveStreams - 1] = {};
   cudaEvent_t ev_fork = nullptr, ev_join[kWaveStreams - 1] = {}, ev_film[kWaveStreams] = {};
