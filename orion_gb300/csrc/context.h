@@ -190,8 +190,8 @@ struct orion_gpu_ctx {
   // that order the film writes wave after wave.
   static constexpr int kWaveStreams = orion_gb300::kMaxWaveStreams;
   // Four: the eight-sphere 1080p render (eight waves) 2583 -> 2822 Mpaths/s
-  // against two; the displaced sphere (two waves of 32M paths, split into four
-  // of 16M) 1025 -> 1026.
+  // against two. Renders of fewer than two full waves are split two ways
+  // only (render_impl).
   int wave_streams = 4;
   // Pooled or wave-mode batch engines running at once (at most kBatchEngines):
   // orion_gpu_set_config sets min(streams, kBatchEngines), the batch
