@@ -470,7 +470,8 @@ static int render_impl(orion_gpu_ctx* ctx, orion_scene_id id, const orion_render
   if (p.wave_paths <= 0 && !ctx->profiling) {
     // A render smaller than two waves is split into two equal waves (none
     // under 256K paths), so its waves overlap too. (Four ways, one per
-    // stream, made the 1M-path Cornell render slower: 402 -> 355 Mpaths/s.)
+    // stream, made the 1M-path Cornell render slower: 355 Mpaths/s against
+    // 382-402 split two ways, in full bench runs.)
     const int64_t min_split = 1 << 18;
     int64_t nw = (total + wave - 1) / std::max<int64_t>(wave, 1);
     const int64_t want = std::min<int64_t>(std::min(ctx->wave_streams, 2), std::max<int64_t>(1, total / min_split));

@@ -223,7 +223,7 @@ __device__ __forceinline__ int take_child(uint2& ng, uint32_t oct) {
 }
 
 // ANY = false: closest hit over (tnear, tfar]. ANY = true: first hit found,
-// children visited far to near (see lane_step). A stack overflow ends the
+// children visited far to near (see lane_visit). A stack overflow ends the
 // traversal with a miss (see the file comment).
 template <bool ANY, int SMEM, int CAP>
 __device__ __forceinline__ RayHit traverse(const TraceScene& s, V3 o, V3 d, float tnear, float tfar,
