@@ -13,8 +13,11 @@
 //   k_trace       closest hit for the BSDF-sampled MIS rays (traced once;
 //                 the reference traces that ray twice, once inside
 //                 Triangle::pdf and once in estimateDirect)
-//   k_resolve     adds the direct-lighting estimate to the path radiance
 //   k_film        per-pixel sums in sample order (RenderTarget::acumulate)
+//
+// A path's direct-lighting estimate is added to its radiance by its next
+// k_shade, before anything else of that bounce, or by k_film if the path
+// ended after sampling the light (shade_one, DEFER).
 //
 // Sample dimensions are consumed in exactly the reference's order, so every
 // path sees the same Sobol numbers as the reference path with the same index.
@@ -92,27 +95,18 @@ __global__ void __launch_bounds__(128, 5) k_shade(SceneView s, WaveView w, WaveA
   const int* in_q = w.q_cls + (size_t)SC * w.capacity;
   for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
     const int pid = in_q[q];
-    ShadeResult r = shade_one<lobes_of_class(SC), SC == SC_TEXTURED, true>(
+    ShadeResult r = shade_one<lobes_of_class(SC), SC == SC_TEXTURED, true, true>(
         s, w, a.sobol, pid, (uint64_t)(a.base_index + pid), bounce, a.max_depth, a.rr_depth);
-    w.qflags[pid] = (uint8_t)((r.alive ? kQfExt : 0) | (r.did_nee ? kQfNee : 0) | (r.want_sh ? kQfShadow : 0) |
+    w.qflags[pid] = (uint8_t)((r.alive ? kQfExt : 0) | (r.want_sh ? kQfShadow : 0) |
                               (r.want_mis ? kQfMis : 0) | (r.want_mis_env ? kQfMisEnv : 0));
   }
 }
 
-template <int NQ>
-__global__ void __launch_bounds__(kCompactThreads) k_compact_queues(uint8_t* flags, const int* list, const int* count,
-                                                                    CompactTargets tg) {
-  compact_queues<NQ>(flags, list, count, tg);
-}
-
-__global__ void k_resolve(SceneView s, WaveView w) {
-  const int n = w.counters[CNT_NEE];
-  for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) resolve_one(s, w, w.q_nee[q]);
-}
-
 // Per-pixel accumulation in sample order: thread t owns the pixel of sample
 // base + t and walks that pixel's samples of the wave in index order.
-__global__ void k_film(WaveView w, WaveArgs a, FilmView film) {
+// A path whose last light sample is still pending (it ended right after
+// sampling it) gets it added here, before its radiance is summed.
+__global__ void k_film(SceneView s, WaveView w, WaveArgs a, FilmView film) {
   const int64_t wh = (int64_t)a.width * a.height;
   const int64_t nt = a.n_paths < wh ? a.n_paths : wh;
   for (int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; t < nt; t += (int64_t)gridDim.x * blockDim.x) {
@@ -122,6 +116,12 @@ __global__ void k_film(WaveView w, WaveArgs a, FilmView film) {
     uint32_t c = 0;
     for (int64_t k = t; k < a.n_paths; k += wh) {
       float4 l = w.L[k];
+      if (w.dim[k] & kNeePending) {
+        const V3 e = xyz(l) + nee_estimate(s, w, (int)k);
+        l.x = e.x;
+        l.y = e.y;
+        l.z = e.z;
+      }
       r += l.x;
       g += l.y;
       b += l.z;
@@ -148,6 +148,12 @@ __global__ void k_film(WaveView w, WaveArgs a, FilmView film) {
       film.sumsq64[3 * pix + 2] += bb;
     }
   }
+}
+
+template <int NQ>
+__global__ void __launch_bounds__(kCompactThreads) k_compact_queues(uint8_t* flags, const int* list, const int* count,
+                                                                    CompactTargets tg) {
+  compact_queues<NQ>(flags, list, count, tg);
 }
 
 __global__ void k_reset_counters(int* counters, int slots, int keep_slot, int keep_value) {
@@ -426,15 +432,14 @@ void launch_wave(const SceneView& s, const WaveView& w, const WaveArgs& a, const
       }
       nl += mis - 1;  // end() counts one
       end();
-      begin(ST_RESOLVE);
-      k_resolve<<<sgrid, cfg.shade_block, 0, stream>>>(s, w);
-      end();
+      // No resolve pass: each path's light sample is added to its radiance by
+      // its next shading, or by k_film if the path ends here (shade_one, DEFER).
     }
     cur ^= 1;
   }
   if (film_wait) cudaStreamWaitEvent(stream, film_wait, 0);
   begin(ST_FILM);
-  k_film<<<grid_for(a.n_paths, 256, persistent * 4), 256, 0, stream>>>(w, a, film);
+  k_film<<<grid_for(a.n_paths, 256, persistent * 4), 256, 0, stream>>>(s, w, a, film);
   end();
   if (film_done) cudaEventRecord(film_done, stream);
   if (launches) *launches += nl;
@@ -492,7 +497,7 @@ cudaError_t configure_kernels(int smem_bytes, KernelLimits* lim) {
   const void* shade[] = {(const void*)k_shade<SC_DIFFUSE>, (const void*)k_shade<SC_CONDUCTOR>,
                          (const void*)k_shade<SC_SPECULAR>, (const void*)k_shade<SC_DIELECTRIC>,
                          (const void*)k_shade<SC_PLASTIC>, (const void*)k_shade<SC_GENERAL>, (const void*)k_shade<SC_TEXTURED>,
-                         (const void*)k_shade<SC_MISS>, (const void*)k_resolve};
+                         (const void*)k_shade<SC_MISS>};
   for (const void* f : trace) {
     cudaError_t e = limit_of(f, smem_bytes, &lim->max_trace_block);
     if (e != cudaSuccess) return e;

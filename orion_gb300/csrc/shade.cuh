@@ -14,6 +14,9 @@ namespace orion_gb300 {
 
 constexpr int kNonSpecular = BXDF_ALL & ~BXDF_SPECULAR;
 constexpr int kFlagShadow = 1, kFlagMis = 2, kFlagEnv = 4;
+// Plain waves: set in a path's Sobol dimension word (rec.meta.x) while its
+// last light sample waits to be added to its radiance (shade_one, k_film).
+constexpr int kNeePending = 1 << 30;
 
 __device__ __forceinline__ void queue_append(int* counter, int* queue, int value, bool pred) {
   unsigned active = __activemask();
@@ -203,11 +206,55 @@ __host__ __device__ constexpr unsigned lobes_of_class(int sc) {
                                : kLobeAll;
 }
 
+// beta * Ld / selPdf of the light sample a path's shading left in its NEE
+// record (path.cpp:77-80), once its shadow and MIS rays are traced; the
+// radiance adds it next (resolve_one, or the next bounce's shading).
+__device__ __forceinline__ V3 nee_estimate(const SceneView& s, const WaveView& w, int pid) {
+    float4 pb = w.nee_beta[pid];
+    int fl = __float_as_int(pb.w);
+    int li = fl >> 8;
+    float4 np = w.nee_p[pid];
+    float4 ldv = w.nee_ld[pid];
+    V3 Ld = V3{0, 0, 0};
+    if ((fl & kFlagShadow) && !w.occluded[pid]) Ld = Ld + xyz(ldv);
+    if (fl & kFlagMis) {
+      const DevLight& lt = s.lights[li];
+      float4 fv = w.nee_f[pid];
+      V3 fb = xyz(fv);
+      float bpdf = ldv.w;
+      if (fl & kFlagEnv) {
+        if (!w.mis_occluded[pid]) Ld = Ld + sdiv(mul(fb, env_le(lt, s.envmaps, xyz(w.mis_d[pid]))) * fv.w, bpdf);
+      } else {
+        const float4 mh = w.mis_hit[pid];
+        const int prim = __float_as_int(mh.w);  // primitive hit by the MIS ray, -1 for a miss
+        const V3 wi = xyz(w.mis_d[pid]);
+        if (prim == lt.prim) {
+          // Triangle::pdf (src/core/triangle.cpp:123-135) on the traced hit.
+          const PrimShade& sh = s.prims[prim];
+          V3 ip = point_on(sh, mh.y, mh.z);
+          V3 ing = geometric_normal(sh);
+          float lpdf = length_sq(xyz(np) - ip) / (absdot(ing, -wi) * lt.area);
+          if (isinf(lpdf)) lpdf = 0.f;
+          if (lpdf != 0.f) {
+            float wgt = power_heuristic(bpdf, lpdf);
+            V3 Li = dot(ing, -wi) > 0.f ? ld3(lt.L) : V3{0, 0, 0};
+            if (!is_black(Li)) Ld = Ld + sdiv(mul(fb, Li) * wgt, bpdf);
+          }
+        }
+      }
+    }
+    return mul(xyz(pb), sdiv(Ld, np.w));
+}
+
 // One bounce of PathTracing::Li for the path in slot `pid`, whose material
 // (if it hit one) holds only lobe kinds in KM; TEX: the material is textured.
 // FRESH: at bounce 0 the path's throughput is 1 and its radiance 0, and its
 // record does not hold them (plain waves: k_camera leaves them out).
-template <unsigned KM = kLobeAll, bool TEX = false, bool FRESH = false>
+// DEFER (plain waves): the light sample of the path's previous bounce is
+// added to its radiance here, first, as a separate resolve pass would have
+// added it before this bounce; this bounce's sample is left pending
+// (kNeePending) for the next shading or, if the path ends, for k_film.
+template <unsigned KM = kLobeAll, bool TEX = false, bool FRESH = false, bool DEFER = false>
 __device__ __forceinline__ ShadeResult shade_one(const SceneView& s, const WaveView& w, const uint32_t* sobol,
                                                  int pid, uint64_t index, int bounce, int max_depth, int rr_depth) {
   LightDistrib distrib{s.light_func, s.light_cdf, s.light_func_int, s.num_lights};
@@ -221,6 +268,8 @@ __device__ __forceinline__ ShadeResult shade_one(const SceneView& s, const WaveV
     const bool spec_prev = b4.w != 0.f;
     const float4 L4 = fresh ? make_float4(0.f, 0.f, 0.f, 0.f) : w.L[pid];
     V3 L = xyz(L4);
+    const int dimw = DEFER ? w.dim[pid] : 0;
+    if (DEFER && (dimw & kNeePending)) L = L + nee_estimate(s, w, pid);
 
     // Emission on the first hit or after a specular bounce (path.cpp:61-69).
     if (bounce == 0 || spec_prev) {
@@ -252,7 +301,7 @@ __device__ __forceinline__ ShadeResult shade_one(const SceneView& s, const WaveV
       // This bounce consumes at most 8 sample dimensions (light choice 1,
       // light point 2, BSDF for MIS 2, continuation 2, roulette 1), drawn
       // together: their table lookups are independent.
-      const uint32_t d0 = (uint32_t)w.dim[pid];
+      const uint32_t d0 = DEFER ? (uint32_t)(dimw & ~kNeePending) : (uint32_t)w.dim[pid];
       float u[8];
       sobol_dims<8>(sobol, index, d0, u);
       int used = 0;
@@ -359,7 +408,9 @@ __device__ __forceinline__ ShadeResult shade_one(const SceneView& s, const WaveV
           w.beta[pid] = f4(beta, spec ? 1.f : 0.f);
         }
       }
-      w.dim[pid] = (int)(d0 + used);
+      w.dim[pid] = (int)(d0 + used) | (DEFER && did_nee ? kNeePending : 0);
+    } else if (DEFER && (dimw & kNeePending)) {
+      w.dim[pid] = dimw & ~kNeePending;  // added above
     }
     w.L[pid] = f4(L, L4.w);  // w holds batched mode's sample index bits
   return ShadeResult{alive, did_nee, want_sh, want_mis, want_mis_env};
@@ -570,42 +621,8 @@ __device__ __forceinline__ void compact_queues(uint8_t* flags, const int* list, 
 // Adds beta * Ld / selPdf for a path that sampled a light this bounce
 // (path.cpp:77-80 with the shadow and MIS rays traced).
 __device__ __forceinline__ void resolve_one(const SceneView& s, const WaveView& w, int pid) {
-    float4 pb = w.nee_beta[pid];
-    int fl = __float_as_int(pb.w);
-    int li = fl >> 8;
-    float4 np = w.nee_p[pid];
-    float4 ldv = w.nee_ld[pid];
-    V3 Ld = V3{0, 0, 0};
-    if ((fl & kFlagShadow) && !w.occluded[pid]) Ld = Ld + xyz(ldv);
-    if (fl & kFlagMis) {
-      const DevLight& lt = s.lights[li];
-      float4 fv = w.nee_f[pid];
-      V3 fb = xyz(fv);
-      float bpdf = ldv.w;
-      if (fl & kFlagEnv) {
-        if (!w.mis_occluded[pid]) Ld = Ld + sdiv(mul(fb, env_le(lt, s.envmaps, xyz(w.mis_d[pid]))) * fv.w, bpdf);
-      } else {
-        const float4 mh = w.mis_hit[pid];
-        const int prim = __float_as_int(mh.w);  // primitive hit by the MIS ray, -1 for a miss
-        const V3 wi = xyz(w.mis_d[pid]);
-        if (prim == lt.prim) {
-          // Triangle::pdf (src/core/triangle.cpp:123-135) on the traced hit.
-          const PrimShade& sh = s.prims[prim];
-          V3 ip = point_on(sh, mh.y, mh.z);
-          V3 ing = geometric_normal(sh);
-          float lpdf = length_sq(xyz(np) - ip) / (absdot(ing, -wi) * lt.area);
-          if (isinf(lpdf)) lpdf = 0.f;
-          if (lpdf != 0.f) {
-            float wgt = power_heuristic(bpdf, lpdf);
-            V3 Li = dot(ing, -wi) > 0.f ? ld3(lt.L) : V3{0, 0, 0};
-            if (!is_black(Li)) Ld = Ld + sdiv(mul(fb, Li) * wgt, bpdf);
-          }
-        }
-      }
-    }
-    const float4 L4 = w.L[pid];
-    const V3 L = xyz(L4) + mul(xyz(pb), sdiv(Ld, np.w));
-    w.L[pid] = f4(L, L4.w);
+  const float4 L4 = w.L[pid];
+  w.L[pid] = f4(xyz(L4) + nee_estimate(s, w, pid), L4.w);
 }
 
 }  // namespace orion_gb300
