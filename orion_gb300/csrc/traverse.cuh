@@ -390,7 +390,9 @@ __host__ __device__ constexpr size_t trace_smem_bytes(int smem_entries, int bloc
 // Dealing a lane's triangle tests to the whole warp pays when one lane holds
 // many more than the others: a dealt round costs about as much as this many
 // one-by-one tests (closest hit: keeping the least hit takes shared-memory
-// atomics; occlusion: one vote).
+// atomics; occlusion: one vote). Measured on the 1024x1024 x 64 spp displaced
+// sphere: 986 Mpaths/s at 4 / 2, 985 at 3 / 2, 974 at 6 / 1, 971 dealing
+// every step; occlusion at 3 a little ahead of 2.
 constexpr int kDealClosest = 4, kDealAny = 3;
 
 // Tests the triangles of every lane's r.tg (all 32 lanes call it; lanes
