@@ -347,7 +347,10 @@ def run_ours(args) -> dict:
                 "unit": "GB/s", "frac": round(achieved / peaks["hbm_gbs"], 5), "traffic": traffic,
                 "peak_source": peaks["source"],
                 "alg_bytes_per_unit": ALG_BYTES[top], "units": int(units[top]),
-                "launches": stages[top]["launches"], "stage_ms": round(stages[top]["ms"], 3)}
+                "launches": stages[top]["launches"], "stage_ms": round(stages[top]["ms"], 3),
+                "timing": "one profiled render on one stream, CUDA events around each stage; the trace grids "
+                          "keep the production size (6 blocks of 128 threads per SM, leaving the rest of each "
+                          "SM to the other waves' shading), which a one-stream render leaves idle"}
     # Model bytes: BVH nodes (80 B) and triangles (48 B) the trace kernels
     # fetch, counted on the device over the workload's first sample pass
     # (1/spp of its paths, every bounce); per ray, then scaled to the timed
